@@ -1,0 +1,320 @@
+"""Python front end of the fd23 CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` import this module.  It wraps ``libfd23_oracle.so`` (built from
+``oracle/fd23_oracle.c`` by ``oracle/build.py``) with ctypes and adds the
+small host-side pieces of the reference setup: the ``.mdl`` parser, the CPML
+assignment table and the receiver pair duplication.
+
+Reference citations are relative to the fd23 project root
+(PD = PSV/psv_clean_double, PN = PSV/clean_nobox, SH = SH).
+"""
+import ctypes as C
+import math
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        _lib = C.CDLL(path)
+        d, i, l, vp = C.c_double, C.c_int, C.c_long, C.c_void_p
+        _lib.or_psv_material.argtypes = [i, i, d, d, vp, vp, vp, vp, vp]
+        _lib.or_sh_material.argtypes = [i, i, d, d, vp, vp, vp, vp]
+        _lib.or_cpml_profile.argtypes = [i, d, i, d, d, d, d, vp, vp, vp]
+        _lib.or_cpml_profile.restype = None
+        _lib.or_gaussian.argtypes = [d, i, vp, i]
+        _lib.or_trapezoid.argtypes = [d, d, d, d, vp, i]
+        _lib.or_moment_psv.argtypes = [d, d, d, d, vp]
+        _lib.or_moment_psv.restype = None
+        _lib.or_moment_sh.argtypes = [d, d, d, d, vp]
+        _lib.or_moment_sh.restype = None
+        _lib.or_psv_source_terms.argtypes = [i, i, i, i, vp, d, d, vp, i, i, vp, vp, vp]
+        _lib.or_sh_source_terms.argtypes = [i, i, i, i, vp, d, d, vp, i, i, vp, vp, vp]
+        _lib.or_mdl_raster.argtypes = [i, i, d, i, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+        _lib.or_mdl_raster.restype = None
+        for nm in ("or_psv_run_f64", "or_psv_run_f32"):
+            getattr(_lib, nm).argtypes = [i, i, i, i, vp, vp, i, vp, vp, vp, i, i, vp, i, vp,
+                                          i, i, i, vp, vp, vp, i]
+        for nm in ("or_sh_run_f64", "or_sh_run_f32"):
+            getattr(_lib, nm).argtypes = [i, i, i, i, vp, vp, i, vp, vp, vp, i, i, vp,
+                                          i, i, i, vp, vp, i]
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+# --------------------------------------------------------------------------
+# model input
+# --------------------------------------------------------------------------
+def parse_mdl(path):
+    """Parse a ``.mdl`` polygon model (BACK / POLY / DEF keywords), following
+    the grammar read by PD/model/model.cpp:240-369.  Returns a list of
+    (vp, vs, den, [(x, z), ...]) with the background first."""
+    with open(path) as fh:
+        lines = fh.read().split("\n")
+    polys, defs = [], {}
+    k = 0
+    while k < len(lines):
+        line = lines[k]
+        k += 1
+        if not line.strip() or line.startswith("#"):
+            continue
+        args = line.split()
+        key = args[0].upper()
+        if key == "DEF":
+            defs[args[1]] = (float(args[2]), float(args[3]))
+            continue
+        if key in ("BACK", "POLY"):
+            vp, vs, den = (float(a) for a in args[1:4])
+            if vs < 0:
+                vs = -vp * vs
+            if den < 0:
+                den = -vp * den
+            verts = []
+            if key == "POLY":
+                while k < len(lines) and lines[k].startswith("\t"):
+                    toks = lines[k].split()
+                    k += 1
+                    j = 0
+                    while j < len(toks):
+                        if toks[0][0].isalpha():
+                            verts.append(defs[toks[j]])
+                            j += 1
+                        else:
+                            verts.append((float(toks[j]), float(toks[j + 1])))
+                            j += 2
+                polys.append((vp, vs, den, verts))
+            else:
+                polys.insert(0, (vp, vs, den, []))
+            continue
+        raise ValueError("bad model command %r" % line)
+    return polys
+
+
+def mdl_raster(polys, nx, nz, h):
+    nvert = np.array([len(p[3]) for p in polys], dtype=np.int32)
+    vx = np.array([v[0] for p in polys for v in p[3]] + [0.0], dtype=np.float64)
+    vz = np.array([v[1] for p in polys for v in p[3]] + [0.0], dtype=np.float64)
+    pvp = np.array([p[0] for p in polys], dtype=np.float64)
+    pvs = np.array([p[1] for p in polys], dtype=np.float64)
+    pden = np.array([p[2] for p in polys], dtype=np.float64)
+    out = [np.empty(nx * nz, dtype=np.float64) for _ in range(3)]
+    lib().or_mdl_raster(nx, nz, h, len(polys), _p(nvert), _p(vx), _p(vz), _p(pvp), _p(pvs),
+                        _p(pden), _p(out[0]), _p(out[1]), _p(out[2]))
+    return [o.reshape(nz, nx) for o in out]
+
+
+# --------------------------------------------------------------------------
+# material / CPML / source / receivers
+# --------------------------------------------------------------------------
+def psv_material(vp, vs, den, h, dt):
+    nz, nx = vp.shape
+    out = np.empty(5 * nx * nz, dtype=np.float64)
+    stab = C.c_double(0.0)
+    a = [np.ascontiguousarray(x, dtype=np.float64) for x in (vp, vs, den)]
+    rc = lib().or_psv_material(nx, nz, h, dt, _p(a[0]), _p(a[1]), _p(a[2]), _p(out),
+                               C.cast(C.pointer(stab), C.c_void_p))
+    return out.reshape(5, nz, nx), stab.value, rc
+
+
+def sh_material(vs, den, h, dt):
+    nz, nx = vs.shape
+    out = np.empty(3 * nx * nz, dtype=np.float64)
+    stab = C.c_double(0.0)
+    a = [np.ascontiguousarray(x, dtype=np.float64) for x in (vs, den)]
+    rc = lib().or_sh_material(nx, nz, h, dt, _p(a[0]), _p(a[1]), _p(out),
+                              C.cast(C.pointer(stab), C.c_void_p))
+    return out.reshape(3, nz, nx), stab.value, rc
+
+
+def cpml_profile(npml, startpos, n, pml_dt, pml_r, pml_v, pml_fc):
+    b, c, k = (np.empty(n, dtype=np.float64) for _ in range(3))
+    lib().or_cpml_profile(npml, startpos, n, pml_dt, pml_r, pml_v, pml_fc, _p(b), _p(c), _p(k))
+    return b, c, k
+
+
+def cpml_psv(nx, nz, npml, pml_dt, pml_r, pml_v, pml_fc):
+    """b|c|k blocks; each block = Txx_x, Txz_x, U_x, W_x (nx) then
+    Tzz_z, Txz_z, U_z, W_z (nz).  Start offsets from PD/cpml/cpml.cpp:177-185."""
+    xs = [0.5, 0.0, 0.0, 0.5]  # Txx_x, Txz_x, U_x, W_x
+    zs = [0.0, 0.5, 0.0, 0.5]  # Tzz_z, Txz_z, U_z, W_z
+    out = np.empty((3, 4 * nx + 4 * nz), dtype=np.float64)
+    for j, s in enumerate(xs):
+        b, c, k = cpml_profile(npml, s, nx, pml_dt, pml_r, pml_v, pml_fc)
+        for q, arr in enumerate((b, c, k)):
+            out[q, j * nx:(j + 1) * nx] = arr
+    for j, s in enumerate(zs):
+        b, c, k = cpml_profile(npml, s, nz, pml_dt, pml_r, pml_v, pml_fc)
+        for q, arr in enumerate((b, c, k)):
+            out[q, 4 * nx + j * nz:4 * nx + (j + 1) * nz] = arr
+    return out
+
+
+def cpml_sh(nx, nz, npml, pml_dt, pml_r, pml_v, pml_fc):
+    """b|c|k blocks; each block = Tx_x, V_x (nx) then Tz_z, V_z (nz).
+    Start offsets from SH/cpml/cpml.cpp:172-176."""
+    out = np.empty((3, 2 * nx + 2 * nz), dtype=np.float64)
+    for j, (s, n, off) in enumerate(((0.0, nx, 0), (0.5, nx, nx), (0.5, nz, 2 * nx),
+                                     (0.0, nz, 2 * nx + nz))):
+        b, c, k = cpml_profile(npml, s, n, pml_dt, pml_r, pml_v, pml_fc)
+        for q, arr in enumerate((b, c, k)):
+            out[q, off:off + n] = arr
+    return out
+
+
+def gaussian(dt, alpha):
+    cap = 2 * abs(int(alpha * 3.0)) + 2
+    src = np.zeros(cap, dtype=np.float64)
+    n = lib().or_gaussian(dt, int(alpha), _p(src), cap)
+    return src[:n].copy()
+
+
+def trapezoid(dt, t1, t2, t3):
+    cap = int(t1 / dt) + int(t2 / dt) + int(t3 / dt) + 2
+    src = np.zeros(cap, dtype=np.float64)
+    n = lib().or_trapezoid(dt, t1, t2, t3, _p(src), cap)
+    return src[:n].copy()
+
+
+def ricker(dt, f0, t0=None):
+    """Ricker wavelet sampled as s(t)*dt (the integral form the reference uses
+    for its wavelets).  Not part of the reference; t0 defaults to 1.2/f0 and
+    the length to round(2*t0/dt)+1 samples."""
+    if t0 is None:
+        t0 = 1.2 / f0
+    n = int(round(2.0 * t0 / dt)) + 1
+    t = np.arange(n, dtype=np.float64) * dt - t0
+    a = (math.pi * f0 * t) ** 2
+    return (1.0 - 2.0 * a) * np.exp(-a) * dt
+
+
+def moment_psv(strike, dip, rake, azimuth):
+    m = np.empty(3, dtype=np.float64)
+    lib().or_moment_psv(strike, dip, rake, azimuth, _p(m))
+    return m
+
+
+def moment_sh(strike, dip, rake, azimuth):
+    m = np.empty(2, dtype=np.float64)
+    lib().or_moment_sh(strike, dip, rake, azimuth, _p(m))
+    return m
+
+
+PSV_FIELDS = {"U": 0, "W": 1, "Txx": 2, "Txz": 3, "Tzz": 4}
+SH_FIELDS = {"V": 0, "Tx": 1, "Tz": 2}
+
+
+def source_terms(wave, kind, nx, xs, zs, moment, h, dt, src, nt):
+    """Returns (field ids int32, flat cell idx int64, amp float64 [nterms, nt])."""
+    src = np.ascontiguousarray(src, dtype=np.float64)
+    field = np.zeros(16, dtype=np.int32)
+    idx = np.zeros(16, dtype=np.int64)
+    amp = np.zeros((16, nt), dtype=np.float64)
+    m = np.ascontiguousarray(moment, dtype=np.float64)
+    fn = lib().or_psv_source_terms if wave == "psv" else lib().or_sh_source_terms
+    n = fn(kind, nx, xs, zs, _p(m), h, dt, _p(src), len(src), nt, _p(field), _p(idx), _p(amp))
+    return field[:n].copy(), idx[:n].copy(), np.ascontiguousarray(amp[:n])
+
+
+def receivers_line(nrec, ix0, iz0, idx, idz):
+    """PD/record/cu_record.cu:12-28: each receiver is recorded as the pair
+    (x, z), (x-1, z)."""
+    rx, rz = [], []
+    for i in range(nrec):
+        x, z = ix0 + idx * i, iz0 + idz * i
+        rx += [x, x - 1]
+        rz += [z, z]
+    return np.array(rx, dtype=np.int64), np.array(rz, dtype=np.int64)
+
+
+def receivers_file(path):
+    """Station file of (z x) pairs, PD/record/cu_record.cu:30-76."""
+    vals = [int(t) for t in open(path).read().split()]
+    rx, rz = [], []
+    for j in range(0, len(vals) - 1, 2):
+        z, x = vals[j], vals[j + 1]
+        rx += [x, x - 1]
+        rz += [z, z]
+    return np.array(rx, dtype=np.int64), np.array(rz, dtype=np.int64)
+
+
+# --------------------------------------------------------------------------
+# time stepping
+# --------------------------------------------------------------------------
+def psv_state_size(nx, nz, npml):
+    return 5 * nx * nz + 4 * 2 * npml * nz + 4 * 2 * npml * nx
+
+
+def sh_state_size(nx, nz, npml):
+    return 3 * nx * nz + 2 * 2 * npml * nz + 2 * 2 * npml * nx
+
+
+def psv_run(prec, nx, nz, npml, topabsorb, mat, bck, terms, rec_u, rec_w, nt, itrecord=1, it0=0,
+            state=None, nthreads=0):
+    """Run nt steps of the P-SV oracle.  prec 'f64' or 'f32'.  mat (5,nz,nx)
+    and bck (3, 4nx+4nz) FP64 arrays are rounded to prec.  terms = (field,
+    idx, amp[nterms, nt_amp]) with absolute step indexing.  rec_* = flat
+    indices.  Returns (seis_u, seis_w, state)."""
+    dt_ = np.float64 if prec == "f64" else np.float32
+    fn = lib().or_psv_run_f64 if prec == "f64" else lib().or_psv_run_f32
+    mat_r = np.ascontiguousarray(mat, dtype=dt_)
+    bck_r = np.ascontiguousarray(bck, dtype=dt_)
+    field, idx, amp = terms
+    field = np.ascontiguousarray(field, dtype=np.int32)
+    idx = np.ascontiguousarray(idx, dtype=np.int64)
+    amp_r = np.ascontiguousarray(amp, dtype=dt_)
+    ru = np.ascontiguousarray(rec_u, dtype=np.int64)
+    rw = np.ascontiguousarray(rec_w, dtype=np.int64)
+    if state is None:
+        state = np.zeros(psv_state_size(nx, nz, npml), dtype=dt_)
+    else:
+        state = np.ascontiguousarray(state, dtype=dt_).copy()
+    nrecs = len([it for it in range(it0, it0 + nt) if it % itrecord == 0])
+    su = np.zeros((nrecs, len(ru)), dtype=dt_)
+    sw = np.zeros((nrecs, len(rw)), dtype=dt_)
+    nt_amp = amp_r.shape[1] if amp_r.ndim == 2 and len(field) else 0
+    fn(nx, nz, npml, int(topabsorb), _p(mat_r), _p(bck_r), len(field), _p(field), _p(idx),
+       _p(amp_r) if len(field) else None, nt_amp, len(ru), _p(ru), len(rw), _p(rw), it0, nt,
+       itrecord, _p(state), _p(su), _p(sw), nthreads)
+    return su, sw, state
+
+
+def sh_run(prec, nx, nz, npml, topabsorb, mat, bck, terms, rec, nt, itrecord=1, it0=0, state=None,
+           nthreads=0):
+    dt_ = np.float64 if prec == "f64" else np.float32
+    fn = lib().or_sh_run_f64 if prec == "f64" else lib().or_sh_run_f32
+    mat_r = np.ascontiguousarray(mat, dtype=dt_)
+    bck_r = np.ascontiguousarray(bck, dtype=dt_)
+    field, idx, amp = terms
+    field = np.ascontiguousarray(field, dtype=np.int32)
+    idx = np.ascontiguousarray(idx, dtype=np.int64)
+    amp_r = np.ascontiguousarray(amp, dtype=dt_)
+    r = np.ascontiguousarray(rec, dtype=np.int64)
+    if state is None:
+        state = np.zeros(sh_state_size(nx, nz, npml), dtype=dt_)
+    else:
+        state = np.ascontiguousarray(state, dtype=dt_).copy()
+    nrecs = len([it for it in range(it0, it0 + nt) if it % itrecord == 0])
+    s = np.zeros((nrecs, len(r)), dtype=dt_)
+    nt_amp = amp_r.shape[1] if amp_r.ndim == 2 and len(field) else 0
+    fn(nx, nz, npml, int(topabsorb), _p(mat_r), _p(bck_r), len(field), _p(field), _p(idx),
+       _p(amp_r) if len(field) else None, nt_amp, len(r), _p(r), it0, nt, itrecord, _p(state),
+       _p(s), nthreads)
+    return s, state
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    den = np.linalg.norm(b.ravel())
+    return float(np.linalg.norm((a - b).ravel()) / (den if den > 0 else 1.0))
