@@ -1,0 +1,301 @@
+"""Benchmark: P-SV time stepping on GB300, cell-updates per second.
+
+Workload (one bench "step" = one whole shot from a zero wavefield):
+  P-SV, nx=4000, nz=2000, h=5 m, dt=4e-4 s, 5000 time steps; 12 seeded flat
+  layers with vp ~ U[1500, 4500] m/s plus a seeded Gaussian-smoothed 5 %
+  perturbation, vs = vp/1.73, rho = 310 vp^0.25; 15 Hz Ricker explosion;
+  40-cell CPML; 400 surface stations recorded as 800 traces per component.
+  Synthetic data (the reference publishes no data set for this path).
+
+value: cell-updates/s with the model already resident in HBM (CUDA events on
+       the solver's stream around K whole shots).
+e2e:   the same metric through the public API with host buffers: material
+       build + host->device upload, the shot, device->host seismograms.
+roofline: the fused sweep kernel against the measured HBM copy bandwidth.
+cpu_baseline: the oracle's restatement of the reference update loop on the
+       host cores, on a bounded sample of the same grid.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--nt NT] [--prec f32|bf16|f16|f64] [--kernel fused|twopass]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+NX, NZ, H, DT, NT, NPML, F0 = 4000, 2000, 5.0, 4e-4, 5000, 40, 15.0
+NSTA = 400
+
+
+def c1_model(nx=NX, nz=NZ, seed=1):
+    rng = np.random.default_rng(seed)
+    bounds = np.sort(rng.choice(np.arange(nz // 20, nz - nz // 20), size=11, replace=False))
+    vel = rng.uniform(1500.0, 4500.0, size=12)
+    layer = np.searchsorted(bounds, np.arange(nz), side="right")
+    vp = np.repeat(vel[layer][:, None], nx, axis=1)
+    noise = rng.standard_normal((nz, nx))
+    kz = np.fft.fftfreq(nz)[:, None]
+    kx = np.fft.rfftfreq(nx)[None, :]
+    sig = 20.0
+    smooth = np.fft.irfft2(np.fft.rfft2(noise) * np.exp(-2 * (np.pi * sig) ** 2 * (kx ** 2 + kz ** 2)),
+                           s=(nz, nx))
+    smooth *= 0.05 / np.abs(smooth).max()
+    vp *= 1.0 + smooth
+    vs = vp / 1.73
+    rho = 310.0 * vp ** 0.25
+    return vp, vs, rho
+
+
+def alg_bytes(nx, nz, npml, es, topabsorb=0):
+    """Compulsory HBM bytes of one time step: every wavefield read and written
+    once and every material array read once (5+5 arrays of es bytes), plus the
+    CPML memory variables (4 per PML cell, read and written, FP32/FP64)."""
+    cs = 8 if es == 8 else 4
+    npml_cells = 2 * npml * nz + npml * nx * (1 + topabsorb)
+    return (5 * 2 + 5) * es * nx * nz + 4 * 2 * cs * npml_cells
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(budget_s=12.0, threads=0):
+    """Oracle restatement of the reference update loop (FP32, all host
+    threads) on the benchmark grid for as many steps as fit the budget."""
+    from oracle import fd23_oracle as O
+    vp, vs, rho = c1_model()
+    mat, _, _ = O.psv_material(vp, vs, rho, H, DT)
+    bck = O.cpml_psv(NX, NZ, NPML, DT, 1e-11, vp.max() / H, F0)
+    src = O.ricker(DT, F0)
+    terms = O.source_terms("psv", 1, NX, NX // 2, 20, np.array([1.0, 0, 1.0]), H, DT, src, NT)
+    rec = np.arange(200, 200 + 9 * NSTA, 9)
+    # one step to size the sample, then one contiguous run that fits the budget
+    t0 = time.perf_counter()
+    O.psv_run("f32", NX, NZ, NPML, 0, mat, bck, terms, rec, rec + NX, 1, nthreads=threads)
+    one = time.perf_counter() - t0
+    steps = int(max(3, min(200, budget_s / max(one, 1e-3))))
+    t0 = time.perf_counter()
+    O.psv_run("f32", NX, NZ, NPML, 0, mat, bck, terms, rec, rec + NX, steps, nthreads=threads)
+    t_used = time.perf_counter() - t0
+    cores = threads if threads > 0 else (os.cpu_count() or 1)
+    return {"value": NX * NZ * steps / t_used, "unit": "cell-updates/s", "cores": cores,
+            "kind": "port",
+            "sample": "%d steps of the %dx%d grid (%.1f s), FP32 oracle, %d threads" % (
+                steps, NX, NZ, t_used, cores)}
+
+
+def run_reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    cb = cpu_baseline(budget_s=max(5.0, 20.0 / max(1, args.steps)))
+    line = {"impl": "reference", "metric": "cell-updates/s", "value": cb["value"],
+            "unit": "cell-updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": NX * NZ * NT / cb["value"] * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "psv_4000x2000_5000steps_c1", "nx": NX, "nz": NZ, "nt": NT,
+                       "note": "reference CPU update loop (oracle restatement); the reference's "
+                               "own sources are not on the GPU host"},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours")
+    ap.add_argument("--nt", type=int, default=NT)
+    ap.add_argument("--prec", default="f32")
+    ap.add_argument("--kernel", default="fused")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    if args.impl == "reference":
+        run_reference_arm(args, rank, world)
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    import torch
+    import fd23_gb300 as F
+    torch.cuda.set_device(local)
+    nt = args.nt
+    vp, vs, rho = c1_model(seed=1 + rank)
+    pml_v = float(vp.max()) / H
+    s = F.Solver("psv", NX, NZ, NPML, H, DT, prec=args.prec, pml_dt=DT, pml_v=pml_v, pml_r=1e-11,
+                 pml_fc=F0, device=local, kernel=args.kernel)
+    s.set_model(vp, vs, rho)
+    src = F.wavelet_ricker(DT, F0)
+    s.set_source(F.SRC_EXPLOSION, NX // 2, 20, None, src, nt)
+    rxu, rzu = F.receivers_line(NSTA, 200, 0, 9, 0)
+    rxw, rzw = F.receivers_line(NSTA, 200, 1, 9, 0)
+    s.set_receivers(0, rxu, rzu)
+    s.set_receivers(1, rxw, rzw)
+    stream = torch.cuda.ExternalStream(s.stream, device=local)
+
+    def shot():
+        s.reset()
+        s.run(nt, 1)
+
+    for _ in range(args.warmup):
+        shot()
+    s.sync()
+    sampler = ClockSampler(local)
+    if rank == 0:
+        sampler.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        shot()
+    e1.record(stream)
+    s.sync()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    clocks = sampler.stop() if rank == 0 else None
+    t = torch.tensor([ms], dtype=torch.float64)
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t[0])
+    cells = NX * NZ * nt * args.steps * world
+    value = cells / (ms_max * 1e-3)
+
+    # end to end through the public API with host buffers
+    e2e = None
+    if not args.no_e2e:
+        es = {"f32": 4, "f64": 8, "bf16": 2, "f16": 2}[args.prec]
+        cs = 8 if args.prec == "f64" else 4
+        times = []
+        seis_bytes = 0
+        for _ in range(max(1, min(args.steps, 2))):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            s.set_model(vp, vs, rho)
+            shot()
+            su, sw = s.seismograms(0), s.seismograms(1)
+            times.append(time.perf_counter() - t0)
+            seis_bytes = su.nbytes + sw.nbytes
+        e2e = {"value": NX * NZ * nt / statistics.mean(times) * world, "unit": "cell-updates/s",
+               "h2d_bytes_per_step": 5 * NX * NZ * es + 2 * nt * cs,
+               "d2h_bytes_per_step": seis_bytes}
+
+    hbm, peak_kind = load_peaks()
+    es = {"f32": 4, "f64": 8, "bf16": 2, "f16": 2}[args.prec]
+    per_launch_ms = ms_max / (args.steps * nt)
+    ab = alg_bytes(NX, NZ, NPML, es)
+    achieved = ab / (per_launch_ms * 1e-3) / 1e9
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "traffic_per_cell.json")
+    if os.path.exists(tfile):
+        tb = json.load(open(tfile)).get("fused_psv_%s" % args.prec)
+        if tb:
+            traffic = tb * NX * NZ
+    line = {"metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.prec,
+            "data": "synthetic",
+            "config": {"workload": "psv_4000x2000_5000steps_c1", "nx": NX, "nz": NZ, "nt": nt,
+                       "h_m": H, "dt_s": DT, "npml": NPML, "source": "15 Hz Ricker explosion",
+                       "traces": 4 * NSTA, "kernel": args.kernel, "prec": args.prec,
+                       "l2": "inputs larger than L2 (%.0f MB resident)" % (
+                           (15 * es) * NX * NZ / 1e6),
+                       "parallelism": "replicas x%d" % world},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "traffic": traffic,
+                         "peak_source": peak_kind,
+                         "alg_bytes_per_launch": ab,
+                         "launch_ms": per_launch_ms},
+            "gpu_launches": args.steps * (nt + 1),
+            "clocks": clocks,
+            "e2e": e2e}
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    s.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,353 @@
+"""fd23_gb300 -- GB300 (sm_103a) 2-D elastic time stepping (P-SV and SH).
+
+Python front end of the C ABI in include/fd23.h.  The compute path is the
+CUDA library fd23_gb300/_lib/libfd23.so (build it with
+``python -c "import fd23_gb300.build as b; b.build()"``); there is no CPU
+fallback and importing this package without the library raises.
+
+The objects mirror the operator surface of the reference fd23 programs
+(paths relative to the fd23 project root):
+
+  Solver(...)                PARAM + FIELD + CPML set-up (PD/param/param.cpp,
+                             PD/field/cu_field.cu, PD/cpml/cpml.cpp)
+  Solver.set_model           MATERIAL::get_model (PD/material/material.cpp:101)
+  Solver.set_source          gaussian/trapozoid + cu_point_source(_p)
+                             (PD/source/waveform.cpp, PD/point_source/)
+  Solver.set_receivers       RECORD::init_line / init_list (PD/record/cu_record.cu)
+  Solver.run                 the time loop of PN/main.cpp:117-170
+  Solver.seismograms         the <output>_U / _W records ([step][receiver])
+  Solver.get_state/set_state savestate / restart (PN/main.cpp:253-317)
+"""
+import ctypes as _C
+import os as _os
+
+import numpy as _np
+
+_HERE = _os.path.dirname(_os.path.abspath(__file__))
+LIB_PATH = _os.path.join(_HERE, "_lib", "libfd23.so")
+
+PSV, SH = 0, 1
+F32, F64, BF16, F16 = 0, 1, 2, 3
+KERNEL_AUTO, KERNEL_FUSED, KERNEL_TWOPASS = 0, 1, 2
+U, W, TXX, TXZ, TZZ = 0, 1, 2, 3, 4
+V, TX, TZ = 0, 1, 2
+SRC_EXPLOSION, SRC_FORCE, SRC_MOMENT, SRC_MOMENT_P = 1, 2, 3, 13
+
+_WAVES = {"psv": PSV, "sh": SH, PSV: PSV, SH: SH}
+_PRECS = {"f32": F32, "fp32": F32, "f64": F64, "fp64": F64, "bf16": BF16, "f16": F16,
+          "fp16": F16, F32: F32, F64: F64, BF16: BF16, F16: F16}
+_KERNELS = {"auto": KERNEL_AUTO, "fused": KERNEL_FUSED, "twopass": KERNEL_TWOPASS,
+            KERNEL_AUTO: KERNEL_AUTO, KERNEL_FUSED: KERNEL_FUSED, KERNEL_TWOPASS: KERNEL_TWOPASS}
+
+# every function the C ABI exports (checked against include/fd23.h by the tests)
+ABI_FUNCTIONS = [
+    "fd23_create", "fd23_destroy", "fd23_strerror", "fd23_version", "fd23_set_model",
+    "fd23_set_material", "fd23_set_cpml", "fd23_set_source", "fd23_set_source_terms",
+    "fd23_wavelet_gaussian", "fd23_wavelet_trapezoid", "fd23_wavelet_ricker", "fd23_moment_psv",
+    "fd23_moment_sh", "fd23_set_receivers", "fd23_receivers_line", "fd23_run", "fd23_sync",
+    "fd23_get_seismograms", "fd23_reset", "fd23_get_stream", "fd23_get_step", "fd23_state_bytes", "fd23_get_state",
+    "fd23_set_state", "fd23_field_norm2", "fd23_build_material", "fd23_build_cpml",
+    "fd23_build_source_terms",
+]
+
+
+class Fd23Error(RuntimeError):
+    def __init__(self, status, where=""):
+        self.status = status
+        msg = lib().fd23_strerror(status).decode() if _lib is not None else str(status)
+        super().__init__("%s: %s (status %d)" % (where, msg, status))
+
+
+class Desc(_C.Structure):
+    _fields_ = [("wave", _C.c_int), ("prec", _C.c_int), ("nx", _C.c_int), ("nz", _C.c_int),
+                ("npml", _C.c_int), ("topabsorb", _C.c_int), ("h", _C.c_double),
+                ("dt", _C.c_double), ("pml_dt", _C.c_double), ("pml_v", _C.c_double),
+                ("pml_r", _C.c_double), ("pml_fc", _C.c_double), ("device", _C.c_int),
+                ("kernel", _C.c_int)]
+
+
+_lib = None
+
+
+def lib():
+    """Load libfd23.so (raises when it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not _os.path.exists(LIB_PATH):
+        raise ImportError("fd23 CUDA library not built: %s is missing (run fd23_gb300/build.py)"
+                          % LIB_PATH)
+    L = _C.CDLL(LIB_PATH)
+    vp, i, d, sz = _C.c_void_p, _C.c_int, _C.c_double, _C.c_size_t
+    sig = {
+        "fd23_create": ([_C.POINTER(Desc), _C.POINTER(vp)], i),
+        "fd23_destroy": ([vp], None),
+        "fd23_strerror": ([i], _C.c_char_p),
+        "fd23_version": ([], i),
+        "fd23_set_model": ([vp, vp, vp, vp, vp], i),
+        "fd23_set_material": ([vp, vp], i),
+        "fd23_set_cpml": ([vp, vp], i),
+        "fd23_set_source": ([vp, i, i, i, vp, vp, i, i], i),
+        "fd23_set_source_terms": ([vp, i, vp, vp, vp, vp, i], i),
+        "fd23_wavelet_gaussian": ([d, i, vp, i], i),
+        "fd23_wavelet_trapezoid": ([d, d, d, d, vp, i], i),
+        "fd23_wavelet_ricker": ([d, d, d, vp, i], i),
+        "fd23_moment_psv": ([d, d, d, d, vp], None),
+        "fd23_moment_sh": ([d, d, d, d, vp], None),
+        "fd23_set_receivers": ([vp, i, vp, vp, i], i),
+        "fd23_receivers_line": ([i, i, i, i, i, vp, vp], i),
+        "fd23_run": ([vp, i, i], i),
+        "fd23_sync": ([vp], i),
+        "fd23_get_seismograms": ([vp, i, vp, sz, _C.POINTER(i)], i),
+        "fd23_reset": ([vp], i),
+        "fd23_get_stream": ([vp, _C.POINTER(vp)], i),
+        "fd23_get_step": ([vp, _C.POINTER(i)], i),
+        "fd23_state_bytes": ([vp], sz),
+        "fd23_get_state": ([vp, vp, sz], i),
+        "fd23_set_state": ([vp, vp, sz, i], i),
+        "fd23_field_norm2": ([vp, _C.POINTER(d)], i),
+        "fd23_build_material": ([i, i, i, d, d, vp, vp, vp, vp, vp], i),
+        "fd23_build_cpml": ([i, i, i, i, d, d, d, d, vp, sz], i),
+        "fd23_build_source_terms": ([i, i, i, i, vp, d, d, vp, i, i, vp, vp, vp, vp, i], i),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = L
+    return L
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(_C.c_void_p)
+
+
+def _f64(a):
+    return _np.ascontiguousarray(a, dtype=_np.float64)
+
+
+def _i32(a):
+    return _np.ascontiguousarray(a, dtype=_np.int32)
+
+
+def _check(rc, where):
+    if rc < 0:
+        raise Fd23Error(rc, where)
+    return rc
+
+
+# ---------------------------------------------------------------------------
+# host-side builders (no GPU needed)
+def build_material(wave, vp, vs, den, h, dt):
+    """FP64 staggered material, dt/h scaled.  Returns (mat[nmat, nz, nx], stab, status)."""
+    w = _WAVES[wave]
+    vs = _f64(vs)
+    nz, nx = vs.shape
+    nmat = 5 if w == PSV else 3
+    out = _np.empty((nmat, nz, nx), dtype=_np.float64)
+    stab = _C.c_double(0.0)
+    rc = lib().fd23_build_material(w, nx, nz, h, dt, _p(_f64(vp)) if vp is not None else None,
+                                   _p(vs), _p(_f64(den)), _p(out),
+                                   _C.cast(_C.pointer(stab), _C.c_void_p))
+    return out, stab.value, rc
+
+
+def build_cpml(wave, nx, nz, npml, pml_dt, pml_r, pml_v, pml_fc):
+    w = _WAVES[wave]
+    n = 3 * ((8 if w == PSV else 4) // 2) * (nx + nz)
+    out = _np.empty(n, dtype=_np.float64)
+    k = _check(lib().fd23_build_cpml(w, nx, nz, npml, pml_dt, pml_r, pml_v, pml_fc, _p(out), n),
+               "fd23_build_cpml")
+    return out[:k].reshape(3, -1)
+
+
+def wavelet_gaussian(dt, alpha):
+    cap = 2 * abs(int(alpha * 3.0)) + 2
+    out = _np.zeros(cap)
+    n = _check(lib().fd23_wavelet_gaussian(dt, int(alpha), _p(out), cap), "gaussian")
+    return out[:n].copy()
+
+
+def wavelet_trapezoid(dt, t1, t2, t3):
+    cap = int(t1 / dt) + int(t2 / dt) + int(t3 / dt) + 4
+    out = _np.zeros(cap)
+    n = _check(lib().fd23_wavelet_trapezoid(dt, t1, t2, t3, _p(out), cap), "trapezoid")
+    return out[:n].copy()
+
+
+def wavelet_ricker(dt, f0, t0=0.0):
+    cap = int(round(2.0 * (t0 if t0 > 0 else 1.2 / f0) / dt)) + 4
+    out = _np.zeros(cap)
+    n = _check(lib().fd23_wavelet_ricker(dt, f0, t0, _p(out), cap), "ricker")
+    return out[:n].copy()
+
+
+def moment_psv(strike, dip, rake, azimuth):
+    m = _np.zeros(3)
+    lib().fd23_moment_psv(strike, dip, rake, azimuth, _p(m))
+    return m
+
+
+def moment_sh(strike, dip, rake, azimuth):
+    m = _np.zeros(2)
+    lib().fd23_moment_sh(strike, dip, rake, azimuth, _p(m))
+    return m
+
+
+def build_source_terms(wave, kind, xs, zs, moment, h, dt, src, nt):
+    src = _f64(src)
+    f, x, z = (_np.zeros(16, dtype=_np.int32) for _ in range(3))
+    amp = _np.zeros((16, nt))
+    m = _f64(moment) if moment is not None else _np.zeros(3)
+    n = _check(lib().fd23_build_source_terms(_WAVES[wave], kind, xs, zs, _p(m), h, dt, _p(src),
+                                             len(src), nt, _p(f), _p(x), _p(z), _p(amp), 16),
+               "fd23_build_source_terms")
+    return f[:n].copy(), x[:n].copy(), z[:n].copy(), _np.ascontiguousarray(amp[:n])
+
+
+def receivers_line(nsta, ix0, iz0, idx, idz):
+    """Reference line receivers: station i at (ix0+i*idx, iz0+i*idz) recorded
+    as the pair (x, z), (x-1, z) (PD/record/cu_record.cu:12-28)."""
+    rx = _np.zeros(2 * nsta, dtype=_np.int32)
+    rz = _np.zeros(2 * nsta, dtype=_np.int32)
+    _check(lib().fd23_receivers_line(nsta, ix0, iz0, idx, idz, _p(rx), _p(rz)), "receivers_line")
+    return rx, rz
+
+
+def receivers_file(path):
+    """Station file of whitespace-separated (z x) pairs, each recorded as the
+    pair (x, z), (x-1, z) (PD/record/cu_record.cu:30-76)."""
+    vals = [int(t) for t in open(path).read().split()]
+    rx, rz = [], []
+    for j in range(0, len(vals) - 1, 2):
+        z, x = vals[j], vals[j + 1]
+        rx += [x, x - 1]
+        rz += [z, z]
+    return _np.array(rx, dtype=_np.int32), _np.array(rz, dtype=_np.int32)
+
+
+def read_raster_model(prefix, nx, nz, wave="psv"):
+    """Float32 raster model files <prefix>.vp, .vs, .den (PD/model/util.cpp:12-28)."""
+    def rd(ext):
+        return _np.fromfile("%s.%s" % (prefix, ext), dtype=_np.float32,
+                            count=nx * nz).astype(_np.float64).reshape(nz, nx)
+    vp = rd("vp") if _WAVES[wave] == PSV else None
+    return vp, rd("vs"), rd("den")
+
+
+# ---------------------------------------------------------------------------
+class Solver:
+    """One shot on one GPU (owns its device buffers)."""
+
+    def __init__(self, wave, nx, nz, npml, h, dt, prec="f32", topabsorb=0, pml_dt=None,
+                 pml_v=None, pml_r=1e-11, pml_fc=None, device=0, kernel="auto"):
+        self.wave = _WAVES[wave]
+        self.prec = _PRECS[prec]
+        self.nx, self.nz, self.npml = nx, nz, npml
+        d = Desc(self.wave, self.prec, nx, nz, npml, int(topabsorb), h, dt,
+                 dt if pml_dt is None else pml_dt, 30.0 if pml_v is None else pml_v, pml_r,
+                 2.0 if pml_fc is None else pml_fc, device, _KERNELS[kernel])
+        self._h = _C.c_void_p()
+        _check(lib().fd23_create(_C.byref(d), _C.byref(self._h)), "fd23_create")
+        self.dtype = _np.float64 if self.prec == F64 else _np.float32
+        self.nfields = 5 if self.wave == PSV else 3
+        self._nrec = {}
+
+    def close(self):
+        if self._h:
+            lib().fd23_destroy(self._h)
+            self._h = _C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- inputs --
+    def set_model(self, vp, vs, den):
+        stab = _C.c_double(0.0)
+        _check(lib().fd23_set_model(self._h, _p(_f64(vp)) if vp is not None else None,
+                                    _p(_f64(vs)), _p(_f64(den)),
+                                    _C.cast(_C.pointer(stab), _C.c_void_p)), "fd23_set_model")
+        return stab.value
+
+    def set_material(self, mat):
+        _check(lib().fd23_set_material(self._h, _p(_f64(mat))), "fd23_set_material")
+
+    def set_cpml(self, bck):
+        _check(lib().fd23_set_cpml(self._h, _p(_f64(bck))), "fd23_set_cpml")
+
+    def set_source(self, kind, xs, zs, moment, src, nt_max):
+        src = _f64(src)
+        _check(lib().fd23_set_source(self._h, kind, xs, zs,
+                                     _p(_f64(moment)) if moment is not None else None, _p(src),
+                                     len(src), nt_max), "fd23_set_source")
+
+    def set_source_terms(self, field, ix, iz, amp):
+        amp = _f64(amp)
+        n = len(field)
+        _check(lib().fd23_set_source_terms(self._h, n, _p(_i32(field)), _p(_i32(ix)),
+                                           _p(_i32(iz)), _p(amp), amp.shape[1] if n else 0),
+               "fd23_set_source_terms")
+
+    def set_receivers(self, field, rx, rz):
+        rx, rz = _i32(rx), _i32(rz)
+        _check(lib().fd23_set_receivers(self._h, field, _p(rx), _p(rz), len(rx)),
+               "fd23_set_receivers")
+        self._nrec[field] = len(rx)
+
+    # -- time stepping --
+    def run(self, nsteps, itrecord=1):
+        _check(lib().fd23_run(self._h, nsteps, itrecord), "fd23_run")
+
+    def sync(self):
+        _check(lib().fd23_sync(self._h), "fd23_sync")
+
+    @property
+    def stream(self):
+        """cudaStream_t (as an int) all launches of this solver use."""
+        p = _C.c_void_p()
+        _check(lib().fd23_get_stream(self._h, _C.byref(p)), "fd23_get_stream")
+        return p.value or 0
+
+    @property
+    def step(self):
+        it = _C.c_int(0)
+        _check(lib().fd23_get_step(self._h, _C.byref(it)), "fd23_get_step")
+        return it.value
+
+    def seismograms(self, field):
+        n = self._nrec.get(field, 0)
+        nr = _C.c_int(0)
+        _check(lib().fd23_get_seismograms(self._h, field, None, 0, _C.byref(nr)), "seismograms")
+        out = _np.zeros((nr.value, n), dtype=self.dtype)
+        _check(lib().fd23_get_seismograms(self._h, field, _p(out), out.nbytes, _C.byref(nr)),
+               "seismograms")
+        return out
+
+    def reset(self):
+        _check(lib().fd23_reset(self._h), "fd23_reset")
+
+    def state_size(self):
+        return lib().fd23_state_bytes(self._h) // _np.dtype(self.dtype).itemsize
+
+    def get_state(self):
+        out = _np.zeros(self.state_size(), dtype=self.dtype)
+        _check(lib().fd23_get_state(self._h, _p(out), out.nbytes), "fd23_get_state")
+        return out
+
+    def set_state(self, state, it0):
+        st = _np.ascontiguousarray(state, dtype=self.dtype)
+        _check(lib().fd23_set_state(self._h, _p(st), st.nbytes, it0), "fd23_set_state")
+
+    def norm2(self):
+        v = _C.c_double(0.0)
+        _check(lib().fd23_field_norm2(self._h, _C.byref(v)), "fd23_field_norm2")
+        return v.value

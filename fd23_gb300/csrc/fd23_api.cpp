@@ -1,0 +1,832 @@
+// C ABI of the fd23 engine (include/fd23.h): solver lifecycle, uploads into
+// the padded HBM layout, the time loop and state transfer.  No call exits
+// the process; every failure returns a status.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "fd23_internal.h"
+#include "fd23_kernels.h"
+
+using namespace fd23;
+
+namespace fd23 {
+Layout make_layout(int nx, int nz, int cover_x, int cover_z)
+{
+    Layout L;
+    L.nx = nx;
+    L.nz = nz;
+    const int cols = kXPad + std::max(cover_x, nx) + 8;
+    L.pitch = (cols + 31) / 32 * 32;
+    L.rows = kZPad + std::max(cover_z, nz) + 8;
+    L.origin = (long long)kZPad * L.pitch + kXPad;
+    return L;
+}
+}  // namespace fd23
+
+namespace {
+
+// float -> bfloat16, round to nearest even (NaN kept quiet)
+uint16_t f32_to_bf16(float f)
+{
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    if ((u & 0x7fffffffu) > 0x7f800000u) return (uint16_t)((u >> 16) | 0x40);
+    u += 0x7fffu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+float bf16_to_f32(uint16_t h)
+{
+    uint32_t u = (uint32_t)h << 16;
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+uint16_t f32_to_f16(float f)
+{
+    _Float16 h = (_Float16)f;
+    uint16_t u;
+    std::memcpy(&u, &h, 2);
+    return u;
+}
+float f16_to_f32(uint16_t u)
+{
+    _Float16 h;
+    std::memcpy(&h, &u, 2);
+    return (float)h;
+}
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace
+
+struct fd23_solver {
+    fd23_desc d{};
+    int nfld = 0, nmat = 0, npsi = 0;
+    size_t es = 4, cs = 4;  // storage / compute element size
+    Layout L;
+    cudaStream_t stream = nullptr;
+    int fused = 1;
+    void *fld[2][5] = {};
+    void *mat[5] = {};
+    void *psi[2][8] = {};
+    size_t psi_elems[8] = {};
+    void *cpml = nullptr;
+    int cpml_blk = 0;
+    bool have_material = false;
+    int *err_flag = nullptr;
+    double *norm_buf = nullptr;
+    // source
+    int nterms = 0;
+    int4 *d_terms = nullptr;
+    void *d_tamp = nullptr;
+    int tamp_nt = 0;
+    // receivers
+    int nrec[2] = {0, 0};
+    long long *d_rec[2] = {nullptr, nullptr};
+    void *d_seis[2] = {nullptr, nullptr};
+    int rec_cap = 0;      // record rows allocated
+    int nrec_steps = 0;   // record rows filled (or pending)
+    int pending_rec = -1; // record row to gather from the current buffer set
+    // time
+    int it = 0;
+    int par = 0;
+    // fused work list
+    WorkItem *d_items = nullptr;
+    int *d_item_off = nullptr;
+    int nblocks = 0;
+};
+
+namespace {
+
+#define CK(call)                                      \
+    do {                                              \
+        if ((call) != cudaSuccess) {                  \
+            cudaGetLastError();                       \
+            return FD23_ERR_CUDA;                     \
+        }                                             \
+    } while (0)
+
+int dev_alloc(void **p, size_t bytes)
+{
+    if (cudaMalloc(p, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return FD23_ERR_NOMEM;
+    }
+    return FD23_OK;
+}
+
+size_t storage_size(int prec) { return prec == FD23_F64 ? 8 : (prec == FD23_F32 ? 4 : 2); }
+size_t compute_size(int prec) { return prec == FD23_F64 ? 8 : 4; }
+
+// convert a double array to the storage type into dst (bytes = n*es)
+void to_storage(int prec, const double *src, size_t n, unsigned char *dst)
+{
+    switch (prec) {
+        case FD23_F64: std::memcpy(dst, src, n * 8); break;
+        case FD23_F32:
+            for (size_t i = 0; i < n; ++i) reinterpret_cast<float *>(dst)[i] = (float)src[i];
+            break;
+        case FD23_BF16:
+            for (size_t i = 0; i < n; ++i) reinterpret_cast<uint16_t *>(dst)[i] = f32_to_bf16((float)src[i]);
+            break;
+        default:
+            for (size_t i = 0; i < n; ++i) reinterpret_cast<uint16_t *>(dst)[i] = f32_to_f16((float)src[i]);
+    }
+}
+void to_compute(int prec, const double *src, size_t n, unsigned char *dst)
+{
+    if (prec == FD23_F64) std::memcpy(dst, src, n * 8);
+    else
+        for (size_t i = 0; i < n; ++i) reinterpret_cast<float *>(dst)[i] = (float)src[i];
+}
+// storage element -> compute element
+void storage_to_compute(int prec, const unsigned char *src, size_t n, unsigned char *dst)
+{
+    switch (prec) {
+        case FD23_F64: std::memcpy(dst, src, n * 8); break;
+        case FD23_F32: std::memcpy(dst, src, n * 4); break;
+        case FD23_BF16:
+            for (size_t i = 0; i < n; ++i)
+                reinterpret_cast<float *>(dst)[i] = bf16_to_f32(reinterpret_cast<const uint16_t *>(src)[i]);
+            break;
+        default:
+            for (size_t i = 0; i < n; ++i)
+                reinterpret_cast<float *>(dst)[i] = f16_to_f32(reinterpret_cast<const uint16_t *>(src)[i]);
+    }
+}
+void compute_to_storage(int prec, const unsigned char *src, size_t n, unsigned char *dst)
+{
+    switch (prec) {
+        case FD23_F64: std::memcpy(dst, src, n * 8); break;
+        case FD23_F32: std::memcpy(dst, src, n * 4); break;
+        case FD23_BF16:
+            for (size_t i = 0; i < n; ++i)
+                reinterpret_cast<uint16_t *>(dst)[i] = f32_to_bf16(reinterpret_cast<const float *>(src)[i]);
+            break;
+        default:
+            for (size_t i = 0; i < n; ++i)
+                reinterpret_cast<uint16_t *>(dst)[i] = f32_to_f16(reinterpret_cast<const float *>(src)[i]);
+    }
+}
+
+// upload an nx*nz array (already in element format, es bytes each) into the padded layout
+int upload_grid(fd23_solver *s, void *dptr, const unsigned char *host, size_t es)
+{
+    const Layout &L = s->L;
+    CK(cudaMemcpy2DAsync((unsigned char *)dptr + (size_t)L.origin * es, (size_t)L.pitch * es, host,
+                         (size_t)L.nx * es, (size_t)L.nx * es, (size_t)L.nz, cudaMemcpyHostToDevice,
+                         s->stream));
+    return FD23_OK;
+}
+int download_grid(fd23_solver *s, const void *dptr, unsigned char *host, size_t es)
+{
+    const Layout &L = s->L;
+    CK(cudaMemcpy2DAsync(host, (size_t)L.nx * es, (const unsigned char *)dptr + (size_t)L.origin * es,
+                         (size_t)L.pitch * es, (size_t)L.nx * es, (size_t)L.nz, cudaMemcpyDeviceToHost,
+                         s->stream));
+    return FD23_OK;
+}
+
+template <class S, class C>
+Shot<S, C> make_shot(const fd23_solver *s)
+{
+    Shot<S, C> sh{};
+    for (int b = 0; b < 2; ++b)
+        for (int f = 0; f < 5; ++f) sh.f[b][f] = (S *)s->fld[b][f];
+    for (int m = 0; m < 5; ++m) sh.mat[m] = (const S *)s->mat[m];
+    for (int b = 0; b < 2; ++b)
+        for (int p = 0; p < 8; ++p) sh.psi[b][p] = (C *)s->psi[b][p];
+    sh.cpml = (const C *)s->cpml;
+    sh.nx = s->d.nx;
+    sh.nz = s->d.nz;
+    sh.npml = s->d.npml;
+    sh.topabsorb = s->d.topabsorb;
+    sh.pitch = s->L.pitch;
+    sh.origin = s->L.origin;
+    sh.cpml_blk = s->cpml_blk;
+    sh.nterms = s->nterms;
+    sh.terms = s->d_terms;
+    sh.tamp = (const C *)s->d_tamp;
+    sh.tamp_nt = s->nterms > 0 ? s->tamp_nt : 0;
+    for (int c = 0; c < 2; ++c) {
+        sh.nrec[c] = s->nrec[c];
+        sh.rec[c] = s->d_rec[c];
+        sh.seis[c] = (C *)s->d_seis[c];
+    }
+    return sh;
+}
+
+template <class S, class C>
+int step_impl(fd23_solver *s, int rec_now)
+{
+    Shot<S, C> sh = make_shot<S, C>(s);
+    if (s->fused) {
+        const int rc = launch_step_fused<S, C>(sh, s->d.wave, s->d_items, s->d_item_off, s->nblocks,
+                                               s->par, s->it, s->pending_rec, s->err_flag, s->stream);
+        if (rc) return rc;
+        s->pending_rec = -1;
+        s->par = 1 - s->par;
+        if (rec_now) s->pending_rec = s->nrec_steps++;
+    } else {
+        const int rc = launch_step_twopass<S, C>(sh, s->d.wave, s->it, s->stream);
+        if (rc) return rc;
+        if (rec_now) {
+            const int r2 = launch_record<S, C>(sh, 0, s->nrec_steps++, s->stream);
+            if (r2) return r2;
+        }
+    }
+    s->it++;
+    return FD23_OK;
+}
+
+template <class S, class C>
+int flush_records(fd23_solver *s)
+{
+    if (s->pending_rec < 0) return FD23_OK;
+    Shot<S, C> sh = make_shot<S, C>(s);
+    const int rc = launch_record<S, C>(sh, s->par, s->pending_rec, s->stream);
+    s->pending_rec = -1;
+    return rc;
+}
+
+int dispatch_step(fd23_solver *s, int rec_now)
+{
+    switch (s->d.prec) {
+        case FD23_F64: return step_impl<double, double>(s, rec_now);
+        case FD23_BF16: return step_impl<__nv_bfloat16, float>(s, rec_now);
+        case FD23_F16: return step_impl<__half, float>(s, rec_now);
+        default: return step_impl<float, float>(s, rec_now);
+    }
+}
+int dispatch_flush(fd23_solver *s)
+{
+    switch (s->d.prec) {
+        case FD23_F64: return flush_records<double, double>(s);
+        case FD23_BF16: return flush_records<__nv_bfloat16, float>(s);
+        case FD23_F16: return flush_records<__half, float>(s);
+        default: return flush_records<float, float>(s);
+    }
+}
+
+// Work list: strips of TX columns, split into row ranges of 4-row blocks so
+// that every CTA gets the same number of blocks (a range may span two
+// strips; each strip piece is one item).
+int build_worklist(fd23_solver *s)
+{
+    const FusedGeom g = fused_geom(s->d.wave, s->d.prec);
+    const int nx = s->d.nx, nz = s->d.nz;
+    const int ntx = (nx + g.tile_x - 1) / g.tile_x;
+    const int nzb = (nz + 3) / 4;
+    const long long total = (long long)ntx * nzb;
+    int sms = 0, per_sm = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->d.device));
+    const size_t smem = fused_smem_bytes(s->d.wave, s->d.prec);
+    int smem_sm = 0;
+    CK(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, s->d.device));
+    per_sm = std::max(1, std::min(8, (int)(smem_sm / (smem + 1024))));
+    long long nb = (long long)sms * per_sm;
+    nb = std::min(nb, total);
+    nb = std::max(nb, (long long)(ntx + 5) / 6);  // at most ~7 items per CTA
+    std::vector<WorkItem> items;
+    std::vector<int> off;
+    off.push_back(0);
+    for (long long c = 0; c < nb; ++c) {
+        long long b0 = c * total / nb, b1 = (c + 1) * total / nb;
+        while (b0 < b1) {
+            const int strip = (int)(b0 / nzb);
+            const long long send = (long long)(strip + 1) * nzb;
+            const long long e = std::min(b1, send);
+            items.push_back(WorkItem{0, strip * g.tile_x, (int)(b0 - (long long)strip * nzb) * 4,
+                                     (int)(e - (long long)strip * nzb) * 4});
+            b0 = e;
+        }
+        off.push_back((int)items.size());
+    }
+    for (size_t c = 0; c + 1 < off.size(); ++c)
+        if (off[c + 1] - off[c] > 8) return FD23_ERR_ARG;
+    if (s->d_items) cudaFree(s->d_items);
+    if (s->d_item_off) cudaFree(s->d_item_off);
+    s->d_items = nullptr;
+    s->d_item_off = nullptr;
+    int rc = dev_alloc((void **)&s->d_items, items.size() * sizeof(WorkItem));
+    if (rc) return rc;
+    rc = dev_alloc((void **)&s->d_item_off, off.size() * sizeof(int));
+    if (rc) return rc;
+    CK(cudaMemcpy(s->d_items, items.data(), items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s->d_item_off, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice));
+    s->nblocks = (int)nb;
+    return FD23_OK;
+}
+
+int upload_cpml(fd23_solver *s, const std::vector<double> &bck)
+{
+    std::vector<unsigned char> tmp(bck.size() * s->cs);
+    to_compute(s->d.prec, bck.data(), bck.size(), tmp.data());
+    CK(cudaMemcpyAsync(s->cpml, tmp.data(), tmp.size(), cudaMemcpyHostToDevice, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return FD23_OK;
+}
+
+int zero_state(fd23_solver *s)
+{
+    const size_t gbytes = s->L.elems() * s->es;
+    for (int b = 0; b < 2; ++b) {
+        for (int f = 0; f < s->nfld; ++f) CK(cudaMemsetAsync(s->fld[b][f], 0, gbytes, s->stream));
+        for (int p = 0; p < s->npsi; ++p)
+            CK(cudaMemsetAsync(s->psi[b][p], 0, s->psi_elems[p] * s->cs, s->stream));
+    }
+    CK(cudaMemsetAsync(s->err_flag, 0, sizeof(int), s->stream));
+    s->it = 0;
+    s->par = 0;
+    s->nrec_steps = 0;
+    s->pending_rec = -1;
+    return FD23_OK;
+}
+
+void free_all(fd23_solver *s)
+{
+    for (int b = 0; b < 2; ++b) {
+        for (int f = 0; f < 5; ++f) cudaFree(s->fld[b][f]);
+        for (int p = 0; p < 8; ++p) cudaFree(s->psi[b][p]);
+    }
+    for (int m = 0; m < 5; ++m) cudaFree(s->mat[m]);
+    cudaFree(s->cpml);
+    cudaFree(s->err_flag);
+    cudaFree(s->norm_buf);
+    cudaFree(s->d_terms);
+    cudaFree(s->d_tamp);
+    for (int c = 0; c < 2; ++c) {
+        cudaFree(s->d_rec[c]);
+        cudaFree(s->d_seis[c]);
+    }
+    cudaFree(s->d_items);
+    cudaFree(s->d_item_off);
+    if (s->stream) cudaStreamDestroy(s->stream);
+}
+
+int ensure_record_capacity(fd23_solver *s, int need)
+{
+    if (need <= s->rec_cap) return FD23_OK;
+    int cap = std::max(need, s->rec_cap * 2);
+    for (int c = 0; c < 2; ++c) {
+        if (s->nrec[c] <= 0) continue;
+        void *np = nullptr;
+        int rc = dev_alloc(&np, (size_t)cap * s->nrec[c] * s->cs);
+        if (rc) return rc;
+        if (s->d_seis[c] && s->nrec_steps > 0)
+            CK(cudaMemcpyAsync(np, s->d_seis[c], (size_t)s->nrec_steps * s->nrec[c] * s->cs,
+                               cudaMemcpyDeviceToDevice, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        cudaFree(s->d_seis[c]);
+        s->d_seis[c] = np;
+    }
+    s->rec_cap = cap;
+    return FD23_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fd23_version(void) { return 1; }
+
+const char *fd23_strerror(int st)
+{
+    switch (st) {
+        case FD23_OK: return "ok";
+        case FD23_ERR_ARG: return "invalid argument";
+        case FD23_ERR_CUDA: return "CUDA runtime error";
+        case FD23_ERR_UNSTABLE: return "model fails the CFL stability check (stab > 1)";
+        case FD23_ERR_ORDER: return "call made before what it depends on";
+        case FD23_ERR_NOMEM: return "device allocation failed";
+        case FD23_ERR_NONFINITE: return "wavefield holds NaN or Inf";
+        case FD23_ERR_TIMEOUT: return "a bounded device-side wait gave up";
+        case FD23_ERR_UNSUPPORTED: return "unsupported configuration";
+        default: return "unknown status";
+    }
+}
+
+int fd23_create(const fd23_desc *desc, fd23_solver **out)
+{
+    if (!desc || !out) return FD23_ERR_ARG;
+    *out = nullptr;
+    const fd23_desc &d = *desc;
+    if (d.wave != FD23_PSV && d.wave != FD23_SH) return FD23_ERR_ARG;
+    if (d.prec < FD23_F32 || d.prec > FD23_F16) return FD23_ERR_ARG;
+    if (d.nx < 2 || d.nz < 2 || d.npml < 0 || 2 * d.npml > d.nx || 2 * d.npml > d.nz) return FD23_ERR_ARG;
+    if ((long long)d.nx * d.nz > (1LL << 31)) return FD23_ERR_ARG;
+    if (!(d.h > 0) || !(d.dt > 0)) return FD23_ERR_ARG;
+    if (d.kernel < FD23_KERNEL_AUTO || d.kernel > FD23_KERNEL_TWOPASS) return FD23_ERR_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || d.device < 0 || d.device >= ndev) {
+        cudaGetLastError();
+        return FD23_ERR_CUDA;
+    }
+    CK(cudaSetDevice(d.device));
+    fd23_solver *s = new (std::nothrow) fd23_solver();
+    if (!s) return FD23_ERR_NOMEM;
+    s->d = d;
+    s->nfld = d.wave == FD23_PSV ? 5 : 3;
+    s->nmat = d.wave == FD23_PSV ? 5 : 3;
+    s->npsi = d.wave == FD23_PSV ? 8 : 4;
+    s->es = storage_size(d.prec);
+    s->cs = compute_size(d.prec);
+    s->fused = d.kernel != FD23_KERNEL_TWOPASS;
+    const FusedGeom g = fused_geom(d.wave, d.prec);
+    const int ntx = (d.nx + g.tile_x - 1) / g.tile_x;
+    s->L = make_layout(d.nx, d.nz, ntx * g.tile_x, (d.nz + 3) / 4 * 4);
+    int rc = FD23_OK;
+    auto fail = [&](int r) {
+        free_all(s);
+        delete s;
+        return r;
+    };
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(FD23_ERR_CUDA);
+    const size_t gbytes = s->L.elems() * s->es;
+    for (int b = 0; b < 2; ++b)
+        for (int f = 0; f < s->nfld; ++f)
+            if ((rc = dev_alloc(&s->fld[b][f], gbytes))) return fail(rc);
+    for (int m = 0; m < s->nmat; ++m) {
+        if ((rc = dev_alloc(&s->mat[m], gbytes))) return fail(rc);
+        if (cudaMemset(s->mat[m], 0, gbytes) != cudaSuccess) return fail(FD23_ERR_CUDA);
+    }
+    const size_t px = 2ull * d.npml * d.nz, pz = 2ull * d.npml * d.nx;
+    for (int p = 0; p < s->npsi; ++p) s->psi_elems[p] = (p < s->npsi / 2) ? px : pz;
+    for (int b = 0; b < 2; ++b)
+        for (int p = 0; p < s->npsi; ++p)
+            if ((rc = dev_alloc(&s->psi[b][p], std::max<size_t>(1, s->psi_elems[p]) * s->cs))) return fail(rc);
+    std::vector<double> bck;
+    build_cpml(d.wave, d.nx, d.nz, d.npml, d.pml_dt, d.pml_r, d.pml_v, d.pml_fc, bck);
+    s->cpml_blk = (int)(bck.size() / 3);
+    if ((rc = dev_alloc(&s->cpml, bck.size() * s->cs))) return fail(rc);
+    if ((rc = upload_cpml(s, bck))) return fail(rc);
+    if ((rc = dev_alloc((void **)&s->err_flag, sizeof(int)))) return fail(rc);
+    if ((rc = dev_alloc((void **)&s->norm_buf, 2 * sizeof(double)))) return fail(rc);
+    if (s->fused) {
+        if ((rc = fused_prepare(d.wave, d.prec))) return fail(rc);
+        if ((rc = build_worklist(s))) return fail(rc);
+    }
+    if ((rc = zero_state(s))) return fail(rc);
+    if (cudaStreamSynchronize(s->stream) != cudaSuccess) return fail(FD23_ERR_CUDA);
+    *out = s;
+    return FD23_OK;
+}
+
+void fd23_destroy(fd23_solver *s)
+{
+    if (!s) return;
+    cudaSetDevice(s->d.device);
+    cudaStreamSynchronize(s->stream);
+    free_all(s);
+    delete s;
+}
+
+int fd23_set_material(fd23_solver *s, const double *matv)
+{
+    if (!s || !matv) return FD23_ERR_ARG;
+    CK(cudaSetDevice(s->d.device));
+    const size_t n = (size_t)s->d.nx * s->d.nz;
+    std::vector<unsigned char> tmp(n * s->es);
+    for (int m = 0; m < s->nmat; ++m) {
+        to_storage(s->d.prec, matv + m * n, n, tmp.data());
+        int rc = upload_grid(s, s->mat[m], tmp.data(), s->es);
+        if (rc) return rc;
+        CK(cudaStreamSynchronize(s->stream));
+    }
+    s->have_material = true;
+    return FD23_OK;
+}
+
+int fd23_set_model(fd23_solver *s, const double *vp, const double *vs, const double *den, double *stab)
+{
+    if (!s || !vs || !den || (s->d.wave == FD23_PSV && !vp)) return FD23_ERR_ARG;
+    const size_t n = (size_t)s->d.nx * s->d.nz;
+    std::vector<double> m((size_t)s->nmat * n);
+    double st = 0.0;
+    int rc = s->d.wave == FD23_PSV
+                 ? build_psv_material(s->d.nx, s->d.nz, s->d.h, s->d.dt, vp, vs, den, m.data(), &st)
+                 : build_sh_material(s->d.nx, s->d.nz, s->d.h, s->d.dt, vs, den, m.data(), &st);
+    if (stab) *stab = st;
+    if (rc) return rc;
+    return fd23_set_material(s, m.data());
+}
+
+int fd23_set_cpml(fd23_solver *s, const double *bckp)
+{
+    if (!s || !bckp) return FD23_ERR_ARG;
+    CK(cudaSetDevice(s->d.device));
+    std::vector<double> bck(bckp, bckp + 3 * (size_t)s->cpml_blk);
+    return upload_cpml(s, bck);
+}
+
+int fd23_set_source_terms(fd23_solver *s, int nterms, const int *field, const int *ix, const int *iz,
+                          const double *amp, int nt_amp)
+{
+    if (!s || nterms < 0 || nterms > 16 || (nterms > 0 && (!field || !ix || !iz || !amp || nt_amp <= 0)))
+        return FD23_ERR_ARG;
+    CK(cudaSetDevice(s->d.device));
+    std::vector<int4> t((size_t)std::max(nterms, 1));
+    for (int k = 0; k < nterms; ++k) {
+        if (field[k] < 0 || field[k] >= s->nfld) return FD23_ERR_ARG;
+        if (s->d.wave == FD23_PSV && field[k] < FD23_TXX) return FD23_ERR_ARG;  // stress terms only
+        if (ix[k] < 0 || ix[k] >= s->d.nx || iz[k] < 0 || iz[k] >= s->d.nz) return FD23_ERR_ARG;
+        t[k] = make_int4(field[k], ix[k], iz[k], 0);
+    }
+    cudaFree(s->d_terms);
+    cudaFree(s->d_tamp);
+    s->d_terms = nullptr;
+    s->d_tamp = nullptr;
+    s->nterms = 0;
+    if (nterms == 0) return FD23_OK;
+    int rc = dev_alloc((void **)&s->d_terms, t.size() * sizeof(int4));
+    if (rc) return rc;
+    const size_t na = (size_t)nterms * nt_amp;
+    std::vector<unsigned char> tmp(na * s->cs);
+    to_compute(s->d.prec, amp, na, tmp.data());
+    if ((rc = dev_alloc(&s->d_tamp, tmp.size()))) return rc;
+    CK(cudaMemcpy(s->d_terms, t.data(), nterms * sizeof(int4), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s->d_tamp, tmp.data(), tmp.size(), cudaMemcpyHostToDevice));
+    s->nterms = nterms;
+    s->tamp_nt = nt_amp;
+    return FD23_OK;
+}
+
+int fd23_set_source(fd23_solver *s, int kind, int xs, int zs, const double *moment, const double *src,
+                    int lsrc, int nt_max)
+{
+    if (!s || !src || lsrc <= 0 || nt_max <= 0) return FD23_ERR_ARG;
+    if (kind != FD23_SRC_EXPLOSION && kind != FD23_SRC_FORCE && kind != FD23_SRC_MOMENT &&
+        kind != FD23_SRC_MOMENT_P)
+        return FD23_ERR_ARG;
+    if (kind == FD23_SRC_FORCE && s->d.wave != FD23_SH) return FD23_ERR_ARG;
+    if (kind == FD23_SRC_EXPLOSION && s->d.wave != FD23_PSV) return FD23_ERR_ARG;
+    if (kind != FD23_SRC_EXPLOSION && !moment) return FD23_ERR_ARG;
+    std::vector<SourceTerm> terms;
+    std::vector<double> amp;
+    build_source_terms(s->d.wave, kind, xs, zs, moment, s->d.h, s->d.dt, src, lsrc, nt_max, terms, amp);
+    std::vector<int> f, x, z;
+    for (auto &t : terms) {
+        f.push_back(t.field);
+        x.push_back(t.ix);
+        z.push_back(t.iz);
+    }
+    return fd23_set_source_terms(s, (int)terms.size(), f.data(), x.data(), z.data(), amp.data(), nt_max);
+}
+
+int fd23_set_receivers(fd23_solver *s, int field, const int *rx, const int *rz, int n)
+{
+    if (!s || n < 0 || (n > 0 && (!rx || !rz))) return FD23_ERR_ARG;
+    const int ncomp = s->d.wave == FD23_PSV ? 2 : 1;
+    if (field < 0 || field >= ncomp) return FD23_ERR_ARG;
+    if (s->nrec_steps > 0) return FD23_ERR_ORDER;  // change receivers only before recording
+    CK(cudaSetDevice(s->d.device));
+    std::vector<long long> off((size_t)std::max(n, 1));
+    for (int i = 0; i < n; ++i) {
+        if (rx[i] < 0 || rx[i] >= s->d.nx || rz[i] < 0 || rz[i] >= s->d.nz) return FD23_ERR_ARG;
+        off[i] = s->L.origin + (long long)rz[i] * s->L.pitch + rx[i];
+    }
+    cudaFree(s->d_rec[field]);
+    cudaFree(s->d_seis[field]);
+    s->d_rec[field] = nullptr;
+    s->d_seis[field] = nullptr;
+    s->nrec[field] = n;
+    s->rec_cap = 0;
+    for (int c = 0; c < 2; ++c) {  // record buffers are re-sized together
+        cudaFree(s->d_seis[c]);
+        s->d_seis[c] = nullptr;
+    }
+    if (n == 0) return FD23_OK;
+    int rc = dev_alloc((void **)&s->d_rec[field], off.size() * sizeof(long long));
+    if (rc) return rc;
+    CK(cudaMemcpy(s->d_rec[field], off.data(), n * sizeof(long long), cudaMemcpyHostToDevice));
+    return FD23_OK;
+}
+
+int fd23_receivers_line(int nsta, int ix0, int iz0, int idx, int idz, int *rx, int *rz)
+{
+    // PD/record/cu_record.cu:12-28: station i at (ix0+i*idx, iz0+i*idz),
+    // recorded as the pair (x, z), (x-1, z)
+    if (nsta < 0 || !rx || !rz) return FD23_ERR_ARG;
+    for (int i = 0; i < nsta; ++i) {
+        rx[2 * i] = ix0 + idx * i;
+        rz[2 * i] = iz0 + idz * i;
+        rx[2 * i + 1] = rx[2 * i] - 1;
+        rz[2 * i + 1] = rz[2 * i];
+    }
+    return 2 * nsta;
+}
+
+int fd23_run(fd23_solver *s, int nsteps, int itrecord)
+{
+    if (!s || nsteps < 0 || itrecord <= 0) return FD23_ERR_ARG;
+    if (!s->have_material) return FD23_ERR_ORDER;
+    CK(cudaSetDevice(s->d.device));
+    int nrec_new = 0;
+    for (int k = 0; k < nsteps; ++k)
+        if ((s->it + k) % itrecord == 0) ++nrec_new;
+    const bool any_rec = s->nrec[0] > 0 || s->nrec[1] > 0;
+    if (any_rec) {
+        int rc = ensure_record_capacity(s, s->nrec_steps + nrec_new);
+        if (rc) return rc;
+    }
+    for (int k = 0; k < nsteps; ++k) {
+        const int rec_now = any_rec && (s->it % itrecord == 0);
+        int rc = dispatch_step(s, rec_now);
+        if (rc) return rc;
+    }
+    return dispatch_flush(s);
+}
+
+int fd23_sync(fd23_solver *s)
+{
+    if (!s) return FD23_ERR_ARG;
+    CK(cudaSetDevice(s->d.device));
+    CK(cudaStreamSynchronize(s->stream));
+    int flag = 0;
+    CK(cudaMemcpy(&flag, s->err_flag, sizeof(int), cudaMemcpyDeviceToHost));
+    return flag ? FD23_ERR_TIMEOUT : FD23_OK;
+}
+
+int fd23_get_stream(fd23_solver *s, void **stream)
+{
+    if (!s || !stream) return FD23_ERR_ARG;
+    *stream = (void *)s->stream;
+    return FD23_OK;
+}
+
+int fd23_get_step(fd23_solver *s, int *it)
+{
+    if (!s || !it) return FD23_ERR_ARG;
+    *it = s->it;
+    return FD23_OK;
+}
+
+int fd23_get_seismograms(fd23_solver *s, int field, void *out, size_t out_bytes, int *nrec_steps)
+{
+    if (!s) return FD23_ERR_ARG;
+    const int ncomp = s->d.wave == FD23_PSV ? 2 : 1;
+    if (field < 0 || field >= ncomp) return FD23_ERR_ARG;
+    int rc = fd23_sync(s);
+    if (rc) return rc;
+    if (nrec_steps) *nrec_steps = s->nrec_steps;
+    const size_t need = (size_t)s->nrec_steps * s->nrec[field] * s->cs;
+    if (!out) return FD23_OK;
+    if (out_bytes < need) return FD23_ERR_ARG;
+    if (need) CK(cudaMemcpy(out, s->d_seis[field], need, cudaMemcpyDeviceToHost));
+    return FD23_OK;
+}
+
+int fd23_reset(fd23_solver *s)
+{
+    if (!s) return FD23_ERR_ARG;
+    CK(cudaSetDevice(s->d.device));
+    int rc = zero_state(s);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(s->stream));
+    return FD23_OK;
+}
+
+size_t fd23_state_bytes(fd23_solver *s)
+{
+    if (!s) return 0;
+    size_t n = (size_t)s->nfld * s->d.nx * s->d.nz;
+    for (int p = 0; p < s->npsi; ++p) n += s->psi_elems[p];
+    return n * s->cs;
+}
+
+int fd23_get_state(fd23_solver *s, void *buf, size_t bytes)
+{
+    if (!s || !buf || bytes < fd23_state_bytes(s)) return FD23_ERR_ARG;
+    int rc = fd23_sync(s);
+    if (rc) return rc;
+    const size_t n = (size_t)s->d.nx * s->d.nz;
+    unsigned char *o = (unsigned char *)buf;
+    std::vector<unsigned char> tmp(n * s->es);
+    for (int f = 0; f < s->nfld; ++f) {
+        // reference order P-SV: U W Txx Txz Tzz; SH: V Tx Tz (same as storage order)
+        if ((rc = download_grid(s, s->fld[s->par][f], tmp.data(), s->es))) return rc;
+        CK(cudaStreamSynchronize(s->stream));
+        storage_to_compute(s->d.prec, tmp.data(), n, o);
+        o += n * s->cs;
+    }
+    for (int p = 0; p < s->npsi; ++p) {
+        const size_t b = s->psi_elems[p] * s->cs;
+        if (b) CK(cudaMemcpy(o, s->psi[s->par][p], b, cudaMemcpyDeviceToHost));
+        o += b;
+    }
+    return FD23_OK;
+}
+
+int fd23_set_state(fd23_solver *s, const void *buf, size_t bytes, int it0)
+{
+    if (!s || !buf || bytes < fd23_state_bytes(s) || it0 < 0) return FD23_ERR_ARG;
+    CK(cudaSetDevice(s->d.device));
+    int rc = zero_state(s);
+    if (rc) return rc;
+    const size_t n = (size_t)s->d.nx * s->d.nz;
+    const unsigned char *in = (const unsigned char *)buf;
+    std::vector<unsigned char> tmp(n * s->es);
+    for (int f = 0; f < s->nfld; ++f) {
+        compute_to_storage(s->d.prec, in, n, tmp.data());
+        if ((rc = upload_grid(s, s->fld[0][f], tmp.data(), s->es))) return rc;
+        CK(cudaStreamSynchronize(s->stream));
+        in += n * s->cs;
+    }
+    for (int p = 0; p < s->npsi; ++p) {
+        const size_t b = s->psi_elems[p] * s->cs;
+        if (b) CK(cudaMemcpy(s->psi[0][p], in, b, cudaMemcpyHostToDevice));
+        in += b;
+    }
+    s->it = it0;
+    s->par = 0;
+    return FD23_OK;
+}
+
+int fd23_field_norm2(fd23_solver *s, double *norm2)
+{
+    if (!s || !norm2) return FD23_ERR_ARG;
+    CK(cudaSetDevice(s->d.device));
+    int rc = FD23_OK;
+    switch (s->d.prec) {
+        case FD23_F64: rc = launch_norm2<double, double>(make_shot<double, double>(s), s->par, s->nfld, (long long)s->L.elems(), s->norm_buf, s->stream); break;
+        case FD23_BF16: rc = launch_norm2<__nv_bfloat16, float>(make_shot<__nv_bfloat16, float>(s), s->par, s->nfld, (long long)s->L.elems(), s->norm_buf, s->stream); break;
+        case FD23_F16: rc = launch_norm2<__half, float>(make_shot<__half, float>(s), s->par, s->nfld, (long long)s->L.elems(), s->norm_buf, s->stream); break;
+        default: rc = launch_norm2<float, float>(make_shot<float, float>(s), s->par, s->nfld, (long long)s->L.elems(), s->norm_buf, s->stream);
+    }
+    if (rc) return rc;
+    double h[2];
+    CK(cudaMemcpyAsync(h, s->norm_buf, sizeof(h), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    *norm2 = h[0];
+    return h[1] != 0.0 ? FD23_ERR_NONFINITE : FD23_OK;
+}
+
+// ---- host-only helpers (no GPU needed) ----
+int fd23_build_material(int wave, int nx, int nz, double h, double dt, const double *vp, const double *vs,
+                        const double *den, double *out, double *stab)
+{
+    if (nx < 2 || nz < 2 || !vs || !den || !out || (wave == FD23_PSV && !vp)) return FD23_ERR_ARG;
+    return wave == FD23_PSV ? build_psv_material(nx, nz, h, dt, vp, vs, den, out, stab)
+                            : build_sh_material(nx, nz, h, dt, vs, den, out, stab);
+}
+
+int fd23_build_cpml(int wave, int nx, int nz, int npml, double pml_dt, double pml_r, double pml_v,
+                    double pml_fc, double *out, size_t out_elems)
+{
+    std::vector<double> bck;
+    build_cpml(wave, nx, nz, npml, pml_dt, pml_r, pml_v, pml_fc, bck);
+    if (!out || out_elems < bck.size()) return FD23_ERR_ARG;
+    std::copy(bck.begin(), bck.end(), out);
+    return (int)bck.size();
+}
+
+int fd23_build_source_terms(int wave, int kind, int xs, int zs, const double *moment, double h, double dt,
+                            const double *src, int lsrc, int nt, int *field, int *ix, int *iz, double *amp,
+                            int max_terms)
+{
+    if (!src || lsrc <= 0 || nt <= 0 || !field || !ix || !iz || !amp) return FD23_ERR_ARG;
+    std::vector<SourceTerm> terms;
+    std::vector<double> a;
+    build_source_terms(wave, kind, xs, zs, moment, h, dt, src, lsrc, nt, terms, a);
+    if ((int)terms.size() > max_terms) return FD23_ERR_ARG;
+    for (size_t k = 0; k < terms.size(); ++k) {
+        field[k] = terms[k].field;
+        ix[k] = terms[k].ix;
+        iz[k] = terms[k].iz;
+    }
+    std::copy(a.begin(), a.end(), amp);
+    return (int)terms.size();
+}
+
+int fd23_wavelet_gaussian(double dt, int alpha, double *out, int cap) { return wavelet_gaussian(dt, alpha, out, cap); }
+int fd23_wavelet_trapezoid(double dt, double t1, double t2, double t3, double *out, int cap)
+{
+    return wavelet_trapezoid(dt, t1, t2, t3, out, cap);
+}
+int fd23_wavelet_ricker(double dt, double f0, double t0, double *out, int cap)
+{
+    return wavelet_ricker(dt, f0, t0, out, cap);
+}
+void fd23_moment_psv(double strike, double dip, double rake, double azimuth, double out3[3])
+{
+    moment_psv(strike, dip, rake, azimuth, out3);
+}
+void fd23_moment_sh(double strike, double dip, double rake, double azimuth, double out2[2])
+{
+    moment_sh(strike, dip, rake, azimuth, out2);
+}
+
+}  // extern "C"

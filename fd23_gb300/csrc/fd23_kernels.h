@@ -1,0 +1,42 @@
+// Launch entry points of the sweep kernels (host side).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "fd23_internal.h"
+
+namespace fd23 {
+
+// two-pass sweep, fields updated in place in buffer set 0
+template <class S, class C>
+int launch_step_twopass(const Shot<S, C> &s, int wave, int it, cudaStream_t st);
+
+// receiver gather from buffer set `par` into record row `rec_index`
+template <class S, class C>
+int launch_record(const Shot<S, C> &s, int par, int rec_index, cudaStream_t st);
+
+// Fused single-pass sweep.  Geometry of its tiles (used to size the padded
+// layout and to build the work list):
+struct FusedGeom {
+    int tile_x;   // output columns per strip
+    int rows_per_iter;
+};
+FusedGeom fused_geom(int wave, int prec);
+int fused_prepare(int wave, int prec);       // once per device before the first launch
+size_t fused_smem_bytes(int wave, int prec); // dynamic shared memory of one CTA
+
+// One time step of every work item: reads buffer set `par`, writes `1-par`.
+// `rec_index` >= 0 gathers the receivers of the previous step from buffer set
+// `par` into that record row on the way.
+template <class S, class C>
+int launch_step_fused(const Shot<S, C> &s, int wave, const WorkItem *items, const int *item_off,
+                      int nblocks, int par, int it, int rec_index, int *err_flag, cudaStream_t st);
+
+// FP64 sum of squares over the `elems` stored elements of each of the first
+// `nfields` wavefields of buffer set `par` (the zero padding included); the
+// sum goes to dev_out[0], a NaN/Inf flag to dev_out[1].
+template <class S, class C>
+int launch_norm2(const Shot<S, C> &s, int par, int nfields, long long elems, double *dev_out,
+                 cudaStream_t st);
+
+}  // namespace fd23

@@ -1,0 +1,357 @@
+// Two-pass sweep: one thread per cell, a stress launch then a velocity launch
+// per time step, updating the fields in place (as the reference does; the
+// stress pass reads only velocities and writes only stresses, and vice
+// versa, so in-place updates are race free).  This is the simple GPU form of
+// the reference kernels (PD/fd/cu_fd.cu:209-501, SH/fd/cu_fd.cu:77-288) on the
+// padded layout, for any nx, nz.  The fused single-pass sweep
+// (fd23_fused_psv.cu) is the fast path; this one is the cross-check and the
+// fallback for forms the fused sweep does not cover.
+#include "fd23_device.cuh"
+#include "fd23_kernels.h"
+
+namespace fd23 {
+
+namespace {
+
+// backward (D-minus) and forward (D-plus) differences along a stride
+template <class S, class C>
+__device__ __forceinline__ C dminus(const S *p, long long s, C c0, C c1, C c2, C c3)
+{
+    auto v = [&](int j) { return to_c<C>(p[j * s]); };
+    return comb<C>(c0, c1, c2, c3, v(0) - v(-1), v(1) - v(-2), v(2) - v(-3), v(3) - v(-4));
+}
+template <class S, class C>
+__device__ __forceinline__ C dplus(const S *p, long long s, C c0, C c1, C c2, C c3)
+{
+    auto v = [&](int j) { return to_c<C>(p[j * s]); };
+    return comb<C>(c0, c1, c2, c3, v(1) - v(0), v(2) - v(-1), v(3) - v(-2), v(4) - v(-3));
+}
+
+template <class C>
+__device__ __forceinline__ long long psi_x_index(int ix, int iz, int nx, int npml)
+{
+    // PD/fd/cu_fd.cu:305,315
+    return ix < npml ? (long long)ix + (long long)iz * 2 * npml
+                     : (long long)npml + nx - 1 - ix + (long long)iz * 2 * npml;
+}
+__device__ __forceinline__ long long psi_z_index(int ix, int iz, int nx, int nz, int npml, bool top)
+{
+    // PD/fd/cu_fd.cu:330,339
+    return top ? (long long)iz * nx + ix : (long long)(npml + nz - 1 - iz) * nx + ix;
+}
+
+// ----------------------------- P-SV ---------------------------------------
+template <class S, class C>
+__global__ void __launch_bounds__(256) psv_stress_2p(Shot<S, C> s)
+{
+    const int ix = blockIdx.x * 32 + threadIdx.x, iz = blockIdx.y * 8 + threadIdx.y;
+    if (ix >= s.nx || iz >= s.nz) return;
+    const long long o = s.origin + (long long)iz * s.pitch + ix, P = s.pitch;
+    const S *U = s.f[0][0], *W = s.f[0][1];
+    S *Txx = s.f[0][2], *Txz = s.f[0][3], *Tzz = s.f[0][4];
+    const int ord = stencil_order(ix, iz, s.nx, s.nz);
+    const C c0 = Coef<C>::get(ord, 0), c1 = Coef<C>::get(ord, 1), c2 = Coef<C>::get(ord, 2),
+            c3 = Coef<C>::get(ord, 3);
+    const C ux = dminus<S, C>(U + o, 1, c0, c1, c2, c3);
+    const C uz = dminus<S, C>(U + o, P, c0, c1, c2, c3);
+    const C wx = dplus<S, C>(W + o, 1, c0, c1, c2, c3);
+    const C wz = dplus<S, C>(W + o, P, c0, c1, c2, c3);
+    const C lam = to_c<C>(s.mat[0][o]), mu = to_c<C>(s.mat[1][o]), mua = to_c<C>(s.mat[2][o]);
+    const C gam = lam + (C)2 * mu;
+    C txx = to_c<C>(Txx[o]), tzz = to_c<C>(Tzz[o]), txz = to_c<C>(Txz[o]);
+    const int nx = s.nx, nz = s.nz, npml = s.npml, B = s.cpml_blk;
+    const C *b = s.cpml, *c = s.cpml + B, *k = s.cpml + 2 * B;
+    // x chain, PD/fd/cu_fd.cu:303-326 (components: 0 Txx_x 1 Txz_x 2 U_x 3 W_x)
+    if (ix < npml || ix >= nx - npml) {
+        const long long p = psi_x_index<C>(ix, iz, nx, npml);
+        C *pU = s.psi[0][2], *pW = s.psi[0][3];
+        const C ps = fmaC<C>(b[2 * nx + ix], pU[p], c[2 * nx + ix] * ux);
+        pU[p] = ps;
+        const C t = fmaC<C>(ux, k[2 * nx + ix], ps);
+        txx = fmaC<C>(gam, t, txx);
+        tzz = fmaC<C>(lam, t, tzz);
+        const C pw = fmaC<C>(b[3 * nx + ix], pW[p], c[3 * nx + ix] * wx);
+        pW[p] = pw;
+        txz = fmaC<C>(mua, fmaC<C>(wx, k[3 * nx + ix], pw), txz);
+    } else if (iz != 0) {
+        txx = fmaC<C>(gam, ux, txx);
+        tzz = fmaC<C>(lam, ux, tzz);
+        txz = fmaC<C>(mua, wx, txz);
+    }
+    // z chain, :328-355 (components after 4*nx: 0 Tzz_z 1 Txz_z 2 U_z 3 W_z)
+    const bool top = iz < npml && s.topabsorb;
+    if (top || iz >= nz - npml) {
+        const long long p = psi_z_index(ix, iz, nx, nz, npml, top);
+        C *pU = s.psi[0][6], *pW = s.psi[0][7];
+        const int zb = 4 * nx;
+        const C pw = fmaC<C>(b[zb + 3 * nz + iz], pW[p], c[zb + 3 * nz + iz] * wz);
+        pW[p] = pw;
+        const C t = fmaC<C>(wz, k[zb + 3 * nz + iz], pw);
+        txx = fmaC<C>(lam, t, txx);
+        tzz = fmaC<C>(gam, t, tzz);
+        const C pu = fmaC<C>(b[zb + 2 * nz + iz], pU[p], c[zb + 2 * nz + iz] * uz);
+        pU[p] = pu;
+        txz = fmaC<C>(mua, fmaC<C>(uz, k[zb + 2 * nz + iz], pu), txz);
+    } else if (iz == 0) {
+        txx = fmaC<C>((C)2 * mu, ux, txx);
+        tzz = (C)0;
+        txz = (C)0;
+    } else {
+        txx = fmaC<C>(lam, wz, txx);
+        tzz = fmaC<C>(gam, wz, tzz);
+        txz = fmaC<C>(mua, uz, txz);
+    }
+    Txx[o] = to_s<S>(txx);
+    Tzz[o] = to_s<S>(tzz);
+    Txz[o] = to_s<S>(txz);
+}
+
+template <class S, class C>
+__global__ void __launch_bounds__(256) psv_velocity_2p(Shot<S, C> s)
+{
+    const int ix = blockIdx.x * 32 + threadIdx.x, iz = blockIdx.y * 8 + threadIdx.y;
+    if (ix >= s.nx || iz >= s.nz) return;
+    const long long o = s.origin + (long long)iz * s.pitch + ix, P = s.pitch;
+    S *U = s.f[0][0], *W = s.f[0][1];
+    const S *Txx = s.f[0][2], *Txz = s.f[0][3], *Tzz = s.f[0][4];
+    const int ord = stencil_order(ix, iz, s.nx, s.nz);
+    const C c0 = Coef<C>::get(ord, 0), c1 = Coef<C>::get(ord, 1), c2 = Coef<C>::get(ord, 2),
+            c3 = Coef<C>::get(ord, 3);
+    const C dxTxx = dplus<S, C>(Txx + o, 1, c0, c1, c2, c3);
+    const C dzTzz = dminus<S, C>(Tzz + o, P, c0, c1, c2, c3);
+    const C dxTxz = dminus<S, C>(Txz + o, 1, c0, c1, c2, c3);
+    const C dzTxz = dplus<S, C>(Txz + o, P, c0, c1, c2, c3);
+    const C bu = to_c<C>(s.mat[3][o]), bw = to_c<C>(s.mat[4][o]);
+    C u = to_c<C>(U[o]), w = to_c<C>(W[o]);
+    const int nx = s.nx, nz = s.nz, npml = s.npml, B = s.cpml_blk;
+    const C *b = s.cpml, *c = s.cpml + B, *k = s.cpml + 2 * B;
+    // x chain, PD/fd/cu_fd.cu:455-474
+    if (ix < npml || ix >= nx - npml) {
+        const long long p = psi_x_index<C>(ix, iz, nx, npml);
+        C *pXX = s.psi[0][0], *pXZ = s.psi[0][1];
+        const C a = fmaC<C>(b[ix], pXX[p], c[ix] * dxTxx);
+        pXX[p] = a;
+        u = fmaC<C>(bu, fmaC<C>(dxTxx, k[ix], a), u);
+        const C q = fmaC<C>(b[nx + ix], pXZ[p], c[nx + ix] * dxTxz);
+        pXZ[p] = q;
+        w = fmaC<C>(bw, fmaC<C>(dxTxz, k[nx + ix], q), w);
+    } else if (iz != 0) {
+        u = fmaC<C>(bu, dxTxx, u);
+        w = fmaC<C>(bw, dxTxz, w);
+    }
+    // z chain, :476-499
+    const bool top = iz < npml && s.topabsorb;
+    if (top || iz >= nz - npml) {
+        const long long p = psi_z_index(ix, iz, nx, nz, npml, top);
+        C *pZZ = s.psi[0][4], *pXZ = s.psi[0][5];
+        const int zb = 4 * nx;
+        const C a = fmaC<C>(b[zb + nz + iz], pXZ[p], c[zb + nz + iz] * dzTxz);
+        const C q = fmaC<C>(b[zb + iz], pZZ[p], c[zb + iz] * dzTzz);
+        pXZ[p] = a;
+        pZZ[p] = q;
+        u = fmaC<C>(bu, fmaC<C>(dzTxz, k[zb + nz + iz], a), u);
+        w = fmaC<C>(bw, fmaC<C>(dzTzz, k[zb + iz], q), w);
+    } else if (iz == 0) {
+        u = fmaC<C>(bu, dxTxx + dzTxz, u);
+        w = (C)0;
+    } else {
+        u = fmaC<C>(bu, dzTxz, u);
+        w = fmaC<C>(bw, dzTzz, w);
+    }
+    U[o] = to_s<S>(u);
+    W[o] = to_s<S>(w);
+}
+
+// ------------------------------ SH ----------------------------------------
+template <class S, class C>
+__global__ void __launch_bounds__(256) sh_stress_2p(Shot<S, C> s)
+{
+    const int ix = blockIdx.x * 32 + threadIdx.x, iz = blockIdx.y * 8 + threadIdx.y;
+    if (ix >= s.nx || iz >= s.nz) return;
+    // cells skipped by the reference, SH/fd/cu_fd.cu:140
+    if (ix == 0 || ix >= s.nx - 1 || iz >= s.nz - 1) return;
+    const long long o = s.origin + (long long)iz * s.pitch + ix, P = s.pitch;
+    const S *V = s.f[0][0];
+    S *Tx = s.f[0][1], *Tz = s.f[0][2];
+    const int ord = stencil_order(ix, iz, s.nx, s.nz);
+    const C c0 = Coef<C>::get(ord, 0), c1 = Coef<C>::get(ord, 1), c2 = Coef<C>::get(ord, 2),
+            c3 = Coef<C>::get(ord, 3);
+    const C dxV = dplus<S, C>(V + o, 1, c0, c1, c2, c3);
+    const C dzV = dminus<S, C>(V + o, P, c0, c1, c2, c3);
+    const C mux = to_c<C>(s.mat[0][o]), muz = to_c<C>(s.mat[1][o]);
+    const int nx = s.nx, nz = s.nz, npml = s.npml, B = s.cpml_blk;
+    const C *b = s.cpml, *c = s.cpml + B, *k = s.cpml + 2 * B;
+    C tx = to_c<C>(Tx[o]), tz = to_c<C>(Tz[o]);
+    // components: x: 0 Tx_x 1 V_x ; z (after 2*nx): 0 Tz_z 1 V_z
+    if (ix < npml || ix >= nx - npml) {
+        const long long p = psi_x_index<C>(ix, iz, nx, npml);
+        C *pV = s.psi[0][1];
+        const C a = fmaC<C>(b[nx + ix], pV[p], c[nx + ix] * dxV);
+        pV[p] = a;
+        tx = fmaC<C>(mux, fmaC<C>(dxV, k[nx + ix], a), tx);
+    } else {
+        tx = fmaC<C>(mux, dxV, tx);
+    }
+    const bool top = iz < npml && s.topabsorb;
+    if (top || iz >= nz - npml) {
+        const long long p = psi_z_index(ix, iz, nx, nz, npml, top);
+        C *pV = s.psi[0][3];
+        const int zb = 2 * nx;
+        const C a = fmaC<C>(b[zb + nz + iz], pV[p], c[zb + nz + iz] * dzV);
+        pV[p] = a;
+        tz = fmaC<C>(muz, fmaC<C>(dzV, k[zb + nz + iz], a), tz);
+    } else {
+        tz = fmaC<C>(muz, dzV, tz);
+    }
+    Tx[o] = to_s<S>(tx);
+    Tz[o] = to_s<S>(tz);
+}
+
+template <class S, class C>
+__global__ void __launch_bounds__(256) sh_velocity_2p(Shot<S, C> s)
+{
+    const int ix = blockIdx.x * 32 + threadIdx.x, iz = blockIdx.y * 8 + threadIdx.y;
+    if (ix >= s.nx || iz >= s.nz) return;
+    const long long o = s.origin + (long long)iz * s.pitch + ix, P = s.pitch;
+    S *V = s.f[0][0];
+    const S *Tx = s.f[0][1], *Tz = s.f[0][2];
+    const int ord = stencil_order(ix, iz, s.nx, s.nz);
+    const C c0 = Coef<C>::get(ord, 0), c1 = Coef<C>::get(ord, 1), c2 = Coef<C>::get(ord, 2),
+            c3 = Coef<C>::get(ord, 3);
+    const C dxTx = dminus<S, C>(Tx + o, 1, c0, c1, c2, c3);
+    const C dzTz = dplus<S, C>(Tz + o, P, c0, c1, c2, c3);
+    const C bv = to_c<C>(s.mat[2][o]);
+    const int nx = s.nx, nz = s.nz, npml = s.npml, B = s.cpml_blk;
+    const C *b = s.cpml, *c = s.cpml + B, *k = s.cpml + 2 * B;
+    C v = to_c<C>(V[o]);
+    if (ix < npml || ix >= nx - npml) {
+        const long long p = psi_x_index<C>(ix, iz, nx, npml);
+        C *pT = s.psi[0][0];
+        const C a = fmaC<C>(b[ix], pT[p], c[ix] * dxTx);
+        pT[p] = a;
+        v = fmaC<C>(bv, fmaC<C>(dxTx, k[ix], a), v);
+    } else {
+        v = fmaC<C>(bv, dxTx, v);
+    }
+    const bool top = iz < npml && s.topabsorb;
+    if (top || iz >= nz - npml) {
+        const long long p = psi_z_index(ix, iz, nx, nz, npml, top);
+        C *pT = s.psi[0][2];
+        const int zb = 2 * nx;
+        const C a = fmaC<C>(b[zb + iz], pT[p], c[zb + iz] * dzTz);
+        pT[p] = a;
+        v = fmaC<C>(bv, fmaC<C>(dzTz, k[zb + iz], a), v);
+    } else {
+        v = fmaC<C>(bv, dzTz, v);
+    }
+    V[o] = to_s<S>(v);
+}
+
+// Point-source injection after the stress update (terms in order, one thread),
+// then for SH the free-surface stress image Tz(x,0) = -Tz(x,1) that the
+// reference applies at the top of its velocity kernel (SH/fd/cu_fd.cu:226).
+template <class S, class C>
+__global__ void post_stress_2p(Shot<S, C> s, int it, int sh_image)
+{
+    if (threadIdx.x == 0 && it < s.tamp_nt) {
+        for (int t = 0; t < s.nterms; ++t) {
+            const int4 tm = s.terms[t];
+            S *F = s.f[0][tm.x];
+            const long long o = s.origin + (long long)tm.z * s.pitch + tm.y;
+            F[o] = to_s<S>(to_c<C>(F[o]) + s.tamp[(long long)t * s.tamp_nt + it]);
+        }
+    }
+    if (sh_image && s.nz > 1) {
+        __syncthreads();
+        S *Tz = s.f[0][2];
+        for (int ix = threadIdx.x; ix < s.nx; ix += blockDim.x) {
+            const long long o = s.origin + ix;
+            Tz[o] = to_s<S>(-to_c<C>(Tz[o + s.pitch]));
+        }
+    }
+}
+
+}  // namespace
+
+template <class S, class C>
+__global__ void record_kernel(Shot<S, C> s, int par, int rec_index)
+{
+    // PD/record/cu_record.cu:138-148: rec[i] = F[rx[i] + rz[i]*nx]
+    for (int comp = 0; comp < 2; ++comp) {
+        const int n = s.nrec[comp];
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+            s.seis[comp][(long long)rec_index * n + i] = to_c<C>(s.f[par][comp == 0 ? 0 : 1][s.rec[comp][i]]);
+    }
+}
+
+template <class S, class C>
+int launch_record(const Shot<S, C> &s, int par, int rec_index, cudaStream_t st)
+{
+    const int n = s.nrec[0] > s.nrec[1] ? s.nrec[0] : s.nrec[1];
+    if (n <= 0) return FD23_OK;
+    record_kernel<S, C><<<(n + 255) / 256, 256, 0, st>>>(s, par, rec_index);
+    return cudaPeekAtLastError() == cudaSuccess ? FD23_OK : FD23_ERR_CUDA;
+}
+
+template <class S, class C>
+int launch_step_twopass(const Shot<S, C> &s, int wave, int it, cudaStream_t st)
+{
+    const dim3 blk(32, 8), grd((s.nx + 31) / 32, (s.nz + 7) / 8);
+    if (wave == FD23_PSV) {
+        psv_stress_2p<S, C><<<grd, blk, 0, st>>>(s);
+        if (s.nterms > 0 && it < s.tamp_nt) post_stress_2p<S, C><<<1, 32, 0, st>>>(s, it, 0);
+        psv_velocity_2p<S, C><<<grd, blk, 0, st>>>(s);
+    } else {
+        sh_stress_2p<S, C><<<grd, blk, 0, st>>>(s);
+        post_stress_2p<S, C><<<1, 256, 0, st>>>(s, it, 1);
+        sh_velocity_2p<S, C><<<grd, blk, 0, st>>>(s);
+    }
+    return cudaPeekAtLastError() == cudaSuccess ? FD23_OK : FD23_ERR_CUDA;
+}
+
+// FP64 energy watchdog: sum of squares over every stored wavefield element
+// (the padding is zero) and a NaN/Inf flag.
+template <class S, class C>
+__global__ void norm2_kernel(Shot<S, C> s, int par, int nfields, long long elems, double *out)
+{
+    double acc = 0.0;
+    int bad = 0;
+    for (int f = 0; f < nfields; ++f) {
+        const S *F = s.f[par][f];
+        for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < elems;
+             i += (long long)gridDim.x * blockDim.x) {
+            const double v = (double)to_c<C>(F[i]);
+            if (!isfinite(v)) bad = 1;
+            else acc += v * v;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        acc += __shfl_down_sync(0xffffffffu, acc, o);
+        bad |= __shfl_down_sync(0xffffffffu, bad, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&out[0], acc);
+        if (bad) out[1] = 1.0;
+    }
+}
+
+template <class S, class C>
+int launch_norm2(const Shot<S, C> &s, int par, int nfields, long long elems, double *dev_out,
+                 cudaStream_t st)
+{
+    if (cudaMemsetAsync(dev_out, 0, 2 * sizeof(double), st) != cudaSuccess) return FD23_ERR_CUDA;
+    norm2_kernel<S, C><<<512, 256, 0, st>>>(s, par, nfields, elems, dev_out);
+    return cudaPeekAtLastError() == cudaSuccess ? FD23_OK : FD23_ERR_CUDA;
+}
+
+#define FD23_INST(S, C)                                                                    \
+    template int launch_step_twopass<S, C>(const Shot<S, C> &, int, int, cudaStream_t);   \
+    template int launch_norm2<S, C>(const Shot<S, C> &, int, int, long long, double *, cudaStream_t); \
+    template int launch_record<S, C>(const Shot<S, C> &, int, int, cudaStream_t);
+FD23_INST(float, float)
+FD23_INST(double, double)
+FD23_INST(__nv_bfloat16, float)
+FD23_INST(__half, float)
+#undef FD23_INST
+
+}  // namespace fd23

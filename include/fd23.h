@@ -1,0 +1,191 @@
+/*
+ * fd23.h -- C ABI of the GB300 (sm_103a) 2-D elastic time-stepping engine.
+ *
+ * One solver object owns every device buffer of one shot on one GPU.  The
+ * calls replace the C++ operator surface of the reference fd23 programs
+ * (paths relative to the fd23 project root; PD = PSV/psv_clean_double,
+ * PN = PSV/clean_nobox, SH = SH):
+ *
+ *   reference                                            here
+ *   ---------------------------------------------------  ------------------------
+ *   PARAM::read_param / make_plan  PD/param/param.cpp:7,160   fd23_create (descriptor)
+ *   MATERIAL::get_model            PD/material/material.cpp:101  fd23_set_model
+ *   MATERIAL::init_gpu_full        PD/material/cu_material.cu   fd23_set_material
+ *   CPML::CPML(PARAM&), CPML(int,CPML&) PD/cpml/cpml.cpp:84,
+ *                                  PD/cpml/cu_cpml.cu:5          fd23_create / fd23_set_cpml
+ *   gaussian/trapozoid + cu_point_source(_p)
+ *                                  PD/source/waveform.cpp:8,27,
+ *                                  PD/point_source/cu_point_source.cu:6,66
+ *                                                                fd23_set_source / _terms
+ *   RECORD::init_line/init_list/cu_init_record
+ *                                  PD/record/cu_record.cu:12,30,79  fd23_set_receivers
+ *   cu_step_stress/cu_step_velocity + the time loop
+ *                                  PD/fd/fd.h:18-19, PN/main.cpp:117-170  fd23_run
+ *   RECORD::cu_record/cu_flush     PD/record/cu_record.cu:154,148   fd23_get_seismograms
+ *   FIELD::cu_save_state/cu_load_restart, CPML::cu_save_state
+ *                                  PN/field/cu_field.cu:26,41;
+ *                                  PN/cpml/cu_cpml.cu:92,109     fd23_get_state / fd23_set_state
+ *
+ * Conventions: every call returns FD23_OK (0) or a negative status and never
+ * exits the process; fd23_strerror() names the status.  Host arrays passed in
+ * are copied; host output buffers belong to the caller.  Arrays are row-major
+ * with x fastest: element (ix, iz) of an nx-by-nz grid is at ix + iz*nx, and
+ * iz = 0 is the free surface.  One solver must be driven from one host thread
+ * at a time.
+ */
+#ifndef FD23_H_
+#define FD23_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define FD23_OK 0
+#define FD23_ERR_ARG (-1)       /* invalid argument or size */
+#define FD23_ERR_CUDA (-2)      /* a CUDA runtime call failed */
+#define FD23_ERR_UNSTABLE (-3)  /* CFL check failed (stab > 1), PD/material/material.cpp:304 */
+#define FD23_ERR_ORDER (-4)     /* call made before what it depends on */
+#define FD23_ERR_NOMEM (-5)     /* device allocation failed */
+#define FD23_ERR_NONFINITE (-6) /* watchdog found NaN/Inf in the wavefield */
+#define FD23_ERR_TIMEOUT (-7)   /* a bounded device-side wait gave up */
+#define FD23_ERR_UNSUPPORTED (-8)
+
+/* ---- enums ---- */
+enum fd23_wave { FD23_PSV = 0, FD23_SH = 1 };
+/* storage/arithmetic forms.  F32 and F64 store and compute in that type;
+ * BF16 and F16 store wavefields and material in 16 bits and compute in FP32. */
+enum fd23_prec { FD23_F32 = 0, FD23_F64 = 1, FD23_BF16 = 2, FD23_F16 = 3 };
+/* kernel choice: AUTO picks the fused single-pass sweep */
+enum fd23_kernel { FD23_KERNEL_AUTO = 0, FD23_KERNEL_FUSED = 1, FD23_KERNEL_TWOPASS = 2 };
+/* field ids (source terms, receivers, state) */
+enum fd23_psv_field { FD23_U = 0, FD23_W = 1, FD23_TXX = 2, FD23_TXZ = 3, FD23_TZZ = 4 };
+enum fd23_sh_field { FD23_V = 0, FD23_TX = 1, FD23_TZ = 2 };
+/* point-source kinds (reference stype / srctype) */
+enum fd23_source_kind {
+    FD23_SRC_EXPLOSION = 1, /* Mxx = Mzz = 1, PN/point_source/cu_point_source.cu:16-20 */
+    FD23_SRC_FORCE = 2,     /* SH line force on V, SH/point_source/cu_point_source.cu:162 */
+    FD23_SRC_MOMENT = 3,    /* stype 3, PD/point_source/cu_point_source.cu:6-64 */
+    FD23_SRC_MOMENT_P = 13  /* stype 13 'p' dipole, running-sum wavelet, :66-146 */
+};
+
+typedef struct fd23_solver fd23_solver;
+
+typedef struct {
+    int wave;      /* fd23_wave */
+    int prec;      /* fd23_prec */
+    int nx, nz;    /* grid (any size >= 2*npml+1; no multiple-of-32 rule) */
+    int npml;      /* CPML width in cells */
+    int topabsorb; /* 0: free surface at iz = 0 (reference default); 1: CPML on top */
+    double h, dt;  /* grid spacing and time step (same units as the model) */
+    double pml_dt, pml_v, pml_r, pml_fc; /* CPML profile parameters, PD/cpml/cpml.cpp:7 */
+    int device;    /* CUDA device ordinal */
+    int kernel;    /* fd23_kernel */
+} fd23_desc;
+
+/* ---- lifecycle ---- */
+int fd23_create(const fd23_desc *desc, fd23_solver **out);
+void fd23_destroy(fd23_solver *s);
+const char *fd23_strerror(int status);
+int fd23_version(void);
+
+/* ---- model / material ----
+ * fd23_set_model: vp, vs, den rasters (nx*nz, FP64).  Builds the staggered,
+ * dt/h-scaled material in FP64 on the host with every edge rule of
+ * MATERIAL::get_model (PD/material/material.cpp:156-306; SH:
+ * SH/material/material.cpp:75-125), runs the CFL check, stores *stab and
+ * uploads.  vp is unused for SH and may be NULL.
+ * fd23_set_material: already-built arrays, FP64, concatenated
+ * (P-SV: LAM, MU, MUA, BU, BW; SH: MUX, MUZ, BV), each nx*nz. */
+int fd23_set_model(fd23_solver *s, const double *vp, const double *vs, const double *den,
+                   double *stab);
+int fd23_set_material(fd23_solver *s, const double *mat);
+
+/* ---- CPML ----
+ * fd23_create builds the coefficients from the descriptor.  fd23_set_cpml
+ * replaces them: b | c | k blocks, FP64, each block
+ * P-SV: Txx_x, Txz_x, U_x, W_x (nx each) then Tzz_z, Txz_z, U_z, W_z (nz each);
+ * SH:   Tx_x, V_x (nx each) then Tz_z, V_z (nz each). */
+int fd23_set_cpml(fd23_solver *s, const double *bck);
+
+/* ---- source ----
+ * fd23_set_source: reference point source.  moment = (Mxx, Mxz, Mzz) for
+ * P-SV or (Mxy, Mzy) for SH, unscaled (the 1/(pi*sqrt(2)*h^2) factor is
+ * applied here); may be NULL for EXPLOSION.  src = wavelet as s(t)*dt
+ * (lsrc samples), nt_max = number of steps the amplitude table covers.
+ * fd23_set_source_terms: explicit injections; term t adds
+ * amp[t*nt_amp + it] to field[t] at (ix[t], iz[t]) right after the stress
+ * update of step it (terms applied in order). */
+int fd23_set_source(fd23_solver *s, int kind, int xs, int zs, const double *moment,
+                    const double *src, int lsrc, int nt_max);
+int fd23_set_source_terms(fd23_solver *s, int nterms, const int *field, const int *ix,
+                          const int *iz, const double *amp, int nt_amp);
+/* Helpers: wavelets as s(t)*dt (PD/source/waveform.cpp:8-47); return lsrc or
+ * a negative status.  ricker is an addition: t0 = 1.2/f0 when t0 <= 0. */
+int fd23_wavelet_gaussian(double dt, int alpha, double *out, int cap);
+int fd23_wavelet_trapezoid(double dt, double t1, double t2, double t3, double *out, int cap);
+int fd23_wavelet_ricker(double dt, double f0, double t0, double *out, int cap);
+/* moment tensor projections from strike/dip/rake/azimuth (degrees) */
+void fd23_moment_psv(double strike, double dip, double rake, double azimuth, double out3[3]);
+void fd23_moment_sh(double strike, double dip, double rake, double azimuth, double out2[2]);
+
+/* ---- receivers ----
+ * Positions as given (the reference records each station as the pair
+ * (x, z), (x-1, z); fd23_receivers_line builds that list). */
+int fd23_set_receivers(fd23_solver *s, int field, const int *rx, const int *rz, int n);
+int fd23_receivers_line(int nsta, int ix0, int iz0, int idx, int idz, int *rx, int *rz);
+
+/* ---- time stepping ----
+ * Advances nsteps steps from the current step counter.  At every step it
+ * with it % itrecord == 0 the receivers are sampled after the velocity
+ * update.  Asynchronous on the solver's stream; fd23_sync waits. */
+int fd23_run(fd23_solver *s, int nsteps, int itrecord);
+int fd23_sync(fd23_solver *s);
+/* records so far for a receiver field; out holds nrec_steps x n values in the
+ * compute type (double for F64, float otherwise); *nrec_steps returns the
+ * number of recorded steps. */
+int fd23_get_seismograms(fd23_solver *s, int field, void *out, size_t out_bytes,
+                         int *nrec_steps);
+/* zero wavefields, memory variables, records and the step counter */
+int fd23_reset(fd23_solver *s);
+/* the cudaStream_t every launch of this solver goes to (for event timing) */
+int fd23_get_stream(fd23_solver *s, void **stream);
+int fd23_get_step(fd23_solver *s, int *it);
+
+/* ---- state (restart) ----
+ * Reference state layout (PN/main.cpp:293-317): P-SV U, W, Txx, Txz, Tzz
+ * (nx*nz each) then psi Txx_x, Txz_x, U_x, W_x (2*npml*nz each) then psi
+ * Tzz_z, Txz_z, U_z, W_z (2*npml*nx each); SH V, Tx, Tz, psi Tx_x, V_x,
+ * Tz_z, V_z.  Element type = compute type.  set_state also sets the step
+ * counter to it0 (the reference's nt0). */
+size_t fd23_state_bytes(fd23_solver *s);
+int fd23_get_state(fd23_solver *s, void *buf, size_t bytes);
+int fd23_set_state(fd23_solver *s, const void *buf, size_t bytes, int it0);
+
+/* ---- diagnostics ----
+ * FP64 energy-norm watchdog over the wavefield: sum of squares of all
+ * fields in FP64; returns FD23_ERR_NONFINITE when any value is NaN/Inf. */
+int fd23_field_norm2(fd23_solver *s, double *norm2);
+
+/* ---- host-only builders (no GPU needed) ----
+ * The same FP64 set-up fd23_set_model / fd23_create / fd23_set_source use,
+ * exposed for callers that build inputs themselves.
+ * fd23_build_material: out = nmat*nx*nz (see fd23_set_material); returns
+ *   FD23_OK or FD23_ERR_UNSTABLE (out is filled either way).
+ * fd23_build_cpml: returns the element count written (3 * block size).
+ * fd23_build_source_terms: returns the number of terms (amp: terms x nt). */
+int fd23_build_material(int wave, int nx, int nz, double h, double dt, const double *vp,
+                        const double *vs, const double *den, double *out, double *stab);
+int fd23_build_cpml(int wave, int nx, int nz, int npml, double pml_dt, double pml_r, double pml_v,
+                    double pml_fc, double *out, size_t out_elems);
+int fd23_build_source_terms(int wave, int kind, int xs, int zs, const double *moment, double h,
+                            double dt, const double *src, int lsrc, int nt, int *field, int *ix,
+                            int *iz, double *amp, int max_terms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FD23_H_ */
