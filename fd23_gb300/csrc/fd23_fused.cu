@@ -6,20 +6,26 @@
 // plus host round trips for the source (PD/point_source/cu_point_source.cu)
 // and receivers (PD/record/cu_record.cu:154).
 //
-// Data flow of one CTA (4 warps x WX; every thread owns 4 adjacent cells):
+// Data flow of one CTA (4 compute warps + 1 producer warp; every compute
+// thread owns 4 adjacent cells of one row):
 //   * The CTA works through a list of strips: output columns [x0, x0+TX),
 //     rows [z0, z1).  It marches down in blocks of 4 rows.  Iteration i
 //     updates the stress of rows z0-4+4i .. z0-1+4i on TX+8 columns (4 halo
 //     columns each side, recomputed rather than exchanged) and the velocity of
 //     rows z0-8+4i .. z0-5+4i on the TX output columns, so the velocity front
 //     trails the stress front by exactly the 4 rows its z-stencil needs.
-//   * Rows of the stencil inputs (U, W or V) stream into a ring of NUW 4-row
-//     blocks; rows of the point-wise operands (old stresses, material) into
-//     NPW stages.  Both are filled with 1-D bulk async copies
-//     (cp.async.bulk ... mbarrier::complete_tx) issued by warp 0, two
-//     iterations ahead of use, and consumed after an mbarrier wait.
-//   * Updated stresses (after the point source) go to a 3-block smem ring that
-//     feeds the velocity stencil, and straight to HBM.
+//   * The producer warp streams rows of the stencil inputs (U, W or V) into a
+//     ring of NUW 4-row blocks and rows of the point-wise operands (old
+//     stresses, material) into NPW stages with 1-D bulk async copies
+//     (cp.async.bulk ... mbarrier::complete_tx).  Full/empty mbarrier pairs
+//     gate each slot, so the producer runs ahead as far as the rings allow
+//     and the compute warps never wait on it except for data.
+//   * Updated stresses (after the point source) go to a 4-block smem ring that
+//     feeds the velocity stencil, and straight to HBM; one barrier over the
+//     compute warps per iteration orders the ring.
+//   * Interior cells outside the CPML take a branch-free path with constant
+//     coefficients; edge, CPML, free-surface and outside cells take the
+//     general per-cell path.
 //   * Wavefields and memory variables are ping-pong buffers (read set `par`,
 //     write set 1-par), so the recomputed halo columns and rows of one CTA
 //     never observe another CTA's new values.
@@ -155,12 +161,118 @@ struct Vec4<__half, float> : Vec4Half<__half> {};
 template <class S, class C>
 __device__ __forceinline__ C through(C v) { return to_c<C>(to_s<S>(v)); }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+// barrier over the compute warps only, with an AND vote
+__device__ __forceinline__ int compute_bar_and(int nthreads, int pred)
+{
+    int r;
+    asm volatile(
+        "{\n .reg .pred p, q;\n setp.ne.s32 p, %1, 0;\n"
+        " bar.red.and.pred q, 1, %2, p;\n selp.s32 %0, 1, 0, q;\n}\n"
+        : "=r"(r)
+        : "r"(pred), "r"(nthreads)
+        : "memory");
+    return r;
+}
+__device__ __forceinline__ void compute_bar(int nthreads)
+{
+    asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
+}
+
+// 12 consecutive values x-4 .. x+7 of a stored row (three 4-wide loads)
+template <class S, class C>
+__device__ __forceinline__ void ld12(const S *p, C h[12])
+{
+    Vec4<S, C>::ld(p - 4, h);
+    Vec4<S, C>::ld(p, h + 4);
+    Vec4<S, C>::ld(p + 4, h + 8);
+}
+// x differences of the 4 cells at h[4..7]: backward (D-minus) / forward (D-plus)
+template <class C>
+__device__ __forceinline__ C dmx(const C h[12], int e, C c0, C c1, C c2, C c3)
+{
+    return comb<C>(c0, c1, c2, c3, h[4 + e] - h[3 + e], h[5 + e] - h[2 + e], h[6 + e] - h[1 + e],
+                   h[7 + e] - h[e]);
+}
+template <class C>
+__device__ __forceinline__ C dpx(const C h[12], int e, C c0, C c1, C c2, C c3)
+{
+    return comb<C>(c0, c1, c2, c3, h[5 + e] - h[4 + e], h[6 + e] - h[3 + e], h[7 + e] - h[2 + e],
+                   h[8 + e] - h[1 + e]);
+}
+// z differences with interior coefficients, streaming two rows at a time:
+// rows[k] points at row (j-4+k), column already applied.
+template <class S, class C>
+__device__ __forceinline__ void dmz4(const S *const rows[9], int off, C out[4])
+{
+    C a[4], b[4];
+    Vec4<S, C>::ld(rows[4] + off, a);
+    Vec4<S, C>::ld(rows[3] + off, b);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) out[e] = Coef4<C>::c0 * (a[e] - b[e]);
+    Vec4<S, C>::ld(rows[5] + off, a);
+    Vec4<S, C>::ld(rows[2] + off, b);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) out[e] = fmaC<C>(-Coef4<C>::c1, a[e] - b[e], out[e]);
+    Vec4<S, C>::ld(rows[6] + off, a);
+    Vec4<S, C>::ld(rows[1] + off, b);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) out[e] = fmaC<C>(Coef4<C>::c2, a[e] - b[e], out[e]);
+    Vec4<S, C>::ld(rows[7] + off, a);
+    Vec4<S, C>::ld(rows[0] + off, b);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) out[e] = fmaC<C>(-Coef4<C>::c3, a[e] - b[e], out[e]);
+}
+template <class S, class C>
+__device__ __forceinline__ void dpz4(const S *const rows[9], int off, C out[4])
+{
+    C a[4], b[4];
+    Vec4<S, C>::ld(rows[5] + off, a);
+    Vec4<S, C>::ld(rows[4] + off, b);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) out[e] = Coef4<C>::c0 * (a[e] - b[e]);
+    Vec4<S, C>::ld(rows[6] + off, a);
+    Vec4<S, C>::ld(rows[3] + off, b);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) out[e] = fmaC<C>(-Coef4<C>::c1, a[e] - b[e], out[e]);
+    Vec4<S, C>::ld(rows[7] + off, a);
+    Vec4<S, C>::ld(rows[2] + off, b);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) out[e] = fmaC<C>(Coef4<C>::c2, a[e] - b[e], out[e]);
+    Vec4<S, C>::ld(rows[8] + off, a);
+    Vec4<S, C>::ld(rows[1] + off, b);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) out[e] = fmaC<C>(-Coef4<C>::c3, a[e] - b[e], out[e]);
+}
+// z differences with per-cell coefficient rows (edge cells)
+template <class S, class C>
+__device__ __forceinline__ void zcol(const S *const rows[9], int off, C v[9][4])
+{
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Vec4<S, C>::ld(rows[k] + off, v[k]);
+}
+
+template <class C>
+__device__ __forceinline__ void cell_coef(int ix, int iz, int nx, int nz, C &c0, C &c1, C &c2, C &c3)
+{
+    int o = 4;
+    if (ix >= 0 && ix < nx && iz >= 0 && iz < nz) o = stencil_order(ix, iz, nx, nz);
+    c0 = Coef<C>::get(o, 0);
+    c1 = Coef<C>::get(o, 1);
+    c2 = Coef<C>::get(o, 2);
+    c3 = Coef<C>::get(o, 3);
+}
+
 // ---------------------------------------------------------------------------
-template <class S, class C, int WAVE, int WX>
+template <class S, class C, int WAVE>
 struct Cfg {
     static constexpr bool PSV = (WAVE == FD23_PSV);
-    static constexpr int NTH = 128 * WX;       // threads (4 row groups x 32*WX)
-    static constexpr int SW = 128 * WX;        // stress columns per strip
+    static constexpr int NCW = 4;              // compute warps (one per row of a 4-row block)
+    static constexpr int NTH = 32 * (NCW + 1); // + one producer warp
+    static constexpr int SW = 128;             // stress columns per strip
     static constexpr int TX = SW - 8;          // output columns per strip
     static constexpr int UWW = SW + 8;         // stencil-input row width
     static constexpr int PWOFF = sizeof(S) == 2 ? 4 : 0;  // keeps 16-byte alignment
@@ -170,55 +282,70 @@ struct Cfg {
     static constexpr int NMS = PSV ? 3 : 2;    // stress-update material
     static constexpr int NMV = PSV ? 2 : 1;    // velocity-update material
     static constexpr int NPF = NT + NMS + NMV; // point-wise fields per row
-    static constexpr int NUW = 5, NPW = 3, NTR = 3;
+    static constexpr int NUW = 5, NPW = 3, NTR = 4;
     static constexpr int UW_ELEMS = NUW * 4 * NV * UWW;
-    static constexpr int PW_ELEMS = NPW * 4 * NPF * PWW;
+    static constexpr int PW_ELEMS = NPW * NPF * 4 * PWW;
     static constexpr int TR_ELEMS = NTR * 4 * NT * SW;
     static constexpr int MAX_ITEMS = 8;
     static constexpr int MAX_TERMS = 16;
-    static constexpr size_t SMEM = (((size_t)(UW_ELEMS + PW_ELEMS + TR_ELEMS) * sizeof(S) + 15) & ~(size_t)15) + 256 +
-                                   MAX_ITEMS * sizeof(int4) + MAX_TERMS * sizeof(int4) * MAX_ITEMS;
+    static constexpr int MINB = sizeof(S) == 8 ? 1 : 2;  // CTAs per SM the registers must allow
+    static constexpr size_t RING_BYTES =
+        (((size_t)(UW_ELEMS + PW_ELEMS + TR_ELEMS) * sizeof(S) + 15) & ~(size_t)15);
+    static constexpr size_t SMEM = RING_BYTES + 128 /* 16 barriers */ + MAX_ITEMS * 16 +
+                                   (size_t)MAX_ITEMS * MAX_TERMS * 16;
 };
 
 struct ItemInfo {
     int x0, z0, z1, niter;  // rows [z0, z1), niter = (z1-z0)/4 + 2
 };
 
-template <class S, class C, int WAVE, int WX>
-__global__ void __launch_bounds__(Cfg<S, C, WAVE, WX>::NTH, 1)
+template <class S, class C, int WAVE>
+__global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
     fused_step(Shot<S, C> sh, const WorkItem *__restrict__ items, const int *__restrict__ item_off,
                int par, int it, int rec_index, int *err_flag)
 {
-    using K = Cfg<S, C, WAVE, WX>;
+    using K = Cfg<S, C, WAVE>;
     constexpr bool PSV = K::PSV;
+    constexpr int NCT = 32 * K::NCW;  // compute threads
+    // an earlier launch gave up on a wait: do nothing until the host resets
+    if (err_flag && *(volatile int *)err_flag) return;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     S *uw_s = reinterpret_cast<S *>(smem_raw);
     S *pw_s = uw_s + K::UW_ELEMS;
     S *tr_s = pw_s + K::PW_ELEMS;
-    // NUW + NPW barriers, 16-byte aligned after the rings
-    uint64_t *bars = reinterpret_cast<uint64_t *>(
-        smem_raw + ((((size_t)K::UW_ELEMS + K::PW_ELEMS + K::TR_ELEMS) * sizeof(S) + 15) & ~(size_t)15));
-    uint64_t *bar_uw = bars, *bar_pw = bars + K::NUW;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw + K::RING_BYTES);
+    uint64_t *full_uw = bars, *empty_uw = bars + K::NUW;
+    uint64_t *full_pw = bars + 2 * K::NUW, *empty_pw = full_pw + K::NPW;
     ItemInfo *info = reinterpret_cast<ItemInfo *>(bars + 16);
-    int4 *tlist = reinterpret_cast<int4 *>(info + K::MAX_ITEMS);  // per item: local source terms
+    int4 *tlist = reinterpret_cast<int4 *>(info + K::MAX_ITEMS);
     __shared__ int tcount[K::MAX_ITEMS];
 
-    // an earlier launch gave up on a wait: do nothing until the host resets
-    if (err_flag && *(volatile int *)err_flag) return;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int g = warp / WX;                      // row group 0..3
-    const int q = (warp % WX) * 32 + lane;        // 4-cell column chunk
     const int nx = sh.nx, nz = sh.nz, npml = sh.npml, pitch = sh.pitch;
     const long long origin = sh.origin;
 
+    // read / write pointers selected once (compile-time indices only)
+    const S *rd[5];
+    S *wr[5];
+    const C *prd[8];
+    C *pwr[8];
+#pragma unroll
+    for (int f = 0; f < 5; ++f) {
+        rd[f] = par ? sh.f[1][f] : sh.f[0][f];
+        wr[f] = par ? sh.f[0][f] : sh.f[1][f];
+    }
+#pragma unroll
+    for (int f = 0; f < 8; ++f) {
+        prd[f] = par ? sh.psi[1][f] : sh.psi[0][f];
+        pwr[f] = par ? sh.psi[0][f] : sh.psi[1][f];
+    }
+
     // ---- receivers of the previous step (buffer set `par` is read-only here) ----
     if (rec_index >= 0) {
-#pragma unroll
-        for (int comp = 0; comp < 2; ++comp) {
-            const int n = sh.nrec[comp];
-            for (int r = blockIdx.x * K::NTH + tid; r < n; r += gridDim.x * K::NTH)
-                sh.seis[comp][(long long)rec_index * n + r] = to_c<C>((comp == 0 ? sh.f[par][0] : sh.f[par][1])[sh.rec[comp][r]]);
-        }
+        for (int r = blockIdx.x * K::NTH + tid; r < sh.nrec[0]; r += gridDim.x * K::NTH)
+            sh.seis[0][(long long)rec_index * sh.nrec[0] + r] = to_c<C>(rd[0][sh.rec[0][r]]);
+        for (int r = blockIdx.x * K::NTH + tid; r < sh.nrec[1]; r += gridDim.x * K::NTH)
+            sh.seis[1][(long long)rec_index * sh.nrec[1] + r] = to_c<C>(rd[1][sh.rec[1][r]]);
     }
 
     const int ibeg = item_off[blockIdx.x], iend = item_off[blockIdx.x + 1];
@@ -240,323 +367,292 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE, WX>::NTH, 1)
         tcount[tid] = cnt;
     }
     if (tid == 0) {
-        for (int b = 0; b < K::NUW + K::NPW; ++b) mbar_init(&bars[b], 1);
+        for (int b = 0; b < K::NUW; ++b) {
+            mbar_init(&full_uw[b], 1);
+            mbar_init(&empty_uw[b], K::NCW);
+        }
+        for (int b = 0; b < K::NPW; ++b) {
+            mbar_init(&full_pw[b], 1);
+            mbar_init(&empty_pw[b], K::NCW);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
 
-    // flat iteration space over the CTA's items
     int total_iters = 0;
     for (int k = 0; k < nitems; ++k) total_iters += info[k].niter;
-    // stencil-input stream: item k contributes niter+2 row blocks
-    int total_uw = 0;
-    for (int k = 0; k < nitems; ++k) total_uw += info[k].niter + 2;
 
-    // read / write pointers selected once (compile-time indices only: a
-    // runtime index into the parameter arrays would force a local copy)
-    const S *rd[5];
-    S *wr[5];
-    const C *prd[8];
-    C *pwr[8];
+    // ======================= producer warp =======================
+    if (warp == K::NCW) {
+        // stencil-input stream element e -> item k, block b
+        auto issue_uw = [=](int e) {
+            int k = 0, base = 0;
+            while (k < nitems - 1 && e >= base + info[k].niter + 2) { base += info[k].niter + 2; ++k; }
+            const int b = e - base;
+            const ItemInfo I = info[k];
+            const int slot = e % K::NUW;
+            const int r0 = I.z0 - 8 + 4 * b;
+            constexpr uint32_t ROWB = K::UWW * sizeof(S);
+            if (lane == 0) mbar_arrive_expect_tx(&full_uw[slot], ROWB * 4 * K::NV);
+            __syncwarp();
+            if (lane < 4 * K::NV) {
+                const int rr = lane & 3, v = lane >> 2;
+                const S *src = (v == 0 ? rd[0] : rd[K::NV - 1]) + origin + (long long)(r0 + rr) * pitch + (I.x0 - 8);
+                S *dst = uw_s + ((size_t)(slot * 4 + rr) * K::NV + v) * K::UWW;
+                bulk_g2s(dst, src, ROWB, &full_uw[slot]);
+            }
+        };
+        // point-wise operands of iteration i of item I into stage g % NPW
+        auto issue_pw = [=](int g, const ItemInfo &I, int i) {
+            const int slot = g % K::NPW;
+            constexpr uint32_t ROWB = K::PWW * sizeof(S);
+            if (lane == 0) mbar_arrive_expect_tx(&full_pw[slot], ROWB * 4 * K::NPF);
+            __syncwarp();
+            for (int c = lane; c < 4 * K::NPF; c += 32) {
+                const int rr = c & 3, fidx = c >> 2;
+                const S *b = rd[K::NV];
 #pragma unroll
-    for (int f = 0; f < 5; ++f) {
-        rd[f] = par ? sh.f[1][f] : sh.f[0][f];
-        wr[f] = par ? sh.f[0][f] : sh.f[1][f];
-    }
-#pragma unroll
-    for (int f = 0; f < 8; ++f) {
-        prd[f] = par ? sh.psi[1][f] : sh.psi[0][f];
-        pwr[f] = par ? sh.psi[0][f] : sh.psi[1][f];
-    }
-    // base pointer of point-wise field `fidx` (runtime), chosen by unrolled compare
-    auto pw_base = [=](int fidx) -> const S * {
-        const S *b = rd[K::NV];
-#pragma unroll
-        for (int f = 0; f < K::NPF; ++f) {
-            const S *c = f < K::NT ? rd[K::NV + f] : sh.mat[f - K::NT];
-            if (f == fidx) b = c;
+                for (int f = 0; f < K::NPF; ++f) {
+                    const S *cand = f < K::NT ? rd[K::NV + f] : sh.mat[f - K::NT];
+                    if (f == fidx) b = cand;
+                }
+                // old stresses and stress-update material on stress rows,
+                // velocity-update material on velocity rows
+                const int row = (fidx < K::NT + K::NMS ? I.z0 - 4 : I.z0 - 8) + 4 * i + rr;
+                const S *src = b + origin + (long long)row * pitch + (I.x0 - 4 - K::PWOFF);
+                S *dst = pw_s + ((size_t)(slot * K::NPF + fidx) * 4 + rr) * K::PWW;
+                bulk_g2s(dst, src, ROWB, &full_pw[slot]);
+            }
+        };
+        bool ok = true;
+        int e_uw = 0, g_pw = 0;
+        int k = 0, base_it = 0, base_uw = 0;
+        for (int g = 0; g < total_iters && ok; ++g) {
+            while (g >= base_it + info[k].niter) {
+                base_it += info[k].niter;
+                base_uw += info[k].niter + 2;
+                ++k;
+            }
+            const int i = g - base_it;
+            const int need = base_uw + i + 2;  // iteration g reads blocks need-2 .. need
+            while (ok && e_uw <= need) {
+                if (e_uw >= K::NUW)
+                    ok = mbar_wait_bounded(&empty_uw[e_uw % K::NUW], (uint32_t)(((e_uw / K::NUW) - 1) & 1), err_flag);
+                if (ok) issue_uw(e_uw++);
+            }
+            if (!ok) break;
+            if (g >= K::NPW)
+                ok = mbar_wait_bounded(&empty_pw[g % K::NPW], (uint32_t)(((g / K::NPW) - 1) & 1), err_flag);
+            if (ok) {
+                issue_pw(g, info[k], i);
+                g_pw = g + 1;
+            }
         }
-        return b;
-    };
-
-    // ---- producer: issue stream element `e` of the stencil inputs ----
-    auto issue_uw = [=](int e) {
-        int k = 0, base = 0;
-        while (k < nitems - 1 && e >= base + info[k].niter + 2) { base += info[k].niter + 2; ++k; }
-        const int b = e - base;
-        const ItemInfo &I = info[k];
-        const int slot = e % K::NUW;
-        const int r0 = I.z0 - 8 + 4 * b;
-        constexpr uint32_t ROWB = K::UWW * sizeof(S);
-        if (lane == 0) mbar_arrive_expect_tx(&bar_uw[slot], ROWB * 4 * K::NV);
-        __syncwarp();
-        if (lane < 4 * K::NV) {
-            const int rr = lane & 3, v = lane >> 2;
-            const S *src = (v == 0 ? rd[0] : rd[K::NV - 1]) + origin + (long long)(r0 + rr) * pitch + (I.x0 - 8);
-            S *dst = uw_s + ((size_t)(slot * 4 + rr) * K::NV + v) * K::UWW;
-            bulk_g2s(dst, src, ROWB, &bar_uw[slot]);
-        }
-    };
-    // ---- producer: point-wise operands of flat iteration `e` ----
-    auto issue_pw = [=](int e) {
-        int k = 0, base = 0;
-        while (k < nitems - 1 && e >= base + info[k].niter) { base += info[k].niter; ++k; }
-        const int i = e - base;
-        const ItemInfo &I = info[k];
-        const int slot = e % K::NPW;
-        constexpr uint32_t ROWB = K::PWW * sizeof(S);
-        if (lane == 0) mbar_arrive_expect_tx(&bar_pw[slot], ROWB * 4 * K::NPF);
-        __syncwarp();
-        for (int c = lane; c < 4 * K::NPF; c += 32) {
-            const int rr = c & 3, fidx = c >> 2;
-            // old stresses and stress-update material on stress rows,
-            // velocity-update material on velocity rows
-            const S *base_ptr = pw_base(fidx);
-            const int row = (fidx < K::NT + K::NMS ? I.z0 - 4 : I.z0 - 8) + 4 * i + rr;
-            const S *src = base_ptr + origin + (long long)row * pitch + (I.x0 - 4 - K::PWOFF);
-            S *dst = pw_s + ((size_t)(slot * K::NPF + fidx) * 4 + rr) * K::PWW;
-            bulk_g2s(dst, src, ROWB, &bar_pw[slot]);
-        }
-    };
-
-    int uw_issued = 0, pw_issued = 0;
-    // initial fill: NUW-1 stencil blocks and NPW-1 point-wise stages
-    if (warp == 0) {
-        for (; uw_issued < min(K::NUW - 1, total_uw); ++uw_issued) issue_uw(uw_issued);
-        for (; pw_issued < min(K::NPW - 1, total_iters); ++pw_issued) issue_pw(pw_issued);
+        // every copy issued must land before this CTA can release its shared memory
+        for (int e = max(0, e_uw - K::NUW); e < e_uw; ++e)
+            mbar_wait_bounded(&full_uw[e % K::NUW], (uint32_t)((e / K::NUW) & 1), nullptr);
+        for (int g = max(0, g_pw - K::NPW); g < g_pw; ++g)
+            mbar_wait_bounded(&full_pw[g % K::NPW], (uint32_t)((g / K::NPW) & 1), nullptr);
+        return;
     }
 
-    bool ok = true;
-    int gflat = 0, uw_base = 0;
-    const int bsel = 1 - par;
+    // ======================= compute warps =======================
+    const int grp = warp;  // row of the 4-row block this warp updates
     const C *cp = sh.cpml;
     const int B = sh.cpml_blk;
-
+    bool ok = true;
+    int uw_ready = 0, gflat = 0, uw_base = 0;
     for (int k = 0; k < nitems && ok; ++k) {
         const ItemInfo I = info[k];
         const int ntl = tcount[k];
         const int4 *tl = tlist + k * K::MAX_TERMS;
+        const int x = I.x0 - 4 + 4 * lane;  // first of this thread's 4 cells
+        const bool own_x = lane >= 1 && lane <= 30;
+        // the 4 cells are interior (8th order), outside the x-CPML and inside the grid
+        const bool xfast = x >= max(4, npml) && x + 3 <= min(nx - 5, nx - npml - 1);
         for (int i = 0; i < I.niter; ++i, ++gflat) {
-            // ---- refill: stream elements whose ring slot has been released ----
-            if (warp == 0) {
-                while (uw_issued < total_uw && uw_issued < uw_base + i + K::NUW) issue_uw(uw_issued++);
-                while (pw_issued < total_iters && pw_issued < gflat + K::NPW) issue_pw(pw_issued++);
-            }
-            // ---- wait for stencil blocks i..i+2 and point-wise stage of this iteration ----
-            for (int b = i; b < i + 3 && ok; ++b) {
-                const int e = uw_base + b;
-                ok = mbar_wait_bounded(&bar_uw[e % K::NUW], (uint32_t)((e / K::NUW) & 1), err_flag);
-            }
-            if (ok) ok = mbar_wait_bounded(&bar_pw[gflat % K::NPW], (uint32_t)((gflat / K::NPW) & 1), err_flag);
-            // every thread takes the same exit decision before the next barrier
-            ok = __syncthreads_and(ok) != 0;
-            if (!ok) break;
-
+            for (; ok && uw_ready <= uw_base + i + 2; ++uw_ready)
+                ok = mbar_wait_bounded(&full_uw[uw_ready % K::NUW], (uint32_t)((uw_ready / K::NUW) & 1), err_flag);
+            if (ok) ok = mbar_wait_bounded(&full_pw[gflat % K::NPW], (uint32_t)((gflat / K::NPW) & 1), err_flag);
             const S *pws = pw_s + (size_t)(gflat % K::NPW) * K::NPF * 4 * K::PWW;
-            // address of stencil input v, absolute row r, stored column index col (0 = x0-8)
-            auto uwrow = [=](int v, int r) -> const S * {
-                const int e = uw_base + ((r - (I.z0 - 8)) >> 2);
-                return uw_s + ((size_t)((e % K::NUW) * 4 + ((r - (I.z0 - 8)) & 3)) * K::NV + v) * K::UWW;
-            };
-            // stress ring row (absolute row r of this item)
-            auto trrow = [=](int f, int r) -> S * {
-                const int ii = (r - (I.z0 - 4)) >> 2;  // iteration that produced row r
-                const int slot = (gflat - i + ii) % K::NTR;
-                return tr_s + ((size_t)(slot * 4 + ((r - (I.z0 - 4)) & 3)) * K::NT + f) * K::SW;
-            };
+            auto pwrow = [=](int f) { return pws + ((size_t)f * 4 + grp) * K::PWW + K::PWOFF + 4 * lane; };
 
-            // ================= stress phase: row j, cells x .. x+3 =================
+            // ================= stress: row j, cells x .. x+3 =================
             {
-                const int j = I.z0 - 4 + 4 * i + g;
-                const int x = I.x0 - 4 + 4 * q;
+                const int j = I.z0 - 4 + 4 * i + grp;
+                const S *urow[9];
+#pragma unroll
+                for (int d = 0; d < 9; ++d) {
+                    const int rel = 4 * i + grp + d;  // (j-4+d) - (z0-8)
+                    const int e = uw_base + (rel >> 2);
+                    urow[d] = uw_s + ((size_t)((e % K::NUW) * 4 + (rel & 3)) * K::NV) * K::UWW + 4 * lane + 4;
+                }
+                const bool inrow = j >= 0 && j < nz;
+                const bool zfast = j >= 4 && j <= nz - 5 && j < nz - npml && !(sh.topabsorb && j < npml);
                 C tnew[K::NT][4];
-                const bool inrow = (j >= 0 && j < nz);
-                // point-wise operands
                 C told[K::NT][4], ms[K::NMS][4];
 #pragma unroll
-                for (int f = 0; f < K::NT; ++f)
-                    Vec4<S, C>::ld(pws + ((size_t)f * 4 + g) * K::PWW + K::PWOFF + 4 * q, told[f]);
+                for (int f = 0; f < K::NT; ++f) Vec4<S, C>::ld(pwrow(f), told[f]);
 #pragma unroll
-                for (int m = 0; m < K::NMS; ++m)
-                    Vec4<S, C>::ld(pws + ((size_t)(K::NT + m) * 4 + g) * K::PWW + K::PWOFF + 4 * q, ms[m]);
-
-                const int col = 4 * q + 4;  // stored column of cell x in stencil rows
-                if constexpr (PSV) {
-                    C ux[4], uz[4], wx[4], wz[4];
-                    {
-                        C h[12], zc[9][4];
-                        const S *r0 = uwrow(0, j);
-                        Vec4<S, C>::ld(r0 + col - 4, h);
-                        Vec4<S, C>::ld(r0 + col, h + 4);
-                        Vec4<S, C>::ld(r0 + col + 4, h + 8);
+                for (int m = 0; m < K::NMS; ++m) Vec4<S, C>::ld(pwrow(K::NT + m), ms[m]);
+                if (xfast && zfast) {
+                    constexpr C c0 = Coef4<C>::c0, c1 = Coef4<C>::c1, c2 = Coef4<C>::c2, c3 = Coef4<C>::c3;
+                    if constexpr (PSV) {
+                        C h[12];
+                        C ux[4], wx[4];
+                        ld12<S, C>(urow[4], h);
 #pragma unroll
-                        for (int d = -4; d <= 3; ++d)
-                            if (d != 0) Vec4<S, C>::ld(uwrow(0, j + d) + col, zc[d + 4]);
+                        for (int e = 0; e < 4; ++e) ux[e] = dmx<C>(h, e, c0, c1, c2, c3);
+                        ld12<S, C>(urow[4] + K::UWW, h);
 #pragma unroll
-                        for (int e = 0; e < 4; ++e) zc[4][e] = h[4 + e];
+                        for (int e = 0; e < 4; ++e) wx[e] = dpx<C>(h, e, c0, c1, c2, c3);
 #pragma unroll
                         for (int e = 0; e < 4; ++e) {
-                            const int ix = x + e;
-                            C c0 = Coef4<C>::c0, c1 = Coef4<C>::c1, c2 = Coef4<C>::c2, c3 = Coef4<C>::c3;
-                            if (!(ix >= 4 && ix <= nx - 5 && j >= 4 && j <= nz - 5)) {
-                                const int o = (ix >= 0 && ix < nx && inrow) ? stencil_order(ix, j, nx, nz) : 4;
-                                c0 = Coef<C>::get(o, 0); c1 = Coef<C>::get(o, 1);
-                                c2 = Coef<C>::get(o, 2); c3 = Coef<C>::get(o, 3);
-                            }
-                            ux[e] = comb<C>(c0, c1, c2, c3, h[4 + e] - h[3 + e], h[5 + e] - h[2 + e],
-                                            h[6 + e] - h[1 + e], h[7 + e] - h[e]);
-                            uz[e] = comb<C>(c0, c1, c2, c3, zc[4][e] - zc[3][e], zc[5][e] - zc[2][e],
-                                            zc[6][e] - zc[1][e], zc[7][e] - zc[0][e]);
+                            const C lam = ms[0][e], gam = lam + (C)2 * ms[1][e];
+                            tnew[0][e] = fmaC<C>(gam, ux[e], told[0][e]);
+                            tnew[2][e] = fmaC<C>(lam, ux[e], told[2][e]);
+                            tnew[1][e] = fmaC<C>(ms[2][e], wx[e], told[1][e]);
                         }
-                    }
-                    {
-                        C h[12], zc[9][4];
-                        const S *r0 = uwrow(1, j);
-                        Vec4<S, C>::ld(r0 + col - 4, h);
-                        Vec4<S, C>::ld(r0 + col, h + 4);
-                        Vec4<S, C>::ld(r0 + col + 4, h + 8);
-#pragma unroll
-                        for (int d = -3; d <= 4; ++d)
-                            if (d != 0) Vec4<S, C>::ld(uwrow(1, j + d) + col, zc[d + 4]);
-#pragma unroll
-                        for (int e = 0; e < 4; ++e) zc[4][e] = h[4 + e];
+                        C uz[4], wz[4];
+                        dmz4<S, C>(urow, 0, uz);
+                        dpz4<S, C>(urow, K::UWW, wz);
 #pragma unroll
                         for (int e = 0; e < 4; ++e) {
-                            const int ix = x + e;
-                            C c0 = Coef4<C>::c0, c1 = Coef4<C>::c1, c2 = Coef4<C>::c2, c3 = Coef4<C>::c3;
-                            if (!(ix >= 4 && ix <= nx - 5 && j >= 4 && j <= nz - 5)) {
-                                const int o = (ix >= 0 && ix < nx && inrow) ? stencil_order(ix, j, nx, nz) : 4;
-                                c0 = Coef<C>::get(o, 0); c1 = Coef<C>::get(o, 1);
-                                c2 = Coef<C>::get(o, 2); c3 = Coef<C>::get(o, 3);
-                            }
-                            wx[e] = comb<C>(c0, c1, c2, c3, h[5 + e] - h[4 + e], h[6 + e] - h[3 + e],
-                                            h[7 + e] - h[2 + e], h[8 + e] - h[1 + e]);
-                            wz[e] = comb<C>(c0, c1, c2, c3, zc[5][e] - zc[4][e], zc[6][e] - zc[3][e],
-                                            zc[7][e] - zc[2][e], zc[8][e] - zc[1][e]);
+                            const C lam = ms[0][e], gam = lam + (C)2 * ms[1][e];
+                            tnew[0][e] = fmaC<C>(lam, wz[e], tnew[0][e]);
+                            tnew[2][e] = fmaC<C>(gam, wz[e], tnew[2][e]);
+                            tnew[1][e] = fmaC<C>(ms[2][e], uz[e], tnew[1][e]);
                         }
-                    }
+                    } else {
+                        C h[12], dz[4];
+                        ld12<S, C>(urow[4], h);
+                        dmz4<S, C>(urow, 0, dz);
 #pragma unroll
-                    for (int e = 0; e < 4; ++e) {
-                        const int ix = x + e;
-                        if (!inrow || ix < 0 || ix >= nx) {
-                            tnew[0][e] = tnew[1][e] = tnew[2][e] = (C)0;
-                            continue;
+                        for (int e = 0; e < 4; ++e) {
+                            tnew[0][e] = fmaC<C>(ms[0][e], dpx<C>(h, e, c0, c1, c2, c3), told[0][e]);
+                            tnew[1][e] = fmaC<C>(ms[1][e], dz[e], told[1][e]);
                         }
-                        const bool own = ix >= I.x0 && ix < I.x0 + K::TX && j >= I.z0 && j < I.z1;
-                        const C lam = ms[0][e], mu = ms[1][e], mua = ms[2][e];
-                        const C gam = lam + (C)2 * mu;
-                        C txx = told[0][e], txz = told[1][e], tzz = told[2][e];
-                        if (ix < npml || ix >= nx - npml) {
-                            const long long p = ix < npml ? (long long)ix + (long long)j * 2 * npml
-                                                          : (long long)npml + nx - 1 - ix + (long long)j * 2 * npml;
-                            const C pu = fmaC<C>(cp[2 * nx + ix], prd[2][p], cp[B + 2 * nx + ix] * ux[e]);
-                            const C t = fmaC<C>(ux[e], cp[2 * B + 2 * nx + ix], pu);
-                            txx = fmaC<C>(gam, t, txx);
-                            tzz = fmaC<C>(lam, t, tzz);
-                            const C pw = fmaC<C>(cp[3 * nx + ix], prd[3][p], cp[B + 3 * nx + ix] * wx[e]);
-                            txz = fmaC<C>(mua, fmaC<C>(wx[e], cp[2 * B + 3 * nx + ix], pw), txz);
-                            if (own) { pwr[2][p] = pu; pwr[3][p] = pw; }
-                        } else if (j != 0) {
-                            txx = fmaC<C>(gam, ux[e], txx);
-                            tzz = fmaC<C>(lam, ux[e], tzz);
-                            txz = fmaC<C>(mua, wx[e], txz);
-                        }
-                        const bool top = j < npml && sh.topabsorb;
-                        if (top || j >= nz - npml) {
-                            const long long p = top ? (long long)j * nx + ix : (long long)(npml + nz - 1 - j) * nx + ix;
-                            const int zb = 4 * nx;
-                            const C pw = fmaC<C>(cp[zb + 3 * nz + j], prd[7][p], cp[B + zb + 3 * nz + j] * wz[e]);
-                            const C t = fmaC<C>(wz[e], cp[2 * B + zb + 3 * nz + j], pw);
-                            txx = fmaC<C>(lam, t, txx);
-                            tzz = fmaC<C>(gam, t, tzz);
-                            const C pu = fmaC<C>(cp[zb + 2 * nz + j], prd[6][p], cp[B + zb + 2 * nz + j] * uz[e]);
-                            txz = fmaC<C>(mua, fmaC<C>(uz[e], cp[2 * B + zb + 2 * nz + j], pu), txz);
-                            if (own) { pwr[7][p] = pw; pwr[6][p] = pu; }
-                        } else if (j == 0) {
-                            txx = fmaC<C>((C)2 * mu, ux[e], txx);
-                            tzz = (C)0;
-                            txz = (C)0;
-                        } else {
-                            txx = fmaC<C>(lam, wz[e], txx);
-                            tzz = fmaC<C>(gam, wz[e], tzz);
-                            txz = fmaC<C>(mua, uz[e], txz);
-                        }
-                        // storage order of stresses: Txx, Txz, Tzz
-                        tnew[0][e] = txx;
-                        tnew[1][e] = txz;
-                        tnew[2][e] = tzz;
                     }
                 } else {
-                    // SH stress: dxV = D+x V, dzV = D-z V (SH/fd/cu_fd.cu:77-171)
-                    C dxv[4], dzv[4];
+                    // ---- general cells: edges (reduced order), CPML, free surface, outside ----
+                    C cc[4][4];
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) cell_coef<C>(x + e, j, nx, nz, cc[e][0], cc[e][1], cc[e][2], cc[e][3]);
+                    // derivatives field by field: P-SV ux, uz (U) then wx, wz (W); SH dxV, dzV
+                    C dA[4], dB[4], dC[4], dD[4];
                     {
-                        C h[12], zc[9][4];
-                        const S *r0 = uwrow(0, j);
-                        Vec4<S, C>::ld(r0 + col - 4, h);
-                        Vec4<S, C>::ld(r0 + col, h + 4);
-                        Vec4<S, C>::ld(r0 + col + 4, h + 8);
-#pragma unroll
-                        for (int d = -4; d <= 3; ++d)
-                            if (d != 0) Vec4<S, C>::ld(uwrow(0, j + d) + col, zc[d + 4]);
-#pragma unroll
-                        for (int e = 0; e < 4; ++e) zc[4][e] = h[4 + e];
+                        C h[12], zv[9][4];
+                        ld12<S, C>(urow[4], h);
+                        zcol<S, C>(urow, 0, zv);
 #pragma unroll
                         for (int e = 0; e < 4; ++e) {
-                            const int ix = x + e;
-                            C c0 = Coef4<C>::c0, c1 = Coef4<C>::c1, c2 = Coef4<C>::c2, c3 = Coef4<C>::c3;
-                            if (!(ix >= 4 && ix <= nx - 5 && j >= 4 && j <= nz - 5)) {
-                                const int o = (ix >= 0 && ix < nx && inrow) ? stencil_order(ix, j, nx, nz) : 4;
-                                c0 = Coef<C>::get(o, 0); c1 = Coef<C>::get(o, 1);
-                                c2 = Coef<C>::get(o, 2); c3 = Coef<C>::get(o, 3);
-                            }
-                            dxv[e] = comb<C>(c0, c1, c2, c3, h[5 + e] - h[4 + e], h[6 + e] - h[3 + e],
-                                             h[7 + e] - h[2 + e], h[8 + e] - h[1 + e]);
-                            dzv[e] = comb<C>(c0, c1, c2, c3, zc[4][e] - zc[3][e], zc[5][e] - zc[2][e],
-                                             zc[6][e] - zc[1][e], zc[7][e] - zc[0][e]);
+                            const C *c = cc[e];
+                            dA[e] = PSV ? dmx<C>(h, e, c[0], c[1], c[2], c[3]) : dpx<C>(h, e, c[0], c[1], c[2], c[3]);
+                            dB[e] = comb<C>(c[0], c[1], c[2], c[3], zv[4][e] - zv[3][e], zv[5][e] - zv[2][e],
+                                            zv[6][e] - zv[1][e], zv[7][e] - zv[0][e]);
+                        }
+                    }
+                    if constexpr (PSV) {
+                        C h[12], zv[9][4];
+                        ld12<S, C>(urow[4] + K::UWW, h);
+                        zcol<S, C>(urow, K::UWW, zv);
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) {
+                            const C *c = cc[e];
+                            dC[e] = dpx<C>(h, e, c[0], c[1], c[2], c[3]);
+                            dD[e] = comb<C>(c[0], c[1], c[2], c[3], zv[5][e] - zv[4][e], zv[6][e] - zv[3][e],
+                                            zv[7][e] - zv[2][e], zv[8][e] - zv[1][e]);
                         }
                     }
 #pragma unroll
                     for (int e = 0; e < 4; ++e) {
                         const int ix = x + e;
+#pragma unroll
+                        for (int f = 0; f < K::NT; ++f) tnew[f][e] = told[f][e];
                         if (!inrow || ix < 0 || ix >= nx) {
-                            tnew[0][e] = tnew[1][e] = (C)0;
+#pragma unroll
+                            for (int f = 0; f < K::NT; ++f) tnew[f][e] = (C)0;
                             continue;
                         }
                         const bool own = ix >= I.x0 && ix < I.x0 + K::TX && j >= I.z0 && j < I.z1;
-                        C tx = told[0][e], tz = told[1][e];
                         const bool xp = ix < npml || ix >= nx - npml;
                         const bool top = j < npml && sh.topabsorb;
                         const bool zp = top || j >= nz - npml;
                         const long long px = ix < npml ? (long long)ix + (long long)j * 2 * npml
                                                        : (long long)npml + nx - 1 - ix + (long long)j * 2 * npml;
                         const long long pz = top ? (long long)j * nx + ix : (long long)(npml + nz - 1 - j) * nx + ix;
-                        if (ix == 0 || ix >= nx - 1 || j >= nz - 1) {
-                            // skipped by the reference: carry the old values over
-                            if (own && xp) pwr[1][px] = prd[1][px];
-                            if (own && zp) pwr[3][pz] = prd[3][pz];
-                        } else {
-                            const C mux = ms[0][e], muz = ms[1][e];
+                        if constexpr (PSV) {
+                            const C ux = dA[e], uz = dB[e], wx = dC[e], wz = dD[e];
+                            const C lam = ms[0][e], mu = ms[1][e], mua = ms[2][e];
+                            const C gam = lam + (C)2 * mu;
+                            C txx = told[0][e], txz = told[1][e], tzz = told[2][e];
+                            // x chain, PD/fd/cu_fd.cu:303-326
                             if (xp) {
-                                const C a = fmaC<C>(cp[nx + ix], prd[1][px], cp[B + nx + ix] * dxv[e]);
-                                if (own) pwr[1][px] = a;
-                                tx = fmaC<C>(mux, fmaC<C>(dxv[e], cp[2 * B + nx + ix], a), tx);
+                                const C pu = fmaC<C>(cp[2 * nx + ix], prd[2][px], cp[B + 2 * nx + ix] * ux);
+                                const C t = fmaC<C>(ux, cp[2 * B + 2 * nx + ix], pu);
+                                txx = fmaC<C>(gam, t, txx);
+                                tzz = fmaC<C>(lam, t, tzz);
+                                const C pw = fmaC<C>(cp[3 * nx + ix], prd[3][px], cp[B + 3 * nx + ix] * wx);
+                                txz = fmaC<C>(mua, fmaC<C>(wx, cp[2 * B + 3 * nx + ix], pw), txz);
+                                if (own) { pwr[2][px] = pu; pwr[3][px] = pw; }
+                            } else if (j != 0) {
+                                txx = fmaC<C>(gam, ux, txx);
+                                tzz = fmaC<C>(lam, ux, tzz);
+                                txz = fmaC<C>(mua, wx, txz);
+                            }
+                            // z chain, :328-355
+                            if (zp) {
+                                const int zb = 4 * nx;
+                                const C pw = fmaC<C>(cp[zb + 3 * nz + j], prd[7][pz], cp[B + zb + 3 * nz + j] * wz);
+                                const C t = fmaC<C>(wz, cp[2 * B + zb + 3 * nz + j], pw);
+                                txx = fmaC<C>(lam, t, txx);
+                                tzz = fmaC<C>(gam, t, tzz);
+                                const C pu = fmaC<C>(cp[zb + 2 * nz + j], prd[6][pz], cp[B + zb + 2 * nz + j] * uz);
+                                txz = fmaC<C>(mua, fmaC<C>(uz, cp[2 * B + zb + 2 * nz + j], pu), txz);
+                                if (own) { pwr[7][pz] = pw; pwr[6][pz] = pu; }
+                            } else if (j == 0) {
+                                txx = fmaC<C>((C)2 * mu, ux, txx);
+                                tzz = (C)0;
+                                txz = (C)0;
                             } else {
-                                tx = fmaC<C>(mux, dxv[e], tx);
+                                txx = fmaC<C>(lam, wz, txx);
+                                tzz = fmaC<C>(gam, wz, tzz);
+                                txz = fmaC<C>(mua, uz, txz);
+                            }
+                            tnew[0][e] = txx;
+                            tnew[1][e] = txz;
+                            tnew[2][e] = tzz;
+                        } else {
+                            // SH stress, SH/fd/cu_fd.cu:77-171; cells skipped there keep their values
+                            if (ix == 0 || ix >= nx - 1 || j >= nz - 1) {
+                                if (own && xp) pwr[1][px] = prd[1][px];
+                                if (own && zp) pwr[3][pz] = prd[3][pz];
+                                continue;
+                            }
+                            const C dxv = dA[e], dzv = dB[e];
+                            const C mux = ms[0][e], muz = ms[1][e];
+                            C tx = told[0][e], tz = told[1][e];
+                            if (xp) {
+                                const C a = fmaC<C>(cp[nx + ix], prd[1][px], cp[B + nx + ix] * dxv);
+                                if (own) pwr[1][px] = a;
+                                tx = fmaC<C>(mux, fmaC<C>(dxv, cp[2 * B + nx + ix], a), tx);
+                            } else {
+                                tx = fmaC<C>(mux, dxv, tx);
                             }
                             if (zp) {
                                 const int zb = 2 * nx;
-                                const C a = fmaC<C>(cp[zb + nz + j], prd[3][pz], cp[B + zb + nz + j] * dzv[e]);
+                                const C a = fmaC<C>(cp[zb + nz + j], prd[3][pz], cp[B + zb + nz + j] * dzv);
                                 if (own) pwr[3][pz] = a;
-                                tz = fmaC<C>(muz, fmaC<C>(dzv[e], cp[2 * B + zb + nz + j], a), tz);
+                                tz = fmaC<C>(muz, fmaC<C>(dzv, cp[2 * B + zb + nz + j], a), tz);
                             } else {
-                                tz = fmaC<C>(muz, dzv[e], tz);
+                                tz = fmaC<C>(muz, dzv, tz);
                             }
+                            tnew[0][e] = tx;
+                            tnew[1][e] = tz;
                         }
-                        tnew[0][e] = tx;
-                        tnew[1][e] = tz;
                     }
                 }
-                // ---- point source (terms in list order), then storage rounding ----
+                // ---- point source (terms in list order) ----
                 if (ntl > 0) {
                     for (int t = 0; t < ntl; ++t) {
                         const int4 tm = tl[t];  // (field, ix, iz, term index)
@@ -571,24 +667,18 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE, WX>::NTH, 1)
                         }
                     }
                 }
-                // write the stress ring and, for owned cells, HBM
+                // ---- stress ring (every column) and HBM (owned cells) ----
+                {
+                    const int rel = 4 * i + grp;  // j - (z0-4)
+                    S *tr = tr_s + ((size_t)((gflat % K::NTR) * 4 + (rel & 3)) * K::NT) * K::SW + 4 * lane;
 #pragma unroll
-                for (int f = 0; f < K::NT; ++f) {
-                    C v[4];
-#pragma unroll
-                    for (int e = 0; e < 4; ++e) v[e] = tnew[f][e];
-                    Vec4<S, C>::st(trrow(f, j) + 4 * q, v);
+                    for (int f = 0; f < K::NT; ++f) Vec4<S, C>::st(tr + f * K::SW, tnew[f]);
                 }
-                if (inrow && j >= I.z0 && j < I.z1 && q >= 1 && q <= 32 * WX - 2) {
+                if (inrow && own_x && j >= I.z0 && j < I.z1 && x < nx) {
                     const long long o = origin + (long long)j * pitch + x;
                     if (x + 3 < nx) {
 #pragma unroll
-                        for (int f = 0; f < K::NT; ++f) {
-                            C v[4];
-#pragma unroll
-                            for (int e = 0; e < 4; ++e) v[e] = tnew[f][e];
-                            Vec4<S, C>::st(wr[K::NV + f] + o, v);
-                        }
+                        for (int f = 0; f < K::NT; ++f) Vec4<S, C>::st(wr[K::NV + f] + o, tnew[f]);
                     } else {
 #pragma unroll
                         for (int f = 0; f < K::NT; ++f)
@@ -598,174 +688,202 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE, WX>::NTH, 1)
                     }
                 }
             }
-            __syncthreads();
+            // stresses of this block visible to every compute warp; all agree to go on
+            ok = compute_bar_and(NCT, ok) != 0;
+            if (!ok) break;
 
+            auto trrow = [=](int r) -> const S * {  // stress ring row r (absolute), column of cell x
+                const int rel = r - (I.z0 - 4);
+                const int slot = (gflat - i + (rel >> 2)) % K::NTR;
+                return tr_s + ((size_t)(slot * 4 + (rel & 3)) * K::NT) * K::SW + 4 * lane;
+            };
             if constexpr (!PSV) {
                 // free-surface stress image Tz(x,0) = -Tz(x,1), SH/fd/cu_fd.cu:226,
-                // applied once rows 0 and 1 of the new stresses exist
+                // once rows 0 and 1 of the new stresses exist
                 if (I.z0 == 0 && i == 1) {
-                    for (int c = tid; c < K::SW; c += K::NTH) {
-                        S *r0 = trrow(1, 0), *r1 = trrow(1, 1);
-                        const C v = -to_c<C>(r1[c]);
-                        r0[c] = to_s<S>(v);
-                        const int ix = I.x0 - 4 + c;
-                        if (ix >= I.x0 && ix < I.x0 + K::TX && ix < nx && nz > 1)
-                            wr[K::NV + 1][origin + ix] = to_s<S>(v);
+                    if (grp == 0) {
+                        S *r0 = const_cast<S *>(trrow(0)) + K::SW;
+                        const S *r1 = trrow(1) + K::SW;
+                        C v1[4], v0[4];
+                        Vec4<S, C>::ld(r1, v1);
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) v0[e] = -v1[e];
+                        Vec4<S, C>::st(r0, v0);
+#pragma unroll
+                        for (int e = 0; e < 4; ++e)
+                            if (own_x && x + e < nx && nz > 1) wr[K::NV + 1][origin + x + e] = to_s<S>(v0[e]);
                     }
-                    __syncthreads();
+                    compute_bar(NCT);
                 }
             }
 
-            // ================= velocity phase: row a, cells x .. x+3 =================
+            // ================= velocity: row a, cells x .. x+3 =================
             {
-                const int a = I.z0 - 8 + 4 * i + g;
-                const int x = I.x0 - 4 + 4 * q;
-                if (a >= I.z0 && a < nz && q >= 1 && q <= 32 * WX - 2 && x < nx) {
+                const int a = I.z0 - 8 + 4 * i + grp;
+                if (a >= I.z0 && a < nz && own_x && x < nx) {
+                    const S *trow[9];
+#pragma unroll
+                    for (int d = 0; d < 9; ++d) trow[d] = trrow(a - 4 + d);
                     C mv[K::NMV][4];
 #pragma unroll
-                    for (int m = 0; m < K::NMV; ++m)
-                        Vec4<S, C>::ld(pws + ((size_t)(K::NT + K::NMS + m) * 4 + g) * K::PWW + K::PWOFF + 4 * q, mv[m]);
-                    const int colv = 4 * q + 4;
+                    for (int m = 0; m < K::NMV; ++m) Vec4<S, C>::ld(pwrow(K::NT + K::NMS + m), mv[m]);
+                    const int rel = 4 * i + grp;  // a - (z0-8): block i, row grp
+                    const S *vrow = uw_s + ((size_t)(((uw_base + i) % K::NUW) * 4 + (rel & 3)) * K::NV) * K::UWW + 4 * lane + 4;
                     C vold[K::NV][4];
 #pragma unroll
-                    for (int v = 0; v < K::NV; ++v) Vec4<S, C>::ld(uwrow(v, a) + colv, vold[v]);
-                    const int cs = 4 * q;  // stored column of cell x in stress rows
+                    for (int v = 0; v < K::NV; ++v) Vec4<S, C>::ld(vrow + v * K::UWW, vold[v]);
+                    const bool zfast = a >= 4 && a <= nz - 5 && a < nz - npml && !(sh.topabsorb && a < npml);
                     C vnew[K::NV][4];
-                    if constexpr (PSV) {
-                        C dxTxx[4], dzTzz[4], dxTxz[4], dzTxz[4];
-                        C hxx[12], hxz[12], zzz[9][4], zxz[9][4];
-                        {
-                            const S *r = trrow(0, a);
-                            Vec4<S, C>::ld(r + cs - 4, hxx);
-                            Vec4<S, C>::ld(r + cs, hxx + 4);
-                            Vec4<S, C>::ld(r + cs + 4, hxx + 8);
-                            const S *rz = trrow(1, a);
-                            Vec4<S, C>::ld(rz + cs - 4, hxz);
-                            Vec4<S, C>::ld(rz + cs, hxz + 4);
-                            Vec4<S, C>::ld(rz + cs + 4, hxz + 8);
+                    // line force on V, injected before the velocity update (SH only)
+                    if constexpr (!PSV) {
+                        if (ntl > 0) {
+                            for (int t = 0; t < ntl; ++t) {
+                                const int4 tm = tl[t];
+                                if (tm.x == FD23_V && tm.z == a && tm.y >= x && tm.y < x + 4) {
+                                    const C amp = sh.tamp[(long long)tm.w * sh.tamp_nt + it];
 #pragma unroll
-                            for (int d = -4; d <= 4; ++d) {
-                                if (d <= 3) Vec4<S, C>::ld(trrow(2, a + d) + cs, zzz[d + 4]);
-                                if (d >= -3 && d != 0) Vec4<S, C>::ld(trrow(1, a + d) + cs, zxz[d + 4]);
+                                    for (int e = 0; e < 4; ++e)
+                                        if (e == tm.y - x) vold[0][e] = through<S, C>(vold[0][e]) + amp;
+                                }
                             }
-#pragma unroll
-                            for (int e = 0; e < 4; ++e) zxz[4][e] = hxz[4 + e];
                         }
+                    }
+                    if (xfast && zfast) {
+                        constexpr C c0 = Coef4<C>::c0, c1 = Coef4<C>::c1, c2 = Coef4<C>::c2, c3 = Coef4<C>::c3;
+                        if constexpr (PSV) {
+                            C h[12], dx[4];
+                            ld12<S, C>(trow[4], h);  // Txx
 #pragma unroll
-                        for (int e = 0; e < 4; ++e) {
-                            const int ix = x + e;
-                            C c0 = Coef4<C>::c0, c1 = Coef4<C>::c1, c2 = Coef4<C>::c2, c3 = Coef4<C>::c3;
-                            if (!(ix >= 4 && ix <= nx - 5 && a >= 4 && a <= nz - 5)) {
-                                const int o = ix < nx ? stencil_order(ix, a, nx, nz) : 4;
-                                c0 = Coef<C>::get(o, 0); c1 = Coef<C>::get(o, 1);
-                                c2 = Coef<C>::get(o, 2); c3 = Coef<C>::get(o, 3);
-                            }
-                            dxTxx[e] = comb<C>(c0, c1, c2, c3, hxx[5 + e] - hxx[4 + e], hxx[6 + e] - hxx[3 + e],
-                                               hxx[7 + e] - hxx[2 + e], hxx[8 + e] - hxx[1 + e]);
-                            dzTzz[e] = comb<C>(c0, c1, c2, c3, zzz[4][e] - zzz[3][e], zzz[5][e] - zzz[2][e],
-                                               zzz[6][e] - zzz[1][e], zzz[7][e] - zzz[0][e]);
-                            dxTxz[e] = comb<C>(c0, c1, c2, c3, hxz[4 + e] - hxz[3 + e], hxz[5 + e] - hxz[2 + e],
-                                               hxz[6 + e] - hxz[1 + e], hxz[7 + e] - hxz[e]);
-                            dzTxz[e] = comb<C>(c0, c1, c2, c3, zxz[5][e] - zxz[4][e], zxz[6][e] - zxz[3][e],
-                                               zxz[7][e] - zxz[2][e], zxz[8][e] - zxz[1][e]);
-                        }
+                            for (int e = 0; e < 4; ++e) dx[e] = dpx<C>(h, e, c0, c1, c2, c3);
 #pragma unroll
-                        for (int e = 0; e < 4; ++e) {
-                            const int ix = x + e;
-                            C u = vold[0][e], w = vold[1][e];
-                            if (ix >= nx) { vnew[0][e] = u; vnew[1][e] = w; continue; }
-                            const C bu = mv[0][e], bw = mv[1][e];
-                            if (ix < npml || ix >= nx - npml) {
-                                const long long p = ix < npml ? (long long)ix + (long long)a * 2 * npml
-                                                              : (long long)npml + nx - 1 - ix + (long long)a * 2 * npml;
-                                const C pa = fmaC<C>(cp[ix], prd[0][p], cp[B + ix] * dxTxx[e]);
-                                pwr[0][p] = pa;
-                                u = fmaC<C>(bu, fmaC<C>(dxTxx[e], cp[2 * B + ix], pa), u);
-                                const C pb = fmaC<C>(cp[nx + ix], prd[1][p], cp[B + nx + ix] * dxTxz[e]);
-                                pwr[1][p] = pb;
-                                w = fmaC<C>(bw, fmaC<C>(dxTxz[e], cp[2 * B + nx + ix], pb), w);
-                            } else if (a != 0) {
-                                u = fmaC<C>(bu, dxTxx[e], u);
-                                w = fmaC<C>(bw, dxTxz[e], w);
+                            for (int e = 0; e < 4; ++e) vnew[0][e] = fmaC<C>(mv[0][e], dx[e], vold[0][e]);
+                            ld12<S, C>(trow[4] + K::SW, h);  // Txz
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) dx[e] = dmx<C>(h, e, c0, c1, c2, c3);
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) vnew[1][e] = fmaC<C>(mv[1][e], dx[e], vold[1][e]);
+                            C dz[4];
+                            dpz4<S, C>(trow, K::SW, dz);  // d/dz Txz
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) vnew[0][e] = fmaC<C>(mv[0][e], dz[e], vnew[0][e]);
+                            dmz4<S, C>(trow, 2 * K::SW, dz);  // d/dz Tzz
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) vnew[1][e] = fmaC<C>(mv[1][e], dz[e], vnew[1][e]);
+                        } else {
+                            C h[12], dz[4];
+                            ld12<S, C>(trow[4], h);  // Tx
+                            dpz4<S, C>(trow, K::SW, dz);  // d/dz Tz
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) {
+                                const C t = fmaC<C>(mv[0][e], dmx<C>(h, e, c0, c1, c2, c3), vold[0][e]);
+                                vnew[0][e] = fmaC<C>(mv[0][e], dz[e], t);
                             }
-                            const bool top = a < npml && sh.topabsorb;
-                            if (top || a >= nz - npml) {
-                                const long long p = top ? (long long)a * nx + ix : (long long)(npml + nz - 1 - a) * nx + ix;
-                                const int zb = 4 * nx;
-                                const C pa = fmaC<C>(cp[zb + nz + a], prd[5][p], cp[B + zb + nz + a] * dzTxz[e]);
-                                const C pb = fmaC<C>(cp[zb + a], prd[4][p], cp[B + zb + a] * dzTzz[e]);
-                                pwr[5][p] = pa;
-                                pwr[4][p] = pb;
-                                u = fmaC<C>(bu, fmaC<C>(dzTxz[e], cp[2 * B + zb + nz + a], pa), u);
-                                w = fmaC<C>(bw, fmaC<C>(dzTzz[e], cp[2 * B + zb + a], pb), w);
-                            } else if (a == 0) {
-                                u = fmaC<C>(bu, dxTxx[e] + dzTxz[e], u);
-                                w = (C)0;
-                            } else {
-                                u = fmaC<C>(bu, dzTxz[e], u);
-                                w = fmaC<C>(bw, dzTzz[e], w);
-                            }
-                            vnew[0][e] = u;
-                            vnew[1][e] = w;
                         }
                     } else {
-                        C dxT[4], dzT[4];
-                        C hx[12], zz[9][4];
+                        C cc[4][4];
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) cell_coef<C>(x + e, a, nx, nz, cc[e][0], cc[e][1], cc[e][2], cc[e][3]);
+                        // P-SV: dA = d/dx Txx, dB = d/dx Txz, dC = d/dz Txz, dD = d/dz Tzz
+                        // SH:   dA = d/dx Tx,  dC = d/dz Tz
+                        C dA[4], dB[4], dC[4], dD[4];
                         {
-                            const S *r = trrow(0, a);
-                            Vec4<S, C>::ld(r + cs - 4, hx);
-                            Vec4<S, C>::ld(r + cs, hx + 4);
-                            Vec4<S, C>::ld(r + cs + 4, hx + 8);
+                            C h[12];
+                            ld12<S, C>(trow[4], h);
 #pragma unroll
-                            for (int d = -3; d <= 4; ++d) Vec4<S, C>::ld(trrow(1, a + d) + cs, zz[d + 4]);
+                            for (int e = 0; e < 4; ++e) {
+                                const C *c = cc[e];
+                                dA[e] = PSV ? dpx<C>(h, e, c[0], c[1], c[2], c[3]) : dmx<C>(h, e, c[0], c[1], c[2], c[3]);
+                            }
+                        }
+                        {
+                            C h[12], zv[9][4];
+                            if constexpr (PSV) ld12<S, C>(trow[4] + K::SW, h);
+                            zcol<S, C>(trow, K::SW, zv);
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) {
+                                const C *c = cc[e];
+                                if constexpr (PSV) dB[e] = dmx<C>(h, e, c[0], c[1], c[2], c[3]);
+                                dC[e] = comb<C>(c[0], c[1], c[2], c[3], zv[5][e] - zv[4][e], zv[6][e] - zv[3][e],
+                                                zv[7][e] - zv[2][e], zv[8][e] - zv[1][e]);
+                            }
+                        }
+                        if constexpr (PSV) {
+                            C zv[9][4];
+                            zcol<S, C>(trow, 2 * K::SW, zv);
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) {
+                                const C *c = cc[e];
+                                dD[e] = comb<C>(c[0], c[1], c[2], c[3], zv[4][e] - zv[3][e], zv[5][e] - zv[2][e],
+                                                zv[6][e] - zv[1][e], zv[7][e] - zv[0][e]);
+                            }
                         }
 #pragma unroll
                         for (int e = 0; e < 4; ++e) {
                             const int ix = x + e;
-                            C c0 = Coef4<C>::c0, c1 = Coef4<C>::c1, c2 = Coef4<C>::c2, c3 = Coef4<C>::c3;
-                            if (!(ix >= 4 && ix <= nx - 5 && a >= 4 && a <= nz - 5)) {
-                                const int o = ix < nx ? stencil_order(ix, a, nx, nz) : 4;
-                                c0 = Coef<C>::get(o, 0); c1 = Coef<C>::get(o, 1);
-                                c2 = Coef<C>::get(o, 2); c3 = Coef<C>::get(o, 3);
-                            }
-                            dxT[e] = comb<C>(c0, c1, c2, c3, hx[4 + e] - hx[3 + e], hx[5 + e] - hx[2 + e],
-                                             hx[6 + e] - hx[1 + e], hx[7 + e] - hx[e]);
-                            dzT[e] = comb<C>(c0, c1, c2, c3, zz[5][e] - zz[4][e], zz[6][e] - zz[3][e],
-                                             zz[7][e] - zz[2][e], zz[8][e] - zz[1][e]);
-                        }
 #pragma unroll
-                        for (int e = 0; e < 4; ++e) {
-                            const int ix = x + e;
-                            C v = vold[0][e];
-                            if (ix >= nx) { vnew[0][e] = v; continue; }
-                            // line force on V, injected before the velocity update
-                            if (ntl > 0)
-                                for (int t = 0; t < ntl; ++t) {
-                                    const int4 tm = tl[t];
-                                    if (tm.x == FD23_V && tm.z == a && tm.y == ix)
-                                        v = through<S, C>(v) + sh.tamp[(long long)tm.w * sh.tamp_nt + it];
-                                }
-                            const C bv = mv[0][e];
-                            if (ix < npml || ix >= nx - npml) {
-                                const long long p = ix < npml ? (long long)ix + (long long)a * 2 * npml
-                                                              : (long long)npml + nx - 1 - ix + (long long)a * 2 * npml;
-                                const C pa = fmaC<C>(cp[ix], prd[0][p], cp[B + ix] * dxT[e]);
-                                pwr[0][p] = pa;
-                                v = fmaC<C>(bv, fmaC<C>(dxT[e], cp[2 * B + ix], pa), v);
-                            } else {
-                                v = fmaC<C>(bv, dxT[e], v);
-                            }
+                            for (int v = 0; v < K::NV; ++v) vnew[v][e] = vold[v][e];
+                            if (ix >= nx) continue;
+                            const bool xp = ix < npml || ix >= nx - npml;
                             const bool top = a < npml && sh.topabsorb;
-                            if (top || a >= nz - npml) {
-                                const long long p = top ? (long long)a * nx + ix : (long long)(npml + nz - 1 - a) * nx + ix;
-                                const int zb = 2 * nx;
-                                const C pa = fmaC<C>(cp[zb + a], prd[2][p], cp[B + zb + a] * dzT[e]);
-                                pwr[2][p] = pa;
-                                v = fmaC<C>(bv, fmaC<C>(dzT[e], cp[2 * B + zb + a], pa), v);
+                            const bool zp = top || a >= nz - npml;
+                            const long long px = ix < npml ? (long long)ix + (long long)a * 2 * npml
+                                                           : (long long)npml + nx - 1 - ix + (long long)a * 2 * npml;
+                            const long long pz = top ? (long long)a * nx + ix : (long long)(npml + nz - 1 - a) * nx + ix;
+                            if constexpr (PSV) {
+                                const C dxTxx = dA[e], dxTxz = dB[e], dzTxz = dC[e], dzTzz = dD[e];
+                                const C bu = mv[0][e], bw = mv[1][e];
+                                C u = vold[0][e], w = vold[1][e];
+                                // x chain, PD/fd/cu_fd.cu:455-474
+                                if (xp) {
+                                    const C pa = fmaC<C>(cp[ix], prd[0][px], cp[B + ix] * dxTxx);
+                                    pwr[0][px] = pa;
+                                    u = fmaC<C>(bu, fmaC<C>(dxTxx, cp[2 * B + ix], pa), u);
+                                    const C pb = fmaC<C>(cp[nx + ix], prd[1][px], cp[B + nx + ix] * dxTxz);
+                                    pwr[1][px] = pb;
+                                    w = fmaC<C>(bw, fmaC<C>(dxTxz, cp[2 * B + nx + ix], pb), w);
+                                } else if (a != 0) {
+                                    u = fmaC<C>(bu, dxTxx, u);
+                                    w = fmaC<C>(bw, dxTxz, w);
+                                }
+                                // z chain, :476-499
+                                if (zp) {
+                                    const int zb = 4 * nx;
+                                    const C pa = fmaC<C>(cp[zb + nz + a], prd[5][pz], cp[B + zb + nz + a] * dzTxz);
+                                    const C pb = fmaC<C>(cp[zb + a], prd[4][pz], cp[B + zb + a] * dzTzz);
+                                    pwr[5][pz] = pa;
+                                    pwr[4][pz] = pb;
+                                    u = fmaC<C>(bu, fmaC<C>(dzTxz, cp[2 * B + zb + nz + a], pa), u);
+                                    w = fmaC<C>(bw, fmaC<C>(dzTzz, cp[2 * B + zb + a], pb), w);
+                                } else if (a == 0) {
+                                    u = fmaC<C>(bu, dxTxx + dzTxz, u);
+                                    w = (C)0;
+                                } else {
+                                    u = fmaC<C>(bu, dzTxz, u);
+                                    w = fmaC<C>(bw, dzTzz, w);
+                                }
+                                vnew[0][e] = u;
+                                vnew[1][e] = w;
                             } else {
-                                v = fmaC<C>(bv, dzT[e], v);
+                                const C dxT = dA[e], dzT = dC[e];
+                                const C bv = mv[0][e];
+                                C v = vold[0][e];
+                                if (xp) {
+                                    const C pa = fmaC<C>(cp[ix], prd[0][px], cp[B + ix] * dxT);
+                                    pwr[0][px] = pa;
+                                    v = fmaC<C>(bv, fmaC<C>(dxT, cp[2 * B + ix], pa), v);
+                                } else {
+                                    v = fmaC<C>(bv, dxT, v);
+                                }
+                                if (zp) {
+                                    const int zb = 2 * nx;
+                                    const C pa = fmaC<C>(cp[zb + a], prd[2][pz], cp[B + zb + a] * dzT);
+                                    pwr[2][pz] = pa;
+                                    v = fmaC<C>(bv, fmaC<C>(dzT, cp[2 * B + zb + a], pa), v);
+                                } else {
+                                    v = fmaC<C>(bv, dzT, v);
+                                }
+                                vnew[0][e] = v;
                             }
-                            vnew[0][e] = v;
                         }
                     }
                     const long long o = origin + (long long)a * pitch + x;
@@ -781,30 +899,39 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE, WX>::NTH, 1)
                     }
                 }
             }
-            __syncthreads();
+            // release the ring slots this iteration was the last reader of
+            __syncwarp();
+            if (lane == 0) {
+                mbar_arrive(&empty_uw[(uw_base + i) % K::NUW]);
+                if (i == I.niter - 1) {
+                    mbar_arrive(&empty_uw[(uw_base + i + 1) % K::NUW]);
+                    mbar_arrive(&empty_uw[(uw_base + i + 2) % K::NUW]);
+                }
+                mbar_arrive(&empty_pw[gflat % K::NPW]);
+            }
         }
         uw_base += I.niter + 2;
     }
-    if (!ok && warp == 0) {
-        // a wait gave up: let the copies already issued land before the CTA
-        // exits (each wait is bounded again)
-#pragma unroll
-        for (int e = max(0, uw_issued - K::NUW); e < uw_issued; ++e)
-            mbar_wait_bounded(&bar_uw[e % K::NUW], (uint32_t)((e / K::NUW) & 1), nullptr);
-#pragma unroll
-        for (int e = max(0, pw_issued - K::NPW); e < pw_issued; ++e)
-            mbar_wait_bounded(&bar_pw[e % K::NPW], (uint32_t)((e / K::NPW) & 1), nullptr);
-    }
 }
 
-template <class S, class C, int WAVE, int WX>
+template <class S, class C, int WAVE>
 int launch_fused_impl(const Shot<S, C> &s, const WorkItem *items, const int *item_off, int nblocks,
                       int par, int it, int rec_index, int *err_flag, cudaStream_t st)
 {
-    using K = Cfg<S, C, WAVE, WX>;
-    fused_step<S, C, WAVE, WX><<<nblocks, K::NTH, K::SMEM, st>>>(s, items, item_off, par, it,
-                                                                   rec_index, err_flag);
+    using K = Cfg<S, C, WAVE>;
+    fused_step<S, C, WAVE><<<nblocks, K::NTH, K::SMEM, st>>>(s, items, item_off, par, it, rec_index,
+                                                            err_flag);
     return cudaPeekAtLastError() == cudaSuccess ? FD23_OK : FD23_ERR_CUDA;
+}
+
+template <class S, class C, int WAVE>
+int prepare_one()
+{
+    using K = Cfg<S, C, WAVE>;
+    return cudaFuncSetAttribute(fused_step<S, C, WAVE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)K::SMEM) == cudaSuccess
+               ? FD23_OK
+               : FD23_ERR_CUDA;
 }
 
 }  // namespace
@@ -813,7 +940,7 @@ FusedGeom fused_geom(int wave, int prec)
 {
     (void)wave;
     (void)prec;
-    return FusedGeom{120, 4};  // WX = 1: 128 stress columns, 120 output columns
+    return FusedGeom{120, 4};  // 128 stress columns, 120 output columns, 4-row blocks
 }
 
 template <class S, class C>
@@ -821,20 +948,10 @@ int launch_step_fused(const Shot<S, C> &s, int wave, const WorkItem *items, cons
                       int nblocks, int par, int it, int rec_index, int *err_flag, cudaStream_t st)
 {
     if (wave == FD23_PSV)
-        return launch_fused_impl<S, C, FD23_PSV, 1>(s, items, item_off, nblocks, par, it, rec_index,
-                                                    err_flag, st);
-    return launch_fused_impl<S, C, FD23_SH, 1>(s, items, item_off, nblocks, par, it, rec_index,
-                                              err_flag, st);
-}
-
-template <class S, class C, int WAVE>
-static int prepare_one()
-{
-    using K = Cfg<S, C, WAVE, 1>;
-    return cudaFuncSetAttribute(fused_step<S, C, WAVE, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)K::SMEM) == cudaSuccess
-               ? FD23_OK
-               : FD23_ERR_CUDA;
+        return launch_fused_impl<S, C, FD23_PSV>(s, items, item_off, nblocks, par, it, rec_index,
+                                                 err_flag, st);
+    return launch_fused_impl<S, C, FD23_SH>(s, items, item_off, nblocks, par, it, rec_index, err_flag,
+                                           st);
 }
 
 int fused_prepare(int wave, int prec)
@@ -860,17 +977,17 @@ size_t fused_smem_bytes(int wave, int prec)
 {
     if (wave == FD23_PSV) {
         switch (prec) {
-            case FD23_F64: return Cfg<double, double, FD23_PSV, 1>::SMEM;
-            case FD23_BF16: return Cfg<__nv_bfloat16, float, FD23_PSV, 1>::SMEM;
-            case FD23_F16: return Cfg<__half, float, FD23_PSV, 1>::SMEM;
-            default: return Cfg<float, float, FD23_PSV, 1>::SMEM;
+            case FD23_F64: return Cfg<double, double, FD23_PSV>::SMEM;
+            case FD23_BF16: return Cfg<__nv_bfloat16, float, FD23_PSV>::SMEM;
+            case FD23_F16: return Cfg<__half, float, FD23_PSV>::SMEM;
+            default: return Cfg<float, float, FD23_PSV>::SMEM;
         }
     }
     switch (prec) {
-        case FD23_F64: return Cfg<double, double, FD23_SH, 1>::SMEM;
-        case FD23_BF16: return Cfg<__nv_bfloat16, float, FD23_SH, 1>::SMEM;
-        case FD23_F16: return Cfg<__half, float, FD23_SH, 1>::SMEM;
-        default: return Cfg<float, float, FD23_SH, 1>::SMEM;
+        case FD23_F64: return Cfg<double, double, FD23_SH>::SMEM;
+        case FD23_BF16: return Cfg<__nv_bfloat16, float, FD23_SH>::SMEM;
+        case FD23_F16: return Cfg<__half, float, FD23_SH>::SMEM;
+        default: return Cfg<float, float, FD23_SH>::SMEM;
     }
 }
 
