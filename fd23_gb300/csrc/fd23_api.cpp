@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -281,30 +282,55 @@ int dispatch_flush(fd23_solver *s)
     }
 }
 
-// Work list: strips of TX columns, split into row ranges of 4-row blocks so
-// that every CTA gets the same number of blocks (a range may span two
-// strips; each strip piece is one item).
+// Work list: strips of TX columns cut into row ranges of 4-row blocks.
+// CTAs get contiguous (strip-major) ranges of equal estimated cost; a range
+// may span two strips (each strip piece is one item).  Blocks that touch the
+// CPML run the general per-cell path and cost more; the relative costs
+// (FD23_COST_XPML, FD23_COST_ZPML, default 2.5 / 1.5) come from profiles.
 int build_worklist(fd23_solver *s)
 {
     const FusedGeom g = fused_geom(s->d.wave, s->d.prec);
-    const int nx = s->d.nx, nz = s->d.nz;
+    const int nx = s->d.nx, nz = s->d.nz, npml = s->d.npml;
     const int ntx = (nx + g.tile_x - 1) / g.tile_x;
     const int nzb = (nz + 3) / 4;
     const long long total = (long long)ntx * nzb;
-    int sms = 0, per_sm = 0;
+    int sms = 0, smem_sm = 0;
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->d.device));
     const size_t smem = fused_smem_bytes(s->d.wave, s->d.prec);
-    int smem_sm = 0;
     CK(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, s->d.device));
-    per_sm = std::max(1, std::min(8, (int)(smem_sm / (smem + 1024))));
+    const int per_sm = std::max(1, std::min(2, (int)(smem_sm / (smem + 1024))));
     long long nb = (long long)sms * per_sm;
     nb = std::min(nb, total);
     nb = std::max(nb, (long long)(ntx + 5) / 6);  // at most ~7 items per CTA
+    auto envd = [](const char *k, double dflt) {
+        const char *v = getenv(k);
+        return v ? atof(v) : dflt;
+    };
+    const double wx = envd("FD23_COST_XPML", 2.5), wz = envd("FD23_COST_ZPML", 1.5);
+    const bool top = s->d.topabsorb != 0;
+    std::vector<double> cum((size_t)total + 1, 0.0);
+    for (long long b = 0; b < total; ++b) {
+        const int strip = (int)(b / nzb), zb = (int)(b % nzb);
+        const int x0 = strip * g.tile_x;
+        const bool xp = (x0 - 4 < std::max(npml, 4)) || (x0 + g.tile_x + 4 > std::min(nx - npml, nx - 4));
+        const int r0 = 4 * zb, r1 = r0 + 3;
+        const bool zp = (r1 >= std::min(nz - npml, nz - 4)) || r0 < 4 || (top && r0 < npml);
+        cum[b + 1] = cum[b] + (xp ? wx : (zp ? wz : 1.0));
+    }
     std::vector<WorkItem> items;
     std::vector<int> off;
     off.push_back(0);
+    long long b0 = 0;
     for (long long c = 0; c < nb; ++c) {
-        long long b0 = c * total / nb, b1 = (c + 1) * total / nb;
+        long long b1;
+        if (c == nb - 1) {
+            b1 = total;
+        } else {
+            const double target = cum[total] * (double)(c + 1) / (double)nb;
+            b1 = std::lower_bound(cum.begin() + b0 + 1, cum.end(), target) - cum.begin();
+            b1 = std::max(b1, b0 + 1);
+            b1 = std::min(b1, total - (nb - 1 - c));  // leave a block for every later CTA
+        }
         while (b0 < b1) {
             const int strip = (int)(b0 / nzb);
             const long long send = (long long)(strip + 1) * nzb;

@@ -535,6 +535,26 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
                     }
                 } else {
                     // ---- general cells: edges (reduced order), CPML, free surface, outside ----
+                    // memory variables first, so their load latency overlaps the derivatives
+                    C psx[2][4], psz[2][4];
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        const int ix = x + e;
+                        psx[0][e] = psx[1][e] = psz[0][e] = psz[1][e] = (C)0;
+                        if (!inrow || ix < 0 || ix >= nx) continue;
+                        const bool top = j < npml && sh.topabsorb;
+                        if (ix < npml || ix >= nx - npml) {
+                            const long long px = ix < npml ? (long long)ix + (long long)j * 2 * npml
+                                                           : (long long)npml + nx - 1 - ix + (long long)j * 2 * npml;
+                            if constexpr (PSV) { psx[0][e] = prd[2][px]; psx[1][e] = prd[3][px]; }
+                            else psx[0][e] = prd[1][px];
+                        }
+                        if (top || j >= nz - npml) {
+                            const long long pz = top ? (long long)j * nx + ix : (long long)(npml + nz - 1 - j) * nx + ix;
+                            if constexpr (PSV) { psz[0][e] = prd[7][pz]; psz[1][e] = prd[6][pz]; }
+                            else psz[0][e] = prd[3][pz];
+                        }
+                    }
                     C cc[4][4];
 #pragma unroll
                     for (int e = 0; e < 4; ++e) cell_coef<C>(x + e, j, nx, nz, cc[e][0], cc[e][1], cc[e][2], cc[e][3]);
@@ -588,11 +608,11 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
                             C txx = told[0][e], txz = told[1][e], tzz = told[2][e];
                             // x chain, PD/fd/cu_fd.cu:303-326
                             if (xp) {
-                                const C pu = fmaC<C>(cp[2 * nx + ix], prd[2][px], cp[B + 2 * nx + ix] * ux);
+                                const C pu = fmaC<C>(cp[2 * nx + ix], psx[0][e], cp[B + 2 * nx + ix] * ux);
                                 const C t = fmaC<C>(ux, cp[2 * B + 2 * nx + ix], pu);
                                 txx = fmaC<C>(gam, t, txx);
                                 tzz = fmaC<C>(lam, t, tzz);
-                                const C pw = fmaC<C>(cp[3 * nx + ix], prd[3][px], cp[B + 3 * nx + ix] * wx);
+                                const C pw = fmaC<C>(cp[3 * nx + ix], psx[1][e], cp[B + 3 * nx + ix] * wx);
                                 txz = fmaC<C>(mua, fmaC<C>(wx, cp[2 * B + 3 * nx + ix], pw), txz);
                                 if (own) { pwr[2][px] = pu; pwr[3][px] = pw; }
                             } else if (j != 0) {
@@ -603,11 +623,11 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
                             // z chain, :328-355
                             if (zp) {
                                 const int zb = 4 * nx;
-                                const C pw = fmaC<C>(cp[zb + 3 * nz + j], prd[7][pz], cp[B + zb + 3 * nz + j] * wz);
+                                const C pw = fmaC<C>(cp[zb + 3 * nz + j], psz[0][e], cp[B + zb + 3 * nz + j] * wz);
                                 const C t = fmaC<C>(wz, cp[2 * B + zb + 3 * nz + j], pw);
                                 txx = fmaC<C>(lam, t, txx);
                                 tzz = fmaC<C>(gam, t, tzz);
-                                const C pu = fmaC<C>(cp[zb + 2 * nz + j], prd[6][pz], cp[B + zb + 2 * nz + j] * uz);
+                                const C pu = fmaC<C>(cp[zb + 2 * nz + j], psz[1][e], cp[B + zb + 2 * nz + j] * uz);
                                 txz = fmaC<C>(mua, fmaC<C>(uz, cp[2 * B + zb + 2 * nz + j], pu), txz);
                                 if (own) { pwr[7][pz] = pw; pwr[6][pz] = pu; }
                             } else if (j == 0) {
@@ -625,15 +645,15 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
                         } else {
                             // SH stress, SH/fd/cu_fd.cu:77-171; cells skipped there keep their values
                             if (ix == 0 || ix >= nx - 1 || j >= nz - 1) {
-                                if (own && xp) pwr[1][px] = prd[1][px];
-                                if (own && zp) pwr[3][pz] = prd[3][pz];
+                                if (own && xp) pwr[1][px] = psx[0][e];
+                                if (own && zp) pwr[3][pz] = psz[0][e];
                                 continue;
                             }
                             const C dxv = dA[e], dzv = dB[e];
                             const C mux = ms[0][e], muz = ms[1][e];
                             C tx = told[0][e], tz = told[1][e];
                             if (xp) {
-                                const C a = fmaC<C>(cp[nx + ix], prd[1][px], cp[B + nx + ix] * dxv);
+                                const C a = fmaC<C>(cp[nx + ix], psx[0][e], cp[B + nx + ix] * dxv);
                                 if (own) pwr[1][px] = a;
                                 tx = fmaC<C>(mux, fmaC<C>(dxv, cp[2 * B + nx + ix], a), tx);
                             } else {
@@ -641,7 +661,7 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
                             }
                             if (zp) {
                                 const int zb = 2 * nx;
-                                const C a = fmaC<C>(cp[zb + nz + j], prd[3][pz], cp[B + zb + nz + j] * dzv);
+                                const C a = fmaC<C>(cp[zb + nz + j], psz[0][e], cp[B + zb + nz + j] * dzv);
                                 if (own) pwr[3][pz] = a;
                                 tz = fmaC<C>(muz, fmaC<C>(dzv, cp[2 * B + zb + nz + j], a), tz);
                             } else {
@@ -780,6 +800,25 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
                             }
                         }
                     } else {
+                        C psx[2][4], psz[2][4];
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) {
+                            const int ix = x + e;
+                            psx[0][e] = psx[1][e] = psz[0][e] = psz[1][e] = (C)0;
+                            if (ix >= nx) continue;
+                            const bool top = a < npml && sh.topabsorb;
+                            if (ix < npml || ix >= nx - npml) {
+                                const long long px = ix < npml ? (long long)ix + (long long)a * 2 * npml
+                                                               : (long long)npml + nx - 1 - ix + (long long)a * 2 * npml;
+                                psx[0][e] = prd[0][px];
+                                if constexpr (PSV) psx[1][e] = prd[1][px];
+                            }
+                            if (top || a >= nz - npml) {
+                                const long long pz = top ? (long long)a * nx + ix : (long long)(npml + nz - 1 - a) * nx + ix;
+                                if constexpr (PSV) { psz[0][e] = prd[5][pz]; psz[1][e] = prd[4][pz]; }
+                                else psz[0][e] = prd[2][pz];
+                            }
+                        }
                         C cc[4][4];
 #pragma unroll
                         for (int e = 0; e < 4; ++e) cell_coef<C>(x + e, a, nx, nz, cc[e][0], cc[e][1], cc[e][2], cc[e][3]);
@@ -835,10 +874,10 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
                                 C u = vold[0][e], w = vold[1][e];
                                 // x chain, PD/fd/cu_fd.cu:455-474
                                 if (xp) {
-                                    const C pa = fmaC<C>(cp[ix], prd[0][px], cp[B + ix] * dxTxx);
+                                    const C pa = fmaC<C>(cp[ix], psx[0][e], cp[B + ix] * dxTxx);
                                     pwr[0][px] = pa;
                                     u = fmaC<C>(bu, fmaC<C>(dxTxx, cp[2 * B + ix], pa), u);
-                                    const C pb = fmaC<C>(cp[nx + ix], prd[1][px], cp[B + nx + ix] * dxTxz);
+                                    const C pb = fmaC<C>(cp[nx + ix], psx[1][e], cp[B + nx + ix] * dxTxz);
                                     pwr[1][px] = pb;
                                     w = fmaC<C>(bw, fmaC<C>(dxTxz, cp[2 * B + nx + ix], pb), w);
                                 } else if (a != 0) {
@@ -848,8 +887,8 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
                                 // z chain, :476-499
                                 if (zp) {
                                     const int zb = 4 * nx;
-                                    const C pa = fmaC<C>(cp[zb + nz + a], prd[5][pz], cp[B + zb + nz + a] * dzTxz);
-                                    const C pb = fmaC<C>(cp[zb + a], prd[4][pz], cp[B + zb + a] * dzTzz);
+                                    const C pa = fmaC<C>(cp[zb + nz + a], psz[0][e], cp[B + zb + nz + a] * dzTxz);
+                                    const C pb = fmaC<C>(cp[zb + a], psz[1][e], cp[B + zb + a] * dzTzz);
                                     pwr[5][pz] = pa;
                                     pwr[4][pz] = pb;
                                     u = fmaC<C>(bu, fmaC<C>(dzTxz, cp[2 * B + zb + nz + a], pa), u);
@@ -868,7 +907,7 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
                                 const C bv = mv[0][e];
                                 C v = vold[0][e];
                                 if (xp) {
-                                    const C pa = fmaC<C>(cp[ix], prd[0][px], cp[B + ix] * dxT);
+                                    const C pa = fmaC<C>(cp[ix], psx[0][e], cp[B + ix] * dxT);
                                     pwr[0][px] = pa;
                                     v = fmaC<C>(bv, fmaC<C>(dxT, cp[2 * B + ix], pa), v);
                                 } else {
@@ -876,7 +915,7 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
                                 }
                                 if (zp) {
                                     const int zb = 2 * nx;
-                                    const C pa = fmaC<C>(cp[zb + a], prd[2][pz], cp[B + zb + a] * dzT);
+                                    const C pa = fmaC<C>(cp[zb + a], psz[0][e], cp[B + zb + a] * dzT);
                                     pwr[2][pz] = pa;
                                     v = fmaC<C>(bv, fmaC<C>(dzT, cp[2 * B + zb + a], pa), v);
                                 } else {
