@@ -88,9 +88,9 @@ __device__ __forceinline__ uint64_t globaltimer_ns()
 }
 
 // Bounded wait: gives up after ~2 s, sets the error flag and returns false.
-__device__ __noinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, int *err_flag)
+// The first try is inlined; the polling loop is out of line.
+__device__ __noinline__ bool mbar_wait_slow(uint64_t *bar, uint32_t parity, int *err_flag)
 {
-    if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = globaltimer_ns();
     for (uint32_t n = 0;; ++n) {
         if (mbar_try_wait(bar, parity)) return true;
@@ -99,6 +99,10 @@ __device__ __noinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, i
             return false;
         }
     }
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, int *err_flag)
+{
+    return mbar_try_wait(bar, parity) || mbar_wait_slow(bar, parity, err_flag);
 }
 
 // ---------------------------------------------------------------------------
@@ -282,7 +286,7 @@ struct Cfg {
     static constexpr int NMS = PSV ? 3 : 2;    // stress-update material
     static constexpr int NMV = PSV ? 2 : 1;    // velocity-update material
     static constexpr int NPF = NT + NMS + NMV; // point-wise fields per row
-    static constexpr int NUW = 5, NPW = 3, NTR = 4;
+    static constexpr int NUW = 8, NPW = 3, NTR = 4;  // NUW, NTR powers of two
     static constexpr int UW_ELEMS = NUW * 4 * NV * UWW;
     static constexpr int PW_ELEMS = NPW * NPF * 4 * PWW;
     static constexpr int TR_ELEMS = NTR * 4 * NT * SW;
@@ -291,7 +295,7 @@ struct Cfg {
     static constexpr int MINB = sizeof(S) == 8 ? 1 : 2;  // CTAs per SM the registers must allow
     static constexpr size_t RING_BYTES =
         (((size_t)(UW_ELEMS + PW_ELEMS + TR_ELEMS) * sizeof(S) + 15) & ~(size_t)15);
-    static constexpr size_t SMEM = RING_BYTES + 128 /* 16 barriers */ + MAX_ITEMS * 16 +
+    static constexpr size_t SMEM = RING_BYTES + 256 /* 2*(NUW+NPW) barriers */ + MAX_ITEMS * 16 +
                                    (size_t)MAX_ITEMS * MAX_TERMS * 16;
 };
 
@@ -316,7 +320,7 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw + K::RING_BYTES);
     uint64_t *full_uw = bars, *empty_uw = bars + K::NUW;
     uint64_t *full_pw = bars + 2 * K::NUW, *empty_pw = full_pw + K::NPW;
-    ItemInfo *info = reinterpret_cast<ItemInfo *>(bars + 16);
+    ItemInfo *info = reinterpret_cast<ItemInfo *>(bars + 32);
     int4 *tlist = reinterpret_cast<int4 *>(info + K::MAX_ITEMS);
     __shared__ int tcount[K::MAX_ITEMS];
 
@@ -480,13 +484,12 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
             // ================= stress: row j, cells x .. x+3 =================
             {
                 const int j = I.z0 - 4 + 4 * i + grp;
+                // stencil rows j-4 .. j+4: ring row (4*(uw_base+i) + grp + d) mod 4*NUW
                 const S *urow[9];
+                const int rseq = 4 * (uw_base + i) + grp;
 #pragma unroll
-                for (int d = 0; d < 9; ++d) {
-                    const int rel = 4 * i + grp + d;  // (j-4+d) - (z0-8)
-                    const int e = uw_base + (rel >> 2);
-                    urow[d] = uw_s + ((size_t)((e % K::NUW) * 4 + (rel & 3)) * K::NV) * K::UWW + 4 * lane + 4;
-                }
+                for (int d = 0; d < 9; ++d)
+                    urow[d] = uw_s + ((rseq + d) & (4 * K::NUW - 1)) * (K::NV * K::UWW) + 4 * lane + 4;
                 const bool inrow = j >= 0 && j < nz;
                 const bool zfast = j >= 4 && j <= nz - 5 && j < nz - npml && !(sh.topabsorb && j < npml);
                 C tnew[K::NT][4];
@@ -689,8 +692,7 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
                 }
                 // ---- stress ring (every column) and HBM (owned cells) ----
                 {
-                    const int rel = 4 * i + grp;  // j - (z0-4)
-                    S *tr = tr_s + ((size_t)((gflat % K::NTR) * 4 + (rel & 3)) * K::NT) * K::SW + 4 * lane;
+                    S *tr = tr_s + ((4 * gflat + grp) & (4 * K::NTR - 1)) * (K::NT * K::SW) + 4 * lane;
 #pragma unroll
                     for (int f = 0; f < K::NT; ++f) Vec4<S, C>::st(tr + f * K::SW, tnew[f]);
                 }
@@ -712,10 +714,10 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
             ok = compute_bar_and(NCT, ok) != 0;
             if (!ok) break;
 
-            auto trrow = [=](int r) -> const S * {  // stress ring row r (absolute), column of cell x
-                const int rel = r - (I.z0 - 4);
-                const int slot = (gflat - i + (rel >> 2)) % K::NTR;
-                return tr_s + ((size_t)(slot * 4 + (rel & 3)) * K::NT) * K::SW + 4 * lane;
+            // stress ring row r (absolute): ring row (4*(gflat-i) + r-(z0-4)) mod 4*NTR
+            const int tseq = 4 * (gflat - i) - (I.z0 - 4);
+            auto trrow = [=](int r) -> const S * {
+                return tr_s + ((tseq + r) & (4 * K::NTR - 1)) * (K::NT * K::SW) + 4 * lane;
             };
             if constexpr (!PSV) {
                 // free-surface stress image Tz(x,0) = -Tz(x,1), SH/fd/cu_fd.cu:226,
@@ -748,7 +750,7 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
 #pragma unroll
                     for (int m = 0; m < K::NMV; ++m) Vec4<S, C>::ld(pwrow(K::NT + K::NMS + m), mv[m]);
                     const int rel = 4 * i + grp;  // a - (z0-8): block i, row grp
-                    const S *vrow = uw_s + ((size_t)(((uw_base + i) % K::NUW) * 4 + (rel & 3)) * K::NV) * K::UWW + 4 * lane + 4;
+                    const S *vrow = uw_s + ((4 * (uw_base + i) + (rel & 3)) & (4 * K::NUW - 1)) * (K::NV * K::UWW) + 4 * lane + 4;
                     C vold[K::NV][4];
 #pragma unroll
                     for (int v = 0; v < K::NV; ++v) Vec4<S, C>::ld(vrow + v * K::UWW, vold[v]);

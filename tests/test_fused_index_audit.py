@@ -18,7 +18,7 @@ import pytest
 XPAD = ZPAD = 8
 TX, SW = 120, 128
 UWW = SW + 8
-NUW, NPW, NTR = 5, 3, 4
+NUW, NPW, NTR = 8, 3, 4
 MAX_ITEMS = 8
 
 
