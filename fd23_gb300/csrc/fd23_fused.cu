@@ -569,9 +569,9 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
                         zcol<S, C>(urow, 0, zv);
 #pragma unroll
                         for (int e = 0; e < 4; ++e) {
-                            const C *c = cc[e];
-                            dA[e] = PSV ? dmx<C>(h, e, c[0], c[1], c[2], c[3]) : dpx<C>(h, e, c[0], c[1], c[2], c[3]);
-                            dB[e] = comb<C>(c[0], c[1], c[2], c[3], zv[4][e] - zv[3][e], zv[5][e] - zv[2][e],
+                            
+                            dA[e] = PSV ? dmx<C>(h, e, cc[e][0], cc[e][1], cc[e][2], cc[e][3]) : dpx<C>(h, e, cc[e][0], cc[e][1], cc[e][2], cc[e][3]);
+                            dB[e] = comb<C>(cc[e][0], cc[e][1], cc[e][2], cc[e][3], zv[4][e] - zv[3][e], zv[5][e] - zv[2][e],
                                             zv[6][e] - zv[1][e], zv[7][e] - zv[0][e]);
                         }
                     }
@@ -581,9 +581,9 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
                         zcol<S, C>(urow, K::UWW, zv);
 #pragma unroll
                         for (int e = 0; e < 4; ++e) {
-                            const C *c = cc[e];
-                            dC[e] = dpx<C>(h, e, c[0], c[1], c[2], c[3]);
-                            dD[e] = comb<C>(c[0], c[1], c[2], c[3], zv[5][e] - zv[4][e], zv[6][e] - zv[3][e],
+                            
+                            dC[e] = dpx<C>(h, e, cc[e][0], cc[e][1], cc[e][2], cc[e][3]);
+                            dD[e] = comb<C>(cc[e][0], cc[e][1], cc[e][2], cc[e][3], zv[5][e] - zv[4][e], zv[6][e] - zv[3][e],
                                             zv[7][e] - zv[2][e], zv[8][e] - zv[1][e]);
                         }
                     }
@@ -675,27 +675,29 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
                         }
                     }
                 }
-                // ---- point source (terms in list order) ----
+                // ---- stress ring (every column) ----
+                S *tr = tr_s + ((4 * gflat + grp) & (4 * K::NTR - 1)) * (K::NT * K::SW) + 4 * lane;
+#pragma unroll
+                for (int f = 0; f < K::NT; ++f) Vec4<S, C>::st(tr + f * K::SW, tnew[f]);
+                // ---- point source (terms in list order), as read-modify-writes of
+                // the ring cells just written (keeps tnew in registers) ----
                 if (ntl > 0) {
+                    bool hit = false;
                     for (int t = 0; t < ntl; ++t) {
                         const int4 tm = tl[t];  // (field, ix, iz, term index)
                         const int fi = tm.x - K::NV;
                         if (fi >= 0 && tm.z == j && tm.y >= x && tm.y < x + 4) {
-                            const C a = sh.tamp[(long long)tm.w * sh.tamp_nt + it];
-#pragma unroll
-                            for (int f = 0; f < K::NT; ++f)
-#pragma unroll
-                                for (int e = 0; e < 4; ++e)
-                                    if (f == fi && e == tm.y - x) tnew[f][e] = through<S, C>(tnew[f][e]) + a;
+                            S *cell = tr + fi * K::SW + (tm.y - x);
+                            *cell = to_s<S>(to_c<C>(*cell) + sh.tamp[(long long)tm.w * sh.tamp_nt + it]);
+                            hit = true;
                         }
                     }
-                }
-                // ---- stress ring (every column) and HBM (owned cells) ----
-                {
-                    S *tr = tr_s + ((4 * gflat + grp) & (4 * K::NTR - 1)) * (K::NT * K::SW) + 4 * lane;
+                    if (hit) {
 #pragma unroll
-                    for (int f = 0; f < K::NT; ++f) Vec4<S, C>::st(tr + f * K::SW, tnew[f]);
+                        for (int f = 0; f < K::NT; ++f) Vec4<S, C>::ld(tr + f * K::SW, tnew[f]);
+                    }
                 }
+                // ---- HBM (owned cells) ----
                 if (inrow && own_x && j >= I.z0 && j < I.z1 && x < nx) {
                     const long long o = origin + (long long)j * pitch + x;
                     if (x + 3 < nx) {
@@ -756,18 +758,21 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
                     for (int v = 0; v < K::NV; ++v) Vec4<S, C>::ld(vrow + v * K::UWW, vold[v]);
                     const bool zfast = a >= 4 && a <= nz - 5 && a < nz - npml && !(sh.topabsorb && a < npml);
                     C vnew[K::NV][4];
-                    // line force on V, injected before the velocity update (SH only)
+                    // line force on V, injected before the velocity update (SH only);
+                    // read-modify-write of this thread's own cell of stencil row a,
+                    // which no stress update reads any more
                     if constexpr (!PSV) {
                         if (ntl > 0) {
+                            bool hit = false;
                             for (int t = 0; t < ntl; ++t) {
                                 const int4 tm = tl[t];
                                 if (tm.x == FD23_V && tm.z == a && tm.y >= x && tm.y < x + 4) {
-                                    const C amp = sh.tamp[(long long)tm.w * sh.tamp_nt + it];
-#pragma unroll
-                                    for (int e = 0; e < 4; ++e)
-                                        if (e == tm.y - x) vold[0][e] = through<S, C>(vold[0][e]) + amp;
+                                    S *cell = const_cast<S *>(vrow) + (tm.y - x);
+                                    *cell = to_s<S>(to_c<C>(*cell) + sh.tamp[(long long)tm.w * sh.tamp_nt + it]);
+                                    hit = true;
                                 }
                             }
+                            if (hit) Vec4<S, C>::ld(vrow, vold[0]);
                         }
                     }
                     if (xfast && zfast) {
@@ -832,8 +837,8 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
                             ld12<S, C>(trow[4], h);
 #pragma unroll
                             for (int e = 0; e < 4; ++e) {
-                                const C *c = cc[e];
-                                dA[e] = PSV ? dpx<C>(h, e, c[0], c[1], c[2], c[3]) : dmx<C>(h, e, c[0], c[1], c[2], c[3]);
+                                
+                                dA[e] = PSV ? dpx<C>(h, e, cc[e][0], cc[e][1], cc[e][2], cc[e][3]) : dmx<C>(h, e, cc[e][0], cc[e][1], cc[e][2], cc[e][3]);
                             }
                         }
                         {
@@ -842,9 +847,9 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
                             zcol<S, C>(trow, K::SW, zv);
 #pragma unroll
                             for (int e = 0; e < 4; ++e) {
-                                const C *c = cc[e];
-                                if constexpr (PSV) dB[e] = dmx<C>(h, e, c[0], c[1], c[2], c[3]);
-                                dC[e] = comb<C>(c[0], c[1], c[2], c[3], zv[5][e] - zv[4][e], zv[6][e] - zv[3][e],
+                                
+                                if constexpr (PSV) dB[e] = dmx<C>(h, e, cc[e][0], cc[e][1], cc[e][2], cc[e][3]);
+                                dC[e] = comb<C>(cc[e][0], cc[e][1], cc[e][2], cc[e][3], zv[5][e] - zv[4][e], zv[6][e] - zv[3][e],
                                                 zv[7][e] - zv[2][e], zv[8][e] - zv[1][e]);
                             }
                         }
@@ -853,8 +858,8 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
                             zcol<S, C>(trow, 2 * K::SW, zv);
 #pragma unroll
                             for (int e = 0; e < 4; ++e) {
-                                const C *c = cc[e];
-                                dD[e] = comb<C>(c[0], c[1], c[2], c[3], zv[4][e] - zv[3][e], zv[5][e] - zv[2][e],
+                                
+                                dD[e] = comb<C>(cc[e][0], cc[e][1], cc[e][2], cc[e][3], zv[4][e] - zv[3][e], zv[5][e] - zv[2][e],
                                                 zv[6][e] - zv[1][e], zv[7][e] - zv[0][e]);
                             }
                         }
