@@ -24,7 +24,7 @@ import os as _os
 import numpy as _np
 
 _HERE = _os.path.dirname(_os.path.abspath(__file__))
-LIB_PATH = _os.path.join(_HERE, "_lib", "libfd23.so")
+LIB_PATH = _os.environ.get("FD23_LIB") or _os.path.join(_HERE, "_lib", "libfd23.so")
 
 PSV, SH = 0, 1
 F32, F64, BF16, F16 = 0, 1, 2, 3

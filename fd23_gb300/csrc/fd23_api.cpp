@@ -88,6 +88,14 @@ struct fd23_solver {
     bool have_material = false;
     int *err_flag = nullptr;
     double *norm_buf = nullptr;
+    // 16-bit storage forms keep values in range with exact power-of-two scales:
+    // stored velocity = sigma * v, stored stress = sigma * kappa * T; the
+    // stress-update material is stored times kappa, the velocity-update
+    // material divided by kappa.  Both stay 1 for F32 / F64.
+    double kappa = 1.0, sigma = 1.0;
+    bool kappa_set = false, sigma_set = false;
+    std::vector<int> h_tfield;      // source terms as given (for re-scaling)
+    std::vector<double> h_tamp;
     // source
     int nterms = 0;
     int4 *d_terms = nullptr;
@@ -423,6 +431,68 @@ int ensure_record_capacity(fd23_solver *s, int need)
     return FD23_OK;
 }
 
+bool scaled_form(const fd23_solver *s) { return s->d.prec == FD23_BF16 || s->d.prec == FD23_F16; }
+
+double pow2_round(double v)
+{
+    if (!(v > 0) || !std::isfinite(v)) return 1.0;
+    return std::ldexp(1.0, (int)std::lround(std::log2(v)));
+}
+// scale of wavefield f (storage = scale * physical)
+double field_scale(const fd23_solver *s, int f)
+{
+    const bool stress = f >= (s->d.wave == FD23_PSV ? FD23_TXX : FD23_TX);
+    return stress ? s->sigma * s->kappa : s->sigma;
+}
+// memory variable p holds a derivative of a stress (scale sigma*kappa) or of a velocity (sigma)
+double psi_scale(const fd23_solver *s, int p)
+{
+    bool of_stress;
+    if (s->d.wave == FD23_PSV) of_stress = (p == 0 || p == 1 || p == 4 || p == 5);  // Txx_x Txz_x Tzz_z Txz_z
+    else of_stress = (p == 0 || p == 2);                                            // Tx_x Tz_z
+    return of_stress ? s->sigma * s->kappa : s->sigma;
+}
+
+// sigma: chosen once, when material (kappa) and source are known: the power
+// of two that puts the accumulated source stress near 2^8 (room below the
+// FP16 maximum, far above its subnormals)
+int ensure_sigma(fd23_solver *s);
+
+int upload_source_amps(fd23_solver *s)
+{
+    if (s->nterms == 0) return FD23_OK;
+    const size_t nt = (size_t)s->tamp_nt;
+    std::vector<double> a(s->h_tamp);
+    for (int k = 0; k < s->nterms; ++k) {
+        const double sc = field_scale(s, s->h_tfield[k]);
+        for (size_t it = 0; it < nt; ++it) a[k * nt + it] *= sc;
+    }
+    std::vector<unsigned char> tmp(a.size() * s->cs);
+    to_compute(s->d.prec, a.data(), a.size(), tmp.data());
+    CK(cudaMemcpy(s->d_tamp, tmp.data(), tmp.size(), cudaMemcpyHostToDevice));
+    return FD23_OK;
+}
+
+int ensure_sigma(fd23_solver *s)
+{
+    if (!scaled_form(s) || s->sigma_set || !s->kappa_set) return FD23_OK;
+    double peak = 0.0;
+    const int nt = s->tamp_nt;
+    for (int k = 0; k < s->nterms; ++k) {
+        const bool stress = s->h_tfield[k] >= (s->d.wave == FD23_PSV ? FD23_TXX : FD23_TX);
+        double run = 0.0, amax = 0.0;
+        for (int it = 0; it < nt; ++it) {
+            const double a = std::fabs(s->h_tamp[(size_t)k * nt + it]);
+            run += a;
+            amax = std::max(amax, a);
+        }
+        peak = std::max(peak, std::max(run, amax) * (stress ? s->kappa : 1.0));
+    }
+    s->sigma = peak > 0 ? pow2_round(256.0 / peak) : 1.0;
+    s->sigma_set = true;
+    return upload_source_amps(s);
+}
+
 }  // namespace
 
 extern "C" {
@@ -525,9 +595,33 @@ int fd23_set_material(fd23_solver *s, const double *matv)
     if (!s || !matv) return FD23_ERR_ARG;
     CK(cudaSetDevice(s->d.device));
     const size_t n = (size_t)s->d.nx * s->d.nz;
+    const int nms = s->d.wave == FD23_PSV ? 3 : 2;  // stress-update arrays come first
+    if (scaled_form(s) && !s->kappa_set) {
+        // kappa: power of two that brings the largest stress-update and
+        // velocity-update coefficients to the same magnitude
+        double ms = 0.0, mv = 0.0;
+        for (int m = 0; m < s->nmat; ++m)
+            for (size_t k = 0; k < n; ++k) {
+                const double v = std::fabs(matv[m * n + k]);
+                if (m < nms) ms = std::max(ms, v);
+                else mv = std::max(mv, v);
+            }
+        s->kappa = (ms > 0 && mv > 0) ? pow2_round(std::sqrt(mv / ms)) : 1.0;
+        s->kappa_set = true;
+        int rc = upload_source_amps(s);
+        if (rc) return rc;
+    }
     std::vector<unsigned char> tmp(n * s->es);
+    std::vector<double> scaled;
     for (int m = 0; m < s->nmat; ++m) {
-        to_storage(s->d.prec, matv + m * n, n, tmp.data());
+        const double *src = matv + m * n;
+        if (s->kappa != 1.0) {
+            const double f = m < nms ? s->kappa : 1.0 / s->kappa;
+            scaled.assign(src, src + n);
+            for (auto &v : scaled) v *= f;
+            src = scaled.data();
+        }
+        to_storage(s->d.prec, src, n, tmp.data());
         int rc = upload_grid(s, s->mat[m], tmp.data(), s->es);
         if (rc) return rc;
         CK(cudaStreamSynchronize(s->stream));
@@ -580,14 +674,13 @@ int fd23_set_source_terms(fd23_solver *s, int nterms, const int *field, const in
     int rc = dev_alloc((void **)&s->d_terms, t.size() * sizeof(int4));
     if (rc) return rc;
     const size_t na = (size_t)nterms * nt_amp;
-    std::vector<unsigned char> tmp(na * s->cs);
-    to_compute(s->d.prec, amp, na, tmp.data());
-    if ((rc = dev_alloc(&s->d_tamp, tmp.size()))) return rc;
+    if ((rc = dev_alloc(&s->d_tamp, na * s->cs))) return rc;
     CK(cudaMemcpy(s->d_terms, t.data(), nterms * sizeof(int4), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(s->d_tamp, tmp.data(), tmp.size(), cudaMemcpyHostToDevice));
     s->nterms = nterms;
     s->tamp_nt = nt_amp;
-    return FD23_OK;
+    s->h_tfield.assign(field, field + nterms);
+    s->h_tamp.assign(amp, amp + na);
+    return upload_source_amps(s);
 }
 
 int fd23_set_source(fd23_solver *s, int kind, int xs, int zs, const double *moment, const double *src,
@@ -660,6 +753,8 @@ int fd23_run(fd23_solver *s, int nsteps, int itrecord)
     if (!s || nsteps < 0 || itrecord <= 0) return FD23_ERR_ARG;
     if (!s->have_material) return FD23_ERR_ORDER;
     CK(cudaSetDevice(s->d.device));
+    int rc0 = ensure_sigma(s);
+    if (rc0) return rc0;
     int nrec_new = 0;
     for (int k = 0; k < nsteps; ++k)
         if ((s->it + k) % itrecord == 0) ++nrec_new;
@@ -712,6 +807,11 @@ int fd23_get_seismograms(fd23_solver *s, int field, void *out, size_t out_bytes,
     if (!out) return FD23_OK;
     if (out_bytes < need) return FD23_ERR_ARG;
     if (need) CK(cudaMemcpy(out, s->d_seis[field], need, cudaMemcpyDeviceToHost));
+    if (s->sigma != 1.0) {  // velocities are stored times sigma (exact power of two)
+        const float inv = (float)(1.0 / s->sigma);
+        float *o = (float *)out;
+        for (size_t k = 0; k < need / sizeof(float); ++k) o[k] *= inv;
+    }
     return FD23_OK;
 }
 
@@ -736,7 +836,9 @@ size_t fd23_state_bytes(fd23_solver *s)
 int fd23_get_state(fd23_solver *s, void *buf, size_t bytes)
 {
     if (!s || !buf || bytes < fd23_state_bytes(s)) return FD23_ERR_ARG;
-    int rc = fd23_sync(s);
+    int rc = ensure_sigma(s);
+    if (rc) return rc;
+    rc = fd23_sync(s);
     if (rc) return rc;
     const size_t n = (size_t)s->d.nx * s->d.nz;
     unsigned char *o = (unsigned char *)buf;
@@ -746,11 +848,19 @@ int fd23_get_state(fd23_solver *s, void *buf, size_t bytes)
         if ((rc = download_grid(s, s->fld[s->par][f], tmp.data(), s->es))) return rc;
         CK(cudaStreamSynchronize(s->stream));
         storage_to_compute(s->d.prec, tmp.data(), n, o);
+        if (scaled_form(s)) {
+            const float inv = (float)(1.0 / field_scale(s, f));
+            for (size_t k = 0; k < n; ++k) ((float *)o)[k] *= inv;
+        }
         o += n * s->cs;
     }
     for (int p = 0; p < s->npsi; ++p) {
         const size_t b = s->psi_elems[p] * s->cs;
         if (b) CK(cudaMemcpy(o, s->psi[s->par][p], b, cudaMemcpyDeviceToHost));
+        if (scaled_form(s)) {
+            const float inv = (float)(1.0 / psi_scale(s, p));
+            for (size_t k = 0; k < s->psi_elems[p]; ++k) ((float *)o)[k] *= inv;
+        }
         o += b;
     }
     return FD23_OK;
@@ -762,10 +872,18 @@ int fd23_set_state(fd23_solver *s, const void *buf, size_t bytes, int it0)
     CK(cudaSetDevice(s->d.device));
     int rc = zero_state(s);
     if (rc) return rc;
+    if ((rc = ensure_sigma(s))) return rc;
     const size_t n = (size_t)s->d.nx * s->d.nz;
     const unsigned char *in = (const unsigned char *)buf;
     std::vector<unsigned char> tmp(n * s->es);
+    std::vector<float> sc;
     for (int f = 0; f < s->nfld; ++f) {
+        if (scaled_form(s)) {
+            const float m = (float)field_scale(s, f);
+            sc.assign((const float *)in, (const float *)in + n);
+            for (auto &v : sc) v *= m;
+            compute_to_storage(s->d.prec, (const unsigned char *)sc.data(), n, tmp.data());
+        } else
         compute_to_storage(s->d.prec, in, n, tmp.data());
         if ((rc = upload_grid(s, s->fld[0][f], tmp.data(), s->es))) return rc;
         CK(cudaStreamSynchronize(s->stream));
@@ -773,7 +891,14 @@ int fd23_set_state(fd23_solver *s, const void *buf, size_t bytes, int it0)
     }
     for (int p = 0; p < s->npsi; ++p) {
         const size_t b = s->psi_elems[p] * s->cs;
-        if (b) CK(cudaMemcpy(s->psi[0][p], in, b, cudaMemcpyHostToDevice));
+        if (b && scaled_form(s)) {
+            const float m = (float)psi_scale(s, p);
+            sc.assign((const float *)in, (const float *)in + s->psi_elems[p]);
+            for (auto &v : sc) v *= m;
+            CK(cudaMemcpy(s->psi[0][p], sc.data(), b, cudaMemcpyHostToDevice));
+        } else if (b) {
+            CK(cudaMemcpy(s->psi[0][p], in, b, cudaMemcpyHostToDevice));
+        }
         in += b;
     }
     s->it = it0;

@@ -286,7 +286,11 @@ struct Cfg {
     static constexpr int NMS = PSV ? 3 : 2;    // stress-update material
     static constexpr int NMV = PSV ? 2 : 1;    // velocity-update material
     static constexpr int NPF = NT + NMS + NMV; // point-wise fields per row
-    static constexpr int NUW = 8, NPW = 3, NTR = 4;  // NUW, NTR powers of two
+#ifndef FD23_FUSED_NPW
+#define FD23_FUSED_NPW 3
+#endif
+    // ring depths: NUW and NTR must be powers of two
+    static constexpr int NUW = 8, NPW = FD23_FUSED_NPW, NTR = 4;
     static constexpr int UW_ELEMS = NUW * 4 * NV * UWW;
     static constexpr int PW_ELEMS = NPW * NPF * 4 * PWW;
     static constexpr int TR_ELEMS = NTR * 4 * NT * SW;
