@@ -306,10 +306,10 @@ int build_worklist(fd23_solver *s)
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->d.device));
     const size_t smem = fused_smem_bytes(s->d.wave, s->d.prec);
     CK(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, s->d.device));
-    const int per_sm = std::max(1, std::min(2, (int)(smem_sm / (smem + 1024))));
+    const int per_sm = std::max(1, std::min(3, (int)(smem_sm / (smem + 1024))));
     long long nb = (long long)sms * per_sm;
     nb = std::min(nb, total);
-    nb = std::max(nb, (long long)(ntx + 5) / 6);  // at most ~7 items per CTA
+    nb = std::max(nb, (long long)(ntx + 1) / 2);  // keeps every CTA within 4 items
     auto envd = [](const char *k, double dflt) {
         const char *v = getenv(k);
         return v ? atof(v) : dflt;
@@ -350,7 +350,7 @@ int build_worklist(fd23_solver *s)
         off.push_back((int)items.size());
     }
     for (size_t c = 0; c + 1 < off.size(); ++c)
-        if (off[c + 1] - off[c] > 8) return FD23_ERR_ARG;
+        if (off[c + 1] - off[c] > 4) return FD23_ERR_ARG;
     if (s->d_items) cudaFree(s->d_items);
     if (s->d_item_off) cudaFree(s->d_item_off);
     s->d_items = nullptr;

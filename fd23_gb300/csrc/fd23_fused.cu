@@ -287,16 +287,20 @@ struct Cfg {
     static constexpr int NMV = PSV ? 2 : 1;    // velocity-update material
     static constexpr int NPF = NT + NMS + NMV; // point-wise fields per row
 #ifndef FD23_FUSED_NPW
-#define FD23_FUSED_NPW 3
+#define FD23_FUSED_NPW 2
 #endif
-    // ring depths: NUW and NTR must be powers of two
-    static constexpr int NUW = 8, NPW = FD23_FUSED_NPW, NTR = 4;
+#ifndef FD23_FUSED_NUW
+#define FD23_FUSED_NUW 4
+#endif
+    // ring depths (NUW and NTR powers of two): sized so that three CTAs of the
+    // 4-byte forms fit in the 228 KB of shared memory of one SM
+    static constexpr int NUW = FD23_FUSED_NUW, NPW = FD23_FUSED_NPW, NTR = 4;
     static constexpr int UW_ELEMS = NUW * 4 * NV * UWW;
     static constexpr int PW_ELEMS = NPW * NPF * 4 * PWW;
     static constexpr int TR_ELEMS = NTR * 4 * NT * SW;
-    static constexpr int MAX_ITEMS = 8;
+    static constexpr int MAX_ITEMS = 4;
     static constexpr int MAX_TERMS = 16;
-    static constexpr int MINB = sizeof(S) == 8 ? 1 : 2;  // CTAs per SM the registers must allow
+    static constexpr int MINB = sizeof(S) == 8 ? 1 : 3;  // CTAs per SM the registers must allow
     static constexpr size_t RING_BYTES =
         (((size_t)(UW_ELEMS + PW_ELEMS + TR_ELEMS) * sizeof(S) + 15) & ~(size_t)15);
     static constexpr size_t SMEM = RING_BYTES + 256 /* 2*(NUW+NPW) barriers */ + MAX_ITEMS * 16 +

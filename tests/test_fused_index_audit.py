@@ -18,8 +18,8 @@ import pytest
 XPAD = ZPAD = 8
 TX, SW = 120, 128
 UWW = SW + 8
-NUW, NPW, NTR = 8, 3, 4
-MAX_ITEMS = 8
+NUW, NPW, NTR = 4, 2, 4
+MAX_ITEMS = 4
 
 
 def layout(nx, nz):
@@ -37,7 +37,7 @@ def worklist(nx, nz, sms=152, per_sm=2, npml=40, wx=2.5, wz=1.5, top=False):
     nzb = (nz + 3) // 4
     total = ntx * nzb
     nb = min(sms * per_sm, total)
-    nb = max(nb, (ntx + 5) // 6)
+    nb = max(nb, (ntx + 1) // 2)
     cum = [0.0]
     for b in range(total):
         strip, zb = divmod(b, nzb)
@@ -133,5 +133,5 @@ SIZES = [(96, 96), (96, 64), (250, 130), (257, 131), (500, 300), (1000, 1000), (
 @pytest.mark.parametrize("nx,nz", SIZES)
 @pytest.mark.parametrize("es,wave", [(4, "psv"), (8, "psv"), (2, "psv"), (4, "sh"), (2, "sh")])
 def test_fused_addresses_in_bounds(nx, nz, es, wave):
-    per_sm = 1 if es == 8 else 2
+    per_sm = 1 if es == 8 else 3
     audit(nx, nz, es, wave, per_sm=per_sm)
