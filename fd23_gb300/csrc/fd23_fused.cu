@@ -352,17 +352,8 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
         pwr[f] = par ? sh.psi[0][f] : sh.psi[1][f];
     }
 
-    // ---- receivers of the previous step (buffer set `par` is read-only here) ----
-    if (rec_index >= 0) {
-        for (int r = blockIdx.x * K::NTH + tid; r < sh.nrec[0]; r += gridDim.x * K::NTH)
-            sh.seis[0][(long long)rec_index * sh.nrec[0] + r] = to_c<C>(rd[0][sh.rec[0][r]]);
-        for (int r = blockIdx.x * K::NTH + tid; r < sh.nrec[1]; r += gridDim.x * K::NTH)
-            sh.seis[1][(long long)rec_index * sh.nrec[1] + r] = to_c<C>(rd[1][sh.rec[1][r]]);
-    }
-
     const int ibeg = item_off[blockIdx.x], iend = item_off[blockIdx.x + 1];
     const int nitems = min(iend - ibeg, K::MAX_ITEMS);
-    if (nitems <= 0) return;
 
     // ---- per-item set-up: geometry and the source terms inside its stress region ----
     if (tid < nitems) {
@@ -390,6 +381,10 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
+    // Programmatic dependent launch: the next step's grid may start its
+    // prologue now; it waits (griddepcontrol.wait) before it touches any
+    // wavefield or memory variable, all of which this grid still reads/writes.
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 
     int total_iters = 0;
     for (int k = 0; k < nitems; ++k) total_iters += info[k].niter;
@@ -415,12 +410,15 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
             }
         };
         // point-wise operands of iteration i of item I into stage g % NPW
-        auto issue_pw = [=](int g, const ItemInfo &I, int i) {
+        // part 0: everything; 1: arm the stage and copy the material rows only
+        // (they do not depend on the previous step); 2: the old stresses only
+        auto issue_pw = [=](int g, const ItemInfo &I, int i, int part) {
             const int slot = g % K::NPW;
             constexpr uint32_t ROWB = K::PWW * sizeof(S);
-            if (lane == 0) mbar_arrive_expect_tx(&full_pw[slot], ROWB * 4 * K::NPF);
+            if (lane == 0 && part != 2) mbar_arrive_expect_tx(&full_pw[slot], ROWB * 4 * K::NPF);
             __syncwarp();
-            for (int c = lane; c < 4 * K::NPF; c += 32) {
+            const int c0 = part == 1 ? 4 * K::NT : 0, c1 = part == 2 ? 4 * K::NT : 4 * K::NPF;
+            for (int c = c0 + lane; c < c1; c += 32) {
                 const int rr = c & 3, fidx = c >> 2;
                 const S *b = rd[K::NV];
 #pragma unroll
@@ -439,6 +437,16 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
         bool ok = true;
         int e_uw = 0, g_pw = 0;
         int k = 0, base_it = 0, base_uw = 0;
+        // material rows of the first stages ahead of the dependency wait
+        const int npre = min(K::NPW, total_iters);
+        {
+            int kk = 0, bit = 0;
+            for (int g = 0; g < npre; ++g) {
+                while (g >= bit + info[kk].niter) { bit += info[kk].niter; ++kk; }
+                issue_pw(g, info[kk], g - bit, 1);
+            }
+        }
+        asm volatile("griddepcontrol.wait;" ::: "memory");
         for (int g = 0; g < total_iters && ok; ++g) {
             while (g >= base_it + info[k].niter) {
                 base_it += info[k].niter;
@@ -456,7 +464,7 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
             if (g >= K::NPW)
                 ok = mbar_wait_bounded(&empty_pw[g % K::NPW], (uint32_t)(((g / K::NPW) - 1) & 1), err_flag);
             if (ok) {
-                issue_pw(g, info[k], i);
+                issue_pw(g, info[k], i, g < npre ? 2 : 0);
                 g_pw = g + 1;
             }
         }
@@ -469,6 +477,15 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
     }
 
     // ======================= compute warps =======================
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    // ---- receivers of the previous step (buffer set `par` is read-only here) ----
+    if (rec_index >= 0) {
+        for (int r = blockIdx.x * NCT + tid; r < sh.nrec[0]; r += gridDim.x * NCT)
+            sh.seis[0][(long long)rec_index * sh.nrec[0] + r] = to_c<C>(rd[0][sh.rec[0][r]]);
+        for (int r = blockIdx.x * NCT + tid; r < sh.nrec[1]; r += gridDim.x * NCT)
+            sh.seis[1][(long long)rec_index * sh.nrec[1] + r] = to_c<C>(rd[1][sh.rec[1][r]]);
+    }
+
     const int grp = warp;  // row of the 4-row block this warp updates
     const C *cp = sh.cpml;
     const int B = sh.cpml_blk;
@@ -973,9 +990,19 @@ int launch_fused_impl(const Shot<S, C> &s, const WorkItem *items, const int *ite
                       int par, int it, int rec_index, int *err_flag, cudaStream_t st)
 {
     using K = Cfg<S, C, WAVE>;
-    fused_step<S, C, WAVE><<<nblocks, K::NTH, K::SMEM, st>>>(s, items, item_off, par, it, rec_index,
-                                                            err_flag);
-    return cudaPeekAtLastError() == cudaSuccess ? FD23_OK : FD23_ERR_CUDA;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)nblocks);
+    cfg.blockDim = dim3(K::NTH);
+    cfg.dynamicSmemBytes = K::SMEM;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, fused_step<S, C, WAVE>, s, items, item_off, par, it,
+                                             rec_index, err_flag);
+    return e == cudaSuccess ? FD23_OK : FD23_ERR_CUDA;
 }
 
 template <class S, class C, int WAVE>
