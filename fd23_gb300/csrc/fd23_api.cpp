@@ -294,7 +294,7 @@ int dispatch_flush(fd23_solver *s)
 // CTAs get contiguous (strip-major) ranges of equal estimated cost; a range
 // may span two strips (each strip piece is one item).  Blocks that touch the
 // CPML run the general per-cell path and cost more; the relative costs
-// (FD23_COST_XPML, FD23_COST_ZPML, default 2.5 / 1.5) come from profiles.
+// (FD23_COST_XPML, FD23_COST_ZPML, default 4 / 3) were measured on GB300.
 int build_worklist(fd23_solver *s)
 {
     const FusedGeom g = fused_geom(s->d.wave, s->d.prec);
@@ -314,7 +314,7 @@ int build_worklist(fd23_solver *s)
         const char *v = getenv(k);
         return v ? atof(v) : dflt;
     };
-    const double wx = envd("FD23_COST_XPML", 2.5), wz = envd("FD23_COST_ZPML", 1.5);
+    const double wx = envd("FD23_COST_XPML", 4.0), wz = envd("FD23_COST_ZPML", 3.0);
     const bool top = s->d.topabsorb != 0;
     std::vector<double> cum((size_t)total + 1, 0.0);
     for (long long b = 0; b < total; ++b) {

@@ -30,7 +30,7 @@ def layout(nx, nz):
     return pitch, rows, ZPAD * pitch + XPAD
 
 
-def worklist(nx, nz, sms=152, per_sm=2, npml=40, wx=2.5, wz=1.5, top=False):
+def worklist(nx, nz, sms=152, per_sm=2, npml=40, wx=4.0, wz=3.0, top=False):
     """Cost-weighted contiguous partition of the 4-row blocks (build_worklist)."""
     import bisect
     ntx = (nx + TX - 1) // TX
