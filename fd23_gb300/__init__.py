@@ -47,7 +47,7 @@ ABI_FUNCTIONS = [
     "fd23_moment_sh", "fd23_set_receivers", "fd23_receivers_line", "fd23_run", "fd23_sync",
     "fd23_get_seismograms", "fd23_reset", "fd23_get_stream", "fd23_get_step", "fd23_state_bytes", "fd23_get_state",
     "fd23_set_state", "fd23_field_norm2", "fd23_build_material", "fd23_build_cpml",
-    "fd23_build_source_terms",
+    "fd23_build_source_terms", "fd23_sum_squares_noalloc",
 ]
 
 
@@ -109,6 +109,7 @@ def lib():
         "fd23_build_material": ([i, i, i, d, d, vp, vp, vp, vp, vp], i),
         "fd23_build_cpml": ([i, i, i, i, d, d, d, d, vp, sz], i),
         "fd23_build_source_terms": ([i, i, i, i, vp, d, d, vp, i, i, vp, vp, vp, vp, i], i),
+        "fd23_sum_squares_noalloc": ([i, vp, i, sz, vp, _C.POINTER(d), _C.POINTER(i)], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -203,6 +204,20 @@ def build_source_terms(wave, kind, xs, zs, moment, h, dt, src, nt):
                                              len(src), nt, _p(f), _p(x), _p(z), _p(amp), 16),
                "fd23_build_source_terms")
     return f[:n].copy(), x[:n].copy(), z[:n].copy(), _np.ascontiguousarray(amp[:n])
+
+
+def sum_squares_noalloc(prec, field_ptrs, n, stream=0):
+    """Allocation-free FP64 sum of squares of device arrays (raw device
+    pointers, n elements each, element type prec); returns (sum, nonfinite).
+    Callers that cannot allocate device memory use this instead of
+    Solver.norm2; see include/fd23.h for its limits."""
+    ptrs = (_C.c_void_p * max(1, len(field_ptrs)))(*[_C.c_void_p(int(p)) for p in field_ptrs])
+    total = _C.c_double(0.0)
+    bad = _C.c_int(0)
+    _check(lib().fd23_sum_squares_noalloc(_PRECS[prec], _C.cast(ptrs, _C.c_void_p), len(field_ptrs), n,
+                                          _C.c_void_p(int(stream)) if stream else None,
+                                          _C.byref(total), _C.byref(bad)), "fd23_sum_squares_noalloc")
+    return total.value, bool(bad.value)
 
 
 def receivers_line(nsta, ix0, iz0, idx, idz):

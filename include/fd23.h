@@ -170,6 +170,22 @@ int fd23_set_state(fd23_solver *s, const void *buf, size_t bytes, int it0);
  * fields in FP64; returns FD23_ERR_NONFINITE when any value is NaN/Inf. */
 int fd23_field_norm2(fd23_solver *s, double *norm2);
 
+/* ---- allocation-free watchdog ----
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory (code running inside a CUDA stream capture, programs whose device
+ * memory belongs to another allocator): sums the squares of nfields
+ * caller-owned device arrays of n elements each (element type prec) in FP64
+ * into *sum and sets *nonfinite when any value is NaN or Inf -- the same
+ * quantity fd23_field_norm2 computes for a solver -- without allocating.
+ * Its partial sums live in a fixed 16 KiB file-scope device array that every
+ * GPU loading the library keeps until exit.  At most 8 arrays per call (more
+ * returns FD23_ERR_ARG).  The first call on a device looks up that array's
+ * address for the device: make it before any stream capture.  All calls
+ * share the array, so calls that overlap on the GPU race; serialize them.
+ * Runs on `stream` (a cudaStream_t, NULL = default) and waits for it. */
+int fd23_sum_squares_noalloc(int prec, const void *const *fields, int nfields, size_t n,
+                             void *stream, double *sum, int *nonfinite);
+
 /* ---- host-only builders (no GPU needed) ----
  * The same FP64 set-up fd23_set_model / fd23_create / fd23_set_source use,
  * exposed for callers that build inputs themselves.
