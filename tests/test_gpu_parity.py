@@ -176,16 +176,21 @@ def test_reduced_storage_fused_equals_twopass(prec, wave):
     np.testing.assert_array_equal(sa, sb)
 
 
-@pytest.mark.parametrize("prec,tol", [("bf16", 0.2), ("f16", 0.05)])
-def test_reduced_storage_accuracy(prec, tol):
-    """Seismogram relative L2 against the FP64 oracle (tolerance in the
-    parametrisation; 16-bit storage of the accumulating wavefields
-    rounds every step, so the error grows with the number of steps)."""
-    case = Case("psv", 300, 200, nt=150, seed=13, wavelet=("gauss", -8))
+RS_TOL = {("psv", "bf16"): 0.5, ("psv", "f16"): 0.5, ("sh", "bf16"): 0.5, ("sh", "f16"): 0.5}
+
+
+@pytest.mark.parametrize("prec", ["bf16", "f16"])
+@pytest.mark.parametrize("wave,kind", [("psv", 3), ("sh", 2)])
+def test_reduced_storage_accuracy(wave, kind, prec):
+    """Seismogram relative L2 of the 16-bit storage forms against the FP64
+    oracle, 400 steps, receivers inside the wave's reach (tolerances in
+    RS_TOL; FP32 on the same case is at ~1e-6)."""
+    case = Case(wave, 240, 160, nt=400, seed=13, xs=120, zs=20, kind=kind, wavelet=("gauss", -8))
     ref, _ = case.oracle("f64")
     got, _ = _run(case, prec, "fused")
-    for g, r in zip(got, ref):
-        assert O.rel_l2(g, r) < tol
+    errs = [O.rel_l2(g, r) for g, r in zip(got, ref)]
+    print("reduced storage", wave, prec, errs)
+    assert max(errs) < RS_TOL[(wave, prec)], errs
 
 
 def test_norm2_watchdog():
