@@ -176,7 +176,10 @@ def test_reduced_storage_fused_equals_twopass(prec, wave):
     np.testing.assert_array_equal(sa, sb)
 
 
-RS_TOL = {("psv", "bf16"): 0.5, ("psv", "f16"): 0.5, ("sh", "bf16"): 0.5, ("sh", "f16"): 0.5}
+# measured on GB300 (400 steps): P-SV BF16 4.3e-2 / 2.1e-2, FP16 2.9e-3 / 3.2e-3;
+# SH BF16 3.1e-2, FP16 2.7e-3.  Rounding the material to 16 bits alone gives
+# 1.2e-3 (FP16) and 3.4e-2 (BF16) on this case (FP32 oracle, rounded material).
+RS_TOL = {("psv", "bf16"): 6e-2, ("psv", "f16"): 5e-3, ("sh", "bf16"): 5e-2, ("sh", "f16"): 5e-3}
 
 
 @pytest.mark.parametrize("prec", ["bf16", "f16"])
