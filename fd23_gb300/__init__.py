@@ -32,6 +32,8 @@ KERNEL_AUTO, KERNEL_FUSED, KERNEL_TWOPASS = 0, 1, 2
 U, W, TXX, TXZ, TZZ = 0, 1, 2, 3, 4
 V, TX, TZ = 0, 1, 2
 SRC_EXPLOSION, SRC_FORCE, SRC_MOMENT, SRC_MOMENT_P = 1, 2, 3, 13
+OK, ERR_ARG, ERR_CUDA, ERR_UNSTABLE, ERR_ORDER, ERR_NOMEM, ERR_NONFINITE, ERR_TIMEOUT, \
+    ERR_UNSUPPORTED = 0, -1, -2, -3, -4, -5, -6, -7, -8
 
 _WAVES = {"psv": PSV, "sh": SH, PSV: PSV, SH: SH}
 _PRECS = {"f32": F32, "fp32": F32, "f64": F64, "fp64": F64, "bf16": BF16, "f16": F16,
@@ -47,7 +49,10 @@ ABI_FUNCTIONS = [
     "fd23_moment_sh", "fd23_set_receivers", "fd23_receivers_line", "fd23_run", "fd23_sync",
     "fd23_get_seismograms", "fd23_reset", "fd23_get_stream", "fd23_get_step", "fd23_state_bytes", "fd23_get_state",
     "fd23_set_state", "fd23_field_norm2", "fd23_build_material", "fd23_build_cpml",
-    "fd23_build_source_terms", "fd23_sum_squares_noalloc",
+    "fd23_build_source_terms", "fd23_sum_squares_noalloc", "fd23_set_box", "fd23_set_box_incident",
+    "fd23_box_state_bytes", "fd23_get_box_state", "fd23_set_box_state", "fd23_box_ring_size",
+    "fd23_box_ring_index", "fd23_box_ring_cells", "fd23_box_incident_from_displacement",
+    "fd23_box_material",
 ]
 
 
@@ -110,6 +115,16 @@ def lib():
         "fd23_build_cpml": ([i, i, i, i, d, d, d, d, vp, sz], i),
         "fd23_build_source_terms": ([i, i, i, i, vp, d, d, vp, i, i, vp, vp, vp, vp, i], i),
         "fd23_sum_squares_noalloc": ([i, vp, i, sz, vp, _C.POINTER(d), _C.POINTER(i)], i),
+        "fd23_set_box": ([vp, i, i, i, i, vp], i),
+        "fd23_set_box_incident": ([vp, vp, i, i], i),
+        "fd23_box_state_bytes": ([vp], sz),
+        "fd23_get_box_state": ([vp, vp, sz], i),
+        "fd23_set_box_state": ([vp, vp, sz], i),
+        "fd23_box_ring_size": ([i, i, _C.POINTER(i), _C.POINTER(i)], i),
+        "fd23_box_ring_index": ([i, i, i, i], i),
+        "fd23_box_ring_cells": ([i, i, i, i, vp, vp], i),
+        "fd23_box_incident_from_displacement": ([i, i, d, vp, vp, vp, vp, vp, vp], i),
+        "fd23_box_material": ([i, i, vp, i, i, i, i, d, d, d, d, d, vp], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -218,6 +233,51 @@ def sum_squares_noalloc(prec, field_ptrs, n, stream=0):
                                           _C.c_void_p(int(stream)) if stream else None,
                                           _C.byref(total), _C.byref(bad)), "fd23_sum_squares_noalloc")
     return total.value, bool(bad.value)
+
+
+# ---------------------------------------------------------------- hybrid box
+def box_ring_size(bx, bz):
+    """(nsub, nadd): cells of the sub ring (outer 4 of the box) and of the add
+    ring (the next 4 inward)."""
+    ns, na = _C.c_int(0), _C.c_int(0)
+    _check(lib().fd23_box_ring_size(bx, bz, _C.byref(ns), _C.byref(na)), "fd23_box_ring_size")
+    return ns.value, na.value
+
+
+def box_ring_index(bx, bz, bi, bj):
+    """Ring position of box cell (bi, bj), -1 when it is in neither ring."""
+    return lib().fd23_box_ring_index(bx, bz, bi, bj)
+
+
+def box_ring_cells(x0, z0, bx, bz):
+    """Grid cells (ix, iz) of every ring position, in incident-field order."""
+    n = sum(box_ring_size(bx, bz))
+    ix = _np.zeros(n, _np.int32)
+    iz = _np.zeros(n, _np.int32)
+    _check(lib().fd23_box_ring_cells(x0, z0, bx, bz, _p(ix), _p(iz)), "fd23_box_ring_cells")
+    return ix, iz
+
+
+def box_incident_from_displacement(bx, bz, dt, bmat, u_old, w_old, u_new, w_new):
+    """Incident field [5, nring] of one step from displacement planes of
+    shape (bz+8, bx+8) (BOX::setboxsource)."""
+    n = sum(box_ring_size(bx, bz))
+    out = _np.zeros((5, n))
+    a = [_f64(v) for v in (bmat, u_old, w_old, u_new, w_new)]
+    _check(lib().fd23_box_incident_from_displacement(bx, bz, dt, *[_p(v) for v in a], _p(out)),
+           "fd23_box_incident_from_displacement")
+    return out
+
+
+def box_material(mat, x0, z0, bx, bz, src_vp, src_vs, src_den, dt, h):
+    """(grid material with the box made homogeneous, box material (5, bz, bx),
+    cells replaced): MATERIAL::init_for_box_from_full."""
+    m = _f64(mat).copy()
+    nz, nx = m.shape[-2], m.shape[-1]
+    bm = _np.zeros((5, bz, bx))
+    n = _check(lib().fd23_box_material(nx, nz, _p(m), x0, z0, bx, bz, src_vp, src_vs, src_den, dt, h,
+                                       _p(bm)), "fd23_box_material")
+    return m, bm, n
 
 
 def receivers_line(nsta, ix0, iz0, idx, idz):
@@ -361,6 +421,31 @@ class Solver:
     def set_state(self, state, it0):
         st = _np.ascontiguousarray(state, dtype=self.dtype)
         _check(lib().fd23_set_state(self._h, _p(st), st.nbytes, it0), "fd23_set_state")
+
+    # -- hybrid box --
+    def set_box(self, x0, z0, bx, bz, bmat=None):
+        """Box [x0, x0+bx) x [z0, z0+bz); bmat (5, bz, bx) dt/h-scaled or None
+        for the cut of the grid material.  bx = bz = 0 removes it."""
+        _check(lib().fd23_set_box(self._h, x0, z0, bx, bz, _p(_f64(bmat)) if bmat is not None else None),
+               "fd23_set_box")
+        self._box = (x0, z0, bx, bz) if bx else None
+
+    def set_box_incident(self, inc, it0=0):
+        """inc [nsteps, 5, nring] (U W Txx Txz Tzz on the ring cells) for steps
+        it0 .. it0+nsteps-1."""
+        a = _np.ascontiguousarray(inc, dtype=self.dtype)
+        _check(lib().fd23_set_box_incident(self._h, _p(a), it0, a.shape[0] if a.ndim == 3 else 0),
+               "fd23_set_box_incident")
+
+    def get_box_state(self):
+        n = lib().fd23_box_state_bytes(self._h) // _np.dtype(self.dtype).itemsize
+        out = _np.zeros(n, dtype=self.dtype)
+        _check(lib().fd23_get_box_state(self._h, _p(out), out.nbytes), "fd23_get_box_state")
+        return out
+
+    def set_box_state(self, r):
+        a = _np.ascontiguousarray(r, dtype=self.dtype)
+        _check(lib().fd23_set_box_state(self._h, _p(a), a.nbytes), "fd23_set_box_state")
 
     def norm2(self):
         v = _C.c_double(0.0)

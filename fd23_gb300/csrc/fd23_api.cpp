@@ -101,10 +101,10 @@ struct fd23_solver {
     int4 *d_terms = nullptr;
     void *d_tamp = nullptr;
     int tamp_nt = 0;
-    // receivers
-    int nrec[2] = {0, 0};
-    long long *d_rec[2] = {nullptr, nullptr};
-    void *d_seis[2] = {nullptr, nullptr};
+    // receivers, one list per wavefield
+    int nrec[5] = {};
+    long long *d_rec[5] = {};
+    void *d_seis[5] = {};
     int rec_cap = 0;      // record rows allocated
     int nrec_steps = 0;   // record rows filled (or pending)
     int pending_rec = -1; // record row to gather from the current buffer set
@@ -115,6 +115,16 @@ struct fd23_solver {
     WorkItem *d_items = nullptr;
     int *d_item_off = nullptr;
     int nblocks = 0;
+    // hybrid box: residual field, box material, ring cells, incident field
+    // of steps [box_inc_it0, box_inc_it0 + box_inc_n)
+    bool box_on = false;
+    int box_x0 = 0, box_z0 = 0, box_bx = 0, box_bz = 0, box_nsub = 0, box_nring = 0;
+    void *box_r[5] = {};
+    void *box_mat[5] = {};
+    int2 *box_cells = nullptr;
+    void *box_inc = nullptr;
+    size_t box_inc_bytes = 0;
+    int box_inc_it0 = 0, box_inc_n = 0;
 };
 
 namespace {
@@ -230,32 +240,61 @@ Shot<S, C> make_shot(const fd23_solver *s)
     sh.terms = s->d_terms;
     sh.tamp = (const C *)s->d_tamp;
     sh.tamp_nt = s->nterms > 0 ? s->tamp_nt : 0;
-    for (int c = 0; c < 2; ++c) {
+    for (int c = 0; c < 5; ++c) {
         sh.nrec[c] = s->nrec[c];
         sh.rec[c] = s->d_rec[c];
         sh.seis[c] = (C *)s->d_seis[c];
     }
+    sh.box.on = s->box_on ? 1 : 0;
+    if (s->box_on) {
+        sh.box.x0 = s->box_x0;
+        sh.box.z0 = s->box_z0;
+        sh.box.bx = s->box_bx;
+        sh.box.bz = s->box_bz;
+        sh.box.nsub = s->box_nsub;
+        sh.box.nring = s->box_nring;
+        for (int f = 0; f < 5; ++f) {
+            sh.box.r[f] = (C *)s->box_r[f];
+            sh.box.rmat[f] = (const C *)s->box_mat[f];
+        }
+        sh.box.cells = s->box_cells;
+        // incident field of the current step
+        const bool have = s->box_inc && s->it >= s->box_inc_it0 && s->it < s->box_inc_it0 + s->box_inc_n;
+        sh.box.inc = have ? (const C *)((const unsigned char *)s->box_inc +
+                                        (size_t)(s->it - s->box_inc_it0) * 5 * s->box_nring * s->cs)
+                          : nullptr;
+    }
     return sh;
 }
 
+// One time step.  Without a box the fused sweep gathers the previous step's
+// receivers on its way; with a box the step is
+//   ring(U,W) + residual stress | sweep (stress ring inside) | receivers +
+//   residual velocity
+// (PD/main.cpp:153-199 order; the exchanges that read only fields the next
+// update leaves unchanged run earlier, with the same values).
 template <class S, class C>
 int step_impl(fd23_solver *s, int rec_now)
 {
     Shot<S, C> sh = make_shot<S, C>(s);
+    const bool box = s->box_on;
+    int rc = FD23_OK;
+    if (box && (rc = launch_box_pre<S, C>(sh, s->fused ? s->par : 0, s->stream))) return rc;
     if (s->fused) {
-        const int rc = launch_step_fused<S, C>(sh, s->d.wave, s->d_items, s->d_item_off, s->nblocks,
-                                               s->par, s->it, s->pending_rec, s->err_flag, s->stream);
+        rc = launch_step_fused<S, C>(sh, s->d.wave, s->d_items, s->d_item_off, s->nblocks, s->par, s->it,
+                                     s->pending_rec, s->err_flag, s->stream);
         if (rc) return rc;
         s->pending_rec = -1;
         s->par = 1 - s->par;
-        if (rec_now) s->pending_rec = s->nrec_steps++;
+        if (rec_now && !box) s->pending_rec = s->nrec_steps++;
     } else {
-        const int rc = launch_step_twopass<S, C>(sh, s->d.wave, s->it, s->stream);
+        rc = launch_step_twopass<S, C>(sh, s->d.wave, s->it, s->stream);
         if (rc) return rc;
-        if (rec_now) {
-            const int r2 = launch_record<S, C>(sh, 0, s->nrec_steps++, s->stream);
-            if (r2) return r2;
-        }
+        if (rec_now && !box && (rc = launch_record<S, C>(sh, 0, s->nrec_steps++, s->stream))) return rc;
+    }
+    if (box) {
+        const int ri = rec_now ? s->nrec_steps++ : -1;
+        if ((rc = launch_box_post<S, C>(sh, s->fused ? s->par : 0, ri, s->stream))) return rc;
     }
     s->it++;
     return FD23_OK;
@@ -383,11 +422,27 @@ int zero_state(fd23_solver *s)
             CK(cudaMemsetAsync(s->psi[b][p], 0, s->psi_elems[p] * s->cs, s->stream));
     }
     CK(cudaMemsetAsync(s->err_flag, 0, sizeof(int), s->stream));
+    if (s->box_on)
+        for (int f = 0; f < 5; ++f)
+            CK(cudaMemsetAsync(s->box_r[f], 0, (size_t)s->box_bx * s->box_bz * s->cs, s->stream));
     s->it = 0;
     s->par = 0;
     s->nrec_steps = 0;
     s->pending_rec = -1;
     return FD23_OK;
+}
+
+void free_box(fd23_solver *s)
+{
+    for (int f = 0; f < 5; ++f) {
+        cudaFree(s->box_r[f]);
+        cudaFree(s->box_mat[f]);
+        s->box_r[f] = s->box_mat[f] = nullptr;
+    }
+    cudaFree(s->box_cells);
+    s->box_cells = nullptr;
+    s->box_on = false;
+    s->box_inc_n = 0;
 }
 
 void free_all(fd23_solver *s)
@@ -402,10 +457,12 @@ void free_all(fd23_solver *s)
     cudaFree(s->norm_buf);
     cudaFree(s->d_terms);
     cudaFree(s->d_tamp);
-    for (int c = 0; c < 2; ++c) {
+    for (int c = 0; c < 5; ++c) {
         cudaFree(s->d_rec[c]);
         cudaFree(s->d_seis[c]);
     }
+    free_box(s);
+    cudaFree(s->box_inc);
     cudaFree(s->d_items);
     cudaFree(s->d_item_off);
     if (s->stream) cudaStreamDestroy(s->stream);
@@ -415,7 +472,7 @@ int ensure_record_capacity(fd23_solver *s, int need)
 {
     if (need <= s->rec_cap) return FD23_OK;
     int cap = std::max(need, s->rec_cap * 2);
-    for (int c = 0; c < 2; ++c) {
+    for (int c = 0; c < 5; ++c) {
         if (s->nrec[c] <= 0) continue;
         void *np = nullptr;
         int rc = dev_alloc(&np, (size_t)cap * s->nrec[c] * s->cs);
@@ -708,8 +765,7 @@ int fd23_set_source(fd23_solver *s, int kind, int xs, int zs, const double *mome
 int fd23_set_receivers(fd23_solver *s, int field, const int *rx, const int *rz, int n)
 {
     if (!s || n < 0 || (n > 0 && (!rx || !rz))) return FD23_ERR_ARG;
-    const int ncomp = s->d.wave == FD23_PSV ? 2 : 1;
-    if (field < 0 || field >= ncomp) return FD23_ERR_ARG;
+    if (field < 0 || field >= s->nfld) return FD23_ERR_ARG;
     if (s->nrec_steps > 0) return FD23_ERR_ORDER;  // change receivers only before recording
     CK(cudaSetDevice(s->d.device));
     std::vector<long long> off((size_t)std::max(n, 1));
@@ -723,7 +779,7 @@ int fd23_set_receivers(fd23_solver *s, int field, const int *rx, const int *rz, 
     s->d_seis[field] = nullptr;
     s->nrec[field] = n;
     s->rec_cap = 0;
-    for (int c = 0; c < 2; ++c) {  // record buffers are re-sized together
+    for (int c = 0; c < 5; ++c) {  // record buffers are re-sized together
         cudaFree(s->d_seis[c]);
         s->d_seis[c] = nullptr;
     }
@@ -758,7 +814,10 @@ int fd23_run(fd23_solver *s, int nsteps, int itrecord)
     int nrec_new = 0;
     for (int k = 0; k < nsteps; ++k)
         if ((s->it + k) % itrecord == 0) ++nrec_new;
-    const bool any_rec = s->nrec[0] > 0 || s->nrec[1] > 0;
+    bool any_rec = false;
+    for (int c = 0; c < 5; ++c) any_rec = any_rec || s->nrec[c] > 0;
+    if (s->box_on && (s->it < s->box_inc_it0 || s->it + nsteps > s->box_inc_it0 + s->box_inc_n))
+        return FD23_ERR_ORDER;  // incident field of some step not loaded
     if (any_rec) {
         int rc = ensure_record_capacity(s, s->nrec_steps + nrec_new);
         if (rc) return rc;
@@ -798,8 +857,7 @@ int fd23_get_step(fd23_solver *s, int *it)
 int fd23_get_seismograms(fd23_solver *s, int field, void *out, size_t out_bytes, int *nrec_steps)
 {
     if (!s) return FD23_ERR_ARG;
-    const int ncomp = s->d.wave == FD23_PSV ? 2 : 1;
-    if (field < 0 || field >= ncomp) return FD23_ERR_ARG;
+    if (field < 0 || field >= s->nfld) return FD23_ERR_ARG;
     int rc = fd23_sync(s);
     if (rc) return rc;
     if (nrec_steps) *nrec_steps = s->nrec_steps;
@@ -807,8 +865,8 @@ int fd23_get_seismograms(fd23_solver *s, int field, void *out, size_t out_bytes,
     if (!out) return FD23_OK;
     if (out_bytes < need) return FD23_ERR_ARG;
     if (need) CK(cudaMemcpy(out, s->d_seis[field], need, cudaMemcpyDeviceToHost));
-    if (s->sigma != 1.0) {  // velocities are stored times sigma (exact power of two)
-        const float inv = (float)(1.0 / s->sigma);
+    if (field_scale(s, field) != 1.0) {  // stored times an exact power of two
+        const float inv = (float)(1.0 / field_scale(s, field));
         float *o = (float *)out;
         for (size_t k = 0; k < need / sizeof(float); ++k) o[k] *= inv;
     }
@@ -923,6 +981,176 @@ int fd23_field_norm2(fd23_solver *s, double *norm2)
     CK(cudaStreamSynchronize(s->stream));
     *norm2 = h[0];
     return h[1] != 0.0 ? FD23_ERR_NONFINITE : FD23_OK;
+}
+
+// ---- hybrid box ----
+int fd23_set_box(fd23_solver *s, int x0, int z0, int bx, int bz, const double *bmat)
+{
+    if (!s) return FD23_ERR_ARG;
+    CK(cudaSetDevice(s->d.device));
+    CK(cudaStreamSynchronize(s->stream));
+    if (bx == 0 && bz == 0) {
+        free_box(s);
+        return FD23_OK;
+    }
+    if (s->d.wave != FD23_PSV || scaled_form(s)) return FD23_ERR_UNSUPPORTED;
+    if (bx < kBoxMin || bz < kBoxMin || x0 < 0 || z0 < 0 || x0 + bx > s->d.nx || z0 + bz > s->d.nz)
+        return FD23_ERR_ARG;
+    if (!bmat && !s->have_material) return FD23_ERR_ORDER;
+    free_box(s);
+    const size_t nb = (size_t)bx * bz, bytes = nb * s->cs;
+    int rc = FD23_OK;
+    for (int f = 0; f < 5; ++f) {
+        if ((rc = dev_alloc(&s->box_r[f], bytes)) || (rc = dev_alloc(&s->box_mat[f], bytes))) {
+            free_box(s);
+            return rc;
+        }
+        CK(cudaMemsetAsync(s->box_r[f], 0, bytes, s->stream));
+    }
+    if (bmat) {
+        std::vector<unsigned char> tmp(bytes);
+        for (int m = 0; m < 5; ++m) {
+            to_compute(s->d.prec, bmat + m * nb, nb, tmp.data());
+            CK(cudaMemcpy(s->box_mat[m], tmp.data(), bytes, cudaMemcpyHostToDevice));
+        }
+    } else {
+        // the box cut of the grid material (storage type = compute type here)
+        for (int m = 0; m < 5; ++m)
+            CK(cudaMemcpy2DAsync(s->box_mat[m], (size_t)bx * s->cs,
+                                 (const unsigned char *)s->mat[m] +
+                                     (size_t)(s->L.origin + (long long)z0 * s->L.pitch + x0) * s->es,
+                                 (size_t)s->L.pitch * s->es, (size_t)bx * s->es, (size_t)bz,
+                                 cudaMemcpyDeviceToDevice, s->stream));
+    }
+    // ring cells in incident-field order; the closed-form position used by
+    // the sweep must agree with the enumeration
+    std::vector<int2> cells;
+    for (int pass = 0; pass < 2; ++pass) {
+        const int lo = pass ? 4 : 0, hx = pass ? bx - 4 : bx, hz = pass ? bz - 4 : bz;
+        for (int j = lo; j < hz; ++j)
+            for (int i = lo; i < hx; ++i)
+                if (!(i > lo + 3 && i < hx - 4 && j > lo + 3 && j < hz - 4)) cells.push_back(make_int2(i, j));
+    }
+    for (size_t q = 0; q < cells.size(); ++q)
+        if (box_ring_index(cells[q].x, cells[q].y, bx, bz) != (int)q) {
+            free_box(s);
+            return FD23_ERR_UNSUPPORTED;
+        }
+    if ((rc = dev_alloc((void **)&s->box_cells, cells.size() * sizeof(int2)))) {
+        free_box(s);
+        return rc;
+    }
+    CK(cudaMemcpy(s->box_cells, cells.data(), cells.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    CK(cudaStreamSynchronize(s->stream));
+    s->box_x0 = x0;
+    s->box_z0 = z0;
+    s->box_bx = bx;
+    s->box_bz = bz;
+    s->box_nsub = box_nsub(bx, bz);
+    s->box_nring = (int)cells.size();
+    s->box_on = true;
+    s->box_inc_n = 0;
+    return FD23_OK;
+}
+
+int fd23_set_box_incident(fd23_solver *s, const void *inc, int it0, int nsteps)
+{
+    if (!s || it0 < 0 || nsteps < 0 || (nsteps > 0 && !inc)) return FD23_ERR_ARG;
+    if (!s->box_on) return FD23_ERR_ORDER;
+    CK(cudaSetDevice(s->d.device));
+    const size_t bytes = (size_t)nsteps * 5 * s->box_nring * s->cs;
+    if (bytes > s->box_inc_bytes) {
+        CK(cudaStreamSynchronize(s->stream));
+        cudaFree(s->box_inc);
+        s->box_inc = nullptr;
+        s->box_inc_bytes = 0;
+        s->box_inc_n = 0;
+        int rc = dev_alloc(&s->box_inc, bytes);
+        if (rc) return rc;
+        s->box_inc_bytes = bytes;
+    }
+    if (bytes) {
+        CK(cudaMemcpyAsync(s->box_inc, inc, bytes, cudaMemcpyHostToDevice, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+    }
+    s->box_inc_it0 = it0;
+    s->box_inc_n = nsteps;
+    return FD23_OK;
+}
+
+size_t fd23_box_state_bytes(fd23_solver *s)
+{
+    return (s && s->box_on) ? 5 * (size_t)s->box_bx * s->box_bz * s->cs : 0;
+}
+
+int fd23_get_box_state(fd23_solver *s, void *buf, size_t bytes)
+{
+    if (!s || !buf) return FD23_ERR_ARG;
+    if (!s->box_on) return FD23_ERR_ORDER;
+    if (bytes < fd23_box_state_bytes(s)) return FD23_ERR_ARG;
+    int rc = fd23_sync(s);
+    if (rc) return rc;
+    const size_t b = (size_t)s->box_bx * s->box_bz * s->cs;
+    for (int f = 0; f < 5; ++f) CK(cudaMemcpy((unsigned char *)buf + f * b, s->box_r[f], b, cudaMemcpyDeviceToHost));
+    return FD23_OK;
+}
+
+int fd23_set_box_state(fd23_solver *s, const void *buf, size_t bytes)
+{
+    if (!s || !buf) return FD23_ERR_ARG;
+    if (!s->box_on) return FD23_ERR_ORDER;
+    if (bytes < fd23_box_state_bytes(s)) return FD23_ERR_ARG;
+    CK(cudaSetDevice(s->d.device));
+    CK(cudaStreamSynchronize(s->stream));
+    const size_t b = (size_t)s->box_bx * s->box_bz * s->cs;
+    for (int f = 0; f < 5; ++f)
+        CK(cudaMemcpy(s->box_r[f], (const unsigned char *)buf + f * b, b, cudaMemcpyHostToDevice));
+    return FD23_OK;
+}
+
+int fd23_box_ring_size(int bx, int bz, int *nsub, int *nadd)
+{
+    if (bx < kBoxMin || bz < kBoxMin) return FD23_ERR_ARG;
+    if (nsub) *nsub = box_nsub(bx, bz);
+    if (nadd) *nadd = box_nadd(bx, bz);
+    return box_nsub(bx, bz) + box_nadd(bx, bz);
+}
+
+int fd23_box_ring_index(int bx, int bz, int bi, int bj)
+{
+    if (bx < kBoxMin || bz < kBoxMin) return FD23_ERR_ARG;
+    return box_ring_index(bi, bj, bx, bz);
+}
+
+int fd23_box_ring_cells(int x0, int z0, int bx, int bz, int *ix, int *iz)
+{
+    if (bx < kBoxMin || bz < kBoxMin || !ix || !iz) return FD23_ERR_ARG;
+    for (int j = 0; j < bz; ++j)
+        for (int i = 0; i < bx; ++i) {
+            const int q = box_ring_index(i, j, bx, bz);
+            if (q < 0) continue;
+            ix[q] = x0 + i;
+            iz[q] = z0 + j;
+        }
+    return box_nsub(bx, bz) + box_nadd(bx, bz);
+}
+
+int fd23_box_incident_from_displacement(int bx, int bz, double dt, const double *bmat, const double *u_old,
+                                        const double *w_old, const double *u_new, const double *w_new,
+                                        double *out)
+{
+    if (bx < kBoxMin || bz < kBoxMin || !(dt > 0) || !bmat || !u_old || !w_old || !u_new || !w_new || !out)
+        return FD23_ERR_ARG;
+    return box_incident_from_displacement(bx, bz, dt, bmat, u_old, w_old, u_new, w_new, out);
+}
+
+int fd23_box_material(int nx, int nz, double *mat, int x0, int z0, int bx, int bz, double src_vp,
+                      double src_vs, double src_den, double dt, double h, double *bmat)
+{
+    if (nx < 2 || nz < 2 || !mat || !bmat || bx < 1 || bz < 1 || x0 < 0 || z0 < 0 || x0 + bx > nx ||
+        z0 + bz > nz || !(src_den > 0) || !(dt > 0) || !(h > 0))
+        return FD23_ERR_ARG;
+    return box_material(nx, nz, mat, x0, z0, bx, bz, src_vp, src_vs, src_den, dt, h, bmat);
 }
 
 // ---- host-only helpers (no GPU needed) ----

@@ -1,0 +1,149 @@
+// Hybrid-box kernels (P-SV): the ring exchanges between the grid field g and
+// the residual field r, and the residual-field updates.
+//
+// Reference: ring exchanges PD/box/cu_box.cu:48-79 (ker_subsource,
+// ker_addsource), residual updates PD/fd/cu_fd.cu:93-207 (one 32x32 block,
+// boxes up to 32 cells) and PD/fd/fd.cpp:63-91, 208-234 (host, interior cells
+// 4 .. n-5).  Here a box is any rectangle of at least 16 x 16 cells; the
+// residual updates cover cells 4 .. n-5 of the box (the outer 4 are the sub
+// ring, rewritten from g before every read), with one thread per cell.
+//
+// The stress exchange of the fused sweep is done inside that sweep (after
+// the point source, before the velocity stencil reads the stresses); the
+// kernel here serves the two-pass sweep.
+#include "fd23_device.cuh"
+#include "fd23_kernels.h"
+
+namespace fd23 {
+
+namespace {
+
+template <class C>
+__device__ __forceinline__ C dminus_r(const C *p, long long s)
+{
+    return comb<C>(Coef4<C>::c0, Coef4<C>::c1, Coef4<C>::c2, Coef4<C>::c3, p[0] - p[-s], p[s] - p[-2 * s],
+                   p[2 * s] - p[-3 * s], p[3 * s] - p[-4 * s]);
+}
+template <class C>
+__device__ __forceinline__ C dplus_r(const C *p, long long s)
+{
+    return comb<C>(Coef4<C>::c0, Coef4<C>::c1, Coef4<C>::c2, Coef4<C>::c3, p[s] - p[0], p[2 * s] - p[-s],
+                   p[3 * s] - p[-2 * s], p[4 * s] - p[-3 * s]);
+}
+
+// ring exchange of fields F0 .. F1-1 on buffer set `par`
+template <class S, class C, int F0, int F1>
+__global__ void __launch_bounds__(256) box_ring_kernel(Shot<S, C> s, int par)
+{
+    const Box<C> &b = s.box;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < b.nring; q += gridDim.x * blockDim.x) {
+        const int2 c = b.cells[q];
+        const long long g = s.origin + (long long)(b.z0 + c.y) * s.pitch + (b.x0 + c.x);
+        const long long r = (long long)c.y * b.bx + c.x;
+        const bool add = q >= b.nsub;
+#pragma unroll
+        for (int f = F0; f < F1; ++f) {
+            S *G = par ? s.f[1][f] : s.f[0][f];
+            const C sv = b.inc[(long long)f * b.nring + q];
+            if (add) G[g] = to_s<S>(b.r[f][r] + sv);
+            else b.r[f][r] = to_c<C>(G[g]) - sv;
+        }
+    }
+}
+
+// residual stress update, cells 4 .. n-5 of the box; the accumulation order
+// is that of the main update (x terms, then z terms)
+template <class C>
+__global__ void __launch_bounds__(256) box_stress_r(Box<C> b)
+{
+    const int ix = 4 + blockIdx.x * 32 + threadIdx.x, iz = 4 + blockIdx.y * 8 + threadIdx.y;
+    if (ix >= b.bx - 4 || iz >= b.bz - 4) return;
+    const long long o = (long long)iz * b.bx + ix, P = b.bx;
+    const C ux = dminus_r<C>(b.r[0] + o, 1), uz = dminus_r<C>(b.r[0] + o, P);
+    const C wx = dplus_r<C>(b.r[1] + o, 1), wz = dplus_r<C>(b.r[1] + o, P);
+    const C lam = b.rmat[0][o], mua = b.rmat[2][o];
+    const C gam = lam + (C)2 * b.rmat[1][o];
+    C txx = b.r[2][o], txz = b.r[3][o], tzz = b.r[4][o];
+    txx = fmaC<C>(gam, ux, txx);
+    tzz = fmaC<C>(lam, ux, tzz);
+    txz = fmaC<C>(mua, wx, txz);
+    txx = fmaC<C>(lam, wz, txx);
+    tzz = fmaC<C>(gam, wz, tzz);
+    txz = fmaC<C>(mua, uz, txz);
+    b.r[2][o] = txx;
+    b.r[3][o] = txz;
+    b.r[4][o] = tzz;
+}
+
+// receivers of this step's output (buffer set `par`, before the next ring
+// exchange rewrites the add ring), then the residual velocity update
+template <class S, class C>
+__global__ void __launch_bounds__(256) box_velocity_r(Shot<S, C> s, int par, int rec_index)
+{
+    if (rec_index >= 0) {
+        const int nthr = gridDim.x * gridDim.y * blockDim.x * blockDim.y;
+        const int t0 = (blockIdx.y * gridDim.x + blockIdx.x) * (blockDim.x * blockDim.y) +
+                       threadIdx.y * blockDim.x + threadIdx.x;
+#pragma unroll
+        for (int c = 0; c < 5; ++c) {
+            const S *F = par ? s.f[1][c] : s.f[0][c];
+            for (int i = t0; i < s.nrec[c]; i += nthr)
+                s.seis[c][(long long)rec_index * s.nrec[c] + i] = to_c<C>(F[s.rec[c][i]]);
+        }
+    }
+    const Box<C> &b = s.box;
+    const int ix = 4 + blockIdx.x * 32 + threadIdx.x, iz = 4 + blockIdx.y * 8 + threadIdx.y;
+    if (ix >= b.bx - 4 || iz >= b.bz - 4) return;
+    const long long o = (long long)iz * b.bx + ix, P = b.bx;
+    const C dxTxx = dplus_r<C>(b.r[2] + o, 1), dzTzz = dminus_r<C>(b.r[4] + o, P);
+    const C dxTxz = dminus_r<C>(b.r[3] + o, 1), dzTxz = dplus_r<C>(b.r[3] + o, P);
+    const C bu = b.rmat[3][o], bw = b.rmat[4][o];
+    C u = b.r[0][o], w = b.r[1][o];
+    u = fmaC<C>(bu, dxTxx, u);
+    w = fmaC<C>(bw, dxTxz, w);
+    u = fmaC<C>(bu, dzTxz, u);
+    w = fmaC<C>(bw, dzTzz, w);
+    b.r[0][o] = u;
+    b.r[1][o] = w;
+}
+
+inline dim3 interior_grid(int bx, int bz) { return dim3((unsigned)((bx - 8 + 31) / 32), (unsigned)((bz - 8 + 7) / 8)); }
+inline unsigned ring_blocks(int nring) { return (unsigned)((nring + 255) / 256); }
+
+}  // namespace
+
+template <class S, class C>
+int launch_box_ring(const Shot<S, C> &s, int par, int which, cudaStream_t st)
+{
+    if (which == 0) box_ring_kernel<S, C, 0, 2><<<ring_blocks(s.box.nring), 256, 0, st>>>(s, par);
+    else box_ring_kernel<S, C, 2, 5><<<ring_blocks(s.box.nring), 256, 0, st>>>(s, par);
+    return cudaPeekAtLastError() == cudaSuccess ? FD23_OK : FD23_ERR_CUDA;
+}
+
+template <class S, class C>
+int launch_box_pre(const Shot<S, C> &s, int par, cudaStream_t st)
+{
+    const int rc = launch_box_ring<S, C>(s, par, 0, st);
+    if (rc) return rc;
+    box_stress_r<C><<<interior_grid(s.box.bx, s.box.bz), dim3(32, 8), 0, st>>>(s.box);
+    return cudaPeekAtLastError() == cudaSuccess ? FD23_OK : FD23_ERR_CUDA;
+}
+
+template <class S, class C>
+int launch_box_post(const Shot<S, C> &s, int par, int rec_index, cudaStream_t st)
+{
+    box_velocity_r<S, C><<<interior_grid(s.box.bx, s.box.bz), dim3(32, 8), 0, st>>>(s, par, rec_index);
+    return cudaPeekAtLastError() == cudaSuccess ? FD23_OK : FD23_ERR_CUDA;
+}
+
+#define FD23_INST(S, C)                                                                  \
+    template int launch_box_ring<S, C>(const Shot<S, C> &, int, int, cudaStream_t);     \
+    template int launch_box_pre<S, C>(const Shot<S, C> &, int, cudaStream_t);           \
+    template int launch_box_post<S, C>(const Shot<S, C> &, int, int, cudaStream_t);
+FD23_INST(float, float)
+FD23_INST(double, double)
+FD23_INST(__nv_bfloat16, float)
+FD23_INST(__half, float)
+#undef FD23_INST
+
+}  // namespace fd23

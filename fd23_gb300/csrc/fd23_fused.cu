@@ -36,6 +36,7 @@
 // Arithmetic per cell is the canonical sequence of fd23_device.cuh, which is
 // bit-identical to the CPU oracle and to the two-pass kernels.
 #include <cstdio>
+#include <type_traits>
 
 #include "fd23_device.cuh"
 #include "fd23_kernels.h"
@@ -480,10 +481,10 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
     asm volatile("griddepcontrol.wait;" ::: "memory");
     // ---- receivers of the previous step (buffer set `par` is read-only here) ----
     if (rec_index >= 0) {
-        for (int r = blockIdx.x * NCT + tid; r < sh.nrec[0]; r += gridDim.x * NCT)
-            sh.seis[0][(long long)rec_index * sh.nrec[0] + r] = to_c<C>(rd[0][sh.rec[0][r]]);
-        for (int r = blockIdx.x * NCT + tid; r < sh.nrec[1]; r += gridDim.x * NCT)
-            sh.seis[1][(long long)rec_index * sh.nrec[1] + r] = to_c<C>(rd[1][sh.rec[1][r]]);
+#pragma unroll
+        for (int c = 0; c < K::NV + K::NT; ++c)
+            for (int r = blockIdx.x * NCT + tid; r < sh.nrec[c]; r += gridDim.x * NCT)
+                sh.seis[c][(long long)rec_index * sh.nrec[c] + r] = to_c<C>(rd[c][sh.rec[c][r]]);
     }
 
     const int grp = warp;  // row of the 4-row block this warp updates
@@ -720,6 +721,40 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
                     if (hit) {
 #pragma unroll
                         for (int f = 0; f < K::NT; ++f) Vec4<S, C>::ld(tr + f * K::SW, tnew[f]);
+                    }
+                }
+                // ---- hybrid box, after the point source: add-ring stresses
+                // become r + s (every column, the halo ones feed the velocity
+                // stencil), sub-ring cells give r = T - s (owned cells only) ----
+                if constexpr (PSV && std::is_same<S, C>::value) {
+                    const int bj = j - sh.box.z0;
+                    if (sh.box.on && bj >= 0 && bj < sh.box.bz && x + 3 >= sh.box.x0 &&
+                        x < sh.box.x0 + sh.box.bx) {
+                        const bool own_row = inrow && own_x && j >= I.z0 && j < I.z1;
+                        const int nsub = sh.box.nsub, nring = sh.box.nring;
+                        bool changed = false;
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) {
+                            const int bi = x + e - sh.box.x0;
+                            const int q = box_ring_index(bi, bj, sh.box.bx, sh.box.bz);
+                            if (q < 0) continue;
+                            const long long rr = (long long)bj * sh.box.bx + bi;
+                            // read-modify-write of the ring cells just written
+                            if (q >= nsub) {
+#pragma unroll
+                                for (int f = 0; f < 3; ++f)
+                                    tr[f * K::SW + e] = sh.box.r[2 + f][rr] + sh.box.inc[(long long)(2 + f) * nring + q];
+                                changed = true;
+                            } else if (own_row) {
+#pragma unroll
+                                for (int f = 0; f < 3; ++f)
+                                    sh.box.r[2 + f][rr] = tr[f * K::SW + e] - sh.box.inc[(long long)(2 + f) * nring + q];
+                            }
+                        }
+                        if (changed) {
+#pragma unroll
+                            for (int f = 0; f < K::NT; ++f) Vec4<S, C>::ld(tr + f * K::SW, tnew[f]);
+                        }
                     }
                 }
                 // ---- HBM (owned cells) ----

@@ -334,4 +334,85 @@ void build_source_terms(int wave, int kind, int xs, int zs, const double *moment
     }
 }
 
+// ---------------------------------------------------------------------------
+// Hybrid box, host side.
+
+// Incident field on the ring cells of a bx x bz box from two displacement
+// planes of (bx+8) x (bz+8) values (box cell (i, j) at plane (i+4, j+4)):
+// BOX::setboxsource, PD/box/box.cpp:120-196.  Velocities are the forward
+// difference of the planes over dt; stresses come from the new planes with
+// the box material, at the reference's reduced stencil order around the box
+// centre, evaluated in the reference's expression order (FP64).
+int box_incident_from_displacement(int bx, int bz, double dt, const double *bmat, const double *uo,
+                                   const double *wo, const double *un, const double *wn, double *out)
+{
+    const int nring = box_nsub(bx, bz) + box_nadd(bx, bz);
+    const size_t nb = (size_t)bx * bz;
+    const long pw = bx + 8;
+    auto at = [pw](const double *a, int i, int j) { return a[i + (long)j * pw]; };
+    // 4-term difference along (di, dj); `plus` selects the forward-staggered taps
+    auto diff = [&](const double *a, int tx, int ty, int di, int dj, bool plus, const double *c) {
+        const int p = plus ? 1 : 0;
+        auto d = [&](int k) {
+            return at(a, tx + (k + p) * di, ty + (k + p) * dj) - at(a, tx - (k + 1 - p) * di, ty - (k + 1 - p) * dj);
+        };
+        return c[0] * d(0) - c[1] * d(1) + c[2] * d(2) - c[3] * d(3);
+    };
+    for (int j = 0; j < bz; ++j)
+        for (int i = 0; i < bx; ++i) {
+            const int q = box_ring_index(i, j, bx, bz);
+            if (q < 0) continue;
+            const int tx = i + 4, ty = j + 4;
+            const int oz = std::abs(ty - 3 - (bz + 1) / 2) - 1, ox = std::abs(tx - 3 - (bx + 1) / 2) - 1;
+            const int ord = std::max(0, std::min(4, std::max(oz, ox)));
+            const double *c = kCoef[ord];
+            const double ux = diff(un, tx, ty, 1, 0, false, c), uz = diff(un, tx, ty, 0, 1, false, c);
+            const double wx = diff(wn, tx, ty, 1, 0, true, c), wz = diff(wn, tx, ty, 0, 1, true, c);
+            const size_t b = (size_t)j * bx + i;
+            const double lam = bmat[b], mu = bmat[nb + b], mua = bmat[2 * nb + b];
+            const double gam = lam + 2.0 * mu;
+            out[q] = (at(un, tx, ty) - at(uo, tx, ty)) / dt;
+            out[(size_t)nring + q] = (at(wn, tx, ty) - at(wo, tx, ty)) / dt;
+            out[2 * (size_t)nring + q] = (gam * ux + lam * wz) / dt;
+            out[3 * (size_t)nring + q] = (mua * (wx + uz)) / dt;
+            out[4 * (size_t)nring + q] = (lam * ux + gam * wz) / dt;
+        }
+    return nring;
+}
+
+// Box material from the grid material (LAM MU MUA BU BW, dt/h scaled):
+// MATERIAL::init_for_box_from_full, PD/material/material.cpp:39-97.  Box
+// cells whose coefficients differ from the homogeneous source material by
+// more than 1e-4 (relative) are overwritten in the grid material too.
+int box_material(int nx, int nz, double *mat, int x0, int z0, int bx, int bz, double srcvp,
+                 double srcvs, double srcden, double dt, double h, double *bmat)
+{
+    const size_t n = (size_t)nx * nz, nb = (size_t)bx * bz;
+    const double mu0 = srcvs * srcvs * srcden;
+    const double lam = (srcvp * srcvp * srcden - 2.0 * mu0) * dt / h;
+    const double mu = mu0 * dt / h;
+    const double b = 1.0 / srcden * dt / h;
+    const double eps = 1e-4;
+    int replaced = 0;
+    for (int j = 0; j < bz; ++j)
+        for (int i = 0; i < bx; ++i) {
+            const size_t g = (size_t)(x0 + i) + (size_t)(z0 + j) * nx, k = (size_t)i + (size_t)j * bx;
+            double &LAM = mat[g], &MU = mat[n + g], &MUA = mat[2 * n + g], &BU = mat[3 * n + g],
+                   &BW = mat[4 * n + g];
+            if (std::fabs(b - BU) > b * eps || std::fabs(b - BW) > b * eps || std::fabs(mu - MU) > mu * eps ||
+                std::fabs(mu - MUA) > mu * eps || std::fabs(lam - LAM) > lam * eps) {
+                BU = BW = b;
+                MU = MUA = mu;
+                LAM = lam;
+                ++replaced;
+            }
+            bmat[k] = LAM;
+            bmat[nb + k] = MU;
+            bmat[2 * nb + k] = MUA;
+            bmat[3 * nb + k] = BU;
+            bmat[4 * nb + k] = BW;
+        }
+    return replaced;
+}
+
 }  // namespace fd23

@@ -9,6 +9,12 @@
 
 #include "../../include/fd23.h"
 
+#if defined(__CUDACC__)
+#define FD23_HD __host__ __device__
+#else
+#define FD23_HD
+#endif
+
 namespace fd23 {
 
 extern const double kCoef[5][4];
@@ -44,6 +50,51 @@ struct SourceTerm {
 };
 
 // ---------------------------------------------------------------------------
+// Hybrid box (P-SV).  A box is the grid cells [x0, x0+bx) x [z0, z0+bz),
+// bx, bz >= 16.  Its two rings, box-local (PD/box/box.cpp:59-95 for a square
+// box around the source, generalised to any rectangle):
+//   sub ring: the cells within 4 of the box edge;
+//   add ring: the cells within 4 of the edge of [4, bx-4) x [4, bz-4).
+// The incident field of one step is stored on the ring cells, [5][nring]:
+// sub-ring cells first, then add-ring cells, each ring row by row.
+constexpr int kBoxMin = 16;
+
+FD23_HD inline int box_nsub(int bx, int bz) { return 8 * (bx + bz - 8); }
+FD23_HD inline int box_nadd(int bx, int bz) { return 8 * (bx + bz - 24); }
+
+// row-major position of cell (i, j) of a 4-wide band along the edge of a
+// w x h rectangle (w, h >= 8); the cell must lie in the band
+FD23_HD inline int band_index(int i, int j, int w, int h)
+{
+    if (j < 4) return j * w + i;
+    if (j >= h - 4) return 4 * w + (h - 8) * 8 + (j - (h - 4)) * w + i;
+    return 4 * w + (j - 4) * 8 + (i < 4 ? i : i - (w - 8));
+}
+// ring position of box cell (bi, bj): [0, nsub) sub ring, [nsub, nring) add
+// ring, -1 for cells in neither ring (or outside the box)
+FD23_HD inline int box_ring_index(int bi, int bj, int bx, int bz)
+{
+    if (bi < 0 || bj < 0 || bi >= bx || bj >= bz) return -1;
+    if (bi < 4 || bi >= bx - 4 || bj < 4 || bj >= bz - 4) return band_index(bi, bj, bx, bz);
+    const int ai = bi - 4, aj = bj - 4, w = bx - 8, h = bz - 8;
+    if (ai < 4 || ai >= w - 4 || aj < 4 || aj >= h - 4) return box_nsub(bx, bz) + band_index(ai, aj, w, h);
+    return -1;
+}
+
+// Device view of the box of one shot: residual field r and box material,
+// bx*bz each, row-major; `inc` = the incident field of the current step.
+template <class C>
+struct Box {
+    int on;
+    int x0, z0, bx, bz;
+    int nsub, nring;
+    C *r[5];            // U W Txx Txz Tzz
+    const C *rmat[5];   // LAM MU MUA BU BW (dt/h scaled)
+    const C *inc;       // [5][nring]
+    const int2 *cells;  // ring position -> box-local (bi, bj)
+};
+
+// ---------------------------------------------------------------------------
 // Device-side description of one shot.  S = storage type of wavefields and
 // material, C = arithmetic type (also the type of memory variables, CPML
 // coefficients, source amplitudes and seismograms).
@@ -62,10 +113,11 @@ struct Shot {
     const int4 *terms;  // (field, ix, iz, 0)
     const C *tamp;      // [nterms][tamp_nt]
     int tamp_nt;
-    // receivers: padded element offsets, seismograms [record][n]
-    int nrec[2];
-    const long long *rec[2];
-    C *seis[2];
+    // receivers of each wavefield: padded element offsets, seismograms [record][n]
+    int nrec[5];
+    const long long *rec[5];
+    C *seis[5];
+    Box<C> box;         // hybrid box (box.on == 0: none)
 };
 
 // Work list entry of the fused sweep: one x-strip of one shot, rows [z0, z1)
@@ -90,5 +142,11 @@ int wavelet_ricker(double dt, double f0, double t0, double *out, int cap);
 void build_source_terms(int wave, int kind, int xs, int zs, const double *moment, double h,
                         double dt, const double *src, int lsrc, int nt,
                         std::vector<SourceTerm> &terms, std::vector<double> &amp);
+
+// hybrid-box host builders (fd23_host.cpp)
+int box_incident_from_displacement(int bx, int bz, double dt, const double *bmat, const double *uo,
+                                   const double *wo, const double *un, const double *wn, double *out);
+int box_material(int nx, int nz, double *mat, int x0, int z0, int bx, int bz, double srcvp,
+                 double srcvs, double srcden, double dt, double h, double *bmat);
 
 }  // namespace fd23

@@ -32,6 +32,19 @@ template <class S, class C>
 int launch_step_fused(const Shot<S, C> &s, int wave, const WorkItem *items, const int *item_off,
                       int nblocks, int par, int it, int rec_index, int *err_flag, cudaStream_t st);
 
+// Hybrid box (P-SV), fd23_box.cu.  Ring exchange on buffer set `par`:
+// which = 0 for U, W (start of a step), 1 for the stresses (after the stress
+// update and the point source); add ring g = r + s, sub ring r = g - s.
+template <class S, class C>
+int launch_box_ring(const Shot<S, C> &s, int par, int which, cudaStream_t st);
+// start of a step: ring exchange of U, W, then the residual stress update
+template <class S, class C>
+int launch_box_pre(const Shot<S, C> &s, int par, cudaStream_t st);
+// end of a step: receivers of buffer set `par` into record row `rec_index`
+// (if >= 0), then the residual velocity update
+template <class S, class C>
+int launch_box_post(const Shot<S, C> &s, int par, int rec_index, cudaStream_t st);
+
 // FP64 sum of squares over the `elems` stored elements of each of the first
 // `nfields` wavefields of buffer set `par` (the zero padding included); the
 // sum goes to dev_out[0], a NaN/Inf flag to dev_out[1].

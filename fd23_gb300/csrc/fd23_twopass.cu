@@ -276,18 +276,22 @@ __global__ void post_stress_2p(Shot<S, C> s, int it, int sh_image)
 template <class S, class C>
 __global__ void record_kernel(Shot<S, C> s, int par, int rec_index)
 {
-    // PD/record/cu_record.cu:138-148: rec[i] = F[rx[i] + rz[i]*nx]
-    for (int comp = 0; comp < 2; ++comp) {
+    // PD/record/cu_record.cu:138-148: rec[i] = F[rx[i] + rz[i]*nx], for every
+    // wavefield that has receivers
+#pragma unroll
+    for (int comp = 0; comp < 5; ++comp) {
         const int n = s.nrec[comp];
+        const S *F = par ? s.f[1][comp] : s.f[0][comp];
         for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-            s.seis[comp][(long long)rec_index * n + i] = to_c<C>(s.f[par][comp == 0 ? 0 : 1][s.rec[comp][i]]);
+            s.seis[comp][(long long)rec_index * n + i] = to_c<C>(F[s.rec[comp][i]]);
     }
 }
 
 template <class S, class C>
 int launch_record(const Shot<S, C> &s, int par, int rec_index, cudaStream_t st)
 {
-    const int n = s.nrec[0] > s.nrec[1] ? s.nrec[0] : s.nrec[1];
+    int n = 0;
+    for (int c = 0; c < 5; ++c) n = s.nrec[c] > n ? s.nrec[c] : n;
     if (n <= 0) return FD23_OK;
     record_kernel<S, C><<<(n + 255) / 256, 256, 0, st>>>(s, par, rec_index);
     return cudaPeekAtLastError() == cudaSuccess ? FD23_OK : FD23_ERR_CUDA;
@@ -300,6 +304,10 @@ int launch_step_twopass(const Shot<S, C> &s, int wave, int it, cudaStream_t st)
     if (wave == FD23_PSV) {
         psv_stress_2p<S, C><<<grd, blk, 0, st>>>(s);
         if (s.nterms > 0 && it < s.tamp_nt) post_stress_2p<S, C><<<1, 32, 0, st>>>(s, it, 0);
+        if (s.box.on) {
+            const int rc = launch_box_ring<S, C>(s, 0, 1, st);  // stresses, after the source
+            if (rc) return rc;
+        }
         psv_velocity_2p<S, C><<<grd, blk, 0, st>>>(s);
     } else {
         sh_stress_2p<S, C><<<grd, blk, 0, st>>>(s);

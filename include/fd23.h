@@ -25,6 +25,13 @@
  *   FIELD::cu_save_state/cu_load_restart, CPML::cu_save_state
  *                                  PN/field/cu_field.cu:26,41;
  *                                  PN/cpml/cu_cpml.cu:92,109     fd23_get_state / fd23_set_state
+ *   BOX::init_box                  PD/box/box.cpp:10-119        fd23_set_box, fd23_box_ring_*
+ *   MATERIAL::init_for_box_from_full PD/material/material.cpp:39  fd23_box_material
+ *   BOX::setboxsource / cu_copy_source
+ *                                  PD/box/box.cpp:120, PD/box/cu_box.cu:35
+ *                                         fd23_box_incident_from_displacement + fd23_set_box_incident
+ *   BOX::cu_addsource/cu_subsource, cu_step_stress_r/_velocity_r
+ *                                  PD/box/cu_box.cu:55,71; PD/fd/cu_fd.cu:504,523  fd23_run (box set)
  *
  * Conventions: every call returns FD23_OK (0) or a negative status and never
  * exits the process; fd23_strerror() names the status.  Host arrays passed in
@@ -134,7 +141,9 @@ void fd23_moment_sh(double strike, double dip, double rake, double azimuth, doub
 
 /* ---- receivers ----
  * Positions as given (the reference records each station as the pair
- * (x, z), (x-1, z); fd23_receivers_line builds that list). */
+ * (x, z), (x-1, z); fd23_receivers_line builds that list).  field is any
+ * wavefield id: the reference records U and W (V for SH); stress receivers
+ * are an addition (they record the stress after the step's update). */
 int fd23_set_receivers(fd23_solver *s, int field, const int *rx, const int *rz, int n);
 int fd23_receivers_line(int nsta, int ix0, int iz0, int idx, int idz, int *rx, int *rz);
 
@@ -164,6 +173,54 @@ int fd23_get_step(fd23_solver *s, int *it);
 size_t fd23_state_bytes(fd23_solver *s);
 int fd23_get_state(fd23_solver *s, void *buf, size_t bytes);
 int fd23_set_state(fd23_solver *s, const void *buf, size_t bytes, int it0);
+
+/* ---- hybrid box (P-SV, FD23_F32 / FD23_F64) ----
+ * A box is the grid cells [x0, x0+bx) x [z0, z0+bz), bx, bz >= 16 (the
+ * reference's box is bw x bw around the source at x0 = xs + (bw+1)/2 + 1 - bw,
+ * likewise z0; PD/box/box.cpp:26-45).  It holds a residual field r with its
+ * own material.  Two 4-cell rings couple r and the grid field g through an
+ * incident field s given on the ring cells every step:
+ *   sub ring (the outer 4 cells of the box):    r = g - s
+ *   add ring (the next 4 cells inward):         g = r + s
+ * around both half-steps, in the order of PD/main.cpp:153-199; r advances
+ * on box cells 4 .. n-5 with 8th-order stencils, no CPML (PD/fd/fd.cpp:63,208).
+ * fd23_set_box: bmat = box material LAM, MU, MUA, BU, BW (dt/h scaled,
+ *   bx*bz each, FP64) or NULL for the cut of the solver's material; r starts
+ *   at zero.  bx = bz = 0 removes the box.  FD23_ERR_UNSUPPORTED for SH and
+ *   the 16-bit forms.
+ * fd23_set_box_incident: incident field of steps it0 .. it0+nsteps-1, laid out
+ *   [step][U W Txx Txz Tzz][nring] in the compute type; ring order = sub
+ *   ring then add ring, each row by row (fd23_box_ring_cells).  U, W are the
+ *   velocities before the step, the stresses those after its stress update.
+ *   Copied to the device before the call returns.  fd23_run fails with
+ *   FD23_ERR_ORDER for a step it does not cover.
+ * fd23_get_box_state / fd23_set_box_state: r as U W Txx Txz Tzz, bx*bz each,
+ *   compute type (fd23_box_state_bytes). */
+int fd23_set_box(fd23_solver *s, int x0, int z0, int bx, int bz, const double *bmat);
+int fd23_set_box_incident(fd23_solver *s, const void *inc, int it0, int nsteps);
+size_t fd23_box_state_bytes(fd23_solver *s);
+int fd23_get_box_state(fd23_solver *s, void *buf, size_t bytes);
+int fd23_set_box_state(fd23_solver *s, const void *buf, size_t bytes);
+/* Ring geometry (host only): sizes (returns nsub + nadd), the ring position of
+ * box cell (bi, bj) (-1 if in neither ring), and the grid cells of every ring
+ * position (ix, iz: nsub + nadd entries each; returns that count). */
+int fd23_box_ring_size(int bx, int bz, int *nsub, int *nadd);
+int fd23_box_ring_index(int bx, int bz, int bi, int bj);
+int fd23_box_ring_cells(int x0, int z0, int bx, int bz, int *ix, int *iz);
+/* BOX::setboxsource (host only, FP64): the incident field of one step on the
+ * ring cells (out: 5 x nring) from the displacement planes of this step
+ * (u_old, w_old) and the next (u_new, w_new), each (bx+8) x (bz+8), box cell
+ * (i, j) at plane (i+4, j+4); bmat as for fd23_set_box (LAM, MU, MUA used).
+ * Returns nring. */
+int fd23_box_incident_from_displacement(int bx, int bz, double dt, const double *bmat,
+                                        const double *u_old, const double *w_old,
+                                        const double *u_new, const double *w_new, double *out);
+/* MATERIAL::init_for_box_from_full (host only, FP64): box material from the
+ * grid material mat (LAM MU MUA BU BW, nx*nz each); box cells that differ
+ * from the homogeneous source material (src_vp, src_vs, src_den) by more
+ * than 1e-4 are set to it in mat too.  Returns the number of such cells. */
+int fd23_box_material(int nx, int nz, double *mat, int x0, int z0, int bx, int bz, double src_vp,
+                      double src_vs, double src_den, double dt, double h, double *bmat);
 
 /* ---- diagnostics ----
  * FP64 energy-norm watchdog over the wavefield: sum of squares of all

@@ -429,6 +429,147 @@ void or_mdl_raster(int nx, int nz, double h, int npoly, const int *nvert, const 
 }
 
 /* ------------------------------------------------------------------------- */
+/* Hybrid box, host side.                                                    */
+/* ------------------------------------------------------------------------- */
+
+/* Ring sizes of a bx x bz box (both >= 16): the sub ring is the outer 4 cells
+ * of the box (PD/box/box.cpp:59-76: s0..s7 minus the open interior (s1, s6)),
+ * the add ring the next 4 cells inward (box.cpp:78-95: s2..s5 minus (s3, s4)).
+ * Returns nsub + nadd, or -1. */
+int or_box_ring_count(int bx, int bz, int *nsub, int *nadd)
+{
+    if (bx < 16 || bz < 16) return -1;
+    *nsub = 8 * (bx + bz - 8);
+    *nadd = 8 * (bx + bz - 24);
+    return *nsub + *nadd;
+}
+
+/* Ring cells in incident-field order: the sub ring row by row, then the add
+ * ring row by row (the loops of box.cpp:59-95).  gidx = row-major grid index
+ * (nx columns), ridx = row-major box index.  Returns nsub + nadd or -1. */
+int or_box_rings(int nx, int x0, int z0, int bx, int bz, long *gidx, long *ridx, int *nsub, int *nadd)
+{
+    if (or_box_ring_count(bx, bz, nsub, nadd) < 0) return -1;
+    int k = 0;
+    for (int j = 0; j < bz; j++)
+        for (int i = 0; i < bx; i++)
+            if (!(i > 3 && i < bx - 4 && j > 3 && j < bz - 4)) {
+                ridx[k] = (long)j * bx + i;
+                gidx[k] = (long)(j + z0) * nx + (i + x0);
+                k++;
+            }
+    for (int j = 4; j < bz - 4; j++)
+        for (int i = 4; i < bx - 4; i++)
+            if (!(i > 7 && i < bx - 8 && j > 7 && j < bz - 8)) {
+                ridx[k] = (long)j * bx + i;
+                gidx[k] = (long)(j + z0) * nx + (i + x0);
+                k++;
+            }
+    return k;
+}
+
+/* Incident field on the ring cells from two displacement planes, restating
+ * BOX::setboxsource (PD/box/box.cpp:120-196) for a bx x bz box.  Planes are
+ * (bx+8) x (bz+8), row-major, box cell (i, j) at plane (i+4, j+4); uo / wo
+ * are the planes of this step, un / wn of the next.  rmat = box material
+ * LAM, MU, MUA (dt/h scaled, bx*bz each).  Output [U W Txx Txz Tzz][nring]:
+ *   U = (un - uo)/dt,  W = (wn - wo)/dt,
+ *   Txx = (GAM*ux + LAM*wz)/dt, Tzz = (LAM*ux + GAM*wz)/dt, Txz = MUA*(wx+uz)/dt
+ * with derivatives of the new planes at the reduced order
+ *   ord = max(0, min(4, max(|ty-3-(bz+1)/2| - 1, |tx-3-(bx+1)/2| - 1)))
+ * (the reference's square-box formula per axis).  Expressions are evaluated
+ * left to right as written in the reference. */
+int or_box_incident_from_displacement(int bx, int bz, double dt, const double *rmat, const double *uo,
+                                      const double *wo, const double *un, const double *wn, double *out)
+{
+    int nsub, nadd;
+    const int nring = or_box_ring_count(bx, bz, &nsub, &nadd);
+    if (nring < 0) return -1;
+    const long nb = (long)bx * bz;
+    const int pw = bx + 8;
+    const double *LAM = rmat, *MU = rmat + nb, *MUA = rmat + 2 * nb;
+    long *gidx = (long *)malloc(sizeof(long) * nring), *ridx = (long *)malloc(sizeof(long) * nring);
+    if (!gidx || !ridx) {
+        free(gidx);
+        free(ridx);
+        return -1;
+    }
+    or_box_rings(bx, 0, 0, bx, bz, gidx, ridx, &nsub, &nadd);
+#define PL(a, i, j) (a)[(long)(i) + (long)(j) * pw]
+    for (int q = 0; q < nring; q++) {
+        const int bi = (int)(ridx[q] % bx), bj = (int)(ridx[q] / bx);
+        const int tx = bi + 4, ty = bj + 4;
+        int oz = abs(ty - 3 - (bz + 1) / 2) - 1, ox = abs(tx - 3 - (bx + 1) / 2) - 1;
+        int ord = oz > ox ? oz : ox;
+        if (ord > 4) ord = 4;
+        if (ord < 0) ord = 0;
+        const double *c = OR_COEF[ord];
+        const double ux = c[0] * (PL(un, tx, ty) - PL(un, tx - 1, ty)) - c[1] * (PL(un, tx + 1, ty) - PL(un, tx - 2, ty)) +
+                          c[2] * (PL(un, tx + 2, ty) - PL(un, tx - 3, ty)) - c[3] * (PL(un, tx + 3, ty) - PL(un, tx - 4, ty));
+        const double uz = c[0] * (PL(un, tx, ty) - PL(un, tx, ty - 1)) - c[1] * (PL(un, tx, ty + 1) - PL(un, tx, ty - 2)) +
+                          c[2] * (PL(un, tx, ty + 2) - PL(un, tx, ty - 3)) - c[3] * (PL(un, tx, ty + 3) - PL(un, tx, ty - 4));
+        const double wx = c[0] * (PL(wn, tx + 1, ty) - PL(wn, tx, ty)) - c[1] * (PL(wn, tx + 2, ty) - PL(wn, tx - 1, ty)) +
+                          c[2] * (PL(wn, tx + 3, ty) - PL(wn, tx - 2, ty)) - c[3] * (PL(wn, tx + 4, ty) - PL(wn, tx - 3, ty));
+        const double wz = c[0] * (PL(wn, tx, ty + 1) - PL(wn, tx, ty)) - c[1] * (PL(wn, tx, ty + 2) - PL(wn, tx, ty - 1)) +
+                          c[2] * (PL(wn, tx, ty + 3) - PL(wn, tx, ty - 2)) - c[3] * (PL(wn, tx, ty + 4) - PL(wn, tx, ty - 3));
+        const long b = ridx[q];
+        const double lam = LAM[b], mu = MU[b], mua = MUA[b];
+        const double gam = lam + 2.0 * mu;
+        out[0L * nring + q] = (PL(un, tx, ty) - PL(uo, tx, ty)) / dt;
+        out[1L * nring + q] = (PL(wn, tx, ty) - PL(wo, tx, ty)) / dt;
+        out[2L * nring + q] = (gam * ux + lam * wz) / dt;
+        out[3L * nring + q] = (mua * (wx + uz)) / dt;
+        out[4L * nring + q] = (lam * ux + gam * wz) / dt;
+    }
+#undef PL
+    free(gidx);
+    free(ridx);
+    return nring;
+}
+
+/* Box material cut from the full (dt/h scaled) material, restating
+ * MATERIAL::init_for_box_from_full (PD/material/material.cpp:39-97): every box
+ * cell whose BU, BW differ from b = dt/(h*srcden), MU, MUA from
+ * mu = srcvs^2*srcden*dt/h, or LAM from lam = (srcvp^2*srcden - 2 mu)*dt/h by
+ * more than 1e-4 relative is set to the homogeneous values IN THE FULL
+ * material; the box copy follows.  mat / rmat: LAM MU MUA BU BW.  Returns the
+ * number of cells replaced. */
+int or_box_material(int nx, int nz, double *mat, int x0, int z0, int bx, int bz, double srcvp, double srcvs,
+                    double srcden, double dt, double h, double *rmat)
+{
+    const long n = (long)nx * nz, nb = (long)bx * bz;
+    double mu = srcvs * srcvs * srcden;
+    double lam = (srcvp * srcvp * srcden - 2.0 * mu);
+    double b = 1.0 / srcden;
+    mu = mu * dt / h;
+    lam = lam * dt / h;
+    b = b * dt / h;
+    const double eps = 1E-4;
+    double *LAM = mat, *MU = mat + n, *MUA = mat + 2 * n, *BU = mat + 3 * n, *BW = mat + 4 * n;
+    int nrep = 0;
+    for (int j = 0; j < bz; j++)
+        for (int i = 0; i < bx; i++) {
+            const long g = (long)(i + x0) + (long)(j + z0) * nx, k = (long)i + (long)j * bx;
+            if (fabs(b - BU[g]) > b * eps || fabs(b - BW[g]) > b * eps || fabs(mu - MU[g]) > mu * eps ||
+                fabs(mu - MUA[g]) > mu * eps || fabs(lam - LAM[g]) > lam * eps) {
+                BU[g] = b;
+                BW[g] = b;
+                MU[g] = mu;
+                MUA[g] = mu;
+                LAM[g] = lam;
+                nrep++;
+            }
+            rmat[k] = LAM[g];
+            rmat[nb + k] = MU[g];
+            rmat[2 * nb + k] = MUA[g];
+            rmat[3 * nb + k] = BU[g];
+            rmat[4 * nb + k] = BW[g];
+        }
+    return nrep;
+}
+
+
+/* ------------------------------------------------------------------------- */
 /* Time stepping, instantiated for double and float.                         */
 /* ------------------------------------------------------------------------- */
 #define REAL double

@@ -46,6 +46,13 @@ def lib():
         for nm in ("or_sh_run_f64", "or_sh_run_f32"):
             getattr(_lib, nm).argtypes = [i, i, i, i, vp, vp, i, vp, vp, vp, i, i, vp,
                                           i, i, i, vp, vp, i]
+        _lib.or_box_ring_count.argtypes = [i, i, vp, vp]
+        _lib.or_box_rings.argtypes = [i, i, i, i, i, vp, vp, vp, vp]
+        _lib.or_box_incident_from_displacement.argtypes = [i, i, d, vp, vp, vp, vp, vp, vp]
+        _lib.or_box_material.argtypes = [i, i, vp, i, i, i, i, d, d, d, d, d, vp]
+        for nm in ("or_psv_box_run_f64", "or_psv_box_run_f32"):
+            getattr(_lib, nm).argtypes = [i, i, i, i, vp, vp, i, vp, vp, vp, i, i, vp, vp,
+                                          i, i, i, vp, vp, i, i, i, i, vp, vp, vp, i]
     return _lib
 
 
@@ -311,6 +318,104 @@ def sh_run(prec, nx, nz, npml, topabsorb, mat, bck, terms, rec, nt, itrecord=1, 
        _p(amp_r) if len(field) else None, nt_amp, len(r), _p(r), it0, nt, itrecord, _p(state),
        _p(s), nthreads)
     return s, state
+
+
+# ---------------------------------------------------------------- hybrid box
+def box_ring_count(bx, bz):
+    """(nsub, nadd) ring sizes of a bx x bz box (PD/box/box.cpp:59-95)."""
+    ns = np.zeros(1, np.int32)
+    na = np.zeros(1, np.int32)
+    if lib().or_box_ring_count(bx, bz, _p(ns), _p(na)) < 0:
+        raise ValueError("box must be at least 16 x 16")
+    return int(ns[0]), int(na[0])
+
+
+def box_rings(nx, x0, z0, bx, bz):
+    """Ring cells in incident-field order: (grid flat index, box flat index,
+    nsub)."""
+    nsub, nadd = box_ring_count(bx, bz)
+    g = np.zeros(nsub + nadd, np.int64)
+    r = np.zeros(nsub + nadd, np.int64)
+    ns = np.zeros(1, np.int32)
+    na = np.zeros(1, np.int32)
+    lib().or_box_rings(nx, x0, z0, bx, bz, _p(g), _p(r), _p(ns), _p(na))
+    return g, r, nsub
+
+
+def box_incident_from_displacement(bx, bz, dt, rmat, uo, wo, un, wn):
+    """BOX::setboxsource restated (PD/box/box.cpp:120-196): ring incident
+    field [5, nring] from displacement planes of shape (bz+8, bx+8)."""
+    nsub, nadd = box_ring_count(bx, bz)
+    out = np.zeros((5, nsub + nadd))
+    a = [np.ascontiguousarray(v, dtype=np.float64) for v in (rmat, uo, wo, un, wn)]
+    lib().or_box_incident_from_displacement(bx, bz, dt, *[_p(v) for v in a], _p(out))
+    return out
+
+
+def box_material(mat, x0, z0, bx, bz, srcvp, srcvs, srcden, dt, h):
+    """MATERIAL::init_for_box_from_full restated (PD/material/material.cpp:39-97).
+    Returns (full material with the box homogenised, box material, cells
+    replaced)."""
+    m = np.ascontiguousarray(mat, dtype=np.float64).copy()
+    nz, nx = m.shape[1], m.shape[2]
+    rm = np.zeros((5, bz, bx))
+    n = lib().or_box_material(nx, nz, _p(m), x0, z0, bx, bz, srcvp, srcvs, srcden, dt, h, _p(rm))
+    return m, rm, n
+
+
+def psv_box_run(prec, nx, nz, npml, topabsorb, mat, bck, terms, rec_field, rec_idx, nt, box, rmat,
+                inc, itrecord=1, it0=0, state=None, rstate=None, nthreads=0):
+    """Hybrid-box P-SV run.  box = (x0, z0, bx, bz); rmat (5, bz, bx); inc
+    [nt, 5, nring] for steps it0 .. it0+nt-1; receivers are (field, flat
+    index) pairs.  Returns (seis [nrec_steps, nrec], state, rstate)."""
+    dt_ = np.float64 if prec == "f64" else np.float32
+    fn = lib().or_psv_box_run_f64 if prec == "f64" else lib().or_psv_box_run_f32
+    x0, z0, bx, bz = box
+    mat_r = np.ascontiguousarray(mat, dtype=dt_)
+    bck_r = np.ascontiguousarray(bck, dtype=dt_)
+    field, idx, amp = terms
+    field = np.ascontiguousarray(field, dtype=np.int32)
+    idx = np.ascontiguousarray(idx, dtype=np.int64)
+    amp_r = np.ascontiguousarray(amp, dtype=dt_)
+    rf = np.ascontiguousarray(rec_field, dtype=np.int32)
+    ri = np.ascontiguousarray(rec_idx, dtype=np.int64)
+    state = (np.zeros(psv_state_size(nx, nz, npml), dtype=dt_) if state is None
+             else np.ascontiguousarray(state, dtype=dt_).copy())
+    rstate = (np.zeros(5 * bx * bz, dtype=dt_) if rstate is None
+              else np.ascontiguousarray(rstate, dtype=dt_).copy())
+    rmat_r = np.ascontiguousarray(rmat, dtype=dt_)
+    inc_r = np.ascontiguousarray(inc, dtype=dt_)
+    nrecs = len([it for it in range(it0, it0 + nt) if it % itrecord == 0])
+    seis = np.zeros((nrecs, len(rf)), dtype=dt_)
+    nt_amp = amp_r.shape[1] if amp_r.ndim == 2 and len(field) else 0
+    rc = fn(nx, nz, npml, int(topabsorb), _p(mat_r), _p(bck_r), len(field), _p(field), _p(idx),
+            _p(amp_r) if len(field) else None, nt_amp, len(rf), _p(rf), _p(ri), it0, nt, itrecord,
+            _p(state), _p(seis), x0, z0, bx, bz, _p(rmat_r), _p(rstate), _p(inc_r), nthreads)
+    if rc < 0:
+        raise ValueError("bad box")
+    return seis, state, rstate
+
+
+def psv_ring_history(prec, nx, nz, npml, topabsorb, mat, bck, terms, nt, box, it0=0, state=None):
+    """Run the plain P-SV oracle step by step and collect, for each step it,
+    the incident field a box driven by this run needs: U, W before the step
+    and Txx, Txz, Tzz after its stress update and source, on the ring cells.
+    Returns (inc [nt, 5, nring], final state)."""
+    x0, z0, bx, bz = box
+    g, _, _ = box_rings(nx, x0, z0, bx, bz)
+    n = nx * nz
+    dt_ = np.float64 if prec == "f64" else np.float32
+    st = (np.zeros(psv_state_size(nx, nz, npml), dtype=dt_) if state is None
+          else np.asarray(state, dtype=dt_).copy())
+    inc = np.zeros((nt, 5, len(g)), dtype=dt_)
+    for k in range(nt):
+        inc[k, 0] = st[g]
+        inc[k, 1] = st[n + g]
+        _, _, st = psv_run(prec, nx, nz, npml, topabsorb, mat, bck, terms, [], [], 1, 1,
+                           it0=it0 + k, state=st)
+        for f in range(2, 5):
+            inc[k, f] = st[f * n + g]
+    return inc, st
 
 
 def rel_l2(a, b):
