@@ -15,8 +15,16 @@ roofline: the fused sweep kernel against the measured HBM copy bandwidth.
 cpu_baseline: the oracle's restatement of the reference update loop on the
        host cores, on a bounded sample of the same grid.
 
+Hybrid-box workload (--config c2): the same model and grid, 3000 steps,
+  a 2000 x 1000 box at (1000, 10) around the source with 4-cell add and sub
+  rings.  The incident field on the ring cells (U, W, Txx, Txz, Tzz every
+  step, 2.9 GB FP32) is recorded from a plain run of the same shot; the box
+  run has no point source.  Its surface seismograms must equal the recorded
+  run's bit for bit ("check" in the output line).
+
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--nt NT] [--prec f32|bf16|f16|f64] [--kernel fused|twopass]
+                  [--config c1|c2] [--nt NT] [--prec f32|bf16|f16|f64]
+                  [--kernel fused|twopass]
 """
 import argparse
 import json
@@ -35,6 +43,8 @@ if ROOT not in sys.path:
 
 NX, NZ, H, DT, NT, NPML, F0 = 4000, 2000, 5.0, 4e-4, 5000, 40, 15.0
 NSTA = 400
+# hybrid-box workload: box origin and size, steps
+BOX_X0, BOX_Z0, BOX_BX, BOX_BZ, NT_BOX = 1000, 10, 2000, 1000, 3000
 
 
 def c1_model(nx=NX, nz=NZ, seed=1):
@@ -63,6 +73,15 @@ def alg_bytes(nx, nz, npml, es, topabsorb=0):
     cs = 8 if es == 8 else 4
     npml_cells = 2 * npml * nz + npml * nx * (1 + topabsorb)
     return (5 * 2 + 5) * es * nx * nz + 4 * 2 * cs * npml_cells
+
+
+def box_alg_bytes(bx, bz, nring, es):
+    """Compulsory HBM bytes the box adds to one step: the residual stress
+    update (read U W Txx Txz Tzz LAM MU MUA, write Txx Txz Tzz) and velocity
+    update (read Txx Txz Tzz U W BU BW, write U W) on the (bx-8)(bz-8)
+    interior cells, and per ring cell the incident field (5 values) and the
+    exchange (read r or g, write g or r, for 5 fields)."""
+    return 20 * es * (bx - 8) * (bz - 8) + 15 * es * nring
 
 
 def load_peaks():
@@ -177,6 +196,7 @@ def main():
     ap.add_argument("--kernel", default="fused")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--config", default="c1", choices=["c1", "c2"])
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -196,6 +216,9 @@ def main():
     import torch
     import fd23_gb300 as F
     torch.cuda.set_device(local)
+    if args.config == "c2":
+        bench_box(args, F, torch, rank, world, local, dist)
+        return
     nt = args.nt
     vp, vs, rho = c1_model(seed=1 + rank)
     pml_v = float(vp.max()) / H
@@ -289,6 +312,160 @@ def main():
             "e2e": e2e}
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    s.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def cpu_baseline_box(inc, budget_s=12.0, threads=0):
+    """Oracle box run (FP32, all host threads) on the benchmark grid for as
+    many steps as fit the budget, driven by the first steps of the recorded
+    incident field."""
+    from oracle import fd23_oracle as O
+    vp, vs, rho = c1_model()
+    mat, _, _ = O.psv_material(vp, vs, rho, H, DT)
+    bck = O.cpml_psv(NX, NZ, NPML, DT, 1e-11, vp.max() / H, F0)
+    box = (BOX_X0, BOX_Z0, BOX_BX, BOX_BZ)
+    rmat = np.ascontiguousarray(mat[:, BOX_Z0:BOX_Z0 + BOX_BZ, BOX_X0:BOX_X0 + BOX_BX])
+    none = (np.zeros(0, np.int32), np.zeros(0, np.int64), np.zeros((0, 1)))
+    rf = np.zeros(NSTA, np.int32)
+    ri = np.arange(200, 200 + 9 * NSTA, 9).astype(np.int64)
+    t0 = time.perf_counter()
+    O.psv_box_run("f32", NX, NZ, NPML, 0, mat, bck, none, rf, ri, 1, box, rmat, inc[:1],
+                  nthreads=threads)
+    one = time.perf_counter() - t0
+    steps = int(max(3, min(100, budget_s / max(one, 1e-3), inc.shape[0])))
+    t0 = time.perf_counter()
+    O.psv_box_run("f32", NX, NZ, NPML, 0, mat, bck, none, rf, ri, steps, box, rmat, inc[:steps],
+                  nthreads=threads)
+    t_used = time.perf_counter() - t0
+    cores = threads if threads > 0 else (os.cpu_count() or 1)
+    return {"value": NX * NZ * steps / t_used, "unit": "cell-updates/s", "cores": cores,
+            "kind": "port",
+            "sample": "%d box steps of the %dx%d grid with the %dx%d box (%.1f s), FP32 oracle, "
+                      "%d threads" % (steps, NX, NZ, BOX_BX, BOX_BZ, t_used, cores)}
+
+
+def bench_box(args, F, torch, rank, world, local, dist):
+    """Hybrid-box workload: record the ring field of a plain run, then time box
+    runs driven by it."""
+    nt = min(args.nt, NT_BOX)
+    vp, vs, rho = c1_model(seed=1 + rank)
+    pml_v = float(vp.max()) / H
+    kw = dict(prec="f32", pml_dt=DT, pml_v=pml_v, pml_r=1e-11, pml_fc=F0, device=local,
+              kernel=args.kernel)
+    src = F.wavelet_ricker(DT, F0)
+    rxu, rzu = F.receivers_line(NSTA, 200, 0, 9, 0)
+    rxw, rzw = F.receivers_line(NSTA, 200, 1, 9, 0)
+    rix, riz = F.box_ring_cells(BOX_X0, BOX_Z0, BOX_BX, BOX_BZ)
+    nring = len(rix)
+    # 1. the recorded run: point source, surface lines + every ring cell
+    p = F.Solver("psv", NX, NZ, NPML, H, DT, **kw)
+    p.set_model(vp, vs, rho)
+    p.set_source(F.SRC_EXPLOSION, NX // 2, 20, None, src, nt)
+    lines = {0: (rxu, rzu), 1: (rxw, rzw)}
+    for f in range(5):
+        lx, lz = lines.get(f, (np.zeros(0, np.int32), np.zeros(0, np.int32)))
+        p.set_receivers(f, np.concatenate([lx, rix]), np.concatenate([lz, riz]))
+    p.run(nt, 1)
+    nl = len(rxu)
+    inc = torch.empty((nt, 5, nring), dtype=torch.float32, pin_memory=True).numpy()
+    ref_traces = {}
+    for f in range(5):
+        sg = p.seismograms(f)
+        k = nl if f < 2 else 0
+        if f < 2:
+            ref_traces[f] = sg[:, :nl].copy()
+            inc[0, f] = 0.0
+            inc[1:, f] = sg[:-1, k:]   # velocities before the step
+        else:
+            inc[:, f] = sg[:, k:]      # stresses after the step's stress update
+        del sg
+    p.close()
+    # 2. the box solver: no point source
+    s = F.Solver("psv", NX, NZ, NPML, H, DT, **kw)
+    s.set_model(vp, vs, rho)
+    s.set_receivers(0, rxu, rzu)
+    s.set_receivers(1, rxw, rzw)
+    s.set_box(BOX_X0, BOX_Z0, BOX_BX, BOX_BZ)
+    s.set_box_incident(inc, 0)
+    stream = torch.cuda.ExternalStream(s.stream, device=local)
+
+    def shot():
+        s.reset()
+        s.run(nt, 1)
+
+    for _ in range(args.warmup):
+        shot()
+    check = bool(np.array_equal(s.seismograms(0), ref_traces[0]) and
+                 np.array_equal(s.seismograms(1), ref_traces[1]))
+    s.sync()
+    sampler = ClockSampler(local)
+    if rank == 0:
+        sampler.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        shot()
+    e1.record(stream)
+    s.sync()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    clocks = sampler.stop() if rank == 0 else None
+    t = torch.tensor([ms], dtype=torch.float64)
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t[0])
+    value = NX * NZ * nt * args.steps * world / (ms_max * 1e-3)
+
+    e2e = None
+    if not args.no_e2e:
+        times = []
+        seis_bytes = 0
+        for _ in range(max(1, min(args.steps, 2))):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            s.set_model(vp, vs, rho)
+            s.set_box(BOX_X0, BOX_Z0, BOX_BX, BOX_BZ)
+            s.set_box_incident(inc, 0)
+            shot()
+            su, sw = s.seismograms(0), s.seismograms(1)
+            times.append(time.perf_counter() - t0)
+            seis_bytes = su.nbytes + sw.nbytes
+        e2e = {"value": NX * NZ * nt / statistics.mean(times) * world, "unit": "cell-updates/s",
+               "h2d_bytes_per_step": 5 * NX * NZ * 4 + inc.nbytes, "d2h_bytes_per_step": seis_bytes,
+               "note": "per step = one whole box shot; the incident field is uploaded from pinned "
+                       "host memory inside the timed region"}
+    hbm, peak_kind = load_peaks()
+    per_step_ms = ms_max / (args.steps * nt)
+    ab = alg_bytes(NX, NZ, NPML, 4) + box_alg_bytes(BOX_BX, BOX_BZ, nring, 4)
+    achieved = ab / (per_step_ms * 1e-3) / 1e9
+    line = {"metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "psv_4000x2000_3000steps_box2000x1000_c2", "nx": NX, "nz": NZ,
+                       "nt": nt, "box": [BOX_X0, BOX_Z0, BOX_BX, BOX_BZ], "ring_cells": nring,
+                       "incident_bytes": inc.nbytes, "kernel": args.kernel,
+                       "cells_counted": "grid cells nx*nz per step (the box's residual field is "
+                                        "extra work)",
+                       "l2": "inputs larger than L2", "parallelism": "replicas x%d" % world},
+            "check": {"surface_traces_bit_exact_vs_recorded_run": check},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "traffic": None, "peak_source": peak_kind,
+                         "scope": "whole step: sweep + box kernels",
+                         "alg_bytes_per_launch": ab, "launch_ms": per_step_ms},
+            "gpu_launches": args.steps * nt * 4,
+            "clocks": clocks,
+            "e2e": e2e}
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline_box(inc)
     if rank == 0:
         print(json.dumps(line), flush=True)
     s.close()

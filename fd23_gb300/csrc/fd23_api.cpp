@@ -269,8 +269,8 @@ Shot<S, C> make_shot(const fd23_solver *s)
 
 // One time step.  Without a box the fused sweep gathers the previous step's
 // receivers on its way; with a box the step is
-//   ring(U,W) + residual stress | sweep (stress ring inside) | receivers +
-//   residual velocity
+//   ring(U,W) | residual stress (+ add-ring g) | sweep | sub-ring r |
+//   receivers + residual velocity
 // (PD/main.cpp:153-199 order; the exchanges that read only fields the next
 // update leaves unchanged run earlier, with the same values).
 template <class S, class C>
@@ -279,7 +279,7 @@ int step_impl(fd23_solver *s, int rec_now)
     Shot<S, C> sh = make_shot<S, C>(s);
     const bool box = s->box_on;
     int rc = FD23_OK;
-    if (box && (rc = launch_box_pre<S, C>(sh, s->fused ? s->par : 0, s->stream))) return rc;
+    if (box && (rc = launch_box_pre<S, C>(sh, s->fused ? s->par : 0, s->fused, s->stream))) return rc;
     if (s->fused) {
         rc = launch_step_fused<S, C>(sh, s->d.wave, s->d_items, s->d_item_off, s->nblocks, s->par, s->it,
                                      s->pending_rec, s->err_flag, s->stream);
@@ -294,7 +294,7 @@ int step_impl(fd23_solver *s, int rec_now)
     }
     if (box) {
         const int ri = rec_now ? s->nrec_steps++ : -1;
-        if ((rc = launch_box_post<S, C>(sh, s->fused ? s->par : 0, ri, s->stream))) return rc;
+        if ((rc = launch_box_post<S, C>(sh, s->fused ? s->par : 0, s->fused, ri, s->stream))) return rc;
     }
     s->it++;
     return FD23_OK;

@@ -8,9 +8,12 @@
 // residual updates cover cells 4 .. n-5 of the box (the outer 4 are the sub
 // ring, rewritten from g before every read), with one thread per cell.
 //
-// The stress exchange of the fused sweep is done inside that sweep (after
-// the point source, before the velocity stencil reads the stresses); the
-// kernel here serves the two-pass sweep.
+// Stress exchange around the fused sweep: the residual stress update writes
+// g = r + s into the old-stress slot of every add-ring cell, and the sweep
+// keeps that value there instead of updating it (it is what the exchange
+// after the stress update and the point source would store); after the sweep
+// a ring kernel forms r = g - s on the sub ring.  The two-pass sweep runs the
+// full stress exchange between its passes instead.
 #include "fd23_device.cuh"
 #include "fd23_kernels.h"
 
@@ -31,12 +34,13 @@ __device__ __forceinline__ C dplus_r(const C *p, long long s)
                    p[3 * s] - p[-2 * s], p[4 * s] - p[-3 * s]);
 }
 
-// ring exchange of fields F0 .. F1-1 on buffer set `par`
+// ring exchange of fields F0 .. F1-1 on buffer set `par`, ring positions
+// [0, qend) (qend = nsub: the sub ring only)
 template <class S, class C, int F0, int F1>
-__global__ void __launch_bounds__(256) box_ring_kernel(Shot<S, C> s, int par)
+__global__ void __launch_bounds__(256) box_ring_kernel(Shot<S, C> s, int par, int qend)
 {
     const Box<C> &b = s.box;
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < b.nring; q += gridDim.x * blockDim.x) {
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < qend; q += gridDim.x * blockDim.x) {
         const int2 c = b.cells[q];
         const long long g = s.origin + (long long)(b.z0 + c.y) * s.pitch + (b.x0 + c.x);
         const long long r = (long long)c.y * b.bx + c.x;
@@ -52,10 +56,13 @@ __global__ void __launch_bounds__(256) box_ring_kernel(Shot<S, C> s, int par)
 }
 
 // residual stress update, cells 4 .. n-5 of the box; the accumulation order
-// is that of the main update (x terms, then z terms)
-template <class C>
-__global__ void __launch_bounds__(256) box_stress_r(Box<C> b)
+// is that of the main update (x terms, then z terms).  On add-ring cells it
+// also stores g = r + s into the grid stresses of buffer set `par` (the
+// fused sweep's old-stress slot); add_g = 0 skips that.
+template <class S, class C>
+__global__ void __launch_bounds__(256) box_stress_r(Shot<S, C> s, int par, int add_g)
 {
+    const Box<C> &b = s.box;
     const int ix = 4 + blockIdx.x * 32 + threadIdx.x, iz = 4 + blockIdx.y * 8 + threadIdx.y;
     if (ix >= b.bx - 4 || iz >= b.bz - 4) return;
     const long long o = (long long)iz * b.bx + ix, P = b.bx;
@@ -73,6 +80,18 @@ __global__ void __launch_bounds__(256) box_stress_r(Box<C> b)
     b.r[2][o] = txx;
     b.r[3][o] = txz;
     b.r[4][o] = tzz;
+    if (add_g) {
+        const int q = box_ring_index(ix, iz, b.bx, b.bz);
+        if (q >= b.nsub) {
+            const long long g = s.origin + (long long)(b.z0 + iz) * s.pitch + (b.x0 + ix);
+            const C t[3] = {txx, txz, tzz};
+#pragma unroll
+            for (int f = 0; f < 3; ++f) {
+                S *G = par ? s.f[1][2 + f] : s.f[0][2 + f];
+                G[g] = to_s<S>(t[f] + b.inc[(long long)(2 + f) * b.nring + q]);
+            }
+        }
+    }
 }
 
 // receivers of this step's output (buffer set `par`, before the next ring
@@ -115,31 +134,34 @@ inline unsigned ring_blocks(int nring) { return (unsigned)((nring + 255) / 256);
 template <class S, class C>
 int launch_box_ring(const Shot<S, C> &s, int par, int which, cudaStream_t st)
 {
-    if (which == 0) box_ring_kernel<S, C, 0, 2><<<ring_blocks(s.box.nring), 256, 0, st>>>(s, par);
-    else box_ring_kernel<S, C, 2, 5><<<ring_blocks(s.box.nring), 256, 0, st>>>(s, par);
+    const int n = s.box.nring;
+    if (which == 0) box_ring_kernel<S, C, 0, 2><<<ring_blocks(n), 256, 0, st>>>(s, par, n);
+    else box_ring_kernel<S, C, 2, 5><<<ring_blocks(n), 256, 0, st>>>(s, par, n);
     return cudaPeekAtLastError() == cudaSuccess ? FD23_OK : FD23_ERR_CUDA;
 }
 
 template <class S, class C>
-int launch_box_pre(const Shot<S, C> &s, int par, cudaStream_t st)
+int launch_box_pre(const Shot<S, C> &s, int par, int fused, cudaStream_t st)
 {
     const int rc = launch_box_ring<S, C>(s, par, 0, st);
     if (rc) return rc;
-    box_stress_r<C><<<interior_grid(s.box.bx, s.box.bz), dim3(32, 8), 0, st>>>(s.box);
+    box_stress_r<S, C><<<interior_grid(s.box.bx, s.box.bz), dim3(32, 8), 0, st>>>(s, par, fused);
     return cudaPeekAtLastError() == cudaSuccess ? FD23_OK : FD23_ERR_CUDA;
 }
 
 template <class S, class C>
-int launch_box_post(const Shot<S, C> &s, int par, int rec_index, cudaStream_t st)
+int launch_box_post(const Shot<S, C> &s, int par, int fused, int rec_index, cudaStream_t st)
 {
+    if (fused)  // sub-ring stresses r = g - s (the two-pass sweep did the whole exchange)
+        box_ring_kernel<S, C, 2, 5><<<ring_blocks(s.box.nsub), 256, 0, st>>>(s, par, s.box.nsub);
     box_velocity_r<S, C><<<interior_grid(s.box.bx, s.box.bz), dim3(32, 8), 0, st>>>(s, par, rec_index);
     return cudaPeekAtLastError() == cudaSuccess ? FD23_OK : FD23_ERR_CUDA;
 }
 
 #define FD23_INST(S, C)                                                                  \
     template int launch_box_ring<S, C>(const Shot<S, C> &, int, int, cudaStream_t);     \
-    template int launch_box_pre<S, C>(const Shot<S, C> &, int, cudaStream_t);           \
-    template int launch_box_post<S, C>(const Shot<S, C> &, int, int, cudaStream_t);
+    template int launch_box_pre<S, C>(const Shot<S, C> &, int, int, cudaStream_t);      \
+    template int launch_box_post<S, C>(const Shot<S, C> &, int, int, int, cudaStream_t);
 FD23_INST(float, float)
 FD23_INST(double, double)
 FD23_INST(__nv_bfloat16, float)

@@ -29,6 +29,9 @@
 //   * Wavefields and memory variables are ping-pong buffers (read set `par`,
 //     write set 1-par), so the recomputed halo columns and rows of one CTA
 //     never observe another CTA's new values.
+//   * With a hybrid box (P-SV), add-ring stresses keep the value of their
+//     old-stress slot, r + s, which the residual stress update stored there
+//     before this launch; the rest of the box exchange runs in fd23_box.cu.
 //   * All arrays use the zero-padded layout of fd23_internal.h, so every row
 //     copy is in bounds and 16-byte aligned and the zero halo of the
 //     reference needs no test.
@@ -723,32 +726,24 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
                         for (int f = 0; f < K::NT; ++f) Vec4<S, C>::ld(tr + f * K::SW, tnew[f]);
                     }
                 }
-                // ---- hybrid box, after the point source: add-ring stresses
-                // become r + s (every column, the halo ones feed the velocity
-                // stencil), sub-ring cells give r = T - s (owned cells only) ----
+                // ---- hybrid box, after the point source: an add-ring cell takes
+                // the value its old-stress slot holds, r + s, written there by
+                // the residual stress update before this launch (every column:
+                // halo columns feed the velocity stencil too).  Shared-memory
+                // copies only: the old stresses are still in the point-wise stage.
                 if constexpr (PSV && std::is_same<S, C>::value) {
-                    const int bj = j - sh.box.z0;
-                    if (sh.box.on && bj >= 0 && bj < sh.box.bz && x + 3 >= sh.box.x0 &&
-                        x < sh.box.x0 + sh.box.bx) {
-                        const bool own_row = inrow && own_x && j >= I.z0 && j < I.z1;
-                        const int nsub = sh.box.nsub, nring = sh.box.nring;
+                    const int aj = j - sh.box.z0 - 4, ai0 = x - sh.box.x0 - 4;
+                    const int aw = sh.box.bx - 8, ah = sh.box.bz - 8;
+                    if (sh.box.on && aj >= 0 && aj < ah && ai0 + 3 >= 0 && ai0 < aw &&
+                        (aj < 4 || aj >= ah - 4 || ai0 < 4 || ai0 + 3 >= aw - 4)) {
                         bool changed = false;
 #pragma unroll
                         for (int e = 0; e < 4; ++e) {
-                            const int bi = x + e - sh.box.x0;
-                            const int q = box_ring_index(bi, bj, sh.box.bx, sh.box.bz);
-                            if (q < 0) continue;
-                            const long long rr = (long long)bj * sh.box.bx + bi;
-                            // read-modify-write of the ring cells just written
-                            if (q >= nsub) {
+                            const int ai = ai0 + e;
+                            if (ai >= 0 && ai < aw && (aj < 4 || aj >= ah - 4 || ai < 4 || ai >= aw - 4)) {
 #pragma unroll
-                                for (int f = 0; f < 3; ++f)
-                                    tr[f * K::SW + e] = sh.box.r[2 + f][rr] + sh.box.inc[(long long)(2 + f) * nring + q];
+                                for (int f = 0; f < K::NT; ++f) tr[f * K::SW + e] = pwrow(f)[e];
                                 changed = true;
-                            } else if (own_row) {
-#pragma unroll
-                                for (int f = 0; f < 3; ++f)
-                                    sh.box.r[2 + f][rr] = tr[f * K::SW + e] - sh.box.inc[(long long)(2 + f) * nring + q];
                             }
                         }
                         if (changed) {

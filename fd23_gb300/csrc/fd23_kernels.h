@@ -38,12 +38,15 @@ int launch_step_fused(const Shot<S, C> &s, int wave, const WorkItem *items, cons
 template <class S, class C>
 int launch_box_ring(const Shot<S, C> &s, int par, int which, cudaStream_t st);
 // start of a step: ring exchange of U, W, then the residual stress update
+// (fused != 0: which also stores g = r + s into the add-ring stresses of
+// buffer set `par`, the fused sweep's part of the stress exchange)
 template <class S, class C>
-int launch_box_pre(const Shot<S, C> &s, int par, cudaStream_t st);
-// end of a step: receivers of buffer set `par` into record row `rec_index`
-// (if >= 0), then the residual velocity update
+int launch_box_pre(const Shot<S, C> &s, int par, int fused, cudaStream_t st);
+// end of a step: (fused != 0: sub-ring stresses r = g - s from buffer set
+// `par`), receivers of buffer set `par` into record row `rec_index` (if >= 0),
+// then the residual velocity update
 template <class S, class C>
-int launch_box_post(const Shot<S, C> &s, int par, int rec_index, cudaStream_t st);
+int launch_box_post(const Shot<S, C> &s, int par, int fused, int rec_index, cudaStream_t st);
 
 // FP64 sum of squares over the `elems` stored elements of each of the first
 // `nfields` wavefields of buffer set `par` (the zero padding included); the
