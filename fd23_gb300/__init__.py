@@ -52,7 +52,9 @@ ABI_FUNCTIONS = [
     "fd23_build_source_terms", "fd23_sum_squares_noalloc", "fd23_set_box", "fd23_set_box_incident",
     "fd23_box_state_bytes", "fd23_get_box_state", "fd23_set_box_state", "fd23_box_ring_size",
     "fd23_box_ring_index", "fd23_box_ring_cells", "fd23_box_incident_from_displacement",
-    "fd23_box_material",
+    "fd23_box_material", "fd23_batch_create", "fd23_batch_destroy", "fd23_batch_run", "fd23_batch_sync",
+    "fd23_batch_get_stream", "fd23_batch_set_graph", "fd23_autotune", "fd23_batch_autotune",
+    "fd23_batch_get_plan",
 ]
 
 
@@ -61,6 +63,14 @@ class Fd23Error(RuntimeError):
         self.status = status
         msg = lib().fd23_strerror(status).decode() if _lib is not None else str(status)
         super().__init__("%s: %s (status %d)" % (where, msg, status))
+
+
+class TuneEntry(_C.Structure):
+    _fields_ = [("wx", _C.c_double), ("wz", _C.c_double), ("per_sm", _C.c_int),
+                ("oversub", _C.c_double), ("ms_per_step", _C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class Desc(_C.Structure):
@@ -125,6 +135,15 @@ def lib():
         "fd23_box_ring_cells": ([i, i, i, i, vp, vp], i),
         "fd23_box_incident_from_displacement": ([i, i, d, vp, vp, vp, vp, vp, vp], i),
         "fd23_box_material": ([i, i, vp, i, i, i, i, d, d, d, d, d, vp], i),
+        "fd23_batch_create": ([vp, i, _C.POINTER(vp)], i),
+        "fd23_batch_destroy": ([vp], None),
+        "fd23_batch_run": ([vp, i, i], i),
+        "fd23_batch_sync": ([vp], i),
+        "fd23_batch_get_stream": ([vp, _C.POINTER(vp)], i),
+        "fd23_batch_set_graph": ([vp, i], i),
+        "fd23_autotune": ([vp, i, vp, i], i),
+        "fd23_batch_autotune": ([vp, i, vp, i], i),
+        "fd23_batch_get_plan": ([vp, vp, _C.POINTER(i)], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -280,6 +299,59 @@ def box_material(mat, x0, z0, bx, bz, src_vp, src_vs, src_den, dt, h):
     return m, bm, n
 
 
+class Batch:
+    """Several solvers advanced in lockstep, one sweep launch per step for all
+    shots (CUDA-graph captured)."""
+
+    def __init__(self, solvers):
+        self.solvers = list(solvers)
+        arr = (_C.c_void_p * len(self.solvers))(*[s._h.value for s in self.solvers])
+        self._h = _C.c_void_p()
+        _check(lib().fd23_batch_create(_C.cast(arr, _C.c_void_p), len(self.solvers), _C.byref(self._h)),
+               "fd23_batch_create")
+
+    def close(self):
+        if self._h:
+            lib().fd23_batch_destroy(self._h)
+            self._h = _C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, nsteps, itrecord=1):
+        _check(lib().fd23_batch_run(self._h, nsteps, itrecord), "fd23_batch_run")
+
+    def sync(self):
+        _check(lib().fd23_batch_sync(self._h), "fd23_batch_sync")
+
+    @property
+    def stream(self):
+        p = _C.c_void_p()
+        _check(lib().fd23_batch_get_stream(self._h, _C.byref(p)), "fd23_batch_get_stream")
+        return p.value or 0
+
+    def set_graph(self, on):
+        _check(lib().fd23_batch_set_graph(self._h, int(bool(on))), "fd23_batch_set_graph")
+
+    def plan(self):
+        e = TuneEntry()
+        nb = _C.c_int(0)
+        _check(lib().fd23_batch_get_plan(self._h, _C.cast(_C.pointer(e), _C.c_void_p), _C.byref(nb)),
+               "fd23_batch_get_plan")
+        d = e.as_dict()
+        d["nblocks"] = nb.value
+        return d
+
+    def autotune(self, trial_steps=10):
+        tab = (TuneEntry * 64)()
+        n = _check(lib().fd23_batch_autotune(self._h, trial_steps, _C.cast(tab, _C.c_void_p), 64),
+                   "fd23_batch_autotune")
+        return [tab[k].as_dict() for k in range(n)]
+
+
 def receivers_line(nsta, ix0, iz0, idx, idz):
     """Reference line receivers: station i at (ix0+i*idx, iz0+i*idz) recorded
     as the pair (x, z), (x-1, z) (PD/record/cu_record.cu:12-28)."""
@@ -421,6 +493,14 @@ class Solver:
     def set_state(self, state, it0):
         st = _np.ascontiguousarray(state, dtype=self.dtype)
         _check(lib().fd23_set_state(self._h, _p(st), st.nbytes, it0), "fd23_set_state")
+
+    # -- work plan --
+    def autotune(self, trial_steps=10):
+        """Time the candidate work plans on this shot and keep the fastest;
+        returns the trials as dicts."""
+        tab = (TuneEntry * 64)()
+        n = _check(lib().fd23_autotune(self._h, trial_steps, _C.cast(tab, _C.c_void_p), 64), "fd23_autotune")
+        return [tab[k].as_dict() for k in range(n)]
 
     # -- hybrid box --
     def set_box(self, x0, z0, bx, bz, bmat=None):

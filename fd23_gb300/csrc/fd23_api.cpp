@@ -14,8 +14,7 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
-#include "fd23_internal.h"
-#include "fd23_kernels.h"
+#include "fd23_solver.h"
 
 using namespace fd23;
 
@@ -72,70 +71,7 @@ struct DevBuf {
 
 }  // namespace
 
-struct fd23_solver {
-    fd23_desc d{};
-    int nfld = 0, nmat = 0, npsi = 0;
-    size_t es = 4, cs = 4;  // storage / compute element size
-    Layout L;
-    cudaStream_t stream = nullptr;
-    int fused = 1;
-    void *fld[2][5] = {};
-    void *mat[5] = {};
-    void *psi[2][8] = {};
-    size_t psi_elems[8] = {};
-    void *cpml = nullptr;
-    int cpml_blk = 0;
-    bool have_material = false;
-    int *err_flag = nullptr;
-    double *norm_buf = nullptr;
-    // 16-bit storage forms keep values in range with exact power-of-two scales:
-    // stored velocity = sigma * v, stored stress = sigma * kappa * T; the
-    // stress-update material is stored times kappa, the velocity-update
-    // material divided by kappa.  Both stay 1 for F32 / F64.
-    double kappa = 1.0, sigma = 1.0;
-    bool kappa_set = false, sigma_set = false;
-    std::vector<int> h_tfield;      // source terms as given (for re-scaling)
-    std::vector<double> h_tamp;
-    // source
-    int nterms = 0;
-    int4 *d_terms = nullptr;
-    void *d_tamp = nullptr;
-    int tamp_nt = 0;
-    // receivers, one list per wavefield
-    int nrec[5] = {};
-    long long *d_rec[5] = {};
-    void *d_seis[5] = {};
-    int rec_cap = 0;      // record rows allocated
-    int nrec_steps = 0;   // record rows filled (or pending)
-    int pending_rec = -1; // record row to gather from the current buffer set
-    // time
-    int it = 0;
-    int par = 0;
-    // fused work list
-    WorkItem *d_items = nullptr;
-    int *d_item_off = nullptr;
-    int nblocks = 0;
-    // hybrid box: residual field, box material, ring cells, incident field
-    // of steps [box_inc_it0, box_inc_it0 + box_inc_n)
-    bool box_on = false;
-    int box_x0 = 0, box_z0 = 0, box_bx = 0, box_bz = 0, box_nsub = 0, box_nring = 0;
-    void *box_r[5] = {};
-    void *box_mat[5] = {};
-    int2 *box_cells = nullptr;
-    void *box_inc = nullptr;
-    size_t box_inc_bytes = 0;
-    int box_inc_it0 = 0, box_inc_n = 0;
-};
-
-namespace {
-
-#define CK(call)                                      \
-    do {                                              \
-        if ((call) != cudaSuccess) {                  \
-            cudaGetLastError();                       \
-            return FD23_ERR_CUDA;                     \
-        }                                             \
-    } while (0)
+namespace fd23 {
 
 int dev_alloc(void **p, size_t bytes)
 {
@@ -219,54 +155,6 @@ int download_grid(fd23_solver *s, const void *dptr, unsigned char *host, size_t 
     return FD23_OK;
 }
 
-template <class S, class C>
-Shot<S, C> make_shot(const fd23_solver *s)
-{
-    Shot<S, C> sh{};
-    for (int b = 0; b < 2; ++b)
-        for (int f = 0; f < 5; ++f) sh.f[b][f] = (S *)s->fld[b][f];
-    for (int m = 0; m < 5; ++m) sh.mat[m] = (const S *)s->mat[m];
-    for (int b = 0; b < 2; ++b)
-        for (int p = 0; p < 8; ++p) sh.psi[b][p] = (C *)s->psi[b][p];
-    sh.cpml = (const C *)s->cpml;
-    sh.nx = s->d.nx;
-    sh.nz = s->d.nz;
-    sh.npml = s->d.npml;
-    sh.topabsorb = s->d.topabsorb;
-    sh.pitch = s->L.pitch;
-    sh.origin = s->L.origin;
-    sh.cpml_blk = s->cpml_blk;
-    sh.nterms = s->nterms;
-    sh.terms = s->d_terms;
-    sh.tamp = (const C *)s->d_tamp;
-    sh.tamp_nt = s->nterms > 0 ? s->tamp_nt : 0;
-    for (int c = 0; c < 5; ++c) {
-        sh.nrec[c] = s->nrec[c];
-        sh.rec[c] = s->d_rec[c];
-        sh.seis[c] = (C *)s->d_seis[c];
-    }
-    sh.box.on = s->box_on ? 1 : 0;
-    if (s->box_on) {
-        sh.box.x0 = s->box_x0;
-        sh.box.z0 = s->box_z0;
-        sh.box.bx = s->box_bx;
-        sh.box.bz = s->box_bz;
-        sh.box.nsub = s->box_nsub;
-        sh.box.nring = s->box_nring;
-        for (int f = 0; f < 5; ++f) {
-            sh.box.r[f] = (C *)s->box_r[f];
-            sh.box.rmat[f] = (const C *)s->box_mat[f];
-        }
-        sh.box.cells = s->box_cells;
-        // incident field of the current step
-        const bool have = s->box_inc && s->it >= s->box_inc_it0 && s->it < s->box_inc_it0 + s->box_inc_n;
-        sh.box.inc = have ? (const C *)((const unsigned char *)s->box_inc +
-                                        (size_t)(s->it - s->box_inc_it0) * 5 * s->box_nring * s->cs)
-                          : nullptr;
-    }
-    return sh;
-}
-
 // One time step.  Without a box the fused sweep gathers the previous step's
 // receivers on its way; with a box the step is
 //   ring(U,W) | residual stress (+ add-ring g) | sweep | sub-ring r |
@@ -329,78 +217,48 @@ int dispatch_flush(fd23_solver *s)
     }
 }
 
-// Work list: strips of TX columns cut into row ranges of 4-row blocks.
-// CTAs get contiguous (strip-major) ranges of equal estimated cost; a range
-// may span two strips (each strip piece is one item).  Blocks that touch the
-// CPML run the general per-cell path and cost more; the relative costs
+// CTAs per SM the fused sweep can keep resident (shared memory bound, at most
+// the 3 its register budget is built for)
+int fused_per_sm(int device, int wave, int prec)
+{
+    int smem_sm = 0;
+    if (cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device) != cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    const size_t smem = fused_smem_bytes(wave, prec) + 1024;  // + the per-CTA reserve
+    return std::max(1, std::min(3, (int)(smem_sm / smem)));
+}
+
+int upload_plan(const WorkPlan &plan, WorkItem **d_items, int **d_off)
+{
+    cudaFree(*d_items);
+    cudaFree(*d_off);
+    *d_items = nullptr;
+    *d_off = nullptr;
+    int rc = dev_alloc((void **)d_items, plan.items.size() * sizeof(WorkItem));
+    if (rc) return rc;
+    if ((rc = dev_alloc((void **)d_off, plan.off.size() * sizeof(int)))) return rc;
+    CK(cudaMemcpy(*d_items, plan.items.data(), plan.items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(*d_off, plan.off.data(), plan.off.size() * sizeof(int), cudaMemcpyHostToDevice));
+    return FD23_OK;
+}
+
+// Work list of one solver (fd23_plan.cpp); the relative block costs
 // (FD23_COST_XPML, FD23_COST_ZPML, default 4 / 3) were measured on GB300.
 int build_worklist(fd23_solver *s)
 {
     const FusedGeom g = fused_geom(s->d.wave, s->d.prec);
-    const int nx = s->d.nx, nz = s->d.nz, npml = s->d.npml;
-    const int ntx = (nx + g.tile_x - 1) / g.tile_x;
-    const int nzb = (nz + 3) / 4;
-    const long long total = (long long)ntx * nzb;
-    int sms = 0, smem_sm = 0;
+    int sms = 0;
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->d.device));
-    const size_t smem = fused_smem_bytes(s->d.wave, s->d.prec);
-    CK(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, s->d.device));
-    const int per_sm = std::max(1, std::min(3, (int)(smem_sm / (smem + 1024))));
-    long long nb = (long long)sms * per_sm;
-    nb = std::min(nb, total);
-    nb = std::max(nb, (long long)(ntx + 1) / 2);  // keeps every CTA within 4 items
-    auto envd = [](const char *k, double dflt) {
-        const char *v = getenv(k);
-        return v ? atof(v) : dflt;
-    };
-    const double wx = envd("FD23_COST_XPML", 4.0), wz = envd("FD23_COST_ZPML", 3.0);
-    const bool top = s->d.topabsorb != 0;
-    std::vector<double> cum((size_t)total + 1, 0.0);
-    for (long long b = 0; b < total; ++b) {
-        const int strip = (int)(b / nzb), zb = (int)(b % nzb);
-        const int x0 = strip * g.tile_x;
-        const bool xp = (x0 - 4 < std::max(npml, 4)) || (x0 + g.tile_x + 4 > std::min(nx - npml, nx - 4));
-        const int r0 = 4 * zb, r1 = r0 + 3;
-        const bool zp = (r1 >= std::min(nz - npml, nz - 4)) || r0 < 4 || (top && r0 < npml);
-        cum[b + 1] = cum[b] + (xp ? wx : (zp ? wz : 1.0));
-    }
-    std::vector<WorkItem> items;
-    std::vector<int> off;
-    off.push_back(0);
-    long long b0 = 0;
-    for (long long c = 0; c < nb; ++c) {
-        long long b1;
-        if (c == nb - 1) {
-            b1 = total;
-        } else {
-            const double target = cum[total] * (double)(c + 1) / (double)nb;
-            b1 = std::lower_bound(cum.begin() + b0 + 1, cum.end(), target) - cum.begin();
-            b1 = std::max(b1, b0 + 1);
-            b1 = std::min(b1, total - (nb - 1 - c));  // leave a block for every later CTA
-        }
-        while (b0 < b1) {
-            const int strip = (int)(b0 / nzb);
-            const long long send = (long long)(strip + 1) * nzb;
-            const long long e = std::min(b1, send);
-            items.push_back(WorkItem{0, strip * g.tile_x, (int)(b0 - (long long)strip * nzb) * 4,
-                                     (int)(e - (long long)strip * nzb) * 4});
-            b0 = e;
-        }
-        off.push_back((int)items.size());
-    }
-    for (size_t c = 0; c + 1 < off.size(); ++c)
-        if (off[c + 1] - off[c] > 4) return FD23_ERR_ARG;
-    if (s->d_items) cudaFree(s->d_items);
-    if (s->d_item_off) cudaFree(s->d_item_off);
-    s->d_items = nullptr;
-    s->d_item_off = nullptr;
-    int rc = dev_alloc((void **)&s->d_items, items.size() * sizeof(WorkItem));
+    TuneParams tp = s->tune;
+    tp.per_sm = std::min(tp.per_sm, fused_per_sm(s->d.device, s->d.wave, s->d.prec));
+    WorkPlan plan;
+    const std::vector<ShotGeom> geo{ShotGeom{s->d.nx, s->d.nz, s->d.npml, s->d.topabsorb}};
+    int rc = plan_work(geo, g.tile_x, sms, tp, plan);
     if (rc) return rc;
-    rc = dev_alloc((void **)&s->d_item_off, off.size() * sizeof(int));
-    if (rc) return rc;
-    CK(cudaMemcpy(s->d_items, items.data(), items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(s->d_item_off, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice));
-    s->nblocks = (int)nb;
+    if ((rc = upload_plan(plan, &s->d_items, &s->d_item_off))) return rc;
+    s->nblocks = plan.nblocks;
     return FD23_OK;
 }
 
@@ -550,7 +408,7 @@ int ensure_sigma(fd23_solver *s)
     return upload_source_amps(s);
 }
 
-}  // namespace
+}  // namespace fd23
 
 extern "C" {
 
@@ -598,6 +456,8 @@ int fd23_create(const fd23_desc *desc, fd23_solver **out)
     s->es = storage_size(d.prec);
     s->cs = compute_size(d.prec);
     s->fused = d.kernel != FD23_KERNEL_TWOPASS;
+    if (const char *v = getenv("FD23_COST_XPML")) s->tune.wx = atof(v);
+    if (const char *v = getenv("FD23_COST_ZPML")) s->tune.wz = atof(v);
     const FusedGeom g = fused_geom(d.wave, d.prec);
     const int ntx = (d.nx + g.tile_x - 1) / g.tile_x;
     s->L = make_layout(d.nx, d.nz, ntx * g.tile_x, (d.nz + 3) / 4 * 4);

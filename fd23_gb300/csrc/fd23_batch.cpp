@@ -1,0 +1,490 @@
+// Batched multi-shot sweep and the work-plan autotuner.
+//
+// A batch advances many solvers (shots of any grid size, one wave type and
+// one precision, on one GPU) in lockstep: every time step is ONE launch of the
+// fused sweep over all shots, driven by a work plan whose CTAs each serve one
+// shot (fd23_plan.cpp) and a device table of shot descriptors.  The launches
+// of a run are captured once into a CUDA graph and replayed; a run with the
+// same step range, record pattern and plan replays the cached graph.
+//
+// The reference runs one shot per process (PD/main.cpp:43-183); this has no
+// counterpart there.
+//
+// The autotuner times candidate work plans (block cost weights, CTAs per SM,
+// oversubscription) on the live shots for a few steps each, restoring the
+// wavefields, memory variables and step counters after every trial, and keeps
+// the fastest plan.
+#include <algorithm>
+#include <new>
+#include <vector>
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "fd23_solver.h"
+
+using namespace fd23;
+
+struct fd23_batch {
+    std::vector<fd23_solver *> s;
+    int wave = 0, prec = 0, device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev = nullptr;
+    TuneParams tune;
+    WorkPlan plan;
+    WorkItem *d_items = nullptr;
+    int *d_off = nullptr;
+    void *d_shots = nullptr;
+    int *err_flag = nullptr;
+    int plan_ver = 0;
+    // cached graph of the last run: key = it0, nsteps, itrecord, par0, nrec0, plan version
+    cudaGraphExec_t gexec = nullptr;
+    long long gkey[6] = {-1, -1, -1, -1, -1, -1};
+    int use_graph = 1;
+};
+
+namespace {
+
+int batch_plan(fd23_batch *b, const TuneParams &tp)
+{
+    std::vector<ShotGeom> geo;
+    for (auto *s : b->s) geo.push_back(ShotGeom{s->d.nx, s->d.nz, s->d.npml, s->d.topabsorb});
+    int sms = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
+    TuneParams t = tp;
+    t.per_sm = std::min(t.per_sm, fused_per_sm(b->device, b->wave, b->prec));
+    WorkPlan plan;
+    int rc = plan_work(geo, fused_geom(b->wave, b->prec).tile_x, sms, t, plan);
+    if (rc) return rc;
+    if ((rc = upload_plan(plan, &b->d_items, &b->d_off))) return rc;
+    b->plan = plan;
+    b->tune = tp;
+    ++b->plan_ver;
+    return FD23_OK;
+}
+
+template <class S, class C>
+int upload_shots(fd23_batch *b)
+{
+    std::vector<Shot<S, C>> t(b->s.size());
+    for (size_t k = 0; k < b->s.size(); ++k) {
+        t[k] = make_shot<S, C>(b->s[k]);
+        t[k].cta0 = b->plan.cta0[k];
+        t[k].ncta = b->plan.ncta[k];
+    }
+    if (!b->d_shots) {
+        const int rc = dev_alloc(&b->d_shots, t.size() * sizeof(Shot<S, C>));
+        if (rc) return rc;
+    }
+    CK(cudaMemcpyAsync(b->d_shots, t.data(), t.size() * sizeof(Shot<S, C>), cudaMemcpyHostToDevice, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    return FD23_OK;
+}
+
+// the batch stream waits for every solver's queued work
+int join_in(fd23_batch *b)
+{
+    for (auto *s : b->s) {
+        CK(cudaEventRecord(b->ev, s->stream));
+        CK(cudaStreamWaitEvent(b->stream, b->ev, 0));
+    }
+    return FD23_OK;
+}
+// every solver stream waits for the batch's queued work
+int join_out(fd23_batch *b)
+{
+    CK(cudaEventRecord(b->ev, b->stream));
+    for (auto *s : b->s) CK(cudaStreamWaitEvent(s->stream, b->ev, 0));
+    return FD23_OK;
+}
+
+// launches of nsteps lockstep steps from (it, par, pending); returns the new
+// pending record row through *pending
+template <class S, class C>
+int launch_steps(fd23_batch *b, int it0, int nsteps, int itrecord, bool any_rec, int par0, int nrec0,
+                 int *pending)
+{
+    const Shot<S, C> *shots = (const Shot<S, C> *)b->d_shots;
+    int par = par0, pend = -1, nrec = nrec0;
+    for (int k = 0; k < nsteps; ++k) {
+        const int it = it0 + k;
+        const int rc = launch_step_fused_batch<S, C>(shots, b->wave, b->d_items, b->d_off, b->plan.nblocks, par,
+                                                     it, pend, b->err_flag, b->stream);
+        if (rc) return rc;
+        pend = (any_rec && it % itrecord == 0) ? nrec++ : -1;
+        par = 1 - par;
+    }
+    *pending = pend;
+    return FD23_OK;
+}
+
+template <class S, class C>
+int batch_run_impl(fd23_batch *b, int nsteps, int itrecord)
+{
+    fd23_solver *s0 = b->s[0];
+    for (auto *s : b->s) {
+        if (!s->have_material) return FD23_ERR_ORDER;
+        if (s->box_on || !s->fused) return FD23_ERR_UNSUPPORTED;
+        if (s->it != s0->it || s->par != s0->par || s->nrec_steps != s0->nrec_steps || s->pending_rec >= 0)
+            return FD23_ERR_ORDER;  // shots must be in lockstep
+        int rc = ensure_sigma(s);
+        if (rc) return rc;
+    }
+    int nrec_new = 0;
+    for (int k = 0; k < nsteps; ++k)
+        if ((s0->it + k) % itrecord == 0) ++nrec_new;
+    bool any_rec = false;
+    for (auto *s : b->s)
+        for (int c = 0; c < 5; ++c) any_rec = any_rec || s->nrec[c] > 0;
+    if (any_rec)
+        for (auto *s : b->s) {
+            const int rc = ensure_record_capacity(s, s->nrec_steps + nrec_new);
+            if (rc) return rc;
+        }
+    int rc = join_in(b);
+    if (rc) return rc;
+    if ((rc = upload_shots<S, C>(b))) return rc;
+    const int it0 = s0->it, par0 = s0->par, nrec0 = s0->nrec_steps;
+    int pending = -1;
+    const long long key[6] = {it0, nsteps, itrecord * (any_rec ? 1 : -1), par0, nrec0, b->plan_ver};
+    bool done = false;
+    if (b->use_graph && nsteps >= 2) {
+        if (b->gexec && std::equal(key, key + 6, b->gkey)) {
+            // replay; the pending record row follows from the key
+            int nr = nrec0;
+            for (int k = 0; k < nsteps; ++k) pending = (any_rec && (it0 + k) % itrecord == 0) ? nr++ : -1;
+            done = cudaGraphLaunch(b->gexec, b->stream) == cudaSuccess;
+            if (!done) cudaGetLastError();
+        } else {
+            cudaGraph_t g = nullptr;
+            if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+                const int lr = launch_steps<S, C>(b, it0, nsteps, itrecord, any_rec, par0, nrec0, &pending);
+                const cudaError_t ec = cudaStreamEndCapture(b->stream, &g);
+                cudaGraphExec_t ex = nullptr;
+                if (lr == FD23_OK && ec == cudaSuccess && g &&
+                    cudaGraphInstantiate(&ex, g, 0) == cudaSuccess && cudaGraphLaunch(ex, b->stream) == cudaSuccess) {
+                    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+                    b->gexec = ex;
+                    std::copy(key, key + 6, b->gkey);
+                    done = true;
+                } else if (ex) {
+                    cudaGraphExecDestroy(ex);
+                }
+                if (g) cudaGraphDestroy(g);
+            }
+            if (!done) cudaGetLastError();  // capture unavailable: launch directly
+        }
+    }
+    if (!done && (rc = launch_steps<S, C>(b, it0, nsteps, itrecord, any_rec, par0, nrec0, &pending))) return rc;
+    const int par1 = (nsteps & 1) ? 1 - par0 : par0;
+    int nrec1 = nrec0;
+    for (int k = 0; k < nsteps; ++k)
+        if (any_rec && (it0 + k) % itrecord == 0) ++nrec1;
+    for (auto *s : b->s) {
+        s->it = it0 + nsteps;
+        s->par = par1;
+        s->nrec_steps = nrec1;
+        s->pending_rec = -1;
+        if (pending >= 0 && (rc = launch_record<S, C>(make_shot<S, C>(s), par1, pending, b->stream))) return rc;
+    }
+    return join_out(b);
+}
+
+int batch_run(fd23_batch *b, int nsteps, int itrecord)
+{
+    switch (b->prec) {
+        case FD23_F64: return batch_run_impl<double, double>(b, nsteps, itrecord);
+        case FD23_BF16: return batch_run_impl<__nv_bfloat16, float>(b, nsteps, itrecord);
+        case FD23_F16: return batch_run_impl<__half, float>(b, nsteps, itrecord);
+        default: return batch_run_impl<float, float>(b, nsteps, itrecord);
+    }
+}
+
+// ---- autotuner ----
+
+// state of the solvers (read set of wavefields, memory variables, box
+// residual, step counters) saved before trials and put back after each
+struct Snapshot {
+    std::vector<void *> copy, live;
+    std::vector<size_t> bytes;
+    std::vector<int> it, par, nrec, pend;
+    ~Snapshot()
+    {
+        for (void *p : copy) cudaFree(p);
+    }
+};
+
+int snapshot_take(const std::vector<fd23_solver *> &ss, cudaStream_t st, Snapshot &sn)
+{
+    for (auto *s : ss) {
+        auto add = [&](void *p, size_t n) -> int {
+            if (!p || !n) return FD23_OK;
+            void *c = nullptr;
+            const int rc = dev_alloc(&c, n);
+            if (rc) return rc;
+            sn.copy.push_back(c);
+            sn.live.push_back(p);
+            sn.bytes.push_back(n);
+            CK(cudaMemcpyAsync(c, p, n, cudaMemcpyDeviceToDevice, st));
+            return FD23_OK;
+        };
+        int rc = FD23_OK;
+        for (int f = 0; f < s->nfld && !rc; ++f) rc = add(s->fld[s->par][f], s->L.elems() * s->es);
+        for (int p = 0; p < s->npsi && !rc; ++p) rc = add(s->psi[s->par][p], s->psi_elems[p] * s->cs);
+        if (s->box_on)
+            for (int f = 0; f < 5 && !rc; ++f) rc = add(s->box_r[f], (size_t)s->box_bx * s->box_bz * s->cs);
+        if (rc) return rc;
+        sn.it.push_back(s->it);
+        sn.par.push_back(s->par);
+        sn.nrec.push_back(s->nrec_steps);
+        sn.pend.push_back(s->pending_rec);
+    }
+    CK(cudaStreamSynchronize(st));
+    return FD23_OK;
+}
+
+int snapshot_restore(const std::vector<fd23_solver *> &ss, cudaStream_t st, const Snapshot &sn)
+{
+    for (size_t k = 0; k < ss.size(); ++k) {
+        ss[k]->it = sn.it[k];
+        ss[k]->par = sn.par[k];
+        ss[k]->nrec_steps = sn.nrec[k];
+        ss[k]->pending_rec = sn.pend[k];
+    }
+    for (size_t i = 0; i < sn.copy.size(); ++i)
+        CK(cudaMemcpyAsync(sn.live[i], sn.copy[i], sn.bytes[i], cudaMemcpyDeviceToDevice, st));
+    CK(cudaStreamSynchronize(st));
+    return FD23_OK;
+}
+
+std::vector<TuneParams> candidates()
+{
+    const double w[][2] = {{1.0, 1.0}, {2.5, 1.5}, {4.0, 3.0}, {6.0, 4.0}, {4.0, 2.0}, {3.0, 3.0}};
+    std::vector<TuneParams> c;
+    for (int per_sm : {3, 2})
+        for (double ov : {1.0, 2.0})
+            for (auto &ww : w) {
+                TuneParams t;
+                t.wx = ww[0];
+                t.wz = ww[1];
+                t.per_sm = per_sm;
+                t.oversub = ov;
+                c.push_back(t);
+            }
+    return c;
+}
+
+// Times every candidate: `apply` installs a plan, `steps` runs k steps
+// without recording on `st`.  Keeps the best plan installed.
+template <class Apply, class Steps>
+int autotune_core(const std::vector<fd23_solver *> &ss, cudaStream_t st, int trial_steps, Apply apply,
+                  Steps steps, fd23_tune_entry *table, int cap)
+{
+    Snapshot sn;
+    int rc = snapshot_take(ss, st, sn);
+    if (rc) return rc;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    const std::vector<TuneParams> cand = candidates();
+    int best = -1, n = 0;
+    double best_ms = 0.0;
+    for (size_t i = 0; i < cand.size() && !rc; ++i) {
+        if ((rc = apply(cand[i]))) break;
+        if ((rc = steps(2))) break;  // warm-up
+        CK(cudaEventRecord(e0, st));
+        if ((rc = steps(trial_steps))) break;
+        CK(cudaEventRecord(e1, st));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        const double per = ms / trial_steps;
+        if (table && n < cap)
+            table[n] = fd23_tune_entry{cand[i].wx, cand[i].wz, cand[i].per_sm, cand[i].oversub, per};
+        ++n;
+        if (best < 0 || per < best_ms) {
+            best = (int)i;
+            best_ms = per;
+        }
+        rc = snapshot_restore(ss, st, sn);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) {
+        snapshot_restore(ss, st, sn);
+        return rc;
+    }
+    if ((rc = apply(cand[best]))) return rc;
+    return n;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fd23_batch_create(fd23_solver *const *solvers, int n, fd23_batch **out)
+{
+    if (!solvers || n <= 0 || !out) return FD23_ERR_ARG;
+    *out = nullptr;
+    fd23_solver *s0 = solvers[0];
+    if (!s0) return FD23_ERR_ARG;
+    for (int k = 0; k < n; ++k) {
+        fd23_solver *s = solvers[k];
+        if (!s || s->d.wave != s0->d.wave || s->d.prec != s0->d.prec || s->d.device != s0->d.device)
+            return FD23_ERR_ARG;
+        for (int j = 0; j < k; ++j)
+            if (solvers[j] == s) return FD23_ERR_ARG;
+        if (!s->fused) return FD23_ERR_UNSUPPORTED;
+    }
+    CK(cudaSetDevice(s0->d.device));
+    fd23_batch *b = new (std::nothrow) fd23_batch();
+    if (!b) return FD23_ERR_NOMEM;
+    b->s.assign(solvers, solvers + n);
+    b->wave = s0->d.wave;
+    b->prec = s0->d.prec;
+    b->device = s0->d.device;
+    b->tune = s0->tune;
+    int rc = FD23_OK;
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        rc = FD23_ERR_CUDA;
+    }
+    if (!rc) rc = dev_alloc((void **)&b->err_flag, sizeof(int));
+    if (!rc && cudaMemset(b->err_flag, 0, sizeof(int)) != cudaSuccess) rc = FD23_ERR_CUDA;
+    if (!rc) rc = batch_plan(b, b->tune);
+    if (rc) {
+        fd23_batch_destroy(b);
+        return rc;
+    }
+    *out = b;
+    return FD23_OK;
+}
+
+void fd23_batch_destroy(fd23_batch *b)
+{
+    if (!b) return;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    cudaFree(b->d_items);
+    cudaFree(b->d_off);
+    cudaFree(b->d_shots);
+    cudaFree(b->err_flag);
+    if (b->ev) cudaEventDestroy(b->ev);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+int fd23_batch_run(fd23_batch *b, int nsteps, int itrecord)
+{
+    if (!b || nsteps < 0 || itrecord <= 0) return FD23_ERR_ARG;
+    CK(cudaSetDevice(b->device));
+    if (nsteps == 0) return FD23_OK;
+    return batch_run(b, nsteps, itrecord);
+}
+
+int fd23_batch_sync(fd23_batch *b)
+{
+    if (!b) return FD23_ERR_ARG;
+    CK(cudaSetDevice(b->device));
+    CK(cudaStreamSynchronize(b->stream));
+    int flag = 0;
+    CK(cudaMemcpy(&flag, b->err_flag, sizeof(int), cudaMemcpyDeviceToHost));
+    return flag ? FD23_ERR_TIMEOUT : FD23_OK;
+}
+
+int fd23_batch_get_stream(fd23_batch *b, void **stream)
+{
+    if (!b || !stream) return FD23_ERR_ARG;
+    *stream = (void *)b->stream;
+    return FD23_OK;
+}
+
+int fd23_batch_set_graph(fd23_batch *b, int on)
+{
+    if (!b) return FD23_ERR_ARG;
+    b->use_graph = on ? 1 : 0;
+    return FD23_OK;
+}
+
+int fd23_batch_get_plan(fd23_batch *b, fd23_tune_entry *cur, int *nblocks)
+{
+    if (!b) return FD23_ERR_ARG;
+    if (cur) *cur = fd23_tune_entry{b->tune.wx, b->tune.wz, b->tune.per_sm, b->tune.oversub, 0.0};
+    if (nblocks) *nblocks = b->plan.nblocks;
+    return FD23_OK;
+}
+
+int fd23_batch_autotune(fd23_batch *b, int trial_steps, fd23_tune_entry *table, int cap)
+{
+    if (!b || trial_steps <= 0 || cap < 0 || (cap > 0 && !table)) return FD23_ERR_ARG;
+    CK(cudaSetDevice(b->device));
+    fd23_solver *s0 = b->s[0];
+    for (auto *s : b->s) {
+        if (!s->have_material) return FD23_ERR_ORDER;
+        if (s->it != s0->it || s->par != s0->par || s->pending_rec >= 0) return FD23_ERR_ORDER;
+        const int rc = ensure_sigma(s);
+        if (rc) return rc;
+    }
+    int rc = join_in(b);
+    if (rc) return rc;
+    auto apply = [b](const TuneParams &tp) -> int {
+        const int r = batch_plan(b, tp);
+        if (r) return r;
+        switch (b->prec) {
+            case FD23_F64: return upload_shots<double, double>(b);
+            case FD23_BF16: return upload_shots<__nv_bfloat16, float>(b);
+            case FD23_F16: return upload_shots<__half, float>(b);
+            default: return upload_shots<float, float>(b);
+        }
+    };
+    auto steps = [b](int k) -> int {
+        fd23_solver *s = b->s[0];
+        int pend = -1;
+        int r;
+        switch (b->prec) {
+            case FD23_F64: r = launch_steps<double, double>(b, s->it, k, 1, false, s->par, 0, &pend); break;
+            case FD23_BF16: r = launch_steps<__nv_bfloat16, float>(b, s->it, k, 1, false, s->par, 0, &pend); break;
+            case FD23_F16: r = launch_steps<__half, float>(b, s->it, k, 1, false, s->par, 0, &pend); break;
+            default: r = launch_steps<float, float>(b, s->it, k, 1, false, s->par, 0, &pend);
+        }
+        if (r) return r;
+        for (auto *x : b->s) {
+            x->it += k;
+            x->par = (k & 1) ? 1 - x->par : x->par;
+        }
+        return FD23_OK;
+    };
+    rc = autotune_core(b->s, b->stream, trial_steps, apply, steps, table, cap);
+    const int jr = join_out(b);
+    return rc < 0 ? rc : (jr ? jr : rc);
+}
+
+int fd23_autotune(fd23_solver *s, int trial_steps, fd23_tune_entry *table, int cap)
+{
+    if (!s || trial_steps <= 0 || cap < 0 || (cap > 0 && !table)) return FD23_ERR_ARG;
+    if (!s->fused) return FD23_ERR_UNSUPPORTED;
+    if (!s->have_material) return FD23_ERR_ORDER;
+    CK(cudaSetDevice(s->d.device));
+    int rc = ensure_sigma(s);
+    if (rc) return rc;
+    if (s->box_on && (s->it < s->box_inc_it0 || s->it + trial_steps + 2 > s->box_inc_it0 + s->box_inc_n))
+        return FD23_ERR_ORDER;
+    if ((rc = dispatch_flush(s))) return rc;
+    std::vector<fd23_solver *> ss{s};
+    auto apply = [s](const TuneParams &tp) -> int {
+        s->tune = tp;
+        return build_worklist(s);
+    };
+    auto steps = [s](int k) -> int {
+        for (int i = 0; i < k; ++i) {
+            const int r = dispatch_step(s, 0);
+            if (r) return r;
+        }
+        return FD23_OK;
+    };
+    return autotune_core(ss, s->stream, trial_steps, apply, steps, table, cap);
+}
+
+}  // extern "C"

@@ -315,10 +315,14 @@ struct ItemInfo {
     int x0, z0, z1, niter;  // rows [z0, z1), niter = (z1-z0)/4 + 2
 };
 
-template <class S, class C, int WAVE>
+// BATCH = false: one shot, described by the kernel parameter.  BATCH = true:
+// the shot table `shots`; every CTA works on one shot (the shot of its first
+// item) and copies that shot's descriptor into shared memory.
+template <class S, class C, int WAVE, bool BATCH>
 __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
-    fused_step(Shot<S, C> sh, const WorkItem *__restrict__ items, const int *__restrict__ item_off,
-               int par, int it, int rec_index, int *err_flag)
+    fused_step(const __grid_constant__ Shot<S, C> sh_param, const Shot<S, C> *__restrict__ shots,
+               const WorkItem *__restrict__ items, const int *__restrict__ item_off, int par, int it,
+               int rec_index, int *err_flag)
 {
     using K = Cfg<S, C, WAVE>;
     constexpr bool PSV = K::PSV;
@@ -337,6 +341,22 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
     __shared__ int tcount[K::MAX_ITEMS];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int ibeg = item_off[blockIdx.x], iend = item_off[blockIdx.x + 1];
+    const int nitems = min(iend - ibeg, K::MAX_ITEMS);
+
+    const Shot<S, C> *shp;
+    if constexpr (BATCH) {
+        __shared__ Shot<S, C> sh_s;
+        static_assert(sizeof(Shot<S, C>) % 16 == 0, "shot descriptor copied as 16-byte words");
+        const int4 *src = reinterpret_cast<const int4 *>(shots + items[ibeg].shot);
+        int4 *dst = reinterpret_cast<int4 *>(&sh_s);
+        for (int w = tid; w < (int)(sizeof(Shot<S, C>) / 16); w += K::NTH) dst[w] = src[w];
+        __syncthreads();
+        shp = &sh_s;
+    } else {
+        shp = &sh_param;
+    }
+    const Shot<S, C> &sh = *shp;
     const int nx = sh.nx, nz = sh.nz, npml = sh.npml, pitch = sh.pitch;
     const long long origin = sh.origin;
 
@@ -355,9 +375,6 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
         prd[f] = par ? sh.psi[1][f] : sh.psi[0][f];
         pwr[f] = par ? sh.psi[0][f] : sh.psi[1][f];
     }
-
-    const int ibeg = item_off[blockIdx.x], iend = item_off[blockIdx.x + 1];
-    const int nitems = min(iend - ibeg, K::MAX_ITEMS);
 
     // ---- per-item set-up: geometry and the source terms inside its stress region ----
     if (tid < nitems) {
@@ -486,7 +503,7 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
     if (rec_index >= 0) {
 #pragma unroll
         for (int c = 0; c < K::NV + K::NT; ++c)
-            for (int r = blockIdx.x * NCT + tid; r < sh.nrec[c]; r += gridDim.x * NCT)
+            for (int r = ((int)blockIdx.x - sh.cta0) * NCT + tid; r < sh.nrec[c]; r += sh.ncta * NCT)
                 sh.seis[c][(long long)rec_index * sh.nrec[c] + r] = to_c<C>(rd[c][sh.rec[c][r]]);
     }
 
@@ -1015,9 +1032,9 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
     }
 }
 
-template <class S, class C, int WAVE>
-int launch_fused_impl(const Shot<S, C> &s, const WorkItem *items, const int *item_off, int nblocks,
-                      int par, int it, int rec_index, int *err_flag, cudaStream_t st)
+template <class S, class C, int WAVE, bool BATCH>
+int launch_fused_impl(const Shot<S, C> &s, const Shot<S, C> *shots, const WorkItem *items, const int *item_off,
+                      int nblocks, int par, int it, int rec_index, int *err_flag, cudaStream_t st)
 {
     using K = Cfg<S, C, WAVE>;
     cudaLaunchConfig_t cfg = {};
@@ -1030,8 +1047,8 @@ int launch_fused_impl(const Shot<S, C> &s, const WorkItem *items, const int *ite
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    const cudaError_t e = cudaLaunchKernelEx(&cfg, fused_step<S, C, WAVE>, s, items, item_off, par, it,
-                                             rec_index, err_flag);
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, fused_step<S, C, WAVE, BATCH>, s, shots, items, item_off,
+                                             par, it, rec_index, err_flag);
     return e == cudaSuccess ? FD23_OK : FD23_ERR_CUDA;
 }
 
@@ -1039,10 +1056,11 @@ template <class S, class C, int WAVE>
 int prepare_one()
 {
     using K = Cfg<S, C, WAVE>;
-    return cudaFuncSetAttribute(fused_step<S, C, WAVE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)K::SMEM) == cudaSuccess
-               ? FD23_OK
-               : FD23_ERR_CUDA;
+    const bool ok = cudaFuncSetAttribute(fused_step<S, C, WAVE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)K::SMEM) == cudaSuccess &&
+                    cudaFuncSetAttribute(fused_step<S, C, WAVE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)K::SMEM) == cudaSuccess;
+    return ok ? FD23_OK : FD23_ERR_CUDA;
 }
 
 }  // namespace
@@ -1059,10 +1077,22 @@ int launch_step_fused(const Shot<S, C> &s, int wave, const WorkItem *items, cons
                       int nblocks, int par, int it, int rec_index, int *err_flag, cudaStream_t st)
 {
     if (wave == FD23_PSV)
-        return launch_fused_impl<S, C, FD23_PSV>(s, items, item_off, nblocks, par, it, rec_index,
-                                                 err_flag, st);
-    return launch_fused_impl<S, C, FD23_SH>(s, items, item_off, nblocks, par, it, rec_index, err_flag,
-                                           st);
+        return launch_fused_impl<S, C, FD23_PSV, false>(s, nullptr, items, item_off, nblocks, par, it,
+                                                        rec_index, err_flag, st);
+    return launch_fused_impl<S, C, FD23_SH, false>(s, nullptr, items, item_off, nblocks, par, it, rec_index,
+                                                   err_flag, st);
+}
+
+template <class S, class C>
+int launch_step_fused_batch(const Shot<S, C> *shots, int wave, const WorkItem *items, const int *item_off,
+                            int nblocks, int par, int it, int rec_index, int *err_flag, cudaStream_t st)
+{
+    const Shot<S, C> none{};
+    if (wave == FD23_PSV)
+        return launch_fused_impl<S, C, FD23_PSV, true>(none, shots, items, item_off, nblocks, par, it,
+                                                       rec_index, err_flag, st);
+    return launch_fused_impl<S, C, FD23_SH, true>(none, shots, items, item_off, nblocks, par, it, rec_index,
+                                                  err_flag, st);
 }
 
 int fused_prepare(int wave, int prec)
@@ -1102,9 +1132,11 @@ size_t fused_smem_bytes(int wave, int prec)
     }
 }
 
-#define FD23_INST(S, C)                                                                            \
-    template int launch_step_fused<S, C>(const Shot<S, C> &, int, const WorkItem *, const int *, \
-                                         int, int, int, int, int *, cudaStream_t);
+#define FD23_INST(S, C)                                                                                  \
+    template int launch_step_fused<S, C>(const Shot<S, C> &, int, const WorkItem *, const int *,       \
+                                         int, int, int, int, int *, cudaStream_t);                     \
+    template int launch_step_fused_batch<S, C>(const Shot<S, C> *, int, const WorkItem *, const int *, \
+                                               int, int, int, int, int *, cudaStream_t);
 FD23_INST(float, float)
 FD23_INST(double, double)
 FD23_INST(__nv_bfloat16, float)

@@ -99,7 +99,7 @@ struct Box {
 // material, C = arithmetic type (also the type of memory variables, CPML
 // coefficients, source amplitudes and seismograms).
 template <class S, class C>
-struct Shot {
+struct alignas(16) Shot {
     S *f[2][5];         // ping-pong wavefields (P-SV: U W Txx Txz Tzz; SH: V Tx Tz)
     const S *mat[5];    // P-SV: LAM MU MUA BU BW; SH: MUX MUZ BV
     C *psi[2][8];       // ping-pong memory variables, reference index maps
@@ -118,12 +118,32 @@ struct Shot {
     const long long *rec[5];
     C *seis[5];
     Box<C> box;         // hybrid box (box.on == 0: none)
+    int cta0, ncta;     // CTAs of the launch working on this shot (receiver gather split)
 };
 
 // Work list entry of the fused sweep: one x-strip of one shot, rows [z0, z1)
 struct WorkItem {
     int shot, x0, z0, z1;
 };
+
+// Work plan of one fused launch over one or more shots: CTA c works on
+// items[off[c] .. off[c+1]) (at most 4, all of one shot); shot k is worked
+// on by CTAs [cta0[k], cta0[k] + ncta[k]).
+struct ShotGeom {
+    int nx, nz, npml, topabsorb;
+};
+struct TuneParams {
+    double wx = 4.0, wz = 3.0;  // relative cost of 4-row blocks touching the x / z CPML
+    int per_sm = 3;             // CTAs resident per SM the plan is sized for
+    double oversub = 1.0;       // CTAs launched per resident slot
+};
+struct WorkPlan {
+    std::vector<WorkItem> items;
+    std::vector<int> off, cta0, ncta;
+    int nblocks = 0;
+};
+int plan_work(const std::vector<ShotGeom> &shots, int tile_x, int sms, const TuneParams &tp,
+              WorkPlan &plan);
 
 // host builders (fd23_host.cpp)
 int build_psv_material(int nx, int nz, double h, double dt, const double *vp, const double *vs,

@@ -48,6 +48,12 @@ int launch_box_pre(const Shot<S, C> &s, int par, int fused, cudaStream_t st);
 template <class S, class C>
 int launch_box_post(const Shot<S, C> &s, int par, int fused, int rec_index, cudaStream_t st);
 
+// The same sweep over several shots in one launch: `shots` = device array of
+// shot descriptors; every CTA's items belong to one shot (a WorkPlan).
+template <class S, class C>
+int launch_step_fused_batch(const Shot<S, C> *shots, int wave, const WorkItem *items, const int *item_off,
+                            int nblocks, int par, int it, int rec_index, int *err_flag, cudaStream_t st);
+
 // FP64 sum of squares over the `elems` stored elements of each of the first
 // `nfields` wavefields of buffer set `par` (the zero padding included); the
 // sum goes to dev_out[0], a NaN/Inf flag to dev_out[1].

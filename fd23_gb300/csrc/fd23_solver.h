@@ -1,0 +1,143 @@
+// The solver object behind the C ABI and the helpers the API and the batch
+// code share (fd23_api.cpp, fd23_batch.cpp).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "fd23_internal.h"
+#include "fd23_kernels.h"
+
+#define CK(call)                                      \
+    do {                                              \
+        if ((call) != cudaSuccess) {                  \
+            cudaGetLastError();                       \
+            return FD23_ERR_CUDA;                     \
+        }                                             \
+    } while (0)
+
+struct fd23_solver {
+    fd23_desc d{};
+    int nfld = 0, nmat = 0, npsi = 0;
+    size_t es = 4, cs = 4;  // storage / compute element size
+    fd23::Layout L;
+    cudaStream_t stream = nullptr;
+    int fused = 1;
+    void *fld[2][5] = {};
+    void *mat[5] = {};
+    void *psi[2][8] = {};
+    size_t psi_elems[8] = {};
+    void *cpml = nullptr;
+    int cpml_blk = 0;
+    bool have_material = false;
+    int *err_flag = nullptr;
+    double *norm_buf = nullptr;
+    // 16-bit storage forms keep values in range with exact power-of-two scales:
+    // stored velocity = sigma * v, stored stress = sigma * kappa * T; the
+    // stress-update material is stored times kappa, the velocity-update
+    // material divided by kappa.  Both stay 1 for F32 / F64.
+    double kappa = 1.0, sigma = 1.0;
+    bool kappa_set = false, sigma_set = false;
+    std::vector<int> h_tfield;      // source terms as given (for re-scaling)
+    std::vector<double> h_tamp;
+    // source
+    int nterms = 0;
+    int4 *d_terms = nullptr;
+    void *d_tamp = nullptr;
+    int tamp_nt = 0;
+    // receivers, one list per wavefield
+    int nrec[5] = {};
+    long long *d_rec[5] = {};
+    void *d_seis[5] = {};
+    int rec_cap = 0;      // record rows allocated
+    int nrec_steps = 0;   // record rows filled (or pending)
+    int pending_rec = -1; // record row to gather from the current buffer set
+    // time
+    int it = 0;
+    int par = 0;
+    // fused work list
+    fd23::WorkItem *d_items = nullptr;
+    int *d_item_off = nullptr;
+    int nblocks = 0;
+    // work plan of the fused sweep and the parameters it was built with
+    fd23::TuneParams tune;
+    // hybrid box: residual field, box material, ring cells, incident field
+    // of steps [box_inc_it0, box_inc_it0 + box_inc_n)
+    bool box_on = false;
+    int box_x0 = 0, box_z0 = 0, box_bx = 0, box_bz = 0, box_nsub = 0, box_nring = 0;
+    void *box_r[5] = {};
+    void *box_mat[5] = {};
+    int2 *box_cells = nullptr;
+    void *box_inc = nullptr;
+    size_t box_inc_bytes = 0;
+    int box_inc_it0 = 0, box_inc_n = 0;
+};
+
+namespace fd23 {
+
+int dev_alloc(void **p, size_t bytes);
+size_t storage_size(int prec);
+size_t compute_size(int prec);
+bool scaled_form(const fd23_solver *s);
+double field_scale(const fd23_solver *s, int f);
+int ensure_sigma(fd23_solver *s);
+int ensure_record_capacity(fd23_solver *s, int need);
+int dispatch_flush(fd23_solver *s);
+int zero_state(fd23_solver *s);
+int fused_per_sm(int device, int wave, int prec);
+int upload_plan(const WorkPlan &plan, WorkItem **d_items, int **d_off);
+int build_worklist(fd23_solver *s);
+int dispatch_step(fd23_solver *s, int rec_now);
+
+template <class S, class C>
+Shot<S, C> make_shot(const fd23_solver *s)
+{
+    Shot<S, C> sh{};
+    for (int b = 0; b < 2; ++b)
+        for (int f = 0; f < 5; ++f) sh.f[b][f] = (S *)s->fld[b][f];
+    for (int m = 0; m < 5; ++m) sh.mat[m] = (const S *)s->mat[m];
+    for (int b = 0; b < 2; ++b)
+        for (int p = 0; p < 8; ++p) sh.psi[b][p] = (C *)s->psi[b][p];
+    sh.cpml = (const C *)s->cpml;
+    sh.nx = s->d.nx;
+    sh.nz = s->d.nz;
+    sh.npml = s->d.npml;
+    sh.topabsorb = s->d.topabsorb;
+    sh.pitch = s->L.pitch;
+    sh.origin = s->L.origin;
+    sh.cpml_blk = s->cpml_blk;
+    sh.nterms = s->nterms;
+    sh.terms = s->d_terms;
+    sh.tamp = (const C *)s->d_tamp;
+    sh.tamp_nt = s->nterms > 0 ? s->tamp_nt : 0;
+    for (int c = 0; c < 5; ++c) {
+        sh.nrec[c] = s->nrec[c];
+        sh.rec[c] = s->d_rec[c];
+        sh.seis[c] = (C *)s->d_seis[c];
+    }
+    sh.cta0 = 0;
+    sh.ncta = s->nblocks > 0 ? s->nblocks : 1;
+    sh.box.on = s->box_on ? 1 : 0;
+    if (s->box_on) {
+        sh.box.x0 = s->box_x0;
+        sh.box.z0 = s->box_z0;
+        sh.box.bx = s->box_bx;
+        sh.box.bz = s->box_bz;
+        sh.box.nsub = s->box_nsub;
+        sh.box.nring = s->box_nring;
+        for (int f = 0; f < 5; ++f) {
+            sh.box.r[f] = (C *)s->box_r[f];
+            sh.box.rmat[f] = (const C *)s->box_mat[f];
+        }
+        sh.box.cells = s->box_cells;
+        // incident field of the current step
+        const bool have = s->box_inc && s->it >= s->box_inc_it0 && s->it < s->box_inc_it0 + s->box_inc_n;
+        sh.box.inc = have ? (const C *)((const unsigned char *)s->box_inc +
+                                        (size_t)(s->it - s->box_inc_it0) * 5 * s->box_nring * s->cs)
+                          : nullptr;
+    }
+    return sh;
+}
+
+}  // namespace fd23

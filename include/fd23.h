@@ -222,6 +222,45 @@ int fd23_box_incident_from_displacement(int bx, int bz, double dt, const double 
 int fd23_box_material(int nx, int nz, double *mat, int x0, int z0, int bx, int bz, double src_vp,
                       double src_vs, double src_den, double dt, double h, double *bmat);
 
+/* ---- batched shots (no counterpart in the reference, which runs one shot
+ * per process, PD/main.cpp:43-183) ----
+ * A batch advances several solvers -- shots of any grid sizes, one wave type,
+ * one precision, one device, fused sweep, no box -- in lockstep: every time
+ * step is one launch of the sweep over all shots.  The solvers keep their
+ * buffers, sources and receivers; after fd23_batch_run their step counters,
+ * states and seismograms are as if each had run alone (bit for bit).  All
+ * solvers must be at the same step with the same record count.  The launches
+ * of a run are captured into a CUDA graph; a later run over the same step
+ * range (e.g. after fd23_reset of every solver) replays it.  Work is queued on
+ * the batch's stream, ordered after and before the solvers' own streams.
+ * fd23_batch_set_graph(b, 0) launches step by step instead. */
+typedef struct fd23_batch fd23_batch;
+int fd23_batch_create(fd23_solver *const *solvers, int n, fd23_batch **out);
+void fd23_batch_destroy(fd23_batch *b);
+int fd23_batch_run(fd23_batch *b, int nsteps, int itrecord);
+int fd23_batch_sync(fd23_batch *b);
+int fd23_batch_get_stream(fd23_batch *b, void **stream);
+int fd23_batch_set_graph(fd23_batch *b, int on);
+
+/* ---- work-plan autotuner (no counterpart in the reference) ----
+ * The fused sweep's work plan: 4-row blocks of 120-column strips, weighted by
+ * an estimated cost (wx for blocks touching the x-CPML, wz for the z-CPML and
+ * edge rows, 1 otherwise), cut into equal-cost contiguous ranges for
+ * per_sm x SMs x oversub CTAs.  fd23_autotune / fd23_batch_autotune time
+ * every candidate plan for trial_steps steps on the live shot(s), restore the
+ * wavefields, memory variables and step counters after each trial, and keep
+ * the fastest plan.  table (cap entries) receives every trial; returns the
+ * number of trials or a negative status. */
+typedef struct {
+    double wx, wz;      /* block cost weights */
+    int per_sm;         /* resident CTAs per SM */
+    double oversub;     /* CTAs launched per resident slot */
+    double ms_per_step; /* measured (0 for the current plan) */
+} fd23_tune_entry;
+int fd23_autotune(fd23_solver *s, int trial_steps, fd23_tune_entry *table, int cap);
+int fd23_batch_autotune(fd23_batch *b, int trial_steps, fd23_tune_entry *table, int cap);
+int fd23_batch_get_plan(fd23_batch *b, fd23_tune_entry *current, int *nblocks);
+
 /* ---- diagnostics ----
  * FP64 energy-norm watchdog over the wavefield: sum of squares of all
  * fields in FP64; returns FD23_ERR_NONFINITE when any value is NaN/Inf. */
