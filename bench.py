@@ -22,8 +22,17 @@ Hybrid-box workload (--config c2): the same model and grid, 3000 steps,
   run has no point source.  Its surface seismograms must equal the recorded
   run's bit for bit ("check" in the output line).
 
+Batched workload (--config c4): 64 shots with seeded grid sizes nx in
+  [1000, 4000], nz in [500, 2000] (not tile multiples), h=5 m, dt=4e-4 s,
+  3000 steps, per-shot seeded layered models, Ricker 8-25 Hz explosions,
+  40-cell CPML, 200 stations (400 traces) per component.  All shots advance
+  in one sweep launch per step (a CUDA graph per run); the work plan is
+  autotuned first (not timed).  The line also carries the same shots run one
+  by one with the plain FP32 solver, and for 16-bit storage the seismogram
+  relative-L2 error against FP64 runs of a seeded subset of the shots.
+
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--config c1|c2] [--nt NT] [--prec f32|bf16|f16|f64]
+                  [--config c1|c2|c4] [--nt NT] [--prec f32|bf16|f16|f64]
                   [--kernel fused|twopass]
 """
 import argparse
@@ -45,6 +54,8 @@ NX, NZ, H, DT, NT, NPML, F0 = 4000, 2000, 5.0, 4e-4, 5000, 40, 15.0
 NSTA = 400
 # hybrid-box workload: box origin and size, steps
 BOX_X0, BOX_Z0, BOX_BX, BOX_BZ, NT_BOX = 1000, 10, 2000, 1000, 3000
+# batched workload: shots, steps, stations per shot, shots checked against FP64
+NSHOT_B, NT_B, NSTA_B, NCHECK_B = 64, 3000, 200, 6
 
 
 def c1_model(nx=NX, nz=NZ, seed=1):
@@ -231,7 +242,7 @@ def main():
     ap.add_argument("--kernel", default="fused")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--config", default="c1", choices=["c1", "c2"])
+    ap.add_argument("--config", default="c1", choices=["c1", "c2", "c4"])
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -253,6 +264,9 @@ def main():
     torch.cuda.set_device(local)
     if args.config == "c2":
         bench_box(args, F, torch, rank, world, local, dist)
+        return
+    if args.config == "c4":
+        bench_batch(args, F, torch, rank, world, local, dist)
         return
     nt = args.nt
     vp, vs, rho = c1_model(seed=1 + rank)
@@ -506,6 +520,191 @@ def bench_box(args, F, torch, rank, world, local, dist):
     if rank == 0:
         print(json.dumps(line), flush=True)
     s.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def batch_shots(seed=7, nshot=NSHOT_B):
+    """Seeded shot table of the batched workload: grid, model seed, Ricker
+    frequency, source column."""
+    rng = np.random.default_rng(seed)
+    shots = []
+    for k in range(nshot):
+        nx = int(rng.integers(1000, 4001))
+        nz = int(rng.integers(500, 2001))
+        shots.append(dict(nx=nx, nz=nz, mseed=int(rng.integers(1 << 30)), f0=float(rng.uniform(8.0, 25.0)),
+                          xs=int(rng.integers(NPML + 20, nx - NPML - 20))))
+    return shots
+
+
+def layered_model(nx, nz, seed):
+    """12 seeded flat layers, vp ~ U[1500, 4500] m/s, times 1 + a smooth 5 %
+    perturbation (a coarse Gaussian field, bilinear upsampled); vs = vp/1.73,
+    rho = 310 vp^0.25."""
+    rng = np.random.default_rng(seed)
+    bounds = np.sort(rng.choice(np.arange(nz // 20, nz - nz // 20), size=11, replace=False))
+    vel = rng.uniform(1500.0, 4500.0, size=12)
+    layer = np.searchsorted(bounds, np.arange(nz), side="right")
+    cz, cx = max(2, nz // 40), max(2, nx // 40)
+    coarse = rng.standard_normal((cz, cx))
+
+    def lin(n, c):  # bilinear upsampling weights, c coarse points to n
+        x = np.linspace(0.0, c - 1.0, n)
+        i0 = np.minimum(np.floor(x).astype(np.int64), c - 2)
+        return i0, x - i0
+
+    iz, wz = lin(nz, cz)
+    ix, wx = lin(nx, cx)
+    rows = coarse[:, ix] * (1.0 - wx) + coarse[:, ix + 1] * wx
+    pert = rows[iz] * (1.0 - wz)[:, None] + rows[iz + 1] * wz[:, None]
+    pert *= 0.05 / np.abs(pert).max()
+    vp = vel[layer][:, None] * (1.0 + pert)
+    return vp, vp / 1.73, 310.0 * vp ** 0.25
+
+
+def bench_batch(args, F, torch, rank, world, local, dist):
+    nt = min(args.nt, NT_B)
+    shots = batch_shots(seed=7 + rank)
+    prec = args.prec
+    models = [layered_model(d["nx"], d["nz"], d["mseed"]) for d in shots]
+
+    def make(d, m, p):
+        vp, vs, rho = m
+        s = F.Solver("psv", d["nx"], d["nz"], NPML, H, DT, prec=p, pml_dt=DT, pml_v=float(vp.max()) / H,
+                     pml_r=1e-11, pml_fc=d["f0"], device=local, kernel="fused")
+        s.set_model(vp, vs, rho)
+        s.set_source(F.SRC_EXPLOSION, d["xs"], 20, None, F.wavelet_ricker(DT, d["f0"]), nt)
+        dx = max(1, (d["nx"] - 2 * NPML) // NSTA_B)
+        for f, z in ((0, 0), (1, 1)):
+            rx, rz = F.receivers_line(NSTA_B, NPML + 1, z, dx, 0)
+            s.set_receivers(f, rx, rz)
+        return s
+
+    cells = sum(d["nx"] * d["nz"] for d in shots)
+    solvers = [make(d, m, prec) for d, m in zip(shots, models)]
+    b = F.Batch(solvers)
+    stream = torch.cuda.ExternalStream(b.stream, device=local)
+    tune = b.autotune(5)
+    plan = b.plan()
+
+    def shot():
+        for s in solvers:
+            s.reset()
+        b.run(nt, 1)
+
+    for _ in range(args.warmup):
+        shot()
+    b.sync()
+    sampler = ClockSampler(local)
+    if rank == 0:
+        sampler.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for s in solvers:
+        s.reset()
+    e0.record(stream)
+    for k in range(args.steps):
+        if k:
+            for s in solvers:
+                s.reset()
+        b.run(nt, 1)
+    e1.record(stream)
+    b.sync()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    clocks = sampler.stop() if rank == 0 else None
+    t = torch.tensor([ms], dtype=torch.float64)
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t[0])
+    value = cells * nt * args.steps * world / (ms_max * 1e-3)
+    seis = [(s.seismograms(0), s.seismograms(1)) for s in solvers]
+
+    # the same shots one by one with the plain single-shot FP32 solver
+    single = None
+    if rank == 0 and not args.no_cpu:
+        t_single = 0.0
+        for d, m in zip(shots, models):
+            s = make(d, m, "f32")
+            st = torch.cuda.ExternalStream(s.stream, device=local)
+            a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.run(2, 1)
+            s.reset()
+            s.sync()
+            a0.record(st)
+            s.run(nt, 1)
+            a1.record(st)
+            s.sync()
+            t_single += a0.elapsed_time(a1)
+            s.close()
+        single = {"value": cells * nt / (t_single * 1e-3), "unit": "cell-updates/s",
+                  "what": "the same 64 shots run one after another with the plain single-shot FP32 solver"}
+
+    # accuracy of 16-bit storage: seismograms against FP64 runs of a subset
+    accuracy = None
+    if rank == 0 and prec in ("bf16", "f16"):
+        pick = np.random.default_rng(11).choice(len(shots), size=NCHECK_B, replace=False)
+        errs = []
+        for k in pick:
+            r = make(shots[k], models[k], "f64")
+            r.run(nt, 1)
+            ref = np.concatenate([r.seismograms(0).ravel(), r.seismograms(1).ravel()])
+            got = np.concatenate([seis[k][0].ravel(), seis[k][1].ravel()]).astype(np.float64)
+            errs.append(float(np.linalg.norm(got - ref) / np.linalg.norm(ref)))
+            r.close()
+        accuracy = {"seismogram_rel_l2_vs_fp64": {"max": max(errs), "median": float(np.median(errs)),
+                                                  "shots": [int(k) for k in pick], "per_shot": errs}}
+
+    e2e = None
+    if not args.no_e2e:
+        times = []
+        for _ in range(max(1, min(args.steps, 2))):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for s, m in zip(solvers, models):
+                s.set_model(*m)
+            shot()
+            out = [(s.seismograms(0), s.seismograms(1)) for s in solvers]
+            times.append(time.perf_counter() - t0)
+        es = {"f32": 4, "f64": 8, "bf16": 2, "f16": 2}[prec]
+        e2e = {"value": cells * nt / statistics.mean(times) * world, "unit": "cell-updates/s",
+               "h2d_bytes_per_step": 5 * cells * es, "d2h_bytes_per_step": sum(a.nbytes + w.nbytes for a, w in out),
+               "note": "per step = one whole batch of shots: material build + upload, the run, seismograms"}
+    hbm, peak_kind = load_peaks()
+    es = {"f32": 4, "f64": 8, "bf16": 2, "f16": 2}[prec]
+    per_launch_ms = ms_max / (args.steps * nt)
+    ab = sum(alg_bytes(d["nx"], d["nz"], NPML, es) for d in shots)
+    achieved = ab / (per_launch_ms * 1e-3) / 1e9
+    line = {"metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": prec,
+            "data": "synthetic",
+            "config": {"workload": "psv_batch64_3000steps_c4", "shots": len(shots), "nt": nt,
+                       "cells_per_step": cells, "grids": [[d["nx"], d["nz"]] for d in shots],
+                       "prec": prec, "plan": plan, "autotune_trials": len(tune),
+                       "l2": "inputs larger than L2", "parallelism": "replicas x%d" % world},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "traffic": None, "peak_source": peak_kind,
+                         "scope": "one batched sweep launch over all shots",
+                         "alg_bytes_per_launch": ab, "launch_ms": per_launch_ms},
+            "gpu_launches": args.steps * (nt + len(shots)),
+            "clocks": clocks,
+            "e2e": e2e}
+    if single:
+        line["single_shot_fp32"] = single
+        line["batched_over_single_shot_fp32"] = value / single["value"]
+    if accuracy:
+        line["accuracy"] = accuracy
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    b.close()
+    for s in solvers:
+        s.close()
     if dist:
         dist.barrier()
         dist.destroy_process_group()

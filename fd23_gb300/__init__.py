@@ -54,7 +54,7 @@ ABI_FUNCTIONS = [
     "fd23_box_ring_index", "fd23_box_ring_cells", "fd23_box_incident_from_displacement",
     "fd23_box_material", "fd23_batch_create", "fd23_batch_destroy", "fd23_batch_run", "fd23_batch_sync",
     "fd23_batch_get_stream", "fd23_batch_set_graph", "fd23_autotune", "fd23_batch_autotune",
-    "fd23_batch_get_plan",
+    "fd23_batch_get_plan", "fd23_work_plan",
 ]
 
 
@@ -144,6 +144,7 @@ def lib():
         "fd23_autotune": ([vp, i, vp, i], i),
         "fd23_batch_autotune": ([vp, i, vp, i], i),
         "fd23_batch_get_plan": ([vp, vp, _C.POINTER(i)], i),
+        "fd23_work_plan": ([i, vp, vp, vp, vp, i, vp, vp, i, vp, i], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -297,6 +298,21 @@ def box_material(mat, x0, z0, bx, bz, src_vp, src_vs, src_den, dt, h):
     n = _check(lib().fd23_box_material(nx, nz, _p(m), x0, z0, bx, bz, src_vp, src_vs, src_den, dt, h,
                                        _p(bm)), "fd23_box_material")
     return m, bm, n
+
+
+def work_plan(grids, sms=152, wx=4.0, wz=3.0, per_sm=3, oversub=1.0):
+    """The fused sweep's work plan for grids [(nx, nz, npml, topabsorb)]:
+    list over CTAs of lists of (shot, x0, z0, z1) items."""
+    n = len(grids)
+    a = [_np.ascontiguousarray([g[k] for g in grids], dtype=_np.int32) for k in range(4)]
+    cap = sum(((g[0] + 119) // 120) * ((g[1] + 3) // 4) for g in grids) * 2 + 16
+    items = _np.zeros(4 * cap, _np.int32)
+    off = _np.zeros(cap + 1, _np.int32)
+    t = TuneEntry(wx, wz, per_sm, oversub, 0.0)
+    nb = _check(lib().fd23_work_plan(n, *[_p(v) for v in a], sms, _C.cast(_C.pointer(t), _C.c_void_p),
+                                     _p(items), cap, _p(off), cap), "fd23_work_plan")
+    it = items.reshape(-1, 4)
+    return [[tuple(int(v) for v in it[j]) for j in range(off[c], off[c + 1])] for c in range(nb)]
 
 
 class Batch:

@@ -257,20 +257,20 @@ int snapshot_restore(const std::vector<fd23_solver *> &ss, cudaStream_t st, cons
     return FD23_OK;
 }
 
+// block cost weights x waves of CTAs (the plan rounds the CTA count up to
+// whole waves of the resident slots)
 std::vector<TuneParams> candidates()
 {
     const double w[][2] = {{1.0, 1.0}, {2.5, 1.5}, {4.0, 3.0}, {6.0, 4.0}, {4.0, 2.0}, {3.0, 3.0}};
     std::vector<TuneParams> c;
-    for (int per_sm : {3, 2})
-        for (double ov : {1.0, 2.0})
-            for (auto &ww : w) {
-                TuneParams t;
-                t.wx = ww[0];
-                t.wz = ww[1];
-                t.per_sm = per_sm;
-                t.oversub = ov;
-                c.push_back(t);
-            }
+    for (double ov : {1.0, 2.0, 3.0})
+        for (auto &ww : w) {
+            TuneParams t;
+            t.wx = ww[0];
+            t.wz = ww[1];
+            t.oversub = ov;
+            c.push_back(t);
+        }
     return c;
 }
 
@@ -459,6 +459,34 @@ int fd23_batch_autotune(fd23_batch *b, int trial_steps, fd23_tune_entry *table, 
     rc = autotune_core(b->s, b->stream, trial_steps, apply, steps, table, cap);
     const int jr = join_out(b);
     return rc < 0 ? rc : (jr ? jr : rc);
+}
+
+int fd23_work_plan(int nshots, const int *nx, const int *nz, const int *npml, const int *topabsorb, int sms,
+                   const fd23_tune_entry *tune, int *items, int cap_items, int *off, int cap_ctas)
+{
+    if (nshots <= 0 || !nx || !nz || !npml || !topabsorb || sms <= 0 || !tune || !items || !off) return FD23_ERR_ARG;
+    std::vector<ShotGeom> geo;
+    for (int k = 0; k < nshots; ++k) {
+        if (nx[k] < 2 || nz[k] < 2 || npml[k] < 0) return FD23_ERR_ARG;
+        geo.push_back(ShotGeom{nx[k], nz[k], npml[k], topabsorb[k]});
+    }
+    TuneParams tp;
+    tp.wx = tune->wx;
+    tp.wz = tune->wz;
+    tp.per_sm = tune->per_sm;
+    tp.oversub = tune->oversub;
+    WorkPlan plan;
+    const int rc = plan_work(geo, fused_geom(FD23_PSV, FD23_F32).tile_x, sms, tp, plan);
+    if (rc) return rc;
+    if ((int)plan.items.size() > cap_items || plan.nblocks + 1 > cap_ctas + 1) return FD23_ERR_ARG;
+    for (size_t i = 0; i < plan.items.size(); ++i) {
+        items[4 * i] = plan.items[i].shot;
+        items[4 * i + 1] = plan.items[i].x0;
+        items[4 * i + 2] = plan.items[i].z0;
+        items[4 * i + 3] = plan.items[i].z1;
+    }
+    for (int c = 0; c <= plan.nblocks; ++c) off[c] = plan.off[c];
+    return plan.nblocks;
 }
 
 int fd23_autotune(fd23_solver *s, int trial_steps, fd23_tune_entry *table, int cap)

@@ -28,53 +28,112 @@ double block_cost(const ShotGeom &g, int tile_x, int strip, int zb, const TunePa
 
 }  // namespace
 
+// Cuts the nb blocks of one shot (cumulative costs c) into n contiguous
+// ranges of near-equal cost, none touching more than 4 strips; false if the
+// last range would need more.
+bool cut_shot(const std::vector<double> &c, long long nb, int nzb, int n, std::vector<long long> &ends)
+{
+    ends.clear();
+    long long b0 = 0;
+    for (int q = 0; q < n; ++q) {
+        const long long cap = std::min(nb, (b0 / nzb + 4) * (long long)nzb);  // at most 4 strips
+        long long b1;
+        if (q == n - 1) {
+            b1 = nb;
+            if (b1 > cap) return false;
+        } else {
+            const double target = c[nb] * (double)(q + 1) / (double)n;
+            b1 = std::lower_bound(c.begin() + b0 + 1, c.end(), target) - c.begin();
+            b1 = std::max(b1, b0 + 1);
+            b1 = std::min(b1, nb - (n - 1 - q));  // leave a block for every later CTA
+            b1 = std::min(b1, cap);
+        }
+        ends.push_back(b1);
+        b0 = b1;
+    }
+    return true;
+}
+
 int plan_work(const std::vector<ShotGeom> &shots, int tile_x, int sms, const TuneParams &tp, WorkPlan &plan)
 {
     const int ns = (int)shots.size();
     if (ns <= 0 || tile_x <= 0 || sms <= 0) return FD23_ERR_ARG;
     std::vector<std::vector<double>> cum(ns);
     std::vector<int> ntx(ns), nzb(ns), nmin(ns);
+    std::vector<long long> nbk(ns);
     double total = 0.0;
+    long long sum_min = 0;
     for (int k = 0; k < ns; ++k) {
         const ShotGeom &g = shots[k];
         ntx[k] = (g.nx + tile_x - 1) / tile_x;
         nzb[k] = (g.nz + 3) / 4;
-        const long long nb = (long long)ntx[k] * nzb[k];
-        cum[k].assign((size_t)nb + 1, 0.0);
-        for (long long b = 0; b < nb; ++b)
+        nbk[k] = (long long)ntx[k] * nzb[k];
+        cum[k].assign((size_t)nbk[k] + 1, 0.0);
+        for (long long b = 0; b < nbk[k]; ++b)
             cum[k][b + 1] = cum[k][b] + block_cost(g, tile_x, (int)(b / nzb[k]), (int)(b % nzb[k]), tp);
-        total += cum[k][nb];
-        nmin[k] = std::max(1, (ntx[k] + 1) / 2);  // keeps every CTA within 4 items
+        total += cum[k][nbk[k]];
+        nmin[k] = (int)std::min<long long>(nbk[k], std::max(1, (ntx[k] + 1) / 2));  // within 4 items
+        sum_min += nmin[k];
     }
-    // CTAs: the resident slots times the oversubscription, shared by cost
-    const long long slots = std::max(1LL, (long long)std::llround(sms * tp.per_sm * std::max(tp.oversub, 0.05)));
+    // CTA count: the resident slots times the oversubscription, rounded up to
+    // whole waves once the per-shot minimums are met
+    const long long slots = std::max(1LL, (long long)sms * std::max(1, tp.per_sm));
+    long long want = std::max(1LL, (long long)std::llround(slots * std::max(tp.oversub, 0.05)));
+    want = std::max(want, sum_min);
+    if (want > slots) want = (want + slots - 1) / slots * slots;
+    long long cap_all = 0;
+    for (int k = 0; k < ns; ++k) cap_all += nbk[k];
+    want = std::min(want, cap_all);
+    // share `want` by cost with floors nmin and caps nbk (water filling, then
+    // largest remainders)
+    std::vector<double> share(ns, 0.0);
+    std::vector<char> fixed(ns, 0);
+    for (int iter = 0; iter < ns + 1; ++iter) {
+        double free_cost = 0.0;
+        long long free_ctas = want;
+        for (int k = 0; k < ns; ++k) {
+            if (fixed[k]) free_ctas -= (long long)share[k];
+            else free_cost += cum[k][nbk[k]];
+        }
+        bool changed = false;
+        for (int k = 0; k < ns; ++k) {
+            if (fixed[k]) continue;
+            share[k] = free_cost > 0 ? (double)free_ctas * cum[k][nbk[k]] / free_cost : 0.0;
+            if (share[k] < nmin[k]) { share[k] = nmin[k]; fixed[k] = 1; changed = true; }
+            else if (share[k] > (double)nbk[k]) { share[k] = (double)nbk[k]; fixed[k] = 1; changed = true; }
+        }
+        if (!changed) break;
+    }
     std::vector<int> nc(ns);
+    long long used = 0;
+    std::vector<std::pair<double, int>> rem;
     for (int k = 0; k < ns; ++k) {
-        const long long nb = (long long)ntx[k] * nzb[k];
-        const double share = slots * cum[k][nb] / total;
-        nc[k] = (int)std::min<long long>(nb, std::max<long long>(nmin[k], std::llround(share)));
+        nc[k] = std::max(nmin[k], (int)std::floor(share[k]));
+        used += nc[k];
+        rem.push_back({share[k] - std::floor(share[k]), k});
+    }
+    std::sort(rem.begin(), rem.end(), [](const std::pair<double, int> &a, const std::pair<double, int> &b) {
+        return a.first > b.first || (a.first == b.first && a.second < b.second);
+    });
+    for (size_t i = 0; i < rem.size() && used < want; ++i) {
+        const int k = rem[i].second;
+        if (nc[k] < nbk[k]) { ++nc[k]; ++used; }
     }
     plan.items.clear();
     plan.off.assign(1, 0);
     plan.cta0.assign(ns, 0);
     plan.ncta.assign(ns, 0);
+    std::vector<long long> ends;
     for (int k = 0; k < ns; ++k) {
-        const long long nb = (long long)ntx[k] * nzb[k];
-        const int n = nc[k];
-        const std::vector<double> &c = cum[k];
+        int n = nc[k];
+        while (!cut_shot(cum[k], nbk[k], nzb[k], n, ends)) {
+            if (n >= nbk[k]) return FD23_ERR_ARG;
+            ++n;
+        }
         plan.cta0[k] = (int)plan.off.size() - 1;
         plan.ncta[k] = n;
         long long b0 = 0;
-        for (int q = 0; q < n; ++q) {
-            long long b1;
-            if (q == n - 1) {
-                b1 = nb;
-            } else {
-                const double target = c[nb] * (double)(q + 1) / (double)n;
-                b1 = std::lower_bound(c.begin() + b0 + 1, c.end(), target) - c.begin();
-                b1 = std::max(b1, b0 + 1);
-                b1 = std::min(b1, nb - (n - 1 - q));  // leave a block for every later CTA
-            }
+        for (long long b1 : ends) {
             while (b0 < b1) {
                 const int strip = (int)(b0 / nzb[k]);
                 const long long send = (long long)(strip + 1) * nzb[k];

@@ -260,6 +260,13 @@ typedef struct {
 int fd23_autotune(fd23_solver *s, int trial_steps, fd23_tune_entry *table, int cap);
 int fd23_batch_autotune(fd23_batch *b, int trial_steps, fd23_tune_entry *table, int cap);
 int fd23_batch_get_plan(fd23_batch *b, fd23_tune_entry *current, int *nblocks);
+/* The work plan for nshots grids under the given parameters (host only, for
+ * inspection and tests): items receives 4 ints per item (shot, x0, z0, z1:
+ * 120 columns from x0, rows [z0, z1)), off[c] .. off[c+1] indexes the items of
+ * CTA c (off needs cap_ctas + 1 entries).  Returns the CTA count. */
+int fd23_work_plan(int nshots, const int *nx, const int *nz, const int *npml, const int *topabsorb,
+                   int sms, const fd23_tune_entry *tune, int *items, int cap_items, int *off,
+                   int cap_ctas);
 
 /* ---- diagnostics ----
  * FP64 energy-norm watchdog over the wavefield: sum of squares of all

@@ -1,8 +1,9 @@
 """CPU audit of every address the fused sweep forms (fd23_gb300/csrc/fd23_fused.cu).
 
-Restates the work-list construction (fd23_api.cpp: build_worklist,
-make_layout) and the index arithmetic of the kernel, then checks, for the
-grid sizes the tests and the benchmark use, that
+Takes the work plans from the library (fd23_work_plan: the planner the
+solver and the batch use), restates the padded layout (make_layout) and the
+index arithmetic of the kernel, then checks, for the grid sizes the tests and
+the benchmarks use (and the 64-shot batch), that
 
   * every bulk copy reads inside its HBM buffer, starts on a 16-byte boundary
     in global and shared memory, and moves a multiple of 16 bytes;
@@ -30,44 +31,16 @@ def layout(nx, nz):
     return pitch, rows, ZPAD * pitch + XPAD
 
 
-def worklist(nx, nz, sms=152, per_sm=2, npml=40, wx=4.0, wz=3.0, top=False):
-    """Cost-weighted contiguous partition of the 4-row blocks (build_worklist)."""
-    import bisect
-    ntx = (nx + TX - 1) // TX
-    nzb = (nz + 3) // 4
-    total = ntx * nzb
-    nb = min(sms * per_sm, total)
-    nb = max(nb, (ntx + 1) // 2)
-    cum = [0.0]
-    for b in range(total):
-        strip, zb = divmod(b, nzb)
-        x0 = strip * TX
-        xp = (x0 - 4 < max(npml, 4)) or (x0 + TX + 4 > min(nx - npml, nx - 4))
-        r0, r1 = 4 * zb, 4 * zb + 3
-        zp = (r1 >= min(nz - npml, nz - 4)) or r0 < 4 or (top and r0 < npml)
-        cum.append(cum[-1] + (wx if xp else (wz if zp else 1.0)))
-    ctas = []
-    b0 = 0
-    for c in range(nb):
-        if c == nb - 1:
-            b1 = total
-        else:
-            target = cum[total] * (c + 1) / nb
-            b1 = bisect.bisect_left(cum, target, b0 + 1)
-            b1 = max(b1, b0 + 1)
-            b1 = min(b1, total - (nb - 1 - c))
-        items = []
-        while b0 < b1:
-            strip = b0 // nzb
-            e = min(b1, (strip + 1) * nzb)
-            items.append((strip * TX, (b0 - strip * nzb) * 4, (e - strip * nzb) * 4))
-            b0 = e
-        ctas.append(items)
-    assert b0 == total
-    return ctas
+def worklist(nx, nz, npml, oversub=1.0, per_sm=3):
+    F = pytest.importorskip("fd23_gb300")
+    try:
+        F.lib()
+    except ImportError as e:
+        pytest.skip(str(e))
+    return [[it[1:] for it in cta] for cta in F.work_plan([(nx, nz, npml, 0)], per_sm=per_sm, oversub=oversub)]
 
 
-def audit(nx, nz, es, wave, sms=152, per_sm=2):
+def audit(nx, nz, es, wave, per_sm=3, oversub=1.0, ctas=None):
     pitch, rows, origin = layout(nx, nz)
     npml = min(40, nx // 2, nz // 2)
     elems = pitch * rows
@@ -77,8 +50,16 @@ def audit(nx, nz, es, wave, sms=152, per_sm=2):
     pwoff = 4 if es == 2 else 0
     pww = SW + 2 * pwoff
     assert (pitch * es) % 16 == 0
-    for items in worklist(nx, nz, sms, per_sm, npml=npml):
+    if ctas is None:
+        ctas = worklist(nx, nz, npml, oversub, per_sm)
+    covered = set()
+    for items in ctas:
         assert 1 <= len(items) <= MAX_ITEMS
+        for (x0, z0, z1) in items:
+            for zb in range(z0 // 4, z1 // 4):
+                key = (x0, zb)
+                assert key not in covered  # every block exactly once
+                covered.add(key)
         for (x0, z0, z1) in items:
             assert x0 % TX == 0 and z0 % 4 == 0 and z1 % 4 == 0 and z1 > z0
             niter = (z1 - z0) // 4 + 2
@@ -135,3 +116,31 @@ SIZES = [(96, 96), (96, 64), (250, 130), (257, 131), (500, 300), (1000, 1000), (
 def test_fused_addresses_in_bounds(nx, nz, es, wave):
     per_sm = 1 if es == 8 else 3
     audit(nx, nz, es, wave, per_sm=per_sm)
+    audit(nx, nz, es, wave, per_sm=per_sm, oversub=3.0)
+
+
+def test_batch_plan_in_bounds():
+    """The 64-shot batch of the benchmark under every autotuner candidate:
+    every CTA serves one shot, and every shot's items pass the audit."""
+    import sys, os
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    F = pytest.importorskip("fd23_gb300")
+    try:
+        F.lib()
+    except ImportError as e:
+        pytest.skip(str(e))
+    grids = [(d["nx"], d["nz"], 40, 0) for d in bench.batch_shots()]
+    for wx, wz in ((1.0, 1.0), (2.5, 1.5), (4.0, 3.0), (6.0, 4.0), (4.0, 2.0), (3.0, 3.0)):
+        for ov in (1.0, 2.0, 3.0):
+            ctas = F.work_plan(grids, wx=wx, wz=wz, oversub=ov)
+            assert len(ctas) % 456 == 0
+            per_shot = {}
+            for cta in ctas:
+                shots = {it[0] for it in cta}
+                assert len(shots) == 1
+                per_shot.setdefault(cta[0][0], []).append([it[1:] for it in cta])
+            assert sorted(per_shot) == list(range(len(grids)))
+            if (wx, wz, ov) == (4.0, 3.0, 1.0):
+                for k, c in per_shot.items():
+                    audit(grids[k][0], grids[k][1], 4, "psv", ctas=c)
