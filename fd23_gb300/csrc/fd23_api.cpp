@@ -14,6 +14,8 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include <cudaTypedefs.h>
+
 #include "fd23_solver.h"
 
 using namespace fd23;
@@ -217,6 +219,54 @@ int dispatch_flush(fd23_solver *s)
     }
 }
 
+// Tensor maps of the fused sweep's copies: 3-D views [field][row][column] of
+// the wavefield block of each buffer set and of the material block, with the
+// box shapes the sweep copies (fused_boxes).  Coordinates of a copy are
+// padded-array positions, so every box the sweep asks for lies inside.
+int encode_maps(fd23_solver *s)
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        cudaDriverEntryPointQueryResult q;
+        void *fn = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !fn) {
+            cudaGetLastError();
+            return FD23_ERR_CUDA;
+        }
+        encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+    }
+    const FusedBoxes bx = fused_boxes(s->d.wave, s->d.prec);
+    CUtensorMapDataType dt = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    if (s->d.prec == FD23_F64) dt = CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+    if (s->d.prec == FD23_BF16) dt = CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+    if (s->d.prec == FD23_F16) dt = CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
+    const Layout &L = s->L;
+    auto make = [&](TmaDesc &m, void *base, int nfields, int w, int nf) -> int {
+        const cuuint64_t dims[3] = {(cuuint64_t)L.pitch, (cuuint64_t)L.rows, (cuuint64_t)nfields};
+        const cuuint64_t strides[2] = {(cuuint64_t)L.pitch * s->es, (cuuint64_t)L.elems() * s->es};
+        const cuuint32_t box[3] = {(cuuint32_t)w, 4u, (cuuint32_t)nf};
+        const cuuint32_t estr[3] = {1u, 1u, 1u};
+        const CUresult r = encode(reinterpret_cast<CUtensorMap *>(&m), dt, 3, base, dims, strides, box, estr,
+                                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                  CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        return r == CUDA_SUCCESS ? FD23_OK : FD23_ERR_CUDA;
+    };
+    ShotMaps h{};
+    int rc = FD23_OK;
+    for (int b = 0; b < 2 && !rc; ++b) {
+        rc = make(h.uw[b], s->fld_block[b], s->nfld, bx.uww, bx.nv);
+        if (!rc) rc = make(h.t[b], s->fld_block[b], s->nfld, bx.pww, bx.nt);
+    }
+    if (!rc) rc = make(h.ms, s->mat_block, s->nmat, bx.pww, bx.nms);
+    if (!rc) rc = make(h.mv, s->mat_block, s->nmat, bx.pww, bx.nmv);
+    if (rc) return rc;
+    if (!s->d_maps && (rc = dev_alloc((void **)&s->d_maps, sizeof(ShotMaps)))) return rc;
+    CK(cudaMemcpy(s->d_maps, &h, sizeof(ShotMaps), cudaMemcpyHostToDevice));
+    return FD23_OK;
+}
+
 // CTAs per SM the fused sweep can keep resident (shared memory bound, at most
 // the 3 its register budget is built for)
 int fused_per_sm(int device, int wave, int prec)
@@ -306,10 +356,11 @@ void free_box(fd23_solver *s)
 void free_all(fd23_solver *s)
 {
     for (int b = 0; b < 2; ++b) {
-        for (int f = 0; f < 5; ++f) cudaFree(s->fld[b][f]);
+        cudaFree(s->fld_block[b]);
         for (int p = 0; p < 8; ++p) cudaFree(s->psi[b][p]);
     }
-    for (int m = 0; m < 5; ++m) cudaFree(s->mat[m]);
+    cudaFree(s->mat_block);
+    cudaFree(s->d_maps);
     cudaFree(s->cpml);
     cudaFree(s->err_flag);
     cudaFree(s->norm_buf);
@@ -469,13 +520,13 @@ int fd23_create(const fd23_desc *desc, fd23_solver **out)
     };
     if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(FD23_ERR_CUDA);
     const size_t gbytes = s->L.elems() * s->es;
-    for (int b = 0; b < 2; ++b)
-        for (int f = 0; f < s->nfld; ++f)
-            if ((rc = dev_alloc(&s->fld[b][f], gbytes))) return fail(rc);
-    for (int m = 0; m < s->nmat; ++m) {
-        if ((rc = dev_alloc(&s->mat[m], gbytes))) return fail(rc);
-        if (cudaMemset(s->mat[m], 0, gbytes) != cudaSuccess) return fail(FD23_ERR_CUDA);
+    for (int b = 0; b < 2; ++b) {
+        if ((rc = dev_alloc(&s->fld_block[b], s->nfld * gbytes))) return fail(rc);
+        for (int f = 0; f < s->nfld; ++f) s->fld[b][f] = (unsigned char *)s->fld_block[b] + f * gbytes;
     }
+    if ((rc = dev_alloc(&s->mat_block, s->nmat * gbytes))) return fail(rc);
+    if (cudaMemset(s->mat_block, 0, s->nmat * gbytes) != cudaSuccess) return fail(FD23_ERR_CUDA);
+    for (int m = 0; m < s->nmat; ++m) s->mat[m] = (unsigned char *)s->mat_block + m * gbytes;
     const size_t px = 2ull * d.npml * d.nz, pz = 2ull * d.npml * d.nx;
     for (int p = 0; p < s->npsi; ++p) s->psi_elems[p] = (p < s->npsi / 2) ? px : pz;
     for (int b = 0; b < 2; ++b)
@@ -491,6 +542,7 @@ int fd23_create(const fd23_desc *desc, fd23_solver **out)
     if (s->fused) {
         if ((rc = fused_prepare(d.wave, d.prec))) return fail(rc);
         if ((rc = build_worklist(s))) return fail(rc);
+        if ((rc = encode_maps(s))) return fail(rc);
     }
     if ((rc = zero_state(s))) return fail(rc);
     if (cudaStreamSynchronize(s->stream) != cudaSuccess) return fail(FD23_ERR_CUDA);
@@ -697,6 +749,7 @@ int fd23_sync(fd23_solver *s)
     CK(cudaStreamSynchronize(s->stream));
     int flag = 0;
     CK(cudaMemcpy(&flag, s->err_flag, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag == 2) return FD23_ERR_UNSUPPORTED;  // shared-memory layout check failed
     return flag ? FD23_ERR_TIMEOUT : FD23_OK;
 }
 

@@ -14,12 +14,15 @@
 //     columns each side, recomputed rather than exchanged) and the velocity of
 //     rows z0-8+4i .. z0-5+4i on the TX output columns, so the velocity front
 //     trails the stress front by exactly the 4 rows its z-stencil needs.
-//   * The producer warp streams rows of the stencil inputs (U, W or V) into a
-//     ring of NUW 4-row blocks and rows of the point-wise operands (old
-//     stresses, material) into NPW stages with 1-D bulk async copies
-//     (cp.async.bulk ... mbarrier::complete_tx).  Full/empty mbarrier pairs
-//     gate each slot, so the producer runs ahead as far as the rings allow
-//     and the compute warps never wait on it except for data.
+//   * The producer warp streams 4-row blocks of the stencil inputs (U, W or
+//     V) into a ring of NUW slots and the point-wise operands (old stresses,
+//     material) into NPW stages with tiled tensor copies (TMA,
+//     cp.async.bulk.tensor.3d ... mbarrier::complete_tx): the wavefields of a
+//     buffer set and the materials are each one allocation, viewed as
+//     [field][row][column], so one box carries every field of a block -- four
+//     copies per iteration.  Full/empty mbarrier pairs gate each slot, so the
+//     producer runs ahead as far as the rings allow and the compute warps
+//     never wait on it except for data.
 //   * Updated stresses (after the point source) go to a 4-block smem ring that
 //     feeds the velocity stencil, and straight to HBM; one barrier over the
 //     compute warps per iteration orders the ring.
@@ -43,13 +46,14 @@
 
 #include "fd23_device.cuh"
 #include "fd23_kernels.h"
+#include "fd23_pack.cuh"
 
 namespace fd23 {
 
 namespace {
 
 // ---------------------------------------------------------------------------
-// PTX helpers: mbarrier + 1-D bulk async copy (TMA engine)
+// PTX helpers: mbarrier + tiled tensor copy (TMA engine)
 __device__ __forceinline__ uint32_t smem_u32(const void *p)
 {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -76,12 +80,13 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
         : "memory");
     return ok != 0;
 }
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+// tiled 3-D tensor copy (TMA) of one box at (x, y, z) of a tensor map
+__device__ __forceinline__ void tma_load_3d(void *dst, const void *map, int x, int y, int z, uint64_t *bar)
 {
     asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-            smem_u32(dst)),
-        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_u32(dst)),
+        "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
         : "memory");
 }
 __device__ __forceinline__ uint64_t globaltimer_ns()
@@ -255,6 +260,43 @@ __device__ __forceinline__ void dpz4(const S *const rows[9], int off, C out[4])
 #pragma unroll
     for (int e = 0; e < 4; ++e) out[e] = fmaC<C>(-Coef4<C>::c3, a[e] - b[e], out[e]);
 }
+// 4 stored values as packed operands
+template <class S, class C>
+__device__ __forceinline__ P4<C> ld4p(const S *p)
+{
+    if constexpr (std::is_same<S, float>::value) {
+        const ulonglong2 t = *reinterpret_cast<const ulonglong2 *>(p);
+        return P4<C>{t.x, t.y};
+    } else {
+        C v[4];
+        Vec4<S, C>::ld(p, v);
+        return P4<C>::from(v);
+    }
+}
+// the z differences above on packed operands (same operation sequence)
+template <class S, class C>
+__device__ __forceinline__ P4<C> dmz4p(const S *const rows[9], int off)
+{
+    using P = P4<C>;
+    const typename P::K k0 = P::splat(Coef4<C>::c0), k1 = P::splat(-Coef4<C>::c1), k2 = P::splat(Coef4<C>::c2),
+                        k3 = P::splat(-Coef4<C>::c3);
+    P d = P::mulk(k0, ld4p<S, C>(rows[4] + off) - ld4p<S, C>(rows[3] + off));
+    d = P::fmak(k1, ld4p<S, C>(rows[5] + off) - ld4p<S, C>(rows[2] + off), d);
+    d = P::fmak(k2, ld4p<S, C>(rows[6] + off) - ld4p<S, C>(rows[1] + off), d);
+    return P::fmak(k3, ld4p<S, C>(rows[7] + off) - ld4p<S, C>(rows[0] + off), d);
+}
+template <class S, class C>
+__device__ __forceinline__ P4<C> dpz4p(const S *const rows[9], int off)
+{
+    using P = P4<C>;
+    const typename P::K k0 = P::splat(Coef4<C>::c0), k1 = P::splat(-Coef4<C>::c1), k2 = P::splat(Coef4<C>::c2),
+                        k3 = P::splat(-Coef4<C>::c3);
+    P d = P::mulk(k0, ld4p<S, C>(rows[5] + off) - ld4p<S, C>(rows[4] + off));
+    d = P::fmak(k1, ld4p<S, C>(rows[6] + off) - ld4p<S, C>(rows[3] + off), d);
+    d = P::fmak(k2, ld4p<S, C>(rows[7] + off) - ld4p<S, C>(rows[2] + off), d);
+    return P::fmak(k3, ld4p<S, C>(rows[8] + off) - ld4p<S, C>(rows[1] + off), d);
+}
+
 // z differences with per-cell coefficient rows (edge cells)
 template <class S, class C>
 __device__ __forceinline__ void zcol(const S *const rows[9], int off, C v[9][4])
@@ -299,9 +341,24 @@ struct Cfg {
     // ring depths (NUW and NTR powers of two): sized so that three CTAs of the
     // 4-byte forms fit in the 228 KB of shared memory of one SM
     static constexpr int NUW = FD23_FUSED_NUW, NPW = FD23_FUSED_NPW, NTR = 4;
-    static constexpr int UW_ELEMS = NUW * 4 * NV * UWW;
-    static constexpr int PW_ELEMS = NPW * NPF * 4 * PWW;
+    // Tensor copies land 128-byte aligned: a stencil-input slot holds one box
+    // [NV fields][4 rows][UWW], a point-wise stage three boxes (old stresses,
+    // stress-update material, velocity-update material) [fields][4 rows][PWW],
+    // each group starting on a 128-byte boundary.  Sizes in elements.
+    static constexpr __host__ __device__ int al128(int bytes) { return (bytes + 127) / 128 * 128 / (int)sizeof(S); }
+    static constexpr int UWF = 4 * UWW;                                  // field stride in a slot
+    static constexpr int UW_SLOT = al128(NV * 4 * UWW * (int)sizeof(S));
+    static constexpr int UW_ELEMS = NUW * UW_SLOT;
+    static constexpr int PG_MS = al128(NT * 4 * PWW * (int)sizeof(S));
+    static constexpr int PG_MV = PG_MS + al128(NMS * 4 * PWW * (int)sizeof(S));
+    static constexpr int PW_STAGE = PG_MV + al128(NMV * 4 * PWW * (int)sizeof(S));
+    static constexpr int PW_ELEMS = NPW * PW_STAGE;
     static constexpr int TR_ELEMS = NTR * 4 * NT * SW;
+    // start of point-wise field f (stresses, then the two material groups) in a stage
+    static constexpr __host__ __device__ int pw_field(int f)
+    {
+        return f < NT ? f * 4 * PWW : (f < NT + NMS ? PG_MS + (f - NT) * 4 * PWW : PG_MV + (f - NT - NMS) * 4 * PWW);
+    }
     static constexpr int MAX_ITEMS = 4;
     static constexpr int MAX_TERMS = 16;
     static constexpr int MINB = sizeof(S) == 8 ? 1 : 3;  // CTAs per SM the registers must allow
@@ -330,6 +387,11 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
     // an earlier launch gave up on a wait: do nothing until the host resets
     if (err_flag && *(volatile int *)err_flag) return;
     extern __shared__ __align__(128) unsigned char smem_raw[];
+    // tensor copies need 128-byte aligned destinations: refuse to run otherwise
+    if (smem_u32(smem_raw) & 127u) {
+        if (threadIdx.x == 0 && err_flag) atomicExch(err_flag, 2);
+        return;
+    }
     S *uw_s = reinterpret_cast<S *>(smem_raw);
     S *pw_s = uw_s + K::UW_ELEMS;
     S *tr_s = pw_s + K::PW_ELEMS;
@@ -420,14 +482,11 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
             const ItemInfo I = info[k];
             const int slot = e % K::NUW;
             const int r0 = I.z0 - 8 + 4 * b;
-            constexpr uint32_t ROWB = K::UWW * sizeof(S);
-            if (lane == 0) mbar_arrive_expect_tx(&full_uw[slot], ROWB * 4 * K::NV);
-            __syncwarp();
-            if (lane < 4 * K::NV) {
-                const int rr = lane & 3, v = lane >> 2;
-                const S *src = (v == 0 ? rd[0] : rd[K::NV - 1]) + origin + (long long)(r0 + rr) * pitch + (I.x0 - 8);
-                S *dst = uw_s + ((size_t)(slot * 4 + rr) * K::NV + v) * K::UWW;
-                bulk_g2s(dst, src, ROWB, &full_uw[slot]);
+            // one box: NV fields x rows r0 .. r0+3 x columns x0-8 .. x0+UWW-9
+            if (lane == 0) {
+                mbar_arrive_expect_tx(&full_uw[slot], (uint32_t)(K::NV * 4 * K::UWW * sizeof(S)));
+                tma_load_3d(uw_s + slot * K::UW_SLOT, &sh.maps->uw[par], kXPad + I.x0 - 8, kZPad + r0, 0,
+                            &full_uw[slot]);
             }
         };
         // point-wise operands of iteration i of item I into stage g % NPW
@@ -435,24 +494,19 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
         // (they do not depend on the previous step); 2: the old stresses only
         auto issue_pw = [=](int g, const ItemInfo &I, int i, int part) {
             const int slot = g % K::NPW;
-            constexpr uint32_t ROWB = K::PWW * sizeof(S);
-            if (lane == 0 && part != 2) mbar_arrive_expect_tx(&full_pw[slot], ROWB * 4 * K::NPF);
-            __syncwarp();
-            const int c0 = part == 1 ? 4 * K::NT : 0, c1 = part == 2 ? 4 * K::NT : 4 * K::NPF;
-            for (int c = c0 + lane; c < c1; c += 32) {
-                const int rr = c & 3, fidx = c >> 2;
-                const S *b = rd[K::NV];
-#pragma unroll
-                for (int f = 0; f < K::NPF; ++f) {
-                    const S *cand = f < K::NT ? rd[K::NV + f] : sh.mat[f - K::NT];
-                    if (f == fidx) b = cand;
-                }
+            if (lane == 0) {
+                S *st = pw_s + slot * K::PW_STAGE;
+                if (part != 2)
+                    mbar_arrive_expect_tx(&full_pw[slot], (uint32_t)(K::NPF * 4 * K::PWW * sizeof(S)));
                 // old stresses and stress-update material on stress rows,
                 // velocity-update material on velocity rows
-                const int row = (fidx < K::NT + K::NMS ? I.z0 - 4 : I.z0 - 8) + 4 * i + rr;
-                const S *src = b + origin + (long long)row * pitch + (I.x0 - 4 - K::PWOFF);
-                S *dst = pw_s + ((size_t)(slot * K::NPF + fidx) * 4 + rr) * K::PWW;
-                bulk_g2s(dst, src, ROWB, &full_pw[slot]);
+                const int xs = kXPad + I.x0 - 4 - K::PWOFF;
+                const int ys = kZPad + I.z0 - 4 + 4 * i, yv = kZPad + I.z0 - 8 + 4 * i;
+                if (part != 1) tma_load_3d(st, &sh.maps->t[par], xs, ys, K::NV, &full_pw[slot]);
+                if (part != 2) {
+                    tma_load_3d(st + K::PG_MS, &sh.maps->ms, xs, ys, 0, &full_pw[slot]);
+                    tma_load_3d(st + K::PG_MV, &sh.maps->mv, xs, yv, K::NMS, &full_pw[slot]);
+                }
             }
         };
         bool ok = true;
@@ -524,8 +578,8 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
             for (; ok && uw_ready <= uw_base + i + 2; ++uw_ready)
                 ok = mbar_wait_bounded(&full_uw[uw_ready % K::NUW], (uint32_t)((uw_ready / K::NUW) & 1), err_flag);
             if (ok) ok = mbar_wait_bounded(&full_pw[gflat % K::NPW], (uint32_t)((gflat / K::NPW) & 1), err_flag);
-            const S *pws = pw_s + (size_t)(gflat % K::NPW) * K::NPF * 4 * K::PWW;
-            auto pwrow = [=](int f) { return pws + ((size_t)f * 4 + grp) * K::PWW + K::PWOFF + 4 * lane; };
+            const S *pws = pw_s + (gflat % K::NPW) * K::PW_STAGE;
+            auto pwrow = [=](int f) { return pws + K::pw_field(f) + grp * K::PWW + K::PWOFF + 4 * lane; };
 
             // ================= stress: row j, cells x .. x+3 =================
             {
@@ -534,8 +588,10 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
                 const S *urow[9];
                 const int rseq = 4 * (uw_base + i) + grp;
 #pragma unroll
-                for (int d = 0; d < 9; ++d)
-                    urow[d] = uw_s + ((rseq + d) & (4 * K::NUW - 1)) * (K::NV * K::UWW) + 4 * lane + 4;
+                for (int d = 0; d < 9; ++d) {
+                    const int r = (rseq + d) & (4 * K::NUW - 1);
+                    urow[d] = uw_s + (r >> 2) * K::UW_SLOT + (r & 3) * K::UWW + 4 * lane + 4;
+                }
                 const bool inrow = j >= 0 && j < nz;
                 const bool zfast = j >= 4 && j <= nz - 5 && j < nz - npml && !(sh.topabsorb && j < npml);
                 C tnew[K::NT][4];
@@ -545,42 +601,36 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
 #pragma unroll
                 for (int m = 0; m < K::NMS; ++m) Vec4<S, C>::ld(pwrow(K::NT + m), ms[m]);
                 if (xfast && zfast) {
+                    // interior: packed operands (x differences stay per cell);
+                    // gam = fma(2, mu, lam) equals lam + 2*mu (2*mu is exact)
                     constexpr C c0 = Coef4<C>::c0, c1 = Coef4<C>::c1, c2 = Coef4<C>::c2, c3 = Coef4<C>::c3;
+                    using P = P4<C>;
                     if constexpr (PSV) {
                         C h[12];
                         C ux[4], wx[4];
                         ld12<S, C>(urow[4], h);
 #pragma unroll
                         for (int e = 0; e < 4; ++e) ux[e] = dmx<C>(h, e, c0, c1, c2, c3);
-                        ld12<S, C>(urow[4] + K::UWW, h);
+                        ld12<S, C>(urow[4] + K::UWF, h);
 #pragma unroll
                         for (int e = 0; e < 4; ++e) wx[e] = dpx<C>(h, e, c0, c1, c2, c3);
-#pragma unroll
-                        for (int e = 0; e < 4; ++e) {
-                            const C lam = ms[0][e], gam = lam + (C)2 * ms[1][e];
-                            tnew[0][e] = fmaC<C>(gam, ux[e], told[0][e]);
-                            tnew[2][e] = fmaC<C>(lam, ux[e], told[2][e]);
-                            tnew[1][e] = fmaC<C>(ms[2][e], wx[e], told[1][e]);
-                        }
-                        C uz[4], wz[4];
-                        dmz4<S, C>(urow, 0, uz);
-                        dpz4<S, C>(urow, K::UWW, wz);
-#pragma unroll
-                        for (int e = 0; e < 4; ++e) {
-                            const C lam = ms[0][e], gam = lam + (C)2 * ms[1][e];
-                            tnew[0][e] = fmaC<C>(lam, wz[e], tnew[0][e]);
-                            tnew[2][e] = fmaC<C>(gam, wz[e], tnew[2][e]);
-                            tnew[1][e] = fmaC<C>(ms[2][e], uz[e], tnew[1][e]);
-                        }
+                        const P lam = P::from(ms[0]), mua = P::from(ms[2]);
+                        const P gam = P::fmak(P::splat((C)2), P::from(ms[1]), lam);
+                        const P UX = P::from(ux), WX = P::from(wx);
+                        P t0 = P::fma(gam, UX, P::from(told[0]));
+                        P t2 = P::fma(lam, UX, P::from(told[2]));
+                        P t1 = P::fma(mua, WX, P::from(told[1]));
+                        const P UZ = dmz4p<S, C>(urow, 0), WZ = dpz4p<S, C>(urow, K::UWF);
+                        P::fma(lam, WZ, t0).to(tnew[0]);
+                        P::fma(gam, WZ, t2).to(tnew[2]);
+                        P::fma(mua, UZ, t1).to(tnew[1]);
                     } else {
-                        C h[12], dz[4];
+                        C h[12], dx[4];
                         ld12<S, C>(urow[4], h);
-                        dmz4<S, C>(urow, 0, dz);
 #pragma unroll
-                        for (int e = 0; e < 4; ++e) {
-                            tnew[0][e] = fmaC<C>(ms[0][e], dpx<C>(h, e, c0, c1, c2, c3), told[0][e]);
-                            tnew[1][e] = fmaC<C>(ms[1][e], dz[e], told[1][e]);
-                        }
+                        for (int e = 0; e < 4; ++e) dx[e] = dpx<C>(h, e, c0, c1, c2, c3);
+                        P::fma(P::from(ms[0]), P::from(dx), P::from(told[0])).to(tnew[0]);
+                        P::fma(P::from(ms[1]), dmz4p<S, C>(urow, 0), P::from(told[1])).to(tnew[1]);
                     }
                 } else {
                     // ---- general cells: edges (reduced order), CPML, free surface, outside ----
@@ -623,8 +673,8 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
                     }
                     if constexpr (PSV) {
                         C h[12], zv[9][4];
-                        ld12<S, C>(urow[4] + K::UWW, h);
-                        zcol<S, C>(urow, K::UWW, zv);
+                        ld12<S, C>(urow[4] + K::UWF, h);
+                        zcol<S, C>(urow, K::UWF, zv);
 #pragma unroll
                         for (int e = 0; e < 4; ++e) {
                             
@@ -824,10 +874,11 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
 #pragma unroll
                     for (int m = 0; m < K::NMV; ++m) Vec4<S, C>::ld(pwrow(K::NT + K::NMS + m), mv[m]);
                     const int rel = 4 * i + grp;  // a - (z0-8): block i, row grp
-                    const S *vrow = uw_s + ((4 * (uw_base + i) + (rel & 3)) & (4 * K::NUW - 1)) * (K::NV * K::UWW) + 4 * lane + 4;
+                    const int vr = (4 * (uw_base + i) + (rel & 3)) & (4 * K::NUW - 1);
+                    const S *vrow = uw_s + (vr >> 2) * K::UW_SLOT + (vr & 3) * K::UWW + 4 * lane + 4;
                     C vold[K::NV][4];
 #pragma unroll
-                    for (int v = 0; v < K::NV; ++v) Vec4<S, C>::ld(vrow + v * K::UWW, vold[v]);
+                    for (int v = 0; v < K::NV; ++v) Vec4<S, C>::ld(vrow + v * K::UWF, vold[v]);
                     const bool zfast = a >= 4 && a <= nz - 5 && a < nz - npml && !(sh.topabsorb && a < npml);
                     C vnew[K::NV][4];
                     // line force on V, injected before the velocity update (SH only);
@@ -849,34 +900,28 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
                     }
                     if (xfast && zfast) {
                         constexpr C c0 = Coef4<C>::c0, c1 = Coef4<C>::c1, c2 = Coef4<C>::c2, c3 = Coef4<C>::c3;
+                        using P = P4<C>;
                         if constexpr (PSV) {
                             C h[12], dx[4];
+                            const P bu = P::from(mv[0]), bw = P::from(mv[1]);
                             ld12<S, C>(trow[4], h);  // Txx
 #pragma unroll
                             for (int e = 0; e < 4; ++e) dx[e] = dpx<C>(h, e, c0, c1, c2, c3);
-#pragma unroll
-                            for (int e = 0; e < 4; ++e) vnew[0][e] = fmaC<C>(mv[0][e], dx[e], vold[0][e]);
+                            P u = P::fma(bu, P::from(dx), P::from(vold[0]));
                             ld12<S, C>(trow[4] + K::SW, h);  // Txz
 #pragma unroll
                             for (int e = 0; e < 4; ++e) dx[e] = dmx<C>(h, e, c0, c1, c2, c3);
-#pragma unroll
-                            for (int e = 0; e < 4; ++e) vnew[1][e] = fmaC<C>(mv[1][e], dx[e], vold[1][e]);
-                            C dz[4];
-                            dpz4<S, C>(trow, K::SW, dz);  // d/dz Txz
-#pragma unroll
-                            for (int e = 0; e < 4; ++e) vnew[0][e] = fmaC<C>(mv[0][e], dz[e], vnew[0][e]);
-                            dmz4<S, C>(trow, 2 * K::SW, dz);  // d/dz Tzz
-#pragma unroll
-                            for (int e = 0; e < 4; ++e) vnew[1][e] = fmaC<C>(mv[1][e], dz[e], vnew[1][e]);
+                            P w = P::fma(bw, P::from(dx), P::from(vold[1]));
+                            P::fma(bu, dpz4p<S, C>(trow, K::SW), u).to(vnew[0]);      // d/dz Txz
+                            P::fma(bw, dmz4p<S, C>(trow, 2 * K::SW), w).to(vnew[1]);  // d/dz Tzz
                         } else {
-                            C h[12], dz[4];
+                            C h[12], dx[4];
+                            const P bv = P::from(mv[0]);
                             ld12<S, C>(trow[4], h);  // Tx
-                            dpz4<S, C>(trow, K::SW, dz);  // d/dz Tz
 #pragma unroll
-                            for (int e = 0; e < 4; ++e) {
-                                const C t = fmaC<C>(mv[0][e], dmx<C>(h, e, c0, c1, c2, c3), vold[0][e]);
-                                vnew[0][e] = fmaC<C>(mv[0][e], dz[e], t);
-                            }
+                            for (int e = 0; e < 4; ++e) dx[e] = dmx<C>(h, e, c0, c1, c2, c3);
+                            const P t = P::fma(bv, P::from(dx), P::from(vold[0]));
+                            P::fma(bv, dpz4p<S, C>(trow, K::SW), t).to(vnew[0]);  // d/dz Tz
                         }
                     } else {
                         C psx[2][4], psz[2][4];
@@ -1064,6 +1109,31 @@ int prepare_one()
 }
 
 }  // namespace
+
+template <class S, class C, int WAVE>
+FusedBoxes boxes_of()
+{
+    using K = Cfg<S, C, WAVE>;
+    return FusedBoxes{K::UWW, K::PWW, K::NV, K::NT, K::NMS, K::NMV};
+}
+
+FusedBoxes fused_boxes(int wave, int prec)
+{
+    if (wave == FD23_PSV) {
+        switch (prec) {
+            case FD23_F64: return boxes_of<double, double, FD23_PSV>();
+            case FD23_BF16: return boxes_of<__nv_bfloat16, float, FD23_PSV>();
+            case FD23_F16: return boxes_of<__half, float, FD23_PSV>();
+            default: return boxes_of<float, float, FD23_PSV>();
+        }
+    }
+    switch (prec) {
+        case FD23_F64: return boxes_of<double, double, FD23_SH>();
+        case FD23_BF16: return boxes_of<__nv_bfloat16, float, FD23_SH>();
+        case FD23_F16: return boxes_of<__half, float, FD23_SH>();
+        default: return boxes_of<float, float, FD23_SH>();
+    }
+}
 
 FusedGeom fused_geom(int wave, int prec)
 {

@@ -81,6 +81,20 @@ FD23_HD inline int box_ring_index(int bi, int bj, int bx, int bz)
     return -1;
 }
 
+// TMA tensor maps of one shot (opaque 128-byte CUtensorMap objects built on
+// the host by cuTensorMapEncodeTiled).  Each is a 3-D view [field][row]
+// [column] of a contiguous block of padded arrays (the wavefields of one
+// buffer set, or the materials), one map per copy shape of the fused sweep.
+struct alignas(128) TmaDesc {
+    unsigned char bytes[128];
+};
+struct ShotMaps {
+    TmaDesc uw[2];  // stencil inputs of buffer set 0 / 1 (P-SV U W, SH V), box UWW x 4 x NV
+    TmaDesc t[2];   // old stresses of buffer set 0 / 1, box PWW x 4 x NT
+    TmaDesc ms;     // stress-update material, box PWW x 4 x NMS
+    TmaDesc mv;     // velocity-update material, box PWW x 4 x NMV
+};
+
 // Device view of the box of one shot: residual field r and box material,
 // bx*bz each, row-major; `inc` = the incident field of the current step.
 template <class C>
@@ -117,8 +131,9 @@ struct alignas(16) Shot {
     int nrec[5];
     const long long *rec[5];
     C *seis[5];
-    Box<C> box;         // hybrid box (box.on == 0: none)
+    const ShotMaps *maps;  // tensor maps of the fused sweep's copies (device memory)
     int cta0, ncta;     // CTAs of the launch working on this shot (receiver gather split)
+    Box<C> box;         // hybrid box (box.on == 0: none); last, the batched sweep never reads it
 };
 
 // Work list entry of the fused sweep: one x-strip of one shot, rows [z0, z1)

@@ -22,6 +22,12 @@ struct FusedGeom {
     int rows_per_iter;
 };
 FusedGeom fused_geom(int wave, int prec);
+// copy shapes of the fused sweep (for the tensor maps): stencil-input row
+// width, point-wise row width, fields per copy
+struct FusedBoxes {
+    int uww, pww, nv, nt, nms, nmv;
+};
+FusedBoxes fused_boxes(int wave, int prec);
 int fused_prepare(int wave, int prec);       // once per device before the first launch
 size_t fused_smem_bytes(int wave, int prec); // dynamic shared memory of one CTA
 

@@ -24,8 +24,11 @@ struct fd23_solver {
     fd23::Layout L;
     cudaStream_t stream = nullptr;
     int fused = 1;
-    void *fld[2][5] = {};
-    void *mat[5] = {};
+    void *fld[2][5] = {};   // wavefields; those of one buffer set are one allocation
+    void *mat[5] = {};      // material arrays, one allocation
+    void *fld_block[2] = {};
+    void *mat_block = nullptr;
+    fd23::ShotMaps *d_maps = nullptr;  // tensor maps of the fused sweep
     void *psi[2][8] = {};
     size_t psi_elems[8] = {};
     void *cpml = nullptr;
@@ -116,6 +119,7 @@ Shot<S, C> make_shot(const fd23_solver *s)
         sh.rec[c] = s->d_rec[c];
         sh.seis[c] = (C *)s->d_seis[c];
     }
+    sh.maps = s->d_maps;
     sh.cta0 = 0;
     sh.ncta = s->nblocks > 0 ? s->nblocks : 1;
     sh.box.on = s->box_on ? 1 : 0;

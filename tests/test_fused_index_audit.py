@@ -5,8 +5,11 @@ solver and the batch use), restates the padded layout (make_layout) and the
 index arithmetic of the kernel, then checks, for the grid sizes the tests and
 the benchmarks use (and the 64-shot batch), that
 
-  * every bulk copy reads inside its HBM buffer, starts on a 16-byte boundary
-    in global and shared memory, and moves a multiple of 16 bytes;
+  * every tensor copy (a box [fields][4 rows][width] of a 3-D view
+    [field][row][column] of a padded block) lies inside the tensor's
+    extents, starts at an x coordinate whose byte offset is a multiple of 16,
+    moves rows of a multiple of 16 bytes, and lands on a 128-byte aligned
+    shared-memory address;
   * every shared-memory read and write stays inside its ring;
   * every HBM store lands on a cell of the grid;
   * no CTA holds more work items than its item table.
@@ -40,10 +43,41 @@ def worklist(nx, nz, npml, oversub=1.0, per_sm=3):
     return [[it[1:] for it in cta] for cta in F.work_plan([(nx, nz, npml, 0)], per_sm=per_sm, oversub=oversub)]
 
 
+def al128(b):
+    return (b + 127) // 128 * 128
+
+
+def smem_layout(es, wave):
+    """Byte offsets of the ring slots / stage groups (Cfg in fd23_fused.cu)."""
+    nv, nt = (2, 3) if wave == "psv" else (1, 2)
+    nms, nmv = (3, 2) if wave == "psv" else (2, 1)
+    pwoff = 4 if es == 2 else 0
+    pww = SW + 2 * pwoff
+    uw_slot = al128(nv * 4 * UWW * es)
+    pg_ms = al128(nt * 4 * pww * es)
+    pg_mv = pg_ms + al128(nms * 4 * pww * es)
+    stage = pg_mv + al128(nmv * 4 * pww * es)
+    return dict(nv=nv, nt=nt, nms=nms, nmv=nmv, pwoff=pwoff, pww=pww, uw_slot=uw_slot, pg_ms=pg_ms,
+                pg_mv=pg_mv, stage=stage, pw_base=NUW * uw_slot)
+
+
+def box_ok(x, y, z, w, nf, pitch, rows, nfields, es):
+    assert x >= 0 and x + w <= pitch, (x, w, pitch)
+    assert y >= 0 and y + 4 <= rows, (y, rows)
+    assert z >= 0 and z + nf <= nfields
+    assert (x * es) % 16 == 0 and (w * es) % 16 == 0
+    assert w <= 256 and nf <= 256
+
+
 def audit(nx, nz, es, wave, per_sm=3, oversub=1.0, ctas=None):
     pitch, rows, origin = layout(nx, nz)
     npml = min(40, nx // 2, nz // 2)
     elems = pitch * rows
+    lay = smem_layout(es, wave)
+    nfld = 5 if wave == "psv" else 3
+    for off in [k * lay["uw_slot"] for k in range(NUW)] + \
+               [lay["pw_base"] + g * lay["stage"] + o for g in range(NPW) for o in (0, lay["pg_ms"], lay["pg_mv"])]:
+        assert off % 128 == 0
     nv = 2 if wave == "psv" else 1
     nt = 3 if wave == "psv" else 2
     npf = 8 if wave == "psv" else 5
@@ -65,18 +99,15 @@ def audit(nx, nz, es, wave, per_sm=3, oversub=1.0, ctas=None):
             niter = (z1 - z0) // 4 + 2
             # stencil-input copies: blocks 0 .. niter+1, rows z0-8+4b .. +3
             for b in (0, niter + 1):
-                for rr in (0, 3):
-                    r = z0 - 8 + 4 * b + rr
-                    off = origin + r * pitch + (x0 - 8)
-                    assert 0 <= off and off + UWW <= elems, (nx, nz, x0, r)
-                    assert (off * es) % 16 == 0 and (UWW * es) % 16 == 0
-            # point-wise copies of iterations 0 .. niter-1
+                box_ok(XPAD + x0 - 8, ZPAD + z0 - 8 + 4 * b, 0, UWW, lay["nv"], pitch, rows, nfld, es)
+            # point-wise copies of iterations 0 .. niter-1: old stresses and
+            # stress-update material on stress rows, velocity-update material
+            # on velocity rows
             for i in (0, niter - 1):
-                for rr in (0, 3):
-                    for r in (z0 - 4 + 4 * i + rr, z0 - 8 + 4 * i + rr):
-                        off = origin + r * pitch + (x0 - 4 - pwoff)
-                        assert 0 <= off and off + pww <= elems
-                        assert (off * es) % 16 == 0 and (pww * es) % 16 == 0
+                xs = XPAD + x0 - 4 - lay["pwoff"]
+                box_ok(xs, ZPAD + z0 - 4 + 4 * i, lay["nv"], lay["pww"], lay["nt"], pitch, rows, nfld, es)
+                box_ok(xs, ZPAD + z0 - 4 + 4 * i, 0, lay["pww"], lay["nms"], pitch, rows, nfld, es)
+                box_ok(xs, ZPAD + z0 - 8 + 4 * i, lay["nms"], lay["pww"], lay["nmv"], pitch, rows, nfld, es)
             for i in range(niter):
                 for g in (0, 3):
                     for q in (0, 31):
