@@ -242,6 +242,8 @@ def main():
     ap.add_argument("--kernel", default="fused")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--config", default="c1", choices=["c1", "c2", "c4"])
     args = ap.parse_args()
 
@@ -281,6 +283,9 @@ def main():
     s.set_receivers(0, rxu, rzu)
     s.set_receivers(1, rxw, rzw)
     stream = torch.cuda.ExternalStream(s.stream, device=local)
+    # work plan picked by the autotuner on this shot (set-up, not timed)
+    tune = s.autotune(10) if args.kernel == "fused" and not args.no_tune else []
+    best_plan = min(tune, key=lambda r: r["ms_per_step"]) if tune else None
 
     def shot():
         s.reset()
@@ -310,6 +315,24 @@ def main():
     ms_max = float(t[0])
     cells = NX * NZ * nt * args.steps * world
     value = cells / (ms_max * 1e-3)
+    seis = (s.seismograms(0), s.seismograms(1))
+
+    # seismogram error against an FP64 run of the same shot (GPU FP64 sweep,
+    # bit-identical to the FP64 oracle)
+    accuracy = None
+    if rank == 0 and args.prec != "f64" and not args.no_accuracy:
+        r = F.Solver("psv", NX, NZ, NPML, H, DT, prec="f64", pml_dt=DT, pml_v=pml_v, pml_r=1e-11, pml_fc=F0,
+                     device=local, kernel="fused")
+        r.set_model(vp, vs, rho)
+        r.set_source(F.SRC_EXPLOSION, NX // 2, 20, None, src, nt)
+        r.set_receivers(0, rxu, rzu)
+        r.set_receivers(1, rxw, rzw)
+        r.run(nt, 1)
+        ref = np.concatenate([r.seismograms(0).ravel(), r.seismograms(1).ravel()])
+        got = np.concatenate([seis[0].ravel(), seis[1].ravel()]).astype(np.float64)
+        accuracy = {"seismogram_rel_l2_vs_fp64": float(np.linalg.norm(got - ref) / np.linalg.norm(ref)),
+                    "traces": int(seis[0].shape[1] + seis[1].shape[1]), "steps": nt}
+        r.close()
 
     # end to end through the public API with host buffers
     e2e = None
@@ -359,6 +382,11 @@ def main():
             "gpu_launches": args.steps * (nt + 1),
             "clocks": clocks,
             "e2e": e2e}
+    if best_plan:
+        line["config"]["plan"] = {"wx": best_plan["wx"], "wz": best_plan["wz"], "oversub": best_plan["oversub"],
+                                  "autotune_trials": len(tune)}
+    if accuracy:
+        line["accuracy"] = accuracy
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline()
     if rank == 0:
