@@ -22,6 +22,13 @@ Hybrid-box workload (--config c2): the same model and grid, 3000 steps,
   run has no point source.  Its surface seismograms must equal the recorded
   run's bit for bit ("check" in the output line).
 
+SH workload (--config c0): 800 x 400 SH grid, h=10 m, dt=1e-3 s, 2000 steps,
+  two layers (vs 2000 / 3000 m/s, rho 2200 / 2500, interface at iz=200),
+  10 Hz Ricker line force on V at (400, 20), 20-cell CPML, free surface, 200
+  surface receivers.  The 10 MB working set stays in L2 within a shot, so the
+  step is launch- and latency-bound; the run is captured in a CUDA graph (a
+  one-shot batch) and L2 is flushed between timed shots.
+
 Batched workload (--config c4): 64 shots with seeded grid sizes nx in
   [1000, 4000], nz in [500, 2000] (not tile multiples), h=5 m, dt=4e-4 s,
   3000 steps, per-shot seeded layered models, Ricker 8-25 Hz explosions,
@@ -244,7 +251,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
-    ap.add_argument("--config", default="c1", choices=["c1", "c2", "c4"])
+    ap.add_argument("--config", default="c1", choices=["c0", "c1", "c2", "c4"])
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -269,6 +276,9 @@ def main():
         return
     if args.config == "c4":
         bench_batch(args, F, torch, rank, world, local, dist)
+        return
+    if args.config == "c0":
+        bench_sh(args, F, torch, rank, world, local, dist)
         return
     nt = args.nt
     vp, vs, rho = c1_model(seed=1 + rank)
@@ -547,6 +557,114 @@ def bench_box(args, F, torch, rank, world, local, dist):
         line["cpu_baseline"] = cpu_baseline_box(inc)
     if rank == 0:
         print(json.dumps(line), flush=True)
+    s.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+SH_NX, SH_NZ, SH_H, SH_DT, SH_NT, SH_NPML, SH_F0, SH_NSTA = 800, 400, 10.0, 1e-3, 2000, 20, 10.0, 200
+
+
+def sh_model():
+    vs = np.full((SH_NZ, SH_NX), 2000.0)
+    rho = np.full((SH_NZ, SH_NX), 2200.0)
+    vs[200:] = 3000.0
+    rho[200:] = 2500.0
+    return vs, rho
+
+
+def bench_sh(args, F, torch, rank, world, local, dist):
+    nt = min(args.nt, SH_NT)
+    vs, rho = sh_model()
+    s = F.Solver("sh", SH_NX, SH_NZ, SH_NPML, SH_H, SH_DT, prec=args.prec, pml_dt=SH_DT,
+                 pml_v=float(vs.max()) / SH_H, pml_r=1e-11, pml_fc=SH_F0, device=local, kernel="fused")
+    s.set_model(None, vs, rho)
+    src = F.wavelet_ricker(SH_DT, SH_F0)
+    s.set_source(F.SRC_FORCE, SH_NX // 2, 20, np.array([1.0, 0.0]), src, nt)
+    rx, rz = F.receivers_line(SH_NSTA // 2, 2, 0, 4, 0)
+    s.set_receivers(0, rx, rz)
+    b = F.Batch([s])
+    stream = torch.cuda.ExternalStream(b.stream, device=local)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda:%d" % local)
+
+    def shot():
+        s.reset()
+        b.run(nt, 1)
+
+    for _ in range(args.warmup):
+        shot()
+    b.sync()
+    sampler = ClockSampler(local)
+    if rank == 0:
+        sampler.start()
+    if dist:
+        dist.barrier()
+    ms = 0.0
+    for _ in range(args.steps):
+        flush.zero_()  # L2 flush between timed shots (not timed)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        shot()
+        e1.record(stream)
+        b.sync()
+        ms += e0.elapsed_time(e1)
+    clocks = sampler.stop() if rank == 0 else None
+    t = torch.tensor([ms], dtype=torch.float64)
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t[0])
+    cells = SH_NX * SH_NZ
+    value = cells * nt * args.steps * world / (ms_max * 1e-3)
+    e2e = None
+    if not args.no_e2e:
+        times = []
+        for _ in range(max(1, min(args.steps, 2))):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            s.set_model(None, vs, rho)
+            shot()
+            out = s.seismograms(0)
+            times.append(time.perf_counter() - t0)
+        es = {"f32": 4, "f64": 8, "bf16": 2, "f16": 2}[args.prec]
+        e2e = {"value": cells * nt / statistics.mean(times) * world, "unit": "cell-updates/s",
+               "h2d_bytes_per_step": 3 * cells * es, "d2h_bytes_per_step": int(out.nbytes)}
+    hbm, peak_kind = load_peaks()
+    es = {"f32": 4, "f64": 8, "bf16": 2, "f16": 2}[args.prec]
+    per_launch_ms = ms_max / (args.steps * nt)
+    ab = (3 * 2 + 3) * es * cells + 2 * 2 * (8 if es == 8 else 4) * (2 * SH_NPML * SH_NZ + SH_NPML * SH_NX)
+    achieved = ab / (per_launch_ms * 1e-3) / 1e9
+    line = {"metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.prec,
+            "data": "synthetic",
+            "config": {"workload": "sh_800x400_2000steps_c0", "nx": SH_NX, "nz": SH_NZ, "nt": nt,
+                       "source": "10 Hz Ricker line force", "traces": SH_NSTA, "graph": "one-shot batch",
+                       "l2": "working set (about 10 MB) L2-resident within a shot; L2 flushed between "
+                             "timed shots", "parallelism": "replicas x%d" % world},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "traffic": None, "peak_source": peak_kind,
+                         "note": "L2-resident working set: the HBM fraction is not meaningful here",
+                         "alg_bytes_per_launch": ab, "launch_ms": per_launch_ms},
+            "gpu_launches": args.steps * (nt + 1), "clocks": clocks, "e2e": e2e}
+    if rank == 0 and not args.no_cpu:
+        from oracle import fd23_oracle as O
+        mat, _, _ = O.sh_material(vs, rho, SH_H, SH_DT)
+        bck = O.cpml_sh(SH_NX, SH_NZ, SH_NPML, SH_DT, 1e-11, float(vs.max()) / SH_H, SH_F0)
+        terms = O.source_terms("sh", 2, SH_NX, SH_NX // 2, 20, np.array([1.0, 0.0]), SH_H, SH_DT,
+                               O.ricker(SH_DT, SH_F0), nt)
+        rec = np.asarray(rx) + np.asarray(rz) * SH_NX
+        O.sh_run("f32", SH_NX, SH_NZ, SH_NPML, 0, mat, bck, terms, rec, 10)
+        t0 = time.perf_counter()
+        O.sh_run("f32", SH_NX, SH_NZ, SH_NPML, 0, mat, bck, terms, rec, 400)
+        tt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": cells * 400 / tt, "unit": "cell-updates/s", "cores": os.cpu_count() or 1,
+                                "kind": "port",
+                                "sample": "400 steps of the SH grid (%.1f s), FP32 oracle, all threads" % tt}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    b.close()
     s.close()
     if dist:
         dist.barrier()
