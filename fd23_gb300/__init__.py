@@ -54,7 +54,7 @@ ABI_FUNCTIONS = [
     "fd23_box_ring_index", "fd23_box_ring_cells", "fd23_box_incident_from_displacement",
     "fd23_box_material", "fd23_batch_create", "fd23_batch_destroy", "fd23_batch_run", "fd23_batch_sync",
     "fd23_batch_get_stream", "fd23_batch_set_graph", "fd23_autotune", "fd23_batch_autotune",
-    "fd23_batch_get_plan", "fd23_work_plan",
+    "fd23_batch_get_plan", "fd23_work_plan", "fd23_read_model", "fd23_read_stations",
 ]
 
 
@@ -145,6 +145,8 @@ def lib():
         "fd23_batch_autotune": ([vp, i, vp, i], i),
         "fd23_batch_get_plan": ([vp, vp, _C.POINTER(i)], i),
         "fd23_work_plan": ([i, vp, vp, vp, vp, i, vp, vp, i, vp, i], i),
+        "fd23_read_model": ([_C.c_char_p, i, i, d, vp, vp, vp], i),
+        "fd23_read_stations": ([_C.c_char_p, vp, vp, i], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -387,6 +389,14 @@ def receivers_file(path):
         rx += [x, x - 1]
         rz += [z, z]
     return _np.array(rx, dtype=_np.int32), _np.array(rz, dtype=_np.int32)
+
+
+def read_model(name, nx, nz, h):
+    """vp, vs, den (nz, nx) FP64 from a .mdl polygon model or raster files
+    <name>.vp/.vs/.den (fd23_read_model)."""
+    out = [_np.empty((nz, nx)) for _ in range(3)]
+    _check(lib().fd23_read_model(name.encode(), nx, nz, h, *[_p(o) for o in out]), "fd23_read_model")
+    return out
 
 
 def read_raster_model(prefix, nx, nz, wave="psv"):

@@ -54,12 +54,31 @@ def _compile(src, verbose=False):
     return obj, r.stderr
 
 
+CLI_SRC = os.path.join(HERE, "cli", "fd23_psv2d.cpp")
+CLI = os.path.join(LIBDIR, "fd23_psv2d")
+
+
+def build_cli(force=False):
+    """The parfile program fd23_psv2d next to the library (linked to it,
+    found through the executable's own directory)."""
+    newest = max(os.path.getmtime(p) for p in [CLI_SRC, LIB] + headers())
+    if not force and os.path.exists(CLI) and os.path.getmtime(CLI) >= newest:
+        return CLI
+    cmd = [_nvcc(), "-x", "c++", "-std=c++17", "-O2", CLI_SRC, "-o", CLI, "-L" + LIBDIR, "-lfd23",
+           "-Xlinker", "-rpath=$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("cli build failed: %s\n%s\n%s" % (" ".join(cmd), r.stdout, r.stderr))
+    return CLI
+
+
 def build(force=False, verbose=False):
     os.makedirs(LIBDIR, exist_ok=True)
     os.makedirs(OBJDIR, exist_ok=True)
     srcs = sources()
     newest = max(os.path.getmtime(p) for p in srcs + headers() + [__file__])
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
+        build_cli(force)
         return LIB
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         results = list(ex.map(lambda s: _compile(s, verbose), srcs))
@@ -72,6 +91,7 @@ def build(force=False, verbose=False):
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed: %s\n%s" % (r.stdout, r.stderr))
+    build_cli(True)
     return LIB
 
 

@@ -1,0 +1,338 @@
+// fd23_psv2d: the reference's P-SV program (PN nbpsv2d and its topabsorb /
+// explosion builds, PD psv2d_db without the box) on the fd23 engine.
+//
+//   fd23_psv2d par=run.par [key=value ...]
+//
+// Parameters follow the reference's parameter reader (PN/param/param.cpp:88-200,
+// getpar conventions): key=value words on the command line, "par=file" reads
+// key=value words from a file at that point (# starts a comment), and the
+// last value given for a key wins.  Required: nx nz nt h dt srctime (with
+// alpha for Gaussian, trap1 trap2 trap3 for Trapezoid) strike dip rake
+// azimuth xs zs npml pml_dt pml_v pml_r pml_fc output model, and either
+// U_sta_file / W_sta_file or nrec ixrec0 izrec0_u izrec0_w idxrec idzrec.
+// Optional: srctype (1 moment, p 'p' dipole; default 1), itrecord (1),
+// restart + nt0, savestate.  Accepted and ignored (no effect on this path):
+// ntsnap itprint gpuid ngpu ord bw usetable src_shift_x src_shift_z
+// sourcetime stype.  Not supported here: usepunch=1, usebox=1 (the box is
+// in the C ABI).  Additions: prec (f32, f64, bf16, f16; default f32),
+// explosion (1: Mxx = Mzz = 1, the *_exp builds), topabsorb (1: CPML on top,
+// the *_topabsorb builds), device (CUDA ordinal, default 0), dryrun (1: print
+// the resolved set-up and stop before touching the GPU).
+//
+// Outputs as the reference writes them (PN/main.cpp:216-230, 253-326,
+// PN/record/isis.cpp): <output>_U and <output>_W, raw [recorded step][trace]
+// in the compute type (float, double for f64); <output>_U.isis and
+// <output>_W.isis, one 84-byte trace header and the float trace per
+// receiver (U positions shifted +0.5 cell in x, W -0.5 cell in z); with
+// savestate=1 the state file state%06d (step nt0+nt-1); with restart=1 the
+// run starts from state%06d (step nt0-1).  Header words the reference leaves
+// unset are written as zero.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/fd23.h"
+
+namespace {
+
+struct Params {
+    std::map<std::string, std::string> kv;
+    std::vector<std::string> missing;
+
+    bool has(const std::string &k) const { return kv.count(k) != 0; }
+    std::string str(const std::string &k, const std::string &d = "")
+    {
+        auto it = kv.find(k);
+        if (it != kv.end()) return it->second;
+        return d;
+    }
+    std::string need(const std::string &k)
+    {
+        if (!has(k)) {
+            missing.push_back(k);
+            return "0";
+        }
+        return kv[k];
+    }
+    double num(const std::string &k, double d) { return has(k) ? std::atof(kv[k].c_str()) : d; }
+    double need_num(const std::string &k) { return std::atof(need(k).c_str()); }
+};
+
+bool add_word(Params &p, const std::string &w)
+{
+    const size_t e = w.find('=');
+    if (e == std::string::npos || e == 0) return false;
+    p.kv[w.substr(0, e)] = w.substr(e + 1);
+    return true;
+}
+
+bool load_parfile(Params &p, const std::string &path)
+{
+    std::ifstream f(path);
+    if (!f) return false;
+    for (std::string line; std::getline(f, line);) {
+        const size_t c = line.find('#');
+        if (c != std::string::npos) line.resize(c);
+        std::istringstream is(line);
+        for (std::string w; is >> w;)
+            if (!add_word(p, w)) return false;
+    }
+    return true;
+}
+
+// 84-byte trace header of the .isis trace files (PN/record/isis.h)
+struct IsisTrace {
+    float xs, ys, zs;
+    float xr, yr, zr;
+    float t0;
+    int nt;
+    float samplerate;
+    int srcflagnum, recflagnum, status;
+    float gain, dtstatic, ampstatic;
+    unsigned short recorder, chan, scomp, rcomp;
+    int user[4];
+};
+static_assert(sizeof(IsisTrace) == 84, "isis trace header is 84 bytes");
+
+int fail(const char *what, int rc)
+{
+    std::fprintf(stderr, "fd23_psv2d: %s: %s\n", what, fd23_strerror(rc));
+    return 1;
+}
+
+bool write_file(const std::string &name, const void *p, size_t bytes)
+{
+    std::ofstream f(name, std::ios::binary);
+    return f && f.write((const char *)p, (std::streamsize)bytes);
+}
+
+}  // namespace
+
+int main(int argc, char **argv)
+{
+    Params p;
+    for (int i = 1; i < argc; ++i) {
+        const std::string a(argv[i]);
+        if (a.rfind("par=", 0) == 0) {
+            if (!load_parfile(p, a.substr(4))) {
+                std::fprintf(stderr, "fd23_psv2d: cannot read parameter file %s\n", a.substr(4).c_str());
+                return 1;
+            }
+        } else if (!add_word(p, a)) {
+            std::fprintf(stderr, "fd23_psv2d: expected key=value, got '%s'\n", a.c_str());
+            return 1;
+        }
+    }
+    if (argc < 2) {
+        std::fprintf(stderr, "usage: fd23_psv2d par=file [key=value ...]\n");
+        return 1;
+    }
+    const int restart = (int)p.num("restart", 0), savestate = (int)p.num("savestate", 0);
+    const int nt0 = restart ? (int)p.need_num("nt0") : 0;
+    const int nx = (int)p.need_num("nx"), nz = (int)p.need_num("nz"), nt = (int)p.need_num("nt");
+    const float h = (float)p.need_num("h"), dt = (float)p.need_num("dt");
+    const std::string srctype = p.str("srctype", "1");
+    const std::string srctime = p.need("srctime");
+    double alpha = 0, trap[3] = {0, 0, 0};
+    if (!srctime.empty() && (srctime[0] == 'T' || srctime[0] == 't'))
+        for (int k = 0; k < 3; ++k) trap[k] = p.need_num("trap" + std::to_string(k + 1));
+    if (!srctime.empty() && (srctime[0] == 'G' || srctime[0] == 'g')) alpha = p.need_num("alpha");
+    const double strike = p.need_num("strike"), dip = p.need_num("dip"), rake = p.need_num("rake"),
+                 azimuth = p.need_num("azimuth");
+    const int xs = (int)p.need_num("xs"), zs = (int)p.need_num("zs");
+    const int npml = (int)p.need_num("npml");
+    const double pml_dt = p.need_num("pml_dt"), pml_v = p.need_num("pml_v"), pml_r = p.need_num("pml_r"),
+                 pml_fc = p.need_num("pml_fc");
+    const int itrecord = (int)p.num("itrecord", 1);
+    const std::string output = p.need("output");
+    const std::string ufile = p.str("U_sta_file"), wfile = p.str("W_sta_file");
+    int nrec = 0, ixrec0 = 0, izu = 0, izw = 0, idx = 0, idz = 0;
+    if (ufile.empty() && wfile.empty()) {
+        nrec = (int)p.need_num("nrec");
+        ixrec0 = (int)p.need_num("ixrec0");
+        izu = (int)p.need_num("izrec0_u");
+        izw = (int)p.need_num("izrec0_w");
+        idx = (int)p.need_num("idxrec");
+        idz = (int)p.need_num("idzrec");
+    }
+    const std::string model = p.need("model");
+    const std::string precs = p.str("prec", "f32");
+    const int explosion = (int)p.num("explosion", 0), topabsorb = (int)p.num("topabsorb", 0);
+    const int device = (int)p.num("device", 0);
+    if (!p.missing.empty()) {
+        std::fprintf(stderr, "fd23_psv2d: missing parameter(s):");
+        for (auto &m : p.missing) std::fprintf(stderr, " %s", m.c_str());
+        std::fprintf(stderr, "\n");
+        return 1;
+    }
+    if (p.num("usepunch", 0) != 0 || p.num("usebox", 0) != 0) {
+        std::fprintf(stderr, "fd23_psv2d: usepunch and usebox are not supported by this program\n");
+        return 1;
+    }
+    int prec = FD23_F32;
+    if (precs == "f64") prec = FD23_F64;
+    else if (precs == "bf16") prec = FD23_BF16;
+    else if (precs == "f16") prec = FD23_F16;
+    else if (precs != "f32") {
+        std::fprintf(stderr, "fd23_psv2d: prec must be f32, f64, bf16 or f16\n");
+        return 1;
+    }
+    if (srctype != "1" && srctype != "p" && srctype != "P") {
+        std::fprintf(stderr, "fd23_psv2d: Wrong srctype! Specify 1 or p.\n");
+        return 1;
+    }
+    if (srctime.empty() || !std::strchr("GgTt", srctime[0])) {
+        std::fprintf(stderr, "fd23_psv2d: srctime must be Gaussian or Trapezoid\n");
+        return 1;
+    }
+    // source time function: s(t)*dt samples
+    std::vector<double> src(1 << 20);
+    const int lsrc = (srctime[0] == 'G' || srctime[0] == 'g')
+                         ? fd23_wavelet_gaussian(dt, (int)alpha, src.data(), (int)src.size())
+                         : fd23_wavelet_trapezoid(dt, trap[0], trap[1], trap[2], src.data(), (int)src.size());
+    if (lsrc <= 0) return fail("source time function", lsrc < 0 ? lsrc : FD23_ERR_ARG);
+    // receivers
+    std::vector<int> rxu, rzu, rxw, rzw;
+    auto stations = [](const std::string &f, std::vector<int> &rx, std::vector<int> &rz) -> int {
+        const int n = fd23_read_stations(f.c_str(), nullptr, nullptr, 0);
+        if (n < 0) return n;
+        rx.resize(n);
+        rz.resize(n);
+        return fd23_read_stations(f.c_str(), rx.data(), rz.data(), n);
+    };
+    if (!ufile.empty() || !wfile.empty()) {
+        int rc = stations(ufile.empty() ? wfile : ufile, rxu, rzu);
+        if (rc < 0) return fail(("station file " + ufile).c_str(), rc);
+        if ((rc = stations(wfile.empty() ? ufile : wfile, rxw, rzw)) < 0)
+            return fail(("station file " + wfile).c_str(), rc);
+    } else {
+        rxu.resize(2 * nrec);
+        rzu.resize(2 * nrec);
+        rxw.resize(2 * nrec);
+        rzw.resize(2 * nrec);
+        fd23_receivers_line(nrec, ixrec0, izu, idx, idz, rxu.data(), rzu.data());
+        fd23_receivers_line(nrec, ixrec0, izw, idx, idz, rxw.data(), rzw.data());
+    }
+    if (p.num("dryrun", 0) != 0) {
+        std::printf("{\"nx\": %d, \"nz\": %d, \"nt\": %d, \"nt0\": %d, \"h\": %.9g, \"dt\": %.9g, \"npml\": %d, "
+                    "\"topabsorb\": %d, \"prec\": \"%s\", \"source\": \"%s\", \"xs\": %d, \"zs\": %d, "
+                    "\"lsrc\": %d, \"itrecord\": %d, \"traces_u\": %zu, \"traces_w\": %zu, \"model\": \"%s\", "
+                    "\"output\": \"%s\", \"savestate\": %d}\n",
+                    nx, nz, nt, nt0, h, dt, npml, topabsorb, precs.c_str(),
+                    explosion ? "explosion" : (srctype == "1" ? "moment" : "moment_p"), xs, zs, lsrc, itrecord,
+                    rxu.size(), rxw.size(), model.c_str(), output.c_str(), savestate);
+        return 0;
+    }
+    // model
+    const size_t n = (size_t)nx * nz;
+    std::vector<double> vp(n), vs(n), den(n);
+    int rc = fd23_read_model(model.c_str(), nx, nz, h, vp.data(), vs.data(), den.data());
+    if (rc) return fail(("model " + model).c_str(), rc);
+    fd23_desc d{};
+    d.wave = FD23_PSV;
+    d.prec = prec;
+    d.nx = nx;
+    d.nz = nz;
+    d.npml = npml;
+    d.topabsorb = topabsorb;
+    d.h = h;
+    d.dt = dt;
+    d.pml_dt = pml_dt;
+    d.pml_v = pml_v;
+    d.pml_r = pml_r;
+    d.pml_fc = pml_fc;
+    d.device = device;
+    d.kernel = FD23_KERNEL_AUTO;
+    fd23_solver *s = nullptr;
+    if ((rc = fd23_create(&d, &s))) return fail("create", rc);
+    double stab = 0;
+    rc = fd23_set_model(s, vp.data(), vs.data(), den.data(), &stab);
+    std::printf("stab = %g\n", stab);
+    if (rc) return fail("model", rc);
+    double m[3];
+    fd23_moment_psv(strike, dip, rake, azimuth, m);
+    const int kind = explosion ? FD23_SRC_EXPLOSION : (srctype == "1" ? FD23_SRC_MOMENT : FD23_SRC_MOMENT_P);
+    if ((rc = fd23_set_source(s, kind, xs, zs, m, src.data(), lsrc, nt0 + nt))) return fail("source", rc);
+    if ((rc = fd23_set_receivers(s, FD23_U, rxu.data(), rzu.data(), (int)rxu.size()))) return fail("U receivers", rc);
+    if ((rc = fd23_set_receivers(s, FD23_W, rxw.data(), rzw.data(), (int)rxw.size()))) return fail("W receivers", rc);
+    const size_t sbytes = fd23_state_bytes(s);
+    char statefile[64];
+    if (restart) {
+        std::snprintf(statefile, sizeof statefile, "state%06d", nt0 - 1);
+        std::vector<char> buf(sbytes);
+        std::ifstream f(statefile, std::ios::binary);
+        if (!f || !f.read(buf.data(), (std::streamsize)sbytes)) {
+            std::fprintf(stderr, "fd23_psv2d: cannot read %s\n", statefile);
+            return 1;
+        }
+        if ((rc = fd23_set_state(s, buf.data(), sbytes, nt0))) return fail("restart state", rc);
+    }
+    if ((rc = fd23_run(s, nt, itrecord)) || (rc = fd23_sync(s))) return fail("run", rc);
+    // seismograms
+    const size_t cs = prec == FD23_F64 ? 8 : 4;
+    const std::vector<int> *rx[2] = {&rxu, &rxw}, *rz[2] = {&rzu, &rzw};
+    const char *suffix[2] = {"_U", "_W"};
+    const float shiftx[2] = {0.5f, 0.0f}, shiftz[2] = {0.0f, -0.5f};
+    for (int c = 0; c < 2; ++c) {
+        const size_t ntr = rx[c]->size();
+        int nrs = 0;
+        if ((rc = fd23_get_seismograms(s, c, nullptr, 0, &nrs))) return fail("seismograms", rc);
+        std::vector<unsigned char> raw((size_t)nrs * ntr * cs);
+        if ((rc = fd23_get_seismograms(s, c, raw.data(), raw.size(), &nrs))) return fail("seismograms", rc);
+        const std::string name = output + suffix[c];
+        if (!write_file(name, raw.data(), raw.size())) {
+            std::fprintf(stderr, "fd23_psv2d: cannot write %s\n", name.c_str());
+            return 1;
+        }
+        // .isis: one header + trace per receiver, float samples
+        const int ntrec = std::min(nrs, nt / itrecord);
+        std::ofstream f(name + ".isis", std::ios::binary);
+        std::vector<float> tr((size_t)ntrec);
+        for (size_t r = 0; r < ntr; ++r) {
+            IsisTrace t;
+            std::memset(&t, 0, sizeof t);
+            const int ixr = (*rx[c])[r], izr = (*rz[c])[r];
+            t.xr = ((float)ixr + shiftx[c]) * h;
+            t.zr = ((float)izr + shiftz[c]) * h;
+            t.xs = (float)xs * h;
+            t.zs = (float)zs * h;
+            t.nt = ntrec;
+            t.samplerate = dt * (float)itrecord;
+            t.gain = dt / h;
+            t.ampstatic = 1.0f;
+            t.srcflagnum = xs;
+            t.recflagnum = ixr;
+            t.user[1] = t.user[2] = 123456789;
+            for (int k = 0; k < ntrec; ++k) {
+                const size_t o = (size_t)k * ntr + r;
+                tr[k] = cs == 8 ? (float)reinterpret_cast<const double *>(raw.data())[o]
+                                : reinterpret_cast<const float *>(raw.data())[o];
+            }
+            f.write((const char *)&t, sizeof t);
+            f.write((const char *)tr.data(), (std::streamsize)(tr.size() * sizeof(float)));
+        }
+        if (!f) {
+            std::fprintf(stderr, "fd23_psv2d: cannot write %s.isis\n", name.c_str());
+            return 1;
+        }
+    }
+    if (savestate) {
+        std::snprintf(statefile, sizeof statefile, "state%06d", nt + nt0 - 1);
+        std::vector<char> buf(sbytes);
+        if ((rc = fd23_get_state(s, buf.data(), sbytes))) return fail("state", rc);
+        if (!write_file(statefile, buf.data(), sbytes)) {
+            std::fprintf(stderr, "fd23_psv2d: cannot write %s\n", statefile);
+            return 1;
+        }
+    }
+    fd23_destroy(s);
+    std::printf("finish\n");
+    return 0;
+}

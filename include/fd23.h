@@ -289,6 +289,17 @@ int fd23_field_norm2(fd23_solver *s, double *norm2);
 int fd23_sum_squares_noalloc(int prec, const void *const *fields, int nfields, size_t n,
                              void *stream, double *sum, int *nonfinite);
 
+/* ---- model and station input (host only) ----
+ * fd23_read_model: a ".mdl" polygon model (BACK / POLY / DEF commands,
+ * PD/model/model.cpp:240-369, rasterised at (ix*h, iz*h) as get_elas_model,
+ * :175-232) or raster files <name>.vp, .vs, .den (float32 nx*nz,
+ * PD/model/util.cpp:12-22), into FP64 arrays of nx*nz.
+ * fd23_read_stations: a station file of "z x" lines (PD/record/cu_record.cu:
+ * 30-76), each station listed as the pair (x, z), (x-1, z); returns the
+ * number of receivers (2 per station); cap = 0 only counts. */
+int fd23_read_model(const char *name, int nx, int nz, double h, double *vp, double *vs, double *den);
+int fd23_read_stations(const char *path, int *rx, int *rz, int cap);
+
 /* ---- host-only builders (no GPU needed) ----
  * The same FP64 set-up fd23_set_model / fd23_create / fd23_set_source use,
  * exposed for callers that build inputs themselves.
