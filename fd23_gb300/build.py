@@ -56,19 +56,21 @@ def _compile(src, verbose=False):
 
 CLI_SRC = os.path.join(HERE, "cli", "fd23_psv2d.cpp")
 CLI = os.path.join(LIBDIR, "fd23_psv2d")
+CLI_SH = os.path.join(LIBDIR, "fd23_sh2d")
 
 
 def build_cli(force=False):
-    """The parfile program fd23_psv2d next to the library (linked to it,
-    found through the executable's own directory)."""
+    """The parfile programs fd23_psv2d and fd23_sh2d (one source) next to the
+    library, linked to it and finding it through their own directory."""
     newest = max(os.path.getmtime(p) for p in [CLI_SRC, LIB] + headers())
-    if not force and os.path.exists(CLI) and os.path.getmtime(CLI) >= newest:
-        return CLI
-    cmd = [_nvcc(), "-x", "c++", "-std=c++17", "-O2", CLI_SRC, "-o", CLI, "-L" + LIBDIR, "-lfd23",
-           "-Xlinker", "-rpath=$ORIGIN"]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError("cli build failed: %s\n%s\n%s" % (" ".join(cmd), r.stdout, r.stderr))
+    for exe, sh in ((CLI, 0), (CLI_SH, 1)):
+        if not force and os.path.exists(exe) and os.path.getmtime(exe) >= newest:
+            continue
+        cmd = [_nvcc(), "-x", "c++", "-std=c++17", "-O2", "-DFD23_CLI_SH=%d" % sh, CLI_SRC, "-o", exe,
+               "-L" + LIBDIR, "-lfd23", "-Xlinker", "-rpath=$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("cli build failed: %s\n%s\n%s" % (" ".join(cmd), r.stdout, r.stderr))
     return CLI
 
 

@@ -1,7 +1,16 @@
 // fd23_psv2d: the reference's P-SV program (PN nbpsv2d and its topabsorb /
-// explosion builds, PD psv2d_db without the box) on the fd23 engine.
+// explosion builds, PD psv2d_db without the box) on the fd23 engine; built
+// with FD23_CLI_SH=1 it is fd23_sh2d, the reference's SH program (SH/main.cpp).
 //
 //   fd23_psv2d par=run.par [key=value ...]
+//   fd23_sh2d  par=run.par [key=value ...]
+//
+// SH differences (SH/param/param.cpp:13-85): the source time function key is
+// "sourcetime" (srctime is accepted too), "stype" selects the source (3
+// moment, 13 'p' dipole; 2, the line force on V, is an addition), receivers
+// come from V_sta_file or nrec ixrec0 izrec0_v idxrec idzrec, and the output
+// is <output>_V with <output>_V.isis (no position shift).  ngpu and usepunch
+// (=0) are accepted.
 //
 // Parameters follow the reference's parameter reader (PN/param/param.cpp:88-200,
 // getpar conventions): key=value words on the command line, "par=file" reads
@@ -40,7 +49,14 @@
 
 #include "../../include/fd23.h"
 
+#ifndef FD23_CLI_SH
+#define FD23_CLI_SH 0
+#endif
+
 namespace {
+
+constexpr bool kSH = FD23_CLI_SH != 0;
+const char *kProg = kSH ? "fd23_sh2d" : "fd23_psv2d";
 
 struct Params {
     std::map<std::string, std::string> kv;
@@ -103,7 +119,7 @@ static_assert(sizeof(IsisTrace) == 84, "isis trace header is 84 bytes");
 
 int fail(const char *what, int rc)
 {
-    std::fprintf(stderr, "fd23_psv2d: %s: %s\n", what, fd23_strerror(rc));
+    std::fprintf(stderr, "%s: %s: %s\n", kProg, what, fd23_strerror(rc));
     return 1;
 }
 
@@ -122,16 +138,16 @@ int main(int argc, char **argv)
         const std::string a(argv[i]);
         if (a.rfind("par=", 0) == 0) {
             if (!load_parfile(p, a.substr(4))) {
-                std::fprintf(stderr, "fd23_psv2d: cannot read parameter file %s\n", a.substr(4).c_str());
+                std::fprintf(stderr, "%s: ", kProg); std::fprintf(stderr, "cannot read parameter file %s\n", a.substr(4).c_str());
                 return 1;
             }
         } else if (!add_word(p, a)) {
-            std::fprintf(stderr, "fd23_psv2d: expected key=value, got '%s'\n", a.c_str());
+            std::fprintf(stderr, "%s: ", kProg); std::fprintf(stderr, "expected key=value, got '%s'\n", a.c_str());
             return 1;
         }
     }
     if (argc < 2) {
-        std::fprintf(stderr, "usage: fd23_psv2d par=file [key=value ...]\n");
+        std::fprintf(stderr, "usage: %s par=file [key=value ...]\n", kProg);
         return 1;
     }
     const int restart = (int)p.num("restart", 0), savestate = (int)p.num("savestate", 0);
@@ -139,7 +155,9 @@ int main(int argc, char **argv)
     const int nx = (int)p.need_num("nx"), nz = (int)p.need_num("nz"), nt = (int)p.need_num("nt");
     const float h = (float)p.need_num("h"), dt = (float)p.need_num("dt");
     const std::string srctype = p.str("srctype", "1");
-    const std::string srctime = p.need("srctime");
+    const int stype = (int)p.num("stype", 3);
+    const std::string srctime = (kSH && p.has("sourcetime")) || !p.has("srctime") ? p.need(kSH ? "sourcetime" : "srctime")
+                                                                                   : p.str("srctime");
     double alpha = 0, trap[3] = {0, 0, 0};
     if (!srctime.empty() && (srctime[0] == 'T' || srctime[0] == 't'))
         for (int k = 0; k < 3; ++k) trap[k] = p.need_num("trap" + std::to_string(k + 1));
@@ -152,13 +170,13 @@ int main(int argc, char **argv)
                  pml_fc = p.need_num("pml_fc");
     const int itrecord = (int)p.num("itrecord", 1);
     const std::string output = p.need("output");
-    const std::string ufile = p.str("U_sta_file"), wfile = p.str("W_sta_file");
+    const std::string ufile = p.str(kSH ? "V_sta_file" : "U_sta_file"), wfile = kSH ? "" : p.str("W_sta_file");
     int nrec = 0, ixrec0 = 0, izu = 0, izw = 0, idx = 0, idz = 0;
     if (ufile.empty() && wfile.empty()) {
         nrec = (int)p.need_num("nrec");
         ixrec0 = (int)p.need_num("ixrec0");
-        izu = (int)p.need_num("izrec0_u");
-        izw = (int)p.need_num("izrec0_w");
+        izu = (int)p.need_num(kSH ? "izrec0_v" : "izrec0_u");
+        izw = kSH ? izu : (int)p.need_num("izrec0_w");
         idx = (int)p.need_num("idxrec");
         idz = (int)p.need_num("idzrec");
     }
@@ -167,13 +185,13 @@ int main(int argc, char **argv)
     const int explosion = (int)p.num("explosion", 0), topabsorb = (int)p.num("topabsorb", 0);
     const int device = (int)p.num("device", 0);
     if (!p.missing.empty()) {
-        std::fprintf(stderr, "fd23_psv2d: missing parameter(s):");
+        std::fprintf(stderr, "%s: ", kProg); std::fprintf(stderr, "missing parameter(s):");
         for (auto &m : p.missing) std::fprintf(stderr, " %s", m.c_str());
         std::fprintf(stderr, "\n");
         return 1;
     }
     if (p.num("usepunch", 0) != 0 || p.num("usebox", 0) != 0) {
-        std::fprintf(stderr, "fd23_psv2d: usepunch and usebox are not supported by this program\n");
+        std::fprintf(stderr, "%s: ", kProg); std::fprintf(stderr, "usepunch and usebox are not supported by this program\n");
         return 1;
     }
     int prec = FD23_F32;
@@ -181,15 +199,19 @@ int main(int argc, char **argv)
     else if (precs == "bf16") prec = FD23_BF16;
     else if (precs == "f16") prec = FD23_F16;
     else if (precs != "f32") {
-        std::fprintf(stderr, "fd23_psv2d: prec must be f32, f64, bf16 or f16\n");
+        std::fprintf(stderr, "%s: ", kProg); std::fprintf(stderr, "prec must be f32, f64, bf16 or f16\n");
         return 1;
     }
-    if (srctype != "1" && srctype != "p" && srctype != "P") {
-        std::fprintf(stderr, "fd23_psv2d: Wrong srctype! Specify 1 or p.\n");
+    if (!kSH && srctype != "1" && srctype != "p" && srctype != "P") {
+        std::fprintf(stderr, "%s: ", kProg); std::fprintf(stderr, "Wrong srctype! Specify 1 or p.\n");
+        return 1;
+    }
+    if (kSH && stype != 3 && stype != 13 && stype != 2) {
+        std::fprintf(stderr, "%s: ", kProg); std::fprintf(stderr, "stype must be 3, 13 or 2\n");
         return 1;
     }
     if (srctime.empty() || !std::strchr("GgTt", srctime[0])) {
-        std::fprintf(stderr, "fd23_psv2d: srctime must be Gaussian or Trapezoid\n");
+        std::fprintf(stderr, "%s: ", kProg); std::fprintf(stderr, "srctime must be Gaussian or Trapezoid\n");
         return 1;
     }
     // source time function: s(t)*dt samples
@@ -226,7 +248,9 @@ int main(int argc, char **argv)
                     "\"lsrc\": %d, \"itrecord\": %d, \"traces_u\": %zu, \"traces_w\": %zu, \"model\": \"%s\", "
                     "\"output\": \"%s\", \"savestate\": %d}\n",
                     nx, nz, nt, nt0, h, dt, npml, topabsorb, precs.c_str(),
-                    explosion ? "explosion" : (srctype == "1" ? "moment" : "moment_p"), xs, zs, lsrc, itrecord,
+                    kSH ? (stype == 2 ? "force" : (stype == 13 ? "moment_p" : "moment"))
+                        : (explosion ? "explosion" : (srctype == "1" ? "moment" : "moment_p")),
+                    xs, zs, lsrc, itrecord,
                     rxu.size(), rxw.size(), model.c_str(), output.c_str(), savestate);
         return 0;
     }
@@ -236,7 +260,7 @@ int main(int argc, char **argv)
     int rc = fd23_read_model(model.c_str(), nx, nz, h, vp.data(), vs.data(), den.data());
     if (rc) return fail(("model " + model).c_str(), rc);
     fd23_desc d{};
-    d.wave = FD23_PSV;
+    d.wave = kSH ? FD23_SH : FD23_PSV;
     d.prec = prec;
     d.nx = nx;
     d.nz = nz;
@@ -253,15 +277,22 @@ int main(int argc, char **argv)
     fd23_solver *s = nullptr;
     if ((rc = fd23_create(&d, &s))) return fail("create", rc);
     double stab = 0;
-    rc = fd23_set_model(s, vp.data(), vs.data(), den.data(), &stab);
+    rc = fd23_set_model(s, kSH ? nullptr : vp.data(), vs.data(), den.data(), &stab);
     std::printf("stab = %g\n", stab);
     if (rc) return fail("model", rc);
     double m[3];
-    fd23_moment_psv(strike, dip, rake, azimuth, m);
-    const int kind = explosion ? FD23_SRC_EXPLOSION : (srctype == "1" ? FD23_SRC_MOMENT : FD23_SRC_MOMENT_P);
+    int kind;
+    if (kSH) {
+        fd23_moment_sh(strike, dip, rake, azimuth, m);
+        kind = stype == 2 ? FD23_SRC_FORCE : (stype == 13 ? FD23_SRC_MOMENT_P : FD23_SRC_MOMENT);
+    } else {
+        fd23_moment_psv(strike, dip, rake, azimuth, m);
+        kind = explosion ? FD23_SRC_EXPLOSION : (srctype == "1" ? FD23_SRC_MOMENT : FD23_SRC_MOMENT_P);
+    }
     if ((rc = fd23_set_source(s, kind, xs, zs, m, src.data(), lsrc, nt0 + nt))) return fail("source", rc);
-    if ((rc = fd23_set_receivers(s, FD23_U, rxu.data(), rzu.data(), (int)rxu.size()))) return fail("U receivers", rc);
-    if ((rc = fd23_set_receivers(s, FD23_W, rxw.data(), rzw.data(), (int)rxw.size()))) return fail("W receivers", rc);
+    if ((rc = fd23_set_receivers(s, 0, rxu.data(), rzu.data(), (int)rxu.size()))) return fail("receivers", rc);
+    if (!kSH && (rc = fd23_set_receivers(s, FD23_W, rxw.data(), rzw.data(), (int)rxw.size())))
+        return fail("W receivers", rc);
     const size_t sbytes = fd23_state_bytes(s);
     char statefile[64];
     if (restart) {
@@ -269,7 +300,7 @@ int main(int argc, char **argv)
         std::vector<char> buf(sbytes);
         std::ifstream f(statefile, std::ios::binary);
         if (!f || !f.read(buf.data(), (std::streamsize)sbytes)) {
-            std::fprintf(stderr, "fd23_psv2d: cannot read %s\n", statefile);
+            std::fprintf(stderr, "%s: ", kProg); std::fprintf(stderr, "cannot read %s\n", statefile);
             return 1;
         }
         if ((rc = fd23_set_state(s, buf.data(), sbytes, nt0))) return fail("restart state", rc);
@@ -278,9 +309,9 @@ int main(int argc, char **argv)
     // seismograms
     const size_t cs = prec == FD23_F64 ? 8 : 4;
     const std::vector<int> *rx[2] = {&rxu, &rxw}, *rz[2] = {&rzu, &rzw};
-    const char *suffix[2] = {"_U", "_W"};
-    const float shiftx[2] = {0.5f, 0.0f}, shiftz[2] = {0.0f, -0.5f};
-    for (int c = 0; c < 2; ++c) {
+    const char *suffix[2] = {kSH ? "_V" : "_U", "_W"};
+    const float shiftx[2] = {kSH ? 0.0f : 0.5f, 0.0f}, shiftz[2] = {0.0f, -0.5f};
+    for (int c = 0; c < (kSH ? 1 : 2); ++c) {
         const size_t ntr = rx[c]->size();
         int nrs = 0;
         if ((rc = fd23_get_seismograms(s, c, nullptr, 0, &nrs))) return fail("seismograms", rc);
@@ -288,7 +319,7 @@ int main(int argc, char **argv)
         if ((rc = fd23_get_seismograms(s, c, raw.data(), raw.size(), &nrs))) return fail("seismograms", rc);
         const std::string name = output + suffix[c];
         if (!write_file(name, raw.data(), raw.size())) {
-            std::fprintf(stderr, "fd23_psv2d: cannot write %s\n", name.c_str());
+            std::fprintf(stderr, "%s: ", kProg); std::fprintf(stderr, "cannot write %s\n", name.c_str());
             return 1;
         }
         // .isis: one header + trace per receiver, float samples
@@ -319,7 +350,7 @@ int main(int argc, char **argv)
             f.write((const char *)tr.data(), (std::streamsize)(tr.size() * sizeof(float)));
         }
         if (!f) {
-            std::fprintf(stderr, "fd23_psv2d: cannot write %s.isis\n", name.c_str());
+            std::fprintf(stderr, "%s: ", kProg); std::fprintf(stderr, "cannot write %s.isis\n", name.c_str());
             return 1;
         }
     }
@@ -328,7 +359,7 @@ int main(int argc, char **argv)
         std::vector<char> buf(sbytes);
         if ((rc = fd23_get_state(s, buf.data(), sbytes))) return fail("state", rc);
         if (!write_file(statefile, buf.data(), sbytes)) {
-            std::fprintf(stderr, "fd23_psv2d: cannot write %s\n", statefile);
+            std::fprintf(stderr, "%s: ", kProg); std::fprintf(stderr, "cannot write %s\n", statefile);
             return 1;
         }
     }

@@ -15,6 +15,7 @@ F = pytest.importorskip("fd23_gb300")
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CLI = os.path.join(ROOT, "fd23_gb300", "_lib", "fd23_psv2d")
+CLI_SH = os.path.join(ROOT, "fd23_gb300", "_lib", "fd23_sh2d")
 
 MDL_DEFS = """# overlapping polygons, named vertices, negative vs / den as factors of vp
 DEF a 10 5
@@ -132,3 +133,27 @@ def test_cli_errors(tmp_path):
     assert r.returncode == 1 and "usepunch" in r.stderr
     r = _cli(tmp_path, "par=run.par", "prec=f8", "dryrun=1")
     assert r.returncode == 1
+
+
+SH_PAR = """nx=200 nz=100 nt=20 h=10 dt=0.001
+sourcetime=Gaussian alpha=-5
+strike=0 dip=90 rake=0 azimuth=45
+xs=100 zs=20 npml=20 pml_dt=0.001 pml_v=300 pml_fc=10 pml_r=1e-11
+itrecord=1 output=sh model=m.mdl ntsnap=100 ngpu=1 usepunch=0
+nrec=20 ixrec0=5 izrec0_v=0 idxrec=9 idzrec=0
+"""
+
+
+def test_sh_program_parameters(tmp_path):
+    if not os.path.exists(CLI_SH):
+        pytest.skip("fd23_sh2d not built")
+    (tmp_path / "sh.par").write_text(SH_PAR)
+    run = lambda *a: subprocess.run([CLI_SH, "par=sh.par"] + list(a), cwd=str(tmp_path), capture_output=True,
+                                    text=True)
+    d = json.loads(run("dryrun=1").stdout)
+    assert (d["source"], d["traces_u"], d["nx"]) == ("moment", 40, 200)
+    assert json.loads(run("stype=13", "dryrun=1").stdout)["source"] == "moment_p"
+    assert json.loads(run("stype=2", "dryrun=1").stdout)["source"] == "force"
+    assert run("stype=5", "dryrun=1").returncode == 1
+    (tmp_path / "st").write_text("0 10\n0 30\n")
+    assert json.loads(run("V_sta_file=st", "dryrun=1").stdout)["traces_u"] == 4

@@ -14,6 +14,7 @@ F = pytest.importorskip("fd23_gb300")
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CLI = os.path.join(ROOT, "fd23_gb300", "_lib", "fd23_psv2d")
+CLI_SH = os.path.join(ROOT, "fd23_gb300", "_lib", "fd23_sh2d")
 
 MDL = """BACK 5.5 3.2 2.6
 POLY 6.5 3.7 2.9
@@ -107,3 +108,30 @@ def test_cli_restart(tmp_path):
     second = np.fromfile(str(tmp_path / "second_U"), dtype=np.float32).reshape(30, ntr)
     np.testing.assert_array_equal(first, full[:30])
     np.testing.assert_array_equal(second, full[30:])
+
+
+@pytest.mark.parametrize("stype", [3, 2])
+def test_sh_program_equals_api(tmp_path, stype):
+    _setup(tmp_path)
+    if not os.path.exists(CLI_SH):
+        pytest.skip("fd23_sh2d not built")
+    nt = 50
+    par = PAR.replace("srctime=", "sourcetime=").replace("U_sta_file=st W_sta_file=st", "V_sta_file=st")
+    (tmp_path / "sh.par").write_text(par)
+    r = subprocess.run([CLI_SH, "par=sh.par", "nt=%d" % nt, "output=shr", "stype=%d" % stype], cwd=str(tmp_path),
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    vp, vs, den = F.read_model(str(tmp_path / "layers.mdl"), 150, 100, np.float32(0.3))
+    s = F.Solver("sh", 150, 100, 12, float(np.float32(0.3)), float(np.float32(0.01)), prec="f32", pml_dt=0.005,
+                 pml_v=30.0, pml_r=1e-11, pml_fc=2.0)
+    s.set_model(None, vs, den)
+    kind = F.SRC_FORCE if stype == 2 else F.SRC_MOMENT
+    s.set_source(kind, 75, 20, F.moment_sh(0, 20, 90, 45), F.wavelet_gaussian(float(np.float32(0.01)), -5), nt)
+    rx, rz = F.receivers_file(str(tmp_path / "st"))
+    s.set_receivers(0, rx, rz)
+    s.run(nt, 1)
+    want = s.seismograms(0)
+    s.close()
+    got = np.fromfile(str(tmp_path / "shr_V"), dtype=np.float32).reshape(nt, len(rx))
+    np.testing.assert_array_equal(got, want)
+    assert (tmp_path / "shr_V.isis").stat().st_size == len(rx) * (84 + 4 * nt)
