@@ -102,6 +102,16 @@ def box_alg_bytes(bx, bz, nring, es):
     return 20 * es * (bx - 8) * (bz - 8) + 15 * es * nring
 
 
+def max_over_ranks(ms, dist):
+    """Slowest rank's time (replicas run independent shots; the job's time is
+    the slowest one's)."""
+    import torch
+    t = torch.tensor([float(ms)], dtype=torch.float64)
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t[0])
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -319,10 +329,7 @@ def main():
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     clocks = sampler.stop() if rank == 0 else None
-    t = torch.tensor([ms], dtype=torch.float64)
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t[0])
+    ms_max = max_over_ranks(ms, dist)
     cells = NX * NZ * nt * args.steps * world
     value = cells / (ms_max * 1e-3)
     seis = (s.seismograms(0), s.seismograms(1))
@@ -507,10 +514,7 @@ def bench_box(args, F, torch, rank, world, local, dist):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     clocks = sampler.stop() if rank == 0 else None
-    t = torch.tensor([ms], dtype=torch.float64)
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t[0])
+    ms_max = max_over_ranks(ms, dist)
     value = NX * NZ * nt * args.steps * world / (ms_max * 1e-3)
 
     e2e = None
@@ -611,10 +615,7 @@ def bench_sh(args, F, torch, rank, world, local, dist):
         b.sync()
         ms += e0.elapsed_time(e1)
     clocks = sampler.stop() if rank == 0 else None
-    t = torch.tensor([ms], dtype=torch.float64)
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t[0])
+    ms_max = max_over_ranks(ms, dist)
     cells = SH_NX * SH_NZ
     value = cells * nt * args.steps * world / (ms_max * 1e-3)
     e2e = None
@@ -762,10 +763,7 @@ def bench_batch(args, F, torch, rank, world, local, dist):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     clocks = sampler.stop() if rank == 0 else None
-    t = torch.tensor([ms], dtype=torch.float64)
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t[0])
+    ms_max = max_over_ranks(ms, dist)
     value = cells * nt * args.steps * world / (ms_max * 1e-3)
     seis = [(s.seismograms(0), s.seismograms(1)) for s in solvers]
 
