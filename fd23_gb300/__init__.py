@@ -55,6 +55,7 @@ ABI_FUNCTIONS = [
     "fd23_box_material", "fd23_batch_create", "fd23_batch_destroy", "fd23_batch_run", "fd23_batch_sync",
     "fd23_batch_get_stream", "fd23_batch_set_graph", "fd23_autotune", "fd23_batch_autotune",
     "fd23_batch_get_plan", "fd23_work_plan", "fd23_read_model", "fd23_read_stations",
+    "fd23_debug_expire_wait",
 ]
 
 
@@ -147,6 +148,7 @@ def lib():
         "fd23_work_plan": ([i, vp, vp, vp, vp, i, vp, vp, i, vp, i], i),
         "fd23_read_model": ([_C.c_char_p, i, i, d, vp, vp, vp], i),
         "fd23_read_stations": ([_C.c_char_p, vp, vp, i], i),
+        "fd23_debug_expire_wait": ([vp], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)

@@ -896,6 +896,13 @@ int fd23_field_norm2(fd23_solver *s, double *norm2)
     return h[1] != 0.0 ? FD23_ERR_NONFINITE : FD23_OK;
 }
 
+int fd23_debug_expire_wait(fd23_solver *s)
+{
+    if (!s) return FD23_ERR_ARG;
+    CK(cudaSetDevice(s->d.device));
+    return launch_wait_probe(s->err_flag, s->stream);
+}
+
 // ---- hybrid box ----
 int fd23_set_box(fd23_solver *s, int x0, int z0, int bx, int bz, const double *bmat)
 {

@@ -1108,7 +1108,25 @@ int prepare_one()
     return ok ? FD23_OK : FD23_ERR_CUDA;
 }
 
+// Failure-path probe: one thread waits, with the sweep's bounded wait, on an
+// mbarrier that nothing completes.  The wait gives up after its limit (about
+// 2 s), sets the error flag and the kernel returns.
+__global__ void wait_probe(int *err_flag)
+{
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x != 0) return;
+    mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    mbar_wait_bounded(&bar, 0u, err_flag);
+}
+
 }  // namespace
+
+int launch_wait_probe(int *err_flag, cudaStream_t st)
+{
+    wait_probe<<<1, 32, 0, st>>>(err_flag);
+    return cudaPeekAtLastError() == cudaSuccess ? FD23_OK : FD23_ERR_CUDA;
+}
 
 template <class S, class C, int WAVE>
 FusedBoxes boxes_of()

@@ -60,6 +60,10 @@ template <class S, class C>
 int launch_step_fused_batch(const Shot<S, C> *shots, int wave, const WorkItem *items, const int *item_off,
                             int nblocks, int par, int it, int rec_index, int *err_flag, cudaStream_t st);
 
+// one thread waits on an mbarrier nothing completes, with the sweep's bounded
+// wait: sets *err_flag when the wait gives up (about 2 s)
+int launch_wait_probe(int *err_flag, cudaStream_t st);
+
 // FP64 sum of squares over the `elems` stored elements of each of the first
 // `nfields` wavefields of buffer set `par` (the zero padding included); the
 // sum goes to dev_out[0], a NaN/Inf flag to dev_out[1].

@@ -273,6 +273,15 @@ int fd23_work_plan(int nshots, const int *nx, const int *nz, const int *npml, co
  * fields in FP64; returns FD23_ERR_NONFINITE when any value is NaN/Inf. */
 int fd23_field_norm2(fd23_solver *s, double *norm2);
 
+/* ---- failure-path check ----
+ * Runs, on the solver's stream, the sweep's bounded device-side wait on a
+ * barrier that nothing completes.  The wait gives up after about 2 s and
+ * raises the solver's error flag, exactly as a sweep whose copies never
+ * arrive would: fd23_sync then returns FD23_ERR_TIMEOUT, later sweeps
+ * return at once, and fd23_reset clears the flag.  For tests of the failure
+ * handling; it faults nothing and leaves the GPU usable. */
+int fd23_debug_expire_wait(fd23_solver *s);
+
 /* ---- allocation-free watchdog ----
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory (code running inside a CUDA stream capture, programs whose device
