@@ -175,7 +175,7 @@ def cpu_baseline(budget_s=15.0, threads=0):
     """Oracle restatement of the reference update loop (FP32, all host
     threads) on the benchmark grid for as many steps as fit the budget."""
     from oracle import fd23_oracle as O
-    vp, vs, rho = c1_model()
+    vp, vs, rho = c1_model(NX, NZ)
     mat, _, _ = O.psv_material(vp, vs, rho, H, DT)
     bck = O.cpml_psv(NX, NZ, NPML, DT, 1e-11, vp.max() / H, F0)
     src = O.ricker(DT, F0)
@@ -249,6 +249,7 @@ def run_reference_arm(args, rank, world):
 
 
 def main():
+    global NX, NZ, H, DT, NT
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
@@ -261,8 +262,13 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
-    ap.add_argument("--config", default="c1", choices=["c0", "c1", "c2", "c4"])
+    ap.add_argument("--config", default="c1", choices=["c0", "c1", "c2", "c3", "c4"])
     args = ap.parse_args()
+    if args.config == "c3":
+        # the large grid: 16000 x 8000, h 2.5 m, dt 2e-4 s, 8000 steps, C1-style model
+        NX, NZ, H, DT, NT = 16000, 8000, 2.5, 2e-4, 8000
+        args.nt = min(args.nt, NT) if args.nt != 5000 else NT
+        args.no_accuracy = True  # an FP64 run of this grid takes minutes
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -291,7 +297,7 @@ def main():
         bench_sh(args, F, torch, rank, world, local, dist)
         return
     nt = args.nt
-    vp, vs, rho = c1_model(seed=1 + rank)
+    vp, vs, rho = c1_model(NX, NZ, seed=1 + rank)
     pml_v = float(vp.max()) / H
     s = F.Solver("psv", NX, NZ, NPML, H, DT, prec=args.prec, pml_dt=DT, pml_v=pml_v, pml_r=1e-11,
                  pml_fc=F0, device=local, kernel=args.kernel)
@@ -385,7 +391,8 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.prec,
             "data": "synthetic",
-            "config": {"workload": "psv_4000x2000_5000steps_c1", "nx": NX, "nz": NZ, "nt": nt,
+            "config": {"workload": "psv_%dx%d_%dsteps_%s" % (NX, NZ, NT, args.config), "nx": NX, "nz": NZ,
+                       "nt": nt,
                        "h_m": H, "dt_s": DT, "npml": NPML, "source": "15 Hz Ricker explosion",
                        "traces": 4 * NSTA, "kernel": args.kernel, "prec": args.prec,
                        "l2": "inputs larger than L2 (%.0f MB resident)" % (
