@@ -271,13 +271,17 @@ int encode_maps(fd23_solver *s)
 // the 3 its register budget is built for)
 int fused_per_sm(int device, int wave, int prec)
 {
-    int smem_sm = 0;
-    if (cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device) != cudaSuccess) {
+    // registers and shared memory both bound the residency: ask the runtime
+    // (after fused_prepare has raised the dynamic shared-memory limit)
+    int cur = 0;
+    if (cudaGetDevice(&cur) != cudaSuccess || cur != device) {
         cudaGetLastError();
-        return 1;
+        if (cudaSetDevice(device) != cudaSuccess) {
+            cudaGetLastError();
+            return 1;
+        }
     }
-    const size_t smem = fused_smem_bytes(wave, prec) + 1024;  // + the per-CTA reserve
-    return std::max(1, std::min(3, (int)(smem_sm / smem)));
+    return std::max(1, std::min(3, fused_occupancy(wave, prec)));
 }
 
 int upload_plan(const WorkPlan &plan, WorkItem **d_items, int **d_off)

@@ -361,7 +361,10 @@ struct Cfg {
     }
     static constexpr int MAX_ITEMS = 4;
     static constexpr int MAX_TERMS = 16;
-    static constexpr int MINB = sizeof(S) == 8 ? 1 : 3;  // CTAs per SM the registers must allow
+    // CTAs per SM the register budget is built for: three for the 4-byte
+    // forms (shared memory allows three); two for the 16-bit forms, whose
+    // extra conversions run faster with the larger register budget (measured)
+    static constexpr int MINB = sizeof(S) == 8 ? 1 : (sizeof(S) == 2 ? 2 : 3);
     static constexpr size_t RING_BYTES =
         (((size_t)(UW_ELEMS + PW_ELEMS + TR_ELEMS) * sizeof(S) + 15) & ~(size_t)15);
     static constexpr size_t SMEM = RING_BYTES + 256 /* 2*(NUW+NPW) barriers */ + MAX_ITEMS * 16 +
@@ -1199,6 +1202,37 @@ int fused_prepare(int wave, int prec)
         case FD23_BF16: return prepare_one<__nv_bfloat16, float, FD23_SH>();
         case FD23_F16: return prepare_one<__half, float, FD23_SH>();
         default: return prepare_one<float, float, FD23_SH>();
+    }
+}
+
+template <class S, class C, int WAVE>
+int occupancy_one()
+{
+    using K = Cfg<S, C, WAVE>;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fused_step<S, C, WAVE, false>, K::NTH, K::SMEM) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    return n > 0 ? n : 1;
+}
+
+int fused_occupancy(int wave, int prec)
+{
+    if (wave == FD23_PSV) {
+        switch (prec) {
+            case FD23_F64: return occupancy_one<double, double, FD23_PSV>();
+            case FD23_BF16: return occupancy_one<__nv_bfloat16, float, FD23_PSV>();
+            case FD23_F16: return occupancy_one<__half, float, FD23_PSV>();
+            default: return occupancy_one<float, float, FD23_PSV>();
+        }
+    }
+    switch (prec) {
+        case FD23_F64: return occupancy_one<double, double, FD23_SH>();
+        case FD23_BF16: return occupancy_one<__nv_bfloat16, float, FD23_SH>();
+        case FD23_F16: return occupancy_one<__half, float, FD23_SH>();
+        default: return occupancy_one<float, float, FD23_SH>();
     }
 }
 

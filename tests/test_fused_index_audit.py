@@ -145,8 +145,10 @@ SIZES = [(96, 96), (96, 64), (250, 130), (257, 131), (500, 300), (1000, 1000), (
 @pytest.mark.parametrize("nx,nz", SIZES)
 @pytest.mark.parametrize("es,wave", [(4, "psv"), (8, "psv"), (2, "psv"), (4, "sh"), (2, "sh")])
 def test_fused_addresses_in_bounds(nx, nz, es, wave):
-    per_sm = 1 if es == 8 else 3
+    per_sm = {8: 1, 4: 3, 2: 2}[es]  # the register budget each storage width is built for
     audit(nx, nz, es, wave, per_sm=per_sm)
+    if es == 2:  # and three, should the runtime report three resident CTAs
+        audit(nx, nz, es, wave, per_sm=3)
     audit(nx, nz, es, wave, per_sm=per_sm, oversub=3.0)
 
 
