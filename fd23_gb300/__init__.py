@@ -55,7 +55,7 @@ ABI_FUNCTIONS = [
     "fd23_box_material", "fd23_batch_create", "fd23_batch_destroy", "fd23_batch_run", "fd23_batch_sync",
     "fd23_batch_get_stream", "fd23_batch_set_graph", "fd23_autotune", "fd23_batch_autotune",
     "fd23_batch_get_plan", "fd23_work_plan", "fd23_read_model", "fd23_read_stations",
-    "fd23_debug_expire_wait",
+    "fd23_debug_expire_wait", "fd23_set_plan", "fd23_get_plan", "fd23_punch_tiles", "fd23_punch_windows", "fd23_read_punch", "fd23_set_punch",
 ]
 
 
@@ -149,6 +149,12 @@ def lib():
         "fd23_read_model": ([_C.c_char_p, i, i, d, vp, vp, vp], i),
         "fd23_read_stations": ([_C.c_char_p, vp, vp, i], i),
         "fd23_debug_expire_wait": ([vp], i),
+        "fd23_set_plan": ([vp, vp], i),
+        "fd23_get_plan": ([vp, vp, _C.POINTER(i)], i),
+        "fd23_punch_tiles": ([i, i, _C.POINTER(i), _C.POINTER(i)], i),
+        "fd23_punch_windows": ([vp, i, i, i, d, d, d, vp, vp], i),
+        "fd23_read_punch": ([_C.c_char_p, i, i, i, d, d, d, vp, vp], i),
+        "fd23_set_punch": ([vp, vp, vp, i, i], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -401,6 +407,37 @@ def read_model(name, nx, nz, h):
     return out
 
 
+def punch_tiles(nx, nz):
+    """(nbx, nbz): the 32 x 16 tiles of the step windows."""
+    a, b = _C.c_int(0), _C.c_int(0)
+    _check(lib().fd23_punch_tiles(nx, nz, _C.byref(a), _C.byref(b)), "fd23_punch_tiles")
+    return a.value, b.value
+
+
+def punch_windows(times, before, after, dt, elem="f64"):
+    """Tile step windows (first, last), int32 [nbz*nbx] each, from travel
+    times t[nz, nx] (fd23_punch_windows; elem 'f64' as PD, 'f32' as PN/SH)."""
+    es = 8 if elem == "f64" else 4
+    t = _np.ascontiguousarray(times, dtype=_np.float64 if es == 8 else _np.float32)
+    nz, nx = t.shape
+    nbx, nbz = punch_tiles(nx, nz)
+    first = _np.zeros(nbx * nbz, _np.int32)
+    last = _np.zeros(nbx * nbz, _np.int32)
+    _check(lib().fd23_punch_windows(_p(t), es, nx, nz, before, after, dt, _p(first), _p(last)),
+           "fd23_punch_windows")
+    return first, last
+
+
+def read_punch(timefile, nx, nz, before, after, dt, elem="f64"):
+    """The same from a raw travel-time file (the reference's `timefile`)."""
+    nbx, nbz = punch_tiles(nx, nz)
+    first = _np.zeros(nbx * nbz, _np.int32)
+    last = _np.zeros(nbx * nbz, _np.int32)
+    _check(lib().fd23_read_punch(timefile.encode(), 8 if elem == "f64" else 4, nx, nz, before, after, dt,
+                                 _p(first), _p(last)), "fd23_read_punch")
+    return first, last
+
+
 def read_raster_model(prefix, nx, nz, wave="psv"):
     """Float32 raster model files <prefix>.vp, .vs, .den (PD/model/util.cpp:12-28)."""
     def rd(ext):
@@ -529,6 +566,34 @@ class Solver:
         tab = (TuneEntry * 64)()
         n = _check(lib().fd23_autotune(self._h, trial_steps, _C.cast(tab, _C.c_void_p), 64), "fd23_autotune")
         return [tab[k].as_dict() for k in range(n)]
+
+    def set_plan(self, wx=4.0, wz=3.0, per_sm=3, oversub=1.0):
+        """Install a work plan without timing it (fd23_set_plan)."""
+        t = TuneEntry(wx, wz, per_sm, oversub, 0.0)
+        _check(lib().fd23_set_plan(self._h, _C.cast(_C.pointer(t), _C.c_void_p)), "fd23_set_plan")
+
+    def plan(self):
+        """The current work plan and its CTA count (fd23_get_plan)."""
+        e = TuneEntry()
+        nb = _C.c_int(0)
+        _check(lib().fd23_get_plan(self._h, _C.cast(_C.pointer(e), _C.c_void_p), _C.byref(nb)), "fd23_get_plan")
+        d = e.as_dict()
+        d["nblocks"] = nb.value
+        return d
+
+    # -- usepunch --
+    def set_punch(self, first, last):
+        """Tile step windows (first, last) of punch_windows / read_punch;
+        None, None removes them."""
+        if first is None and last is None:
+            _check(lib().fd23_set_punch(self._h, None, None, 0, 0), "fd23_set_punch")
+            return
+        nbx, nbz = punch_tiles(self.nx, self.nz)
+        f = _np.ascontiguousarray(first, dtype=_np.int32).ravel()
+        l = _np.ascontiguousarray(last, dtype=_np.int32).ravel()
+        if f.size != nbx * nbz or l.size != nbx * nbz:
+            nbx = nbz = -1  # let the library reject the sizes
+        _check(lib().fd23_set_punch(self._h, _p(f), _p(l), nbx, nbz), "fd23_set_punch")
 
     # -- hybrid box --
     def set_box(self, x0, z0, bx, bz, bmat=None):

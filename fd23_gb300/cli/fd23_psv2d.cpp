@@ -9,8 +9,7 @@
 // "sourcetime" (srctime is accepted too), "stype" selects the source (3
 // moment, 13 'p' dipole; 2, the line force on V, is an addition), receivers
 // come from V_sta_file or nrec ixrec0 izrec0_v idxrec idzrec, and the output
-// is <output>_V with <output>_V.isis (no position shift).  ngpu and usepunch
-// (=0) are accepted.
+// is <output>_V with <output>_V.isis (no position shift).  ngpu is accepted.
 //
 // Parameters follow the reference's parameter reader (PN/param/param.cpp:88-200,
 // getpar conventions): key=value words on the command line, "par=file" reads
@@ -22,8 +21,11 @@
 // Optional: srctype (1 moment, p 'p' dipole; default 1), itrecord (1),
 // restart + nt0, savestate.  Accepted and ignored (no effect on this path):
 // ntsnap itprint gpuid ngpu ord bw usetable src_shift_x src_shift_z
-// sourcetime stype.  Not supported here: usepunch=1, usebox=1 (the box is
-// in the C ABI).  Additions: prec (f32, f64, bf16, f16; default f32),
+// sourcetime stype.  usepunch=1 (with before, after, timefile) updates
+// every 32 x 16 tile only inside its step window (PN/slide/cu_slide.cu,
+// PN/param/param.cpp usepunch block): the timefile holds nx*nz float travel
+// times (PN, SH), or doubles with prec=f64 (PD, whose windows use the double
+// dt).  Not supported here: usebox=1 (the box is in the C ABI).  Additions: prec (f32, f64, bf16, f16; default f32),
 // explosion (1: Mxx = Mzz = 1, the *_exp builds), topabsorb (1: CPML on top,
 // the *_topabsorb builds), device (CUDA ordinal, default 0), dryrun (1: print
 // the resolved set-up and stop before touching the GPU).
@@ -190,9 +192,21 @@ int main(int argc, char **argv)
         std::fprintf(stderr, "\n");
         return 1;
     }
-    if (p.num("usepunch", 0) != 0 || p.num("usebox", 0) != 0) {
-        std::fprintf(stderr, "%s: ", kProg); std::fprintf(stderr, "usepunch and usebox are not supported by this program\n");
+    if (p.num("usebox", 0) != 0) {
+        std::fprintf(stderr, "%s: ", kProg); std::fprintf(stderr, "usebox is not supported by this program\n");
         return 1;
+    }
+    const int usepunch = (int)p.num("usepunch", 0);
+    double before = 0, after = 0;
+    std::string timefile;
+    if (usepunch == 1) {
+        before = p.need_num("before");
+        after = p.need_num("after");
+        timefile = p.need("timefile");
+        if (!p.missing.empty()) {
+            std::fprintf(stderr, "%s: ", kProg); std::fprintf(stderr, "usepunch=1 needs before, after and timefile\n");
+            return 1;
+        }
     }
     int prec = FD23_F32;
     if (precs == "f64") prec = FD23_F64;
@@ -242,16 +256,29 @@ int main(int argc, char **argv)
         fd23_receivers_line(nrec, ixrec0, izu, idx, idz, rxu.data(), rzu.data());
         fd23_receivers_line(nrec, ixrec0, izw, idx, idz, rxw.data(), rzw.data());
     }
+    // tile step windows
+    int nbx = 0, nbz = 0;
+    std::vector<int> pfirst, plast;
+    if (usepunch == 1) {
+        fd23_punch_tiles(nx, nz, &nbx, &nbz);
+        pfirst.resize((size_t)nbx * nbz);
+        plast.resize((size_t)nbx * nbz);
+        const int es = precs == "f64" ? 8 : 4;
+        const double pdt = es == 8 ? p.need_num("dt") : (double)dt;
+        const int rc = fd23_read_punch(timefile.c_str(), es, nx, nz, before, after, pdt, pfirst.data(), plast.data());
+        if (rc) return fail(("timefile " + timefile).c_str(), rc);
+    }
     if (p.num("dryrun", 0) != 0) {
         std::printf("{\"nx\": %d, \"nz\": %d, \"nt\": %d, \"nt0\": %d, \"h\": %.9g, \"dt\": %.9g, \"npml\": %d, "
                     "\"topabsorb\": %d, \"prec\": \"%s\", \"source\": \"%s\", \"xs\": %d, \"zs\": %d, "
                     "\"lsrc\": %d, \"itrecord\": %d, \"traces_u\": %zu, \"traces_w\": %zu, \"model\": \"%s\", "
-                    "\"output\": \"%s\", \"savestate\": %d}\n",
+                    "\"output\": \"%s\", \"savestate\": %d, \"punch_tiles\": %d, \"punch_first_min\": %d}\n",
                     nx, nz, nt, nt0, h, dt, npml, topabsorb, precs.c_str(),
                     kSH ? (stype == 2 ? "force" : (stype == 13 ? "moment_p" : "moment"))
                         : (explosion ? "explosion" : (srctype == "1" ? "moment" : "moment_p")),
                     xs, zs, lsrc, itrecord,
-                    rxu.size(), rxw.size(), model.c_str(), output.c_str(), savestate);
+                    rxu.size(), rxw.size(), model.c_str(), output.c_str(), savestate, nbx * nbz,
+                    pfirst.empty() ? 0 : *std::min_element(pfirst.begin(), pfirst.end()));
         return 0;
     }
     // model
@@ -293,6 +320,8 @@ int main(int argc, char **argv)
     if ((rc = fd23_set_receivers(s, 0, rxu.data(), rzu.data(), (int)rxu.size()))) return fail("receivers", rc);
     if (!kSH && (rc = fd23_set_receivers(s, FD23_W, rxw.data(), rzw.data(), (int)rxw.size())))
         return fail("W receivers", rc);
+    if (usepunch == 1 && (rc = fd23_set_punch(s, pfirst.data(), plast.data(), nbx, nbz)))
+        return fail("usepunch", rc);
     const size_t sbytes = fd23_state_bytes(s);
     char statefile[64];
     if (restart) {

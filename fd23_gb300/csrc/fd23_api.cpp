@@ -365,6 +365,7 @@ void free_all(fd23_solver *s)
     }
     cudaFree(s->mat_block);
     cudaFree(s->d_maps);
+    cudaFree(s->d_punch);
     cudaFree(s->cpml);
     cudaFree(s->err_flag);
     cudaFree(s->norm_buf);
@@ -878,7 +879,8 @@ int fd23_set_state(fd23_solver *s, const void *buf, size_t bytes, int it0)
     }
     s->it = it0;
     s->par = 0;
-    return FD23_OK;
+    // the fused sweep may leave steady tiles alone: both sets hold the state
+    return mirror_sets(s, s->stream);
 }
 
 int fd23_field_norm2(fd23_solver *s, double *norm2)
@@ -917,7 +919,7 @@ int fd23_set_box(fd23_solver *s, int x0, int z0, int bx, int bz, const double *b
         free_box(s);
         return FD23_OK;
     }
-    if (s->d.wave != FD23_PSV || scaled_form(s)) return FD23_ERR_UNSUPPORTED;
+    if (s->d.wave != FD23_PSV || scaled_form(s) || s->d_punch) return FD23_ERR_UNSUPPORTED;
     if (bx < kBoxMin || bz < kBoxMin || x0 < 0 || z0 < 0 || x0 + bx > s->d.nx || z0 + bz > s->d.nz)
         return FD23_ERR_ARG;
     if (!bmat && !s->have_material) return FD23_ERR_ORDER;

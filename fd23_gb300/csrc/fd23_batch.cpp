@@ -39,7 +39,7 @@ struct fd23_batch {
     int plan_ver = 0;
     // cached graph of the last run: key = it0, nsteps, itrecord, par0, nrec0, plan version
     cudaGraphExec_t gexec = nullptr;
-    long long gkey[6] = {-1, -1, -1, -1, -1, -1};
+    long long gkey[7] = {-1, -1, -1, -1, -1, -1, -1};
     int use_graph = 1;
 };
 
@@ -102,14 +102,14 @@ int join_out(fd23_batch *b)
 // pending record row through *pending
 template <class S, class C>
 int launch_steps(fd23_batch *b, int it0, int nsteps, int itrecord, bool any_rec, int par0, int nrec0,
-                 int *pending)
+                 bool punch, int *pending)
 {
     const Shot<S, C> *shots = (const Shot<S, C> *)b->d_shots;
     int par = par0, pend = -1, nrec = nrec0;
     for (int k = 0; k < nsteps; ++k) {
         const int it = it0 + k;
         const int rc = launch_step_fused_batch<S, C>(shots, b->wave, b->d_items, b->d_off, b->plan.nblocks, par,
-                                                     it, pend, b->err_flag, b->stream);
+                                                     it, pend, b->err_flag, punch, b->stream);
         if (rc) return rc;
         pend = (any_rec && it % itrecord == 0) ? nrec++ : -1;
         par = 1 - par;
@@ -133,9 +133,11 @@ int batch_run_impl(fd23_batch *b, int nsteps, int itrecord)
     int nrec_new = 0;
     for (int k = 0; k < nsteps; ++k)
         if ((s0->it + k) % itrecord == 0) ++nrec_new;
-    bool any_rec = false;
-    for (auto *s : b->s)
+    bool any_rec = false, punch = false;
+    for (auto *s : b->s) {
         for (int c = 0; c < 5; ++c) any_rec = any_rec || s->nrec[c] > 0;
+        punch = punch || s->d_punch != nullptr;
+    }
     if (any_rec)
         for (auto *s : b->s) {
             const int rc = ensure_record_capacity(s, s->nrec_steps + nrec_new);
@@ -146,10 +148,10 @@ int batch_run_impl(fd23_batch *b, int nsteps, int itrecord)
     if ((rc = upload_shots<S, C>(b))) return rc;
     const int it0 = s0->it, par0 = s0->par, nrec0 = s0->nrec_steps;
     int pending = -1;
-    const long long key[6] = {it0, nsteps, itrecord * (any_rec ? 1 : -1), par0, nrec0, b->plan_ver};
+    const long long key[7] = {it0, nsteps, itrecord * (any_rec ? 1 : -1), par0, nrec0, b->plan_ver, punch};
     bool done = false;
     if (b->use_graph && nsteps >= 2) {
-        if (b->gexec && std::equal(key, key + 6, b->gkey)) {
+        if (b->gexec && std::equal(key, key + 7, b->gkey)) {
             // replay; the pending record row follows from the key
             int nr = nrec0;
             for (int k = 0; k < nsteps; ++k) pending = (any_rec && (it0 + k) % itrecord == 0) ? nr++ : -1;
@@ -158,14 +160,14 @@ int batch_run_impl(fd23_batch *b, int nsteps, int itrecord)
         } else {
             cudaGraph_t g = nullptr;
             if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-                const int lr = launch_steps<S, C>(b, it0, nsteps, itrecord, any_rec, par0, nrec0, &pending);
+                const int lr = launch_steps<S, C>(b, it0, nsteps, itrecord, any_rec, par0, nrec0, punch, &pending);
                 const cudaError_t ec = cudaStreamEndCapture(b->stream, &g);
                 cudaGraphExec_t ex = nullptr;
                 if (lr == FD23_OK && ec == cudaSuccess && g &&
                     cudaGraphInstantiate(&ex, g, 0) == cudaSuccess && cudaGraphLaunch(ex, b->stream) == cudaSuccess) {
                     if (b->gexec) cudaGraphExecDestroy(b->gexec);
                     b->gexec = ex;
-                    std::copy(key, key + 6, b->gkey);
+                    std::copy(key, key + 7, b->gkey);
                     done = true;
                 } else if (ex) {
                     cudaGraphExecDestroy(ex);
@@ -175,7 +177,8 @@ int batch_run_impl(fd23_batch *b, int nsteps, int itrecord)
             if (!done) cudaGetLastError();  // capture unavailable: launch directly
         }
     }
-    if (!done && (rc = launch_steps<S, C>(b, it0, nsteps, itrecord, any_rec, par0, nrec0, &pending))) return rc;
+    if (!done && (rc = launch_steps<S, C>(b, it0, nsteps, itrecord, any_rec, par0, nrec0, punch, &pending)))
+        return rc;
     const int par1 = (nsteps & 1) ? 1 - par0 : par0;
     int nrec1 = nrec0;
     for (int k = 0; k < nsteps; ++k)
@@ -253,6 +256,13 @@ int snapshot_restore(const std::vector<fd23_solver *> &ss, cudaStream_t st, cons
     }
     for (size_t i = 0; i < sn.copy.size(); ++i)
         CK(cudaMemcpyAsync(sn.live[i], sn.copy[i], sn.bytes[i], cudaMemcpyDeviceToDevice, st));
+    // the trial steps wrote the other set: with tile step windows the sweep
+    // relies on both sets agreeing on the tiles it leaves alone
+    for (auto *s : ss)
+        if (s->d_punch) {
+            const int rc = mirror_sets(s, st);
+            if (rc) return rc;
+        }
     CK(cudaStreamSynchronize(st));
     return FD23_OK;
 }
@@ -439,15 +449,17 @@ int fd23_batch_autotune(fd23_batch *b, int trial_steps, fd23_tune_entry *table, 
             default: return upload_shots<float, float>(b);
         }
     };
-    auto steps = [b](int k) -> int {
+    bool punch = false;
+    for (auto *s : b->s) punch = punch || s->d_punch != nullptr;
+    auto steps = [b, punch](int k) -> int {
         fd23_solver *s = b->s[0];
         int pend = -1;
         int r;
         switch (b->prec) {
-            case FD23_F64: r = launch_steps<double, double>(b, s->it, k, 1, false, s->par, 0, &pend); break;
-            case FD23_BF16: r = launch_steps<__nv_bfloat16, float>(b, s->it, k, 1, false, s->par, 0, &pend); break;
-            case FD23_F16: r = launch_steps<__half, float>(b, s->it, k, 1, false, s->par, 0, &pend); break;
-            default: r = launch_steps<float, float>(b, s->it, k, 1, false, s->par, 0, &pend);
+            case FD23_F64: r = launch_steps<double, double>(b, s->it, k, 1, false, s->par, 0, punch, &pend); break;
+            case FD23_BF16: r = launch_steps<__nv_bfloat16, float>(b, s->it, k, 1, false, s->par, 0, punch, &pend); break;
+            case FD23_F16: r = launch_steps<__half, float>(b, s->it, k, 1, false, s->par, 0, punch, &pend); break;
+            default: r = launch_steps<float, float>(b, s->it, k, 1, false, s->par, 0, punch, &pend);
         }
         if (r) return r;
         for (auto *x : b->s) {
@@ -487,6 +499,26 @@ int fd23_work_plan(int nshots, const int *nx, const int *nz, const int *npml, co
     }
     for (int c = 0; c <= plan.nblocks; ++c) off[c] = plan.off[c];
     return plan.nblocks;
+}
+
+int fd23_set_plan(fd23_solver *s, const fd23_tune_entry *tune)
+{
+    if (!s || !tune || !(tune->wx > 0) || !(tune->wz > 0) || tune->per_sm < 1 || !(tune->oversub >= 1.0) ||
+        tune->oversub > 64.0)
+        return FD23_ERR_ARG;
+    if (!s->fused) return FD23_ERR_UNSUPPORTED;
+    CK(cudaSetDevice(s->d.device));
+    CK(cudaStreamSynchronize(s->stream));  // the old work list may still be in use
+    s->tune = TuneParams{tune->wx, tune->wz, tune->per_sm, tune->oversub};
+    return build_worklist(s);
+}
+
+int fd23_get_plan(fd23_solver *s, fd23_tune_entry *cur, int *nblocks)
+{
+    if (!s) return FD23_ERR_ARG;
+    if (cur) *cur = fd23_tune_entry{s->tune.wx, s->tune.wz, s->tune.per_sm, s->tune.oversub, 0.0};
+    if (nblocks) *nblocks = s->nblocks;
+    return FD23_OK;
 }
 
 int fd23_autotune(fd23_solver *s, int trial_steps, fd23_tune_entry *table, int cap)

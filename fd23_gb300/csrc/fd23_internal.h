@@ -108,6 +108,29 @@ struct Box {
     const int2 *cells;  // ring position -> box-local (bi, bj)
 };
 
+// Step windows of the tiles of a shot (usepunch, PD/fd/cu_fd.cu:16-23,
+// PD/slide/cu_slide.cu): the cells of tile (ix / kPunchTX, iz / kPunchTZ)
+// are updated at step it only while first < it < last; outside that window
+// their stresses, velocities and memory variables keep their values.
+constexpr int kPunchTX = 32, kPunchTZ = 16;
+struct Punch {
+    const int2 *win;  // [nbz][nbx] (first, last); null: every cell is updated
+    int nbx, nbz;
+};
+FD23_HD inline bool punch_active(const Punch &p, int ix, int iz, int it)
+{
+    if (!p.win) return true;
+    const int2 w = p.win[(iz / kPunchTZ) * p.nbx + ix / kPunchTX];
+    return w.x < it && it < w.y;
+}
+// A tile whose cells were left alone at step it-1 and are left alone at
+// step it holds the same values in both ping-pong buffer sets, so the fused
+// sweep may skip it at step it.
+FD23_HD inline bool punch_steady(int2 w, int it)
+{
+    return !(w.x < it && it <= w.y && (long long)w.y - w.x >= 2);
+}
+
 // ---------------------------------------------------------------------------
 // Device-side description of one shot.  S = storage type of wavefields and
 // material, C = arithmetic type (also the type of memory variables, CPML
@@ -133,6 +156,7 @@ struct alignas(16) Shot {
     C *seis[5];
     const ShotMaps *maps;  // tensor maps of the fused sweep's copies (device memory)
     int cta0, ncta;     // CTAs of the launch working on this shot (receiver gather split)
+    Punch punch;        // tile step windows (punch.win == nullptr: none)
     Box<C> box;         // hybrid box (box.on == 0: none); last, the batched sweep never reads it
 };
 

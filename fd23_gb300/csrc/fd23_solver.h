@@ -67,6 +67,9 @@ struct fd23_solver {
     fd23::TuneParams tune;
     // hybrid box: residual field, box material, ring cells, incident field
     // of steps [box_inc_it0, box_inc_it0 + box_inc_n)
+    // usepunch tile step windows (device, [nbz][nbx] int2), null when off
+    int2 *d_punch = nullptr;
+    int punch_nbx = 0, punch_nbz = 0;
     bool box_on = false;
     int box_x0 = 0, box_z0 = 0, box_bx = 0, box_bz = 0, box_nsub = 0, box_nring = 0;
     void *box_r[5] = {};
@@ -92,6 +95,8 @@ int fused_per_sm(int device, int wave, int prec);
 int upload_plan(const WorkPlan &plan, WorkItem **d_items, int **d_off);
 int build_worklist(fd23_solver *s);
 int dispatch_step(fd23_solver *s, int rec_now);
+// copies buffer set `par` (wavefields, memory variables) into the other set
+int mirror_sets(fd23_solver *s, cudaStream_t st);
 
 template <class S, class C>
 Shot<S, C> make_shot(const fd23_solver *s)
@@ -122,6 +127,7 @@ Shot<S, C> make_shot(const fd23_solver *s)
     sh.maps = s->d_maps;
     sh.cta0 = 0;
     sh.ncta = s->nblocks > 0 ? s->nblocks : 1;
+    sh.punch = Punch{s->d_punch, s->punch_nbx, s->punch_nbz};
     sh.box.on = s->box_on ? 1 : 0;
     if (s->box_on) {
         sh.box.x0 = s->box_x0;

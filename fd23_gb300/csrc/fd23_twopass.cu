@@ -42,10 +42,11 @@ __device__ __forceinline__ long long psi_z_index(int ix, int iz, int nx, int nz,
 
 // ----------------------------- P-SV ---------------------------------------
 template <class S, class C>
-__global__ void __launch_bounds__(256) psv_stress_2p(Shot<S, C> s)
+__global__ void __launch_bounds__(256) psv_stress_2p(Shot<S, C> s, int it)
 {
     const int ix = blockIdx.x * 32 + threadIdx.x, iz = blockIdx.y * 8 + threadIdx.y;
     if (ix >= s.nx || iz >= s.nz) return;
+    if (!punch_active(s.punch, ix, iz, it)) return;  // outside the tile's step window
     const long long o = s.origin + (long long)iz * s.pitch + ix, P = s.pitch;
     const S *U = s.f[0][0], *W = s.f[0][1];
     S *Txx = s.f[0][2], *Txz = s.f[0][3], *Tzz = s.f[0][4];
@@ -107,10 +108,11 @@ __global__ void __launch_bounds__(256) psv_stress_2p(Shot<S, C> s)
 }
 
 template <class S, class C>
-__global__ void __launch_bounds__(256) psv_velocity_2p(Shot<S, C> s)
+__global__ void __launch_bounds__(256) psv_velocity_2p(Shot<S, C> s, int it)
 {
     const int ix = blockIdx.x * 32 + threadIdx.x, iz = blockIdx.y * 8 + threadIdx.y;
     if (ix >= s.nx || iz >= s.nz) return;
+    if (!punch_active(s.punch, ix, iz, it)) return;  // outside the tile's step window
     const long long o = s.origin + (long long)iz * s.pitch + ix, P = s.pitch;
     S *U = s.f[0][0], *W = s.f[0][1];
     const S *Txx = s.f[0][2], *Txz = s.f[0][3], *Tzz = s.f[0][4];
@@ -164,10 +166,11 @@ __global__ void __launch_bounds__(256) psv_velocity_2p(Shot<S, C> s)
 
 // ------------------------------ SH ----------------------------------------
 template <class S, class C>
-__global__ void __launch_bounds__(256) sh_stress_2p(Shot<S, C> s)
+__global__ void __launch_bounds__(256) sh_stress_2p(Shot<S, C> s, int it)
 {
     const int ix = blockIdx.x * 32 + threadIdx.x, iz = blockIdx.y * 8 + threadIdx.y;
     if (ix >= s.nx || iz >= s.nz) return;
+    if (!punch_active(s.punch, ix, iz, it)) return;  // outside the tile's step window
     // cells skipped by the reference, SH/fd/cu_fd.cu:140
     if (ix == 0 || ix >= s.nx - 1 || iz >= s.nz - 1) return;
     const long long o = s.origin + (long long)iz * s.pitch + ix, P = s.pitch;
@@ -208,10 +211,11 @@ __global__ void __launch_bounds__(256) sh_stress_2p(Shot<S, C> s)
 }
 
 template <class S, class C>
-__global__ void __launch_bounds__(256) sh_velocity_2p(Shot<S, C> s)
+__global__ void __launch_bounds__(256) sh_velocity_2p(Shot<S, C> s, int it)
 {
     const int ix = blockIdx.x * 32 + threadIdx.x, iz = blockIdx.y * 8 + threadIdx.y;
     if (ix >= s.nx || iz >= s.nz) return;
+    if (!punch_active(s.punch, ix, iz, it)) return;  // outside the tile's step window
     const long long o = s.origin + (long long)iz * s.pitch + ix, P = s.pitch;
     S *V = s.f[0][0];
     const S *Tx = s.f[0][1], *Tz = s.f[0][2];
@@ -249,7 +253,8 @@ __global__ void __launch_bounds__(256) sh_velocity_2p(Shot<S, C> s)
 
 // Point-source injection after the stress update (terms in order, one thread),
 // then for SH the free-surface stress image Tz(x,0) = -Tz(x,1) that the
-// reference applies at the top of its velocity kernel (SH/fd/cu_fd.cu:226).
+// reference applies at the top of its velocity kernel (SH/fd/cu_fd.cu:226),
+// so only in the tiles that kernel updates at this step.
 template <class S, class C>
 __global__ void post_stress_2p(Shot<S, C> s, int it, int sh_image)
 {
@@ -265,6 +270,7 @@ __global__ void post_stress_2p(Shot<S, C> s, int it, int sh_image)
         __syncthreads();
         S *Tz = s.f[0][2];
         for (int ix = threadIdx.x; ix < s.nx; ix += blockDim.x) {
+            if (!punch_active(s.punch, ix, 0, it)) continue;
             const long long o = s.origin + ix;
             Tz[o] = to_s<S>(-to_c<C>(Tz[o + s.pitch]));
         }
@@ -302,17 +308,17 @@ int launch_step_twopass(const Shot<S, C> &s, int wave, int it, cudaStream_t st)
 {
     const dim3 blk(32, 8), grd((s.nx + 31) / 32, (s.nz + 7) / 8);
     if (wave == FD23_PSV) {
-        psv_stress_2p<S, C><<<grd, blk, 0, st>>>(s);
+        psv_stress_2p<S, C><<<grd, blk, 0, st>>>(s, it);
         if (s.nterms > 0 && it < s.tamp_nt) post_stress_2p<S, C><<<1, 32, 0, st>>>(s, it, 0);
         if (s.box.on) {
             const int rc = launch_box_ring<S, C>(s, 0, 1, st);  // stresses, after the source
             if (rc) return rc;
         }
-        psv_velocity_2p<S, C><<<grd, blk, 0, st>>>(s);
+        psv_velocity_2p<S, C><<<grd, blk, 0, st>>>(s, it);
     } else {
-        sh_stress_2p<S, C><<<grd, blk, 0, st>>>(s);
+        sh_stress_2p<S, C><<<grd, blk, 0, st>>>(s, it);
         post_stress_2p<S, C><<<1, 256, 0, st>>>(s, it, 1);
-        sh_velocity_2p<S, C><<<grd, blk, 0, st>>>(s);
+        sh_velocity_2p<S, C><<<grd, blk, 0, st>>>(s, it);
     }
     return cudaPeekAtLastError() == cudaSuccess ? FD23_OK : FD23_ERR_CUDA;
 }

@@ -195,7 +195,9 @@ int fd23_set_state(fd23_solver *s, const void *buf, size_t bytes, int it0);
  *   Copied to the device before the call returns.  fd23_run fails with
  *   FD23_ERR_ORDER for a step it does not cover.
  * fd23_get_box_state / fd23_set_box_state: r as U W Txx Txz Tzz, bx*bz each,
- *   compute type (fd23_box_state_bytes). */
+ *   compute type (fd23_box_state_bytes).
+ * A box and tile step windows (fd23_set_punch) exclude each other:
+ *   FD23_ERR_UNSUPPORTED. */
 int fd23_set_box(fd23_solver *s, int x0, int z0, int bx, int bz, const double *bmat);
 int fd23_set_box_incident(fd23_solver *s, const void *inc, int it0, int nsteps);
 size_t fd23_box_state_bytes(fd23_solver *s);
@@ -260,6 +262,11 @@ typedef struct {
 int fd23_autotune(fd23_solver *s, int trial_steps, fd23_tune_entry *table, int cap);
 int fd23_batch_autotune(fd23_batch *b, int trial_steps, fd23_tune_entry *table, int cap);
 int fd23_batch_get_plan(fd23_batch *b, fd23_tune_entry *current, int *nblocks);
+/* fd23_set_plan installs a plan without timing it (ms_per_step ignored;
+ * per_sm is capped at the residency the device reports; oversub in
+ * [1, 64]); fd23_get_plan reports the current one and its CTA count. */
+int fd23_set_plan(fd23_solver *s, const fd23_tune_entry *tune);
+int fd23_get_plan(fd23_solver *s, fd23_tune_entry *current, int *nblocks);
 /* The work plan for nshots grids under the given parameters (host only, for
  * inspection and tests): items receives 4 ints per item (shot, x0, z0, z1:
  * 120 columns from x0, rows [z0, z1)), off[c] .. off[c+1] indexes the items of
@@ -297,6 +304,33 @@ int fd23_debug_expire_wait(fd23_solver *s);
  * Runs on `stream` (a cudaStream_t, NULL = default) and waits for it. */
 int fd23_sum_squares_noalloc(int prec, const void *const *fields, int nfields, size_t n,
                              void *stream, double *sum, int *nonfinite);
+
+/* ---- usepunch: tile step windows ----
+ * Replaces the SLIDE object (PD/slide/slide.h:4-13, PD/slide/cu_slide.cu:6-66)
+ * and its test in the sweep kernels (PD/fd/cu_fd.cu:16-23, called at :249
+ * and :404; SH/fd/cu_fd.cu:106,206).  The grid is cut into tiles of 32
+ * columns x 16 rows, nbx = ceil(nx/32) by nbz = ceil(nz/16)
+ * (fd23_punch_tiles); the reference requires whole tiles.  The cells of
+ * tile (ix/32, iz/16) are updated at step it (0-based, counted across
+ * restarts as PN/main.cpp:115-117) only while first < it < last; otherwise
+ * their stresses, velocities and memory variables keep their values.  Point
+ * sources and receivers act as without windows.
+ * fd23_punch_windows: first = int((tmin - before)/dt), last = int((tmax +
+ *   after)/dt) per tile from travel times t[nz][nx] (tmin, tmax over the
+ *   tile); elem_bytes 8 = double times and arithmetic (PD), 4 = float (PN,
+ *   SH).  The conversion to int saturates; NaN gives 0.
+ * fd23_read_punch: the same from a raw travel-time file (the reference's
+ *   `timefile`, nx*nz values of elem_bytes each).
+ * fd23_set_punch: installs windows [nbz][nbx] (first, last); both NULL
+ *   removes them.  Works with both sweeps and in batches;
+ *   FD23_ERR_UNSUPPORTED with a hybrid box.  The fused sweep skips tiles
+ *   left alone at this step and the last (and without a live source term). */
+int fd23_punch_tiles(int nx, int nz, int *nbx, int *nbz);
+int fd23_punch_windows(const void *times, int elem_bytes, int nx, int nz, double before, double after,
+                       double dt, int *first, int *last);
+int fd23_read_punch(const char *timefile, int elem_bytes, int nx, int nz, double before, double after, double dt,
+                    int *first, int *last);
+int fd23_set_punch(fd23_solver *s, const int *first, const int *last, int nbx, int nbz);
 
 /* ---- model and station input (host only) ----
  * fd23_read_model: a ".mdl" polygon model (BACK / POLY / DEF commands,

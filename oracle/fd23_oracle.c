@@ -572,6 +572,32 @@ int or_box_material(int nx, int nz, double *mat, int x0, int z0, int bx, int bz,
 /* ------------------------------------------------------------------------- */
 /* Time stepping, instantiated for double and float.                         */
 /* ------------------------------------------------------------------------- */
+/* ---- usepunch: tile step windows ----
+ * PD/slide/cu_slide.cu:6-66 turns a travel-time file into per-tile steps
+ * first = int((tmin - before)/dt), last = int((tmax + after)/dt) over tiles of
+ * BDIMX x BDIMY = 32 x 16 cells (PD/param/const.h:20-21); the sweep kernels
+ * return at once for a cell whose tile has it <= first or it >= last
+ * (CHECK_IF_NEED_UPDATE, PD/fd/cu_fd.cu:16-23, at :249 and :404).  The
+ * windows are installed for the next runs by or_set_punch (NULL: none);
+ * tiles are counted ceil(nx/32) per row. */
+static const int *or_pfirst = NULL, *or_plast = NULL;
+static int or_pnbx = 0;
+
+void or_set_punch(const int *first, const int *last, int nbx)
+{
+    or_pfirst = first;
+    or_plast = last;
+    or_pnbx = nbx;
+}
+
+static inline int or_punch_skip(int nx, int ix, int iz, int it)
+{
+    (void)nx;
+    if (!or_pfirst) return 0;
+    const long t = (long)(iz / 16) * or_pnbx + ix / 32;
+    return it <= or_pfirst[t] || it >= or_plast[t];
+}
+
 #define REAL double
 #define FMA fma
 #define SFX f64

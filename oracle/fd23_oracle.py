@@ -46,6 +46,8 @@ def lib():
         for nm in ("or_sh_run_f64", "or_sh_run_f32"):
             getattr(_lib, nm).argtypes = [i, i, i, i, vp, vp, i, vp, vp, vp, i, i, vp,
                                           i, i, i, vp, vp, i]
+        _lib.or_set_punch.argtypes = [vp, vp, i]
+        _lib.or_set_punch.restype = None
         _lib.or_box_ring_count.argtypes = [i, i, vp, vp]
         _lib.or_box_rings.argtypes = [i, i, i, i, i, vp, vp, vp, vp]
         _lib.or_box_incident_from_displacement.argtypes = [i, i, d, vp, vp, vp, vp, vp, vp]
@@ -266,12 +268,32 @@ def sh_state_size(nx, nz, npml):
     return 3 * nx * nz + 2 * 2 * npml * nz + 2 * 2 * npml * nx
 
 
+class _Punch:
+    """Installs tile step windows (first, last) in the C oracle for the
+    duration of a run (None: no windows)."""
+
+    def __init__(self, nx, punch):
+        self.w = None
+        if punch is not None:
+            f, l = punch
+            self.w = (np.ascontiguousarray(f, dtype=np.int32), np.ascontiguousarray(l, dtype=np.int32))
+            self.nbx = (nx + 31) // 32
+
+    def __enter__(self):
+        if self.w is not None:
+            lib().or_set_punch(_p(self.w[0]), _p(self.w[1]), self.nbx)
+
+    def __exit__(self, *a):
+        lib().or_set_punch(None, None, 0)
+
+
 def psv_run(prec, nx, nz, npml, topabsorb, mat, bck, terms, rec_u, rec_w, nt, itrecord=1, it0=0,
-            state=None, nthreads=0):
+            state=None, nthreads=0, punch=None):
     """Run nt steps of the P-SV oracle.  prec 'f64' or 'f32'.  mat (5,nz,nx)
     and bck (3, 4nx+4nz) FP64 arrays are rounded to prec.  terms = (field,
     idx, amp[nterms, nt_amp]) with absolute step indexing.  rec_* = flat
-    indices.  Returns (seis_u, seis_w, state)."""
+    indices.  punch = tile step windows (first, last), [nbz*nbx] each, or
+    None.  Returns (seis_u, seis_w, state)."""
     dt_ = np.float64 if prec == "f64" else np.float32
     fn = lib().or_psv_run_f64 if prec == "f64" else lib().or_psv_run_f32
     mat_r = np.ascontiguousarray(mat, dtype=dt_)
@@ -290,14 +312,15 @@ def psv_run(prec, nx, nz, npml, topabsorb, mat, bck, terms, rec_u, rec_w, nt, it
     su = np.zeros((nrecs, len(ru)), dtype=dt_)
     sw = np.zeros((nrecs, len(rw)), dtype=dt_)
     nt_amp = amp_r.shape[1] if amp_r.ndim == 2 and len(field) else 0
-    fn(nx, nz, npml, int(topabsorb), _p(mat_r), _p(bck_r), len(field), _p(field), _p(idx),
-       _p(amp_r) if len(field) else None, nt_amp, len(ru), _p(ru), len(rw), _p(rw), it0, nt,
-       itrecord, _p(state), _p(su), _p(sw), nthreads)
+    with _Punch(nx, punch):
+        fn(nx, nz, npml, int(topabsorb), _p(mat_r), _p(bck_r), len(field), _p(field), _p(idx),
+           _p(amp_r) if len(field) else None, nt_amp, len(ru), _p(ru), len(rw), _p(rw), it0, nt,
+           itrecord, _p(state), _p(su), _p(sw), nthreads)
     return su, sw, state
 
 
 def sh_run(prec, nx, nz, npml, topabsorb, mat, bck, terms, rec, nt, itrecord=1, it0=0, state=None,
-           nthreads=0):
+           nthreads=0, punch=None):
     dt_ = np.float64 if prec == "f64" else np.float32
     fn = lib().or_sh_run_f64 if prec == "f64" else lib().or_sh_run_f32
     mat_r = np.ascontiguousarray(mat, dtype=dt_)
@@ -314,10 +337,45 @@ def sh_run(prec, nx, nz, npml, topabsorb, mat, bck, terms, rec, nt, itrecord=1, 
     nrecs = len([it for it in range(it0, it0 + nt) if it % itrecord == 0])
     s = np.zeros((nrecs, len(r)), dtype=dt_)
     nt_amp = amp_r.shape[1] if amp_r.ndim == 2 and len(field) else 0
-    fn(nx, nz, npml, int(topabsorb), _p(mat_r), _p(bck_r), len(field), _p(field), _p(idx),
-       _p(amp_r) if len(field) else None, nt_amp, len(r), _p(r), it0, nt, itrecord, _p(state),
-       _p(s), nthreads)
+    with _Punch(nx, punch):
+        fn(nx, nz, npml, int(topabsorb), _p(mat_r), _p(bck_r), len(field), _p(field), _p(idx),
+           _p(amp_r) if len(field) else None, nt_amp, len(r), _p(r), it0, nt, itrecord, _p(state),
+           _p(s), nthreads)
     return s, state
+
+
+def punch_windows(times, before, after, dt, elem="f64"):
+    """Tile step windows from travel times t[nz, nx], restating the SLIDE
+    constructor (PD/slide/cu_slide.cu:23-55): over tiles of 32 columns x 16
+    rows, first = int((tmin - before)/dt), last = int((tmax + after)/dt).
+    elem 'f64': double times and arithmetic (PD); 'f32': float (PN/SH,
+    PN/slide/cu_slide.cu:10-12).  min/max start from +/-1e28 and skip NaN;
+    edge tiles of grids that are not whole tiles cover the cells they have;
+    the int conversion truncates and saturates (NaN gives 0).
+    Returns (first, last), int32 [nbz*nbx]."""
+    T = np.float64 if elem == "f64" else np.float32
+    t = np.asarray(times, dtype=T)
+    nz, nx = t.shape
+    nbx, nbz = (nx + 31) // 32, (nz + 15) // 16
+    lo = np.full((nbz * 16, nbx * 32), np.inf, dtype=T)
+    hi = np.full((nbz * 16, nbx * 32), -np.inf, dtype=T)
+    lo[:nz, :nx] = t
+    hi[:nz, :nx] = t
+    lo = np.fmin.reduce(np.fmin.reduce(lo.reshape(nbz, 16, nbx, 32), axis=3), axis=1)
+    hi = np.fmax.reduce(np.fmax.reduce(hi.reshape(nbz, 16, nbx, 32), axis=3), axis=1)
+    lo = np.fmin(lo, T(1e28))
+    hi = np.fmax(hi, T(-1e28))
+    with np.errstate(all="ignore"):
+        a = (lo - T(before)) / T(dt)
+        b = (hi + T(after)) / T(dt)
+
+    def to_int(v):
+        v = v.astype(np.float64)  # exact for float32 and for the comparisons
+        out = np.where(np.isnan(v), 0.0, np.trunc(v))
+        out = np.clip(out, -2147483648.0, 2147483647.0)
+        return out.astype(np.int64).astype(np.int32).ravel()
+
+    return to_int(a), to_int(b)
 
 
 # ---------------------------------------------------------------- hybrid box

@@ -61,16 +61,23 @@ class Case:
         self.rz = np.clip(self.rz, 0, nz - 1)
         self.rec = self.rx + self.rz * nx
 
-    def oracle(self, prec, nt=None, itrecord=1, it0=0, state=None):
+    def oracle(self, prec, nt=None, itrecord=1, it0=0, state=None, punch=None):
         nt = self.nt if nt is None else nt
         if self.wave == "psv":
             su, sw, st = O.psv_run(prec, self.nx, self.nz, self.npml, self.topabsorb, self.mat,
                                    self.bck, self.terms, self.rec, self.rec, nt, itrecord, it0,
-                                   state)
+                                   state, punch=punch)
             return [su, sw], st
         s, st = O.sh_run(prec, self.nx, self.nz, self.npml, self.topabsorb, self.mat, self.bck,
-                         self.terms, self.rec, nt, itrecord, it0, state)
+                         self.terms, self.rec, nt, itrecord, it0, state, punch=punch)
         return [s], st
+
+    def straight_times(self, vmax=None):
+        """Travel times t[nz, nx] along straight rays from the source at the
+        fastest velocity of the model: never later than the first arrival."""
+        vmax = float(self.vp.max() if self.wave == "psv" else self.vs.max()) if vmax is None else vmax
+        zz, xx = np.mgrid[0:self.nz, 0:self.nx]
+        return np.hypot(xx - self.xs, zz - self.zs) * self.h / vmax
 
     def solver(self, prec, kernel="auto"):
         import fd23_gb300 as F

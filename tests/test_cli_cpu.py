@@ -135,6 +135,26 @@ def test_cli_errors(tmp_path):
     assert r.returncode == 1
 
 
+def test_cli_usepunch_windows(tmp_path):
+    """usepunch=1 reads the float travel-time file (double with prec=f64) and
+    builds the windows of PN/slide/cu_slide.cu (checked against the oracle)."""
+    (tmp_path / "run.par").write_text(PAR)
+    rng = np.random.default_rng(9)
+    t = rng.uniform(0.05, 2.0, size=(90, 120))
+    t.astype(np.float32).tofile(str(tmp_path / "tt32"))
+    t.tofile(str(tmp_path / "tt64"))
+    for prec, name, elem in (("f32", "tt32", "f32"), ("f64", "tt64", "f64")):
+        r = _cli(tmp_path, "par=run.par", "usepunch=1", "before=0.1", "after=0.3", "timefile=" + name,
+                 "prec=" + prec, "dryrun=1")
+        assert r.returncode == 0, r.stderr
+        d = json.loads(r.stdout)
+        first, _ = O.punch_windows(t.astype(np.float32) if elem == "f32" else t, 0.1, 0.3, 0.01, elem)
+        assert d["punch_tiles"] == len(first) == 4 * 6
+        assert d["punch_first_min"] == first.min()
+    r = _cli(tmp_path, "par=run.par", "usepunch=1", "before=0.1", "after=0.3", "timefile=none", "dryrun=1")
+    assert r.returncode == 1 and "timefile" in r.stderr
+
+
 SH_PAR = """nx=200 nz=100 nt=20 h=10 dt=0.001
 sourcetime=Gaussian alpha=-5
 strike=0 dip=90 rake=0 azimuth=45

@@ -69,7 +69,7 @@ def box_ok(x, y, z, w, nf, pitch, rows, nfields, es):
     assert w <= 256 and nf <= 256
 
 
-def audit(nx, nz, es, wave, per_sm=3, oversub=1.0, ctas=None):
+def audit(nx, nz, es, wave, per_sm=3, oversub=1.0, ctas=None, narrowed=False):
     pitch, rows, origin = layout(nx, nz)
     npml = min(40, nx // 2, nz // 2)
     elems = pitch * rows
@@ -88,7 +88,7 @@ def audit(nx, nz, es, wave, per_sm=3, oversub=1.0, ctas=None):
         ctas = worklist(nx, nz, npml, oversub, per_sm)
     covered = set()
     for items in ctas:
-        assert 1 <= len(items) <= MAX_ITEMS
+        assert (0 if narrowed else 1) <= len(items) <= MAX_ITEMS
         for (x0, z0, z1) in items:
             for zb in range(z0 // 4, z1 // 4):
                 key = (x0, zb)
@@ -177,3 +177,46 @@ def test_batch_plan_in_bounds():
             if (wx, wz, ov) == (4.0, 3.0, 1.0):
                 for k, c in per_shot.items():
                     audit(grids[k][0], grids[k][1], 4, "psv", ctas=c)
+
+
+def narrow(nx, nz, items, first, last, it, terms=()):
+    """The item narrowing of the sweep with tile step windows (the PUNCH
+    prologue of fused_step), restated: keep the rows from the first to the
+    last tile row with a tile that is not steady at step it (or holds a
+    source term, while it <= the source length), drop empty items."""
+    nbx = (nx + 31) // 32
+
+    def steady(t):
+        f, l = int(first[t]), int(last[t])
+        return not (f < it <= l and l - f >= 2)
+
+    out = []
+    for (x0, z0, z1) in items:
+        rows = [tz for tz in range(z0 // 16, (min(z1, nz) - 1) // 16 + 1)
+                if any(not steady(tz * nbx + tx) for tx in range(x0 // 32, (min(x0 + TX, nx) - 1) // 32 + 1))]
+        rows += [tz // 16 for (tx, tz) in terms if x0 <= tx < x0 + TX and z0 <= tz < z1]
+        if not rows:
+            continue
+        a, b = max(z0, min(rows) * 16), min(z1, (max(rows) + 1) * 16)
+        assert z0 <= a < b <= z1 and a % 4 == 0 and b % 4 == 0
+        out.append((x0, a, b))
+    return out
+
+
+@pytest.mark.parametrize("nx,nz", [(230, 150), (256, 160), (700, 380), (2000, 1000), (4000, 2000)])
+@pytest.mark.parametrize("es,wave", [(4, "psv"), (8, "psv"), (2, "sh")])
+def test_narrowed_items_in_bounds(nx, nz, es, wave):
+    """Items narrowed by random tile step windows keep every address of the
+    audit in bounds (they are sub-ranges of plan items on 4-row blocks)."""
+    import numpy as np
+    rng = np.random.default_rng(nx + nz + es)
+    nb = ((nx + 31) // 32) * ((nz + 15) // 16)
+    first = rng.integers(-3, 60, size=nb)
+    last = first + rng.integers(-2, 80, size=nb)
+    npml = min(40, nx // 2, nz // 2)
+    per_sm = {8: 1, 4: 3, 2: 2}[es]
+    for ov in (1.0, 3.0):
+        ctas = worklist(nx, nz, npml, ov, per_sm)
+        for it in (0, 7, 31, 90):
+            nar = [narrow(nx, nz, items, first, last, it, terms=[(nx // 2, nz // 3)]) for items in ctas]
+            audit(nx, nz, es, wave, per_sm=per_sm, ctas=nar, narrowed=True)

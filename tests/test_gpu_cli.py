@@ -110,6 +110,32 @@ def test_cli_restart(tmp_path):
     np.testing.assert_array_equal(second, full[30:])
 
 
+def test_cli_usepunch_equals_api(tmp_path):
+    """usepunch=1 in the program = the API run with the same windows."""
+    _setup(tmp_path)
+    nt = 60
+    zz, xx = np.mgrid[0:100, 0:150]
+    t = (np.hypot(xx - 75, zz - 20) * 0.3 / 65.0).astype(np.float32)  # windows close within the run
+    t.tofile(str(tmp_path / "tt"))
+    _cli(tmp_path, "nt=%d" % nt, "output=pun", "usepunch=1", "before=0.05", "after=0.2", "timefile=tt")
+    first, last = F.read_punch(str(tmp_path / "tt"), 150, 100, 0.05, 0.2, float(np.float32(0.01)), "f32")
+    assert last.min() < nt  # some tiles close again within the run
+    vp, vs, den = F.read_model(str(tmp_path / "layers.mdl"), 150, 100, np.float32(0.3))
+    s = F.Solver("psv", 150, 100, 12, float(np.float32(0.3)), float(np.float32(0.01)), prec="f32", pml_dt=0.005,
+                 pml_v=30.0, pml_r=1e-11, pml_fc=2.0)
+    s.set_model(vp, vs, den)
+    s.set_source(F.SRC_MOMENT, 75, 20, F.moment_psv(0, 20, 90, 45), F.wavelet_gaussian(float(np.float32(0.01)), -5),
+                 nt)
+    rx, rz = F.receivers_file(str(tmp_path / "st"))
+    s.set_receivers(0, rx, rz)
+    s.set_punch(first, last)
+    s.run(nt, 1)
+    want = s.seismograms(0)
+    s.close()
+    got = np.fromfile(str(tmp_path / "pun_U"), dtype=np.float32).reshape(nt, len(rx))
+    np.testing.assert_array_equal(got, want)
+
+
 @pytest.mark.parametrize("stype", [3, 2])
 def test_sh_program_equals_api(tmp_path, stype):
     _setup(tmp_path)
