@@ -176,6 +176,13 @@ def _i32(a):
     return _np.ascontiguousarray(a, dtype=_np.int32)
 
 
+def _sized(a, n, what):
+    """a as a contiguous array of exactly n elements (the C side reads n)."""
+    if a.size != n:
+        raise ValueError("%s: %d elements, expected %d" % (what, a.size, n))
+    return a
+
+
 def _check(rc, where):
     if rc < 0:
         raise Fd23Error(rc, where)
@@ -464,6 +471,7 @@ class Solver:
         self.dtype = _np.float64 if self.prec == F64 else _np.float32
         self.nfields = 5 if self.wave == PSV else 3
         self._nrec = {}
+        self._box = None
 
     def close(self):
         if self._h:
@@ -485,16 +493,22 @@ class Solver:
     # -- inputs --
     def set_model(self, vp, vs, den):
         stab = _C.c_double(0.0)
-        _check(lib().fd23_set_model(self._h, _p(_f64(vp)) if vp is not None else None,
-                                    _p(_f64(vs)), _p(_f64(den)),
+        n = self.nx * self.nz
+        vp = _sized(_f64(vp), n, "vp") if vp is not None else None
+        vs, den = _sized(_f64(vs), n, "vs"), _sized(_f64(den), n, "den")
+        _check(lib().fd23_set_model(self._h, _p(vp), _p(vs), _p(den),
                                     _C.cast(_C.pointer(stab), _C.c_void_p)), "fd23_set_model")
         return stab.value
 
     def set_material(self, mat):
-        _check(lib().fd23_set_material(self._h, _p(_f64(mat))), "fd23_set_material")
+        nm = 5 if self.wave == PSV else 3
+        _check(lib().fd23_set_material(self._h, _p(_sized(_f64(mat), nm * self.nx * self.nz, "mat"))),
+               "fd23_set_material")
 
     def set_cpml(self, bck):
-        _check(lib().fd23_set_cpml(self._h, _p(_f64(bck))), "fd23_set_cpml")
+        per = 4 if self.wave == PSV else 2
+        n = 3 * per * (self.nx + self.nz)
+        _check(lib().fd23_set_cpml(self._h, _p(_sized(_f64(bck), n, "bck"))), "fd23_set_cpml")
 
     def set_source(self, kind, xs, zs, moment, src, nt_max):
         src = _f64(src)
@@ -505,12 +519,16 @@ class Solver:
     def set_source_terms(self, field, ix, iz, amp):
         amp = _f64(amp)
         n = len(field)
+        if len(ix) != n or len(iz) != n or (n and (amp.ndim != 2 or amp.shape[0] != n)):
+            raise ValueError("set_source_terms: field, ix, iz and amp rows must agree")
         _check(lib().fd23_set_source_terms(self._h, n, _p(_i32(field)), _p(_i32(ix)),
                                            _p(_i32(iz)), _p(amp), amp.shape[1] if n else 0),
                "fd23_set_source_terms")
 
     def set_receivers(self, field, rx, rz):
         rx, rz = _i32(rx), _i32(rz)
+        if rx.size != rz.size:
+            raise ValueError("set_receivers: rx and rz differ in length")
         _check(lib().fd23_set_receivers(self._h, field, _p(rx), _p(rz), len(rx)),
                "fd23_set_receivers")
         self._nrec[field] = len(rx)
@@ -599,14 +617,19 @@ class Solver:
     def set_box(self, x0, z0, bx, bz, bmat=None):
         """Box [x0, x0+bx) x [z0, z0+bz); bmat (5, bz, bx) dt/h-scaled or None
         for the cut of the grid material.  bx = bz = 0 removes it."""
-        _check(lib().fd23_set_box(self._h, x0, z0, bx, bz, _p(_f64(bmat)) if bmat is not None else None),
-               "fd23_set_box")
+        if bmat is not None:
+            bmat = _sized(_f64(bmat), 5 * max(bx, 0) * max(bz, 0), "bmat")
+        _check(lib().fd23_set_box(self._h, x0, z0, bx, bz, _p(bmat)), "fd23_set_box")
         self._box = (x0, z0, bx, bz) if bx else None
 
     def set_box_incident(self, inc, it0=0):
         """inc [nsteps, 5, nring] (U W Txx Txz Tzz on the ring cells) for steps
         it0 .. it0+nsteps-1."""
         a = _np.ascontiguousarray(inc, dtype=self.dtype)
+        if self._box is not None:
+            nring = sum(box_ring_size(self._box[2], self._box[3]))
+            if a.ndim != 3 or a.shape[1:] != (5, nring):
+                raise ValueError("set_box_incident: shape %s, expected (nsteps, 5, %d)" % (a.shape, nring))
         _check(lib().fd23_set_box_incident(self._h, _p(a), it0, a.shape[0] if a.ndim == 3 else 0),
                "fd23_set_box_incident")
 

@@ -173,3 +173,21 @@ def test_box_argument_errors():
         b16.set_box(10, 10, 40, 30)
     assert e.value.status == F.ERR_UNSUPPORTED
     b16.close()
+
+
+def test_array_size_checks():
+    """Host arrays of the wrong size are refused before the C side reads them."""
+    c = Case("psv", 120, 90, npml=10, nt=10)
+    s = _solver(c, "f32", "fused")
+    with pytest.raises(ValueError):
+        s.set_model(c.vp[:45], c.vs, c.den)
+    with pytest.raises(ValueError):
+        s.set_material(c.mat[:3])
+    with pytest.raises(ValueError):
+        s.set_receivers(0, c.rx, c.rz[:-1])
+    with pytest.raises(ValueError):
+        s.set_box(10, 10, 40, 30, np.zeros((5, 30, 39)))
+    s.set_box(10, 10, 40, 30)
+    with pytest.raises(ValueError):
+        s.set_box_incident(np.zeros((2, 5, 7), np.float32), 0)
+    s.close()
