@@ -56,6 +56,7 @@ ABI_FUNCTIONS = [
     "fd23_batch_get_stream", "fd23_batch_set_graph", "fd23_autotune", "fd23_batch_autotune",
     "fd23_batch_get_plan", "fd23_work_plan", "fd23_read_model", "fd23_read_stations",
     "fd23_debug_expire_wait", "fd23_set_plan", "fd23_get_plan", "fd23_punch_tiles", "fd23_punch_windows", "fd23_read_punch", "fd23_set_punch",
+    "fd23_set_material_table",
 ]
 
 
@@ -155,6 +156,7 @@ def lib():
         "fd23_punch_windows": ([vp, i, i, i, d, d, d, vp, vp], i),
         "fd23_read_punch": ([_C.c_char_p, i, i, i, d, d, d, vp, vp], i),
         "fd23_set_punch": ([vp, vp, vp, i, i], i),
+        "fd23_set_material_table": ([vp, i], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -598,6 +600,13 @@ class Solver:
         d = e.as_dict()
         d["nblocks"] = nb.value
         return d
+
+    # -- material table --
+    def set_material_table(self, on=True):
+        """Index + table form of the material (mktable): returns the number of
+        table entries; raises Fd23Error (ERR_UNSUPPORTED) with more than 255
+        distinct material tuples."""
+        return _check(lib().fd23_set_material_table(self._h, 1 if on else 0), "fd23_set_material_table")
 
     # -- usepunch --
     def set_punch(self, first, last):

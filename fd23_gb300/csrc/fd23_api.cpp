@@ -261,6 +261,18 @@ int encode_maps(fd23_solver *s)
     }
     if (!rc) rc = make(h.ms, s->mat_block, s->nmat, bx.pww, bx.nms);
     if (!rc) rc = make(h.mv, s->mat_block, s->nmat, bx.pww, bx.nmv);
+    if (!rc && s->d_midx) {
+        // material-table indices: bytes, [row][column] of the padded layout
+        const cuuint64_t dims[2] = {(cuuint64_t)L.pitch, (cuuint64_t)L.rows};
+        const cuuint64_t strides[1] = {(cuuint64_t)L.pitch};
+        const cuuint32_t box[2] = {(cuuint32_t)kIdxBoxW, 8u};
+        const cuuint32_t estr[2] = {1u, 1u};
+        const CUresult r = encode(reinterpret_cast<CUtensorMap *>(&h.idx), CU_TENSOR_MAP_DATA_TYPE_UINT8, 2,
+                                  s->d_midx, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                  CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        rc = r == CUDA_SUCCESS ? FD23_OK : FD23_ERR_CUDA;
+    }
     if (rc) return rc;
     if (!s->d_maps && (rc = dev_alloc((void **)&s->d_maps, sizeof(ShotMaps)))) return rc;
     CK(cudaMemcpy(s->d_maps, &h, sizeof(ShotMaps), cudaMemcpyHostToDevice));
@@ -366,6 +378,8 @@ void free_all(fd23_solver *s)
     cudaFree(s->mat_block);
     cudaFree(s->d_maps);
     cudaFree(s->d_punch);
+    cudaFree(s->d_midx);
+    cudaFree(s->d_mtab);
     cudaFree(s->cpml);
     cudaFree(s->err_flag);
     cudaFree(s->norm_buf);
@@ -601,6 +615,18 @@ int fd23_set_material(fd23_solver *s, const double *matv)
         CK(cudaStreamSynchronize(s->stream));
     }
     s->have_material = true;
+    if (s->table_on) {
+        // the table follows the material; with too many distinct tuples it
+        // is dropped (as the reference's mktable gives up) and the sweep
+        // reads the material arrays
+        const int rc = build_material_table(s);
+        if (rc == FD23_ERR_UNSUPPORTED) {
+            free_material_table(s);
+            s->table_on = false;
+            return s->fused ? encode_maps(s) : FD23_OK;
+        }
+        if (rc) return rc;
+    }
     return FD23_OK;
 }
 
@@ -919,7 +945,7 @@ int fd23_set_box(fd23_solver *s, int x0, int z0, int bx, int bz, const double *b
         free_box(s);
         return FD23_OK;
     }
-    if (s->d.wave != FD23_PSV || scaled_form(s) || s->d_punch) return FD23_ERR_UNSUPPORTED;
+    if (s->d.wave != FD23_PSV || scaled_form(s) || s->d_punch || s->table_on) return FD23_ERR_UNSUPPORTED;
     if (bx < kBoxMin || bz < kBoxMin || x0 < 0 || z0 < 0 || x0 + bx > s->d.nx || z0 + bz > s->d.nz)
         return FD23_ERR_ARG;
     if (!bmat && !s->have_material) return FD23_ERR_ORDER;

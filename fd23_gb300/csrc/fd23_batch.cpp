@@ -109,7 +109,7 @@ int launch_steps(fd23_batch *b, int it0, int nsteps, int itrecord, bool any_rec,
     for (int k = 0; k < nsteps; ++k) {
         const int it = it0 + k;
         const int rc = launch_step_fused_batch<S, C>(shots, b->wave, b->d_items, b->d_off, b->plan.nblocks, par,
-                                                     it, pend, b->err_flag, punch, b->stream);
+                                                     it, pend, b->err_flag, punch, b->s[0]->table_on, b->stream);
         if (rc) return rc;
         pend = (any_rec && it % itrecord == 0) ? nrec++ : -1;
         par = 1 - par;
@@ -137,6 +137,7 @@ int batch_run_impl(fd23_batch *b, int nsteps, int itrecord)
     for (auto *s : b->s) {
         for (int c = 0; c < 5; ++c) any_rec = any_rec || s->nrec[c] > 0;
         punch = punch || s->d_punch != nullptr;
+        if (s->table_on != s0->table_on) return FD23_ERR_UNSUPPORTED;  // tables in all shots or none
     }
     if (any_rec)
         for (auto *s : b->s) {
@@ -148,7 +149,8 @@ int batch_run_impl(fd23_batch *b, int nsteps, int itrecord)
     if ((rc = upload_shots<S, C>(b))) return rc;
     const int it0 = s0->it, par0 = s0->par, nrec0 = s0->nrec_steps;
     int pending = -1;
-    const long long key[7] = {it0, nsteps, itrecord * (any_rec ? 1 : -1), par0, nrec0, b->plan_ver, punch};
+    const long long key[7] = {it0, nsteps, itrecord * (any_rec ? 1 : -1), par0, nrec0, b->plan_ver,
+                              (long long)punch + 2 * (long long)s0->table_on};
     bool done = false;
     if (b->use_graph && nsteps >= 2) {
         if (b->gexec && std::equal(key, key + 7, b->gkey)) {
@@ -434,6 +436,7 @@ int fd23_batch_autotune(fd23_batch *b, int trial_steps, fd23_tune_entry *table, 
     for (auto *s : b->s) {
         if (!s->have_material) return FD23_ERR_ORDER;
         if (s->it != s0->it || s->par != s0->par || s->pending_rec >= 0) return FD23_ERR_ORDER;
+        if (s->table_on != s0->table_on) return FD23_ERR_UNSUPPORTED;  // tables in all shots or none
         const int rc = ensure_sigma(s);
         if (rc) return rc;
     }

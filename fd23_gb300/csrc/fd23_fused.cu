@@ -62,6 +62,11 @@ template <class S, class C>
 int launch_step_fused(const Shot<S, C> &s, int wave, const WorkItem *items, const int *item_off,
                       int nblocks, int par, int it, int rec_index, int *err_flag, cudaStream_t st)
 {
+    if (s.midx)
+        return s.punch.win ? launch_step_fused_table_punch<S, C>(s, nullptr, wave, items, item_off, nblocks, par, it,
+                                                                 rec_index, err_flag, st)
+                           : launch_step_fused_table<S, C>(s, nullptr, wave, items, item_off, nblocks, par, it,
+                                                           rec_index, err_flag, st);
     if (s.punch.win)
         return launch_step_fused_punch<S, C>(s, nullptr, wave, items, item_off, nblocks, par, it, rec_index,
                                              err_flag, st);
@@ -75,9 +80,14 @@ int launch_step_fused(const Shot<S, C> &s, int wave, const WorkItem *items, cons
 template <class S, class C>
 int launch_step_fused_batch(const Shot<S, C> *shots, int wave, const WorkItem *items, const int *item_off,
                             int nblocks, int par, int it, int rec_index, int *err_flag, bool punch,
-                            cudaStream_t st)
+                            bool table, cudaStream_t st)
 {
     const Shot<S, C> none{};
+    if (table)
+        return punch ? launch_step_fused_table_punch<S, C>(none, shots, wave, items, item_off, nblocks, par, it,
+                                                           rec_index, err_flag, st)
+                     : launch_step_fused_table<S, C>(none, shots, wave, items, item_off, nblocks, par, it,
+                                                     rec_index, err_flag, st);
     if (punch)
         return launch_step_fused_punch<S, C>(none, shots, wave, items, item_off, nblocks, par, it, rec_index,
                                              err_flag, st);
@@ -107,7 +117,10 @@ int fused_prepare(int wave, int prec)
             default: rc = prepare_one<float, float, FD23_SH, false>();
         }
     }
-    return rc ? rc : fused_prepare_punch(wave, prec);
+    if (!rc) rc = fused_prepare_punch(wave, prec);
+    if (!rc) rc = fused_prepare_table(wave, prec);
+    if (!rc) rc = fused_prepare_table_punch(wave, prec);
+    return rc;
 }
 
 template <class S, class C, int WAVE>
@@ -115,7 +128,7 @@ int occupancy_one()
 {
     using K = Cfg<S, C, WAVE>;
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fused_step<S, C, WAVE, false, false>, K::NTH, K::SMEM) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fused_step<S, C, WAVE, false, false, false>, K::NTH, K::SMEM) !=
         cudaSuccess) {
         cudaGetLastError();
         return 1;
@@ -163,7 +176,7 @@ size_t fused_smem_bytes(int wave, int prec)
     template int launch_step_fused<S, C>(const Shot<S, C> &, int, const WorkItem *, const int *,       \
                                          int, int, int, int, int *, cudaStream_t);                     \
     template int launch_step_fused_batch<S, C>(const Shot<S, C> *, int, const WorkItem *, const int *, \
-                                               int, int, int, int, int *, bool, cudaStream_t);
+                                               int, int, int, int, int *, bool, bool, cudaStream_t);
 FD23_INST(float, float)
 FD23_INST(double, double)
 FD23_INST(__nv_bfloat16, float)

@@ -87,6 +87,14 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
     return ok != 0;
 }
 // tiled 3-D tensor copy (TMA) of one box at (x, y, z) of a tensor map
+__device__ __forceinline__ void tma_load_2d(void *dst, const void *map, int x, int y, uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+        "[%4];" ::"r"(smem_u32(dst)),
+        "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
 __device__ __forceinline__ void tma_load_3d(void *dst, const void *map, int x, int y, int z, uint64_t *bar)
 {
     asm volatile(
@@ -323,7 +331,7 @@ __device__ __forceinline__ void cell_coef(int ix, int iz, int nx, int nz, C &c0,
 }
 
 // ---------------------------------------------------------------------------
-template <class S, class C, int WAVE>
+template <class S, class C, int WAVE, bool TABLE = false>
 struct Cfg {
     static constexpr bool PSV = (WAVE == FD23_PSV);
     static constexpr int NCW = 4;              // compute warps (one per row of a 4-row block)
@@ -356,10 +364,17 @@ struct Cfg {
     static constexpr int UW_SLOT = al128(NV * 4 * UWW * (int)sizeof(S));
     static constexpr int UW_ELEMS = NUW * UW_SLOT;
     static constexpr int PG_MS = al128(NT * 4 * PWW * (int)sizeof(S));
-    static constexpr int PG_MV = PG_MS + al128(NMS * 4 * PWW * (int)sizeof(S));
-    static constexpr int PW_STAGE = PG_MV + al128(NMV * 4 * PWW * (int)sizeof(S));
+    // with a material table the material groups give way to one box of
+    // 8 index rows (velocity rows, then stress rows) of kIdxBoxW bytes
+    static constexpr int PG_MV = TABLE ? PG_MS : PG_MS + al128(NMS * 4 * PWW * (int)sizeof(S));
+    static constexpr int PW_STAGE =
+        TABLE ? PG_MS + al128(8 * kIdxBoxW) : PG_MV + al128(NMV * 4 * PWW * (int)sizeof(S));
     static constexpr int PW_ELEMS = NPW * PW_STAGE;
     static constexpr int TR_ELEMS = NTR * 4 * NT * SW;
+    static constexpr int TAB_ELEMS = TABLE ? (NMS + NMV) * kTabEntries : 0;  // the table, per CTA
+    // bytes the copies of one point-wise stage deliver
+    static constexpr uint32_t PW_TX =
+        TABLE ? (uint32_t)(NT * 4 * PWW * sizeof(S) + 8 * kIdxBoxW) : (uint32_t)(NPF * 4 * PWW * sizeof(S));
     // start of point-wise field f (stresses, then the two material groups) in a stage
     static constexpr __host__ __device__ int pw_field(int f)
     {
@@ -372,7 +387,7 @@ struct Cfg {
     // extra conversions run faster with the larger register budget (measured)
     static constexpr int MINB = sizeof(S) == 8 ? 1 : (sizeof(S) == 2 ? 2 : 3);
     static constexpr size_t RING_BYTES =
-        (((size_t)(UW_ELEMS + PW_ELEMS + TR_ELEMS) * sizeof(S) + 15) & ~(size_t)15);
+        (((size_t)(UW_ELEMS + PW_ELEMS + TR_ELEMS + TAB_ELEMS) * sizeof(S) + 15) & ~(size_t)15);
     static constexpr size_t SMEM = RING_BYTES + 256 /* 2*(NUW+NPW) barriers */ + MAX_ITEMS * 16 +
                                    (size_t)MAX_ITEMS * MAX_TERMS * 16;
 };
@@ -388,13 +403,15 @@ struct ItemInfo {
 // outside their tile's window keep their values; every item first drops the
 // rows of tiles that are steady at this step (left alone at this step and
 // the last, so both buffer sets already hold their values).
-template <class S, class C, int WAVE, bool BATCH, bool PUNCH>
+// TABLE = true: the shots carry material tables; the material of a cell is
+// its index byte looked up in the CTA's shared-memory copy of the table.
+template <class S, class C, int WAVE, bool BATCH, bool PUNCH, bool TABLE>
 __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
     fused_step(const __grid_constant__ Shot<S, C> sh_param, const Shot<S, C> *__restrict__ shots,
                const WorkItem *__restrict__ items, const int *__restrict__ item_off, int par, int it,
                int rec_index, int *err_flag)
 {
-    using K = Cfg<S, C, WAVE>;
+    using K = Cfg<S, C, WAVE, TABLE>;
     constexpr bool PSV = K::PSV;
     constexpr int NCT = 32 * K::NCW;  // compute threads
     // an earlier launch gave up on a wait: do nothing until the host resets
@@ -408,6 +425,7 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
     S *uw_s = reinterpret_cast<S *>(smem_raw);
     S *pw_s = uw_s + K::UW_ELEMS;
     S *tr_s = pw_s + K::PW_ELEMS;
+    S *tab_s = tr_s + K::TR_ELEMS;  // the material table (TABLE only)
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw + K::RING_BYTES);
     uint64_t *full_uw = bars, *empty_uw = bars + K::NUW;
     uint64_t *full_pw = bars + 2 * K::NUW, *empty_pw = full_pw + K::NPW;
@@ -521,6 +539,10 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
             nitems = n_live;
         }
     }
+    if constexpr (TABLE) {
+        // the table is static: copy it ahead of the dependency wait
+        for (int k = tid; k < K::TAB_ELEMS; k += K::NTH) tab_s[k] = sh.mtab[k];
+    }
     if (tid == 0) {
         for (int b = 0; b < K::NUW; ++b) {
             mbar_init(&full_uw[b], 1);
@@ -565,16 +587,20 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
             const int slot = g % K::NPW;
             if (lane == 0) {
                 S *st = pw_s + slot * K::PW_STAGE;
-                if (part != 2)
-                    mbar_arrive_expect_tx(&full_pw[slot], (uint32_t)(K::NPF * 4 * K::PWW * sizeof(S)));
+                if (part != 2) mbar_arrive_expect_tx(&full_pw[slot], K::PW_TX);
                 // old stresses and stress-update material on stress rows,
                 // velocity-update material on velocity rows
                 const int xs = kXPad + I.x0 - 4 - K::PWOFF;
                 const int ys = kZPad + I.z0 - 4 + 4 * i, yv = kZPad + I.z0 - 8 + 4 * i;
                 if (part != 1) tma_load_3d(st, &sh.maps->t[par], xs, ys, K::NV, &full_pw[slot]);
                 if (part != 2) {
-                    tma_load_3d(st + K::PG_MS, &sh.maps->ms, xs, ys, 0, &full_pw[slot]);
-                    tma_load_3d(st + K::PG_MV, &sh.maps->mv, xs, yv, K::NMS, &full_pw[slot]);
+                    if constexpr (TABLE) {
+                        // index rows yv .. yv+7 from the 16-byte boundary at or before xs
+                        tma_load_2d(st + K::PG_MS, &sh.maps->idx, xs & ~15, yv, &full_pw[slot]);
+                    } else {
+                        tma_load_3d(st + K::PG_MS, &sh.maps->ms, xs, ys, 0, &full_pw[slot]);
+                        tma_load_3d(st + K::PG_MV, &sh.maps->mv, xs, yv, K::NMS, &full_pw[slot]);
+                    }
                 }
             }
         };
@@ -641,6 +667,8 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
         const int4 *tl = tlist + k * K::MAX_TERMS;
         const int x = I.x0 - 4 + 4 * lane;  // first of this thread's 4 cells
         const bool own_x = lane >= 1 && lane <= 30;
+        // byte offset of this thread's 4 cells in a row of the index box
+        const int ixo = ((kXPad + I.x0 - 4 - K::PWOFF) & 15) + K::PWOFF + 4 * lane;
         // the 4 cells are interior (8th order), outside the x-CPML and inside the grid
         const bool xfast = x >= max(4, npml) && x + 3 <= min(nx - 5, nx - npml - 1);
         for (int i = 0; i < I.niter; ++i, ++gflat) {
@@ -670,8 +698,17 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
                 C told[K::NT][4], ms[K::NMS][4];
 #pragma unroll
                 for (int f = 0; f < K::NT; ++f) Vec4<S, C>::ld(pwrow(f), told[f]);
+                if constexpr (TABLE) {
+                    const uint32_t q = *reinterpret_cast<const uint32_t *>(
+                        reinterpret_cast<const unsigned char *>(pws + K::PG_MS) + (4 + grp) * kIdxBoxW + ixo);
 #pragma unroll
-                for (int m = 0; m < K::NMS; ++m) Vec4<S, C>::ld(pwrow(K::NT + m), ms[m]);
+                    for (int m = 0; m < K::NMS; ++m)
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) ms[m][e] = to_c<C>(tab_s[m * kTabEntries + ((q >> (8 * e)) & 255u)]);
+                } else {
+#pragma unroll
+                    for (int m = 0; m < K::NMS; ++m) Vec4<S, C>::ld(pwrow(K::NT + m), ms[m]);
+                }
                 if (xfast && zfast) {
                     // interior: packed operands (x differences stay per cell);
                     // gam = fma(2, mu, lam) equals lam + 2*mu (2*mu is exact)
@@ -965,8 +1002,18 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
 #pragma unroll
                     for (int d = 0; d < 9; ++d) trow[d] = trrow(a - 4 + d);
                     C mv[K::NMV][4];
+                    if constexpr (TABLE) {
+                        const uint32_t q = *reinterpret_cast<const uint32_t *>(
+                            reinterpret_cast<const unsigned char *>(pws + K::PG_MS) + grp * kIdxBoxW + ixo);
 #pragma unroll
-                    for (int m = 0; m < K::NMV; ++m) Vec4<S, C>::ld(pwrow(K::NT + K::NMS + m), mv[m]);
+                        for (int m = 0; m < K::NMV; ++m)
+#pragma unroll
+                            for (int e = 0; e < 4; ++e)
+                                mv[m][e] = to_c<C>(tab_s[(K::NMS + m) * kTabEntries + ((q >> (8 * e)) & 255u)]);
+                    } else {
+#pragma unroll
+                        for (int m = 0; m < K::NMV; ++m) Vec4<S, C>::ld(pwrow(K::NT + K::NMS + m), mv[m]);
+                    }
                     const int rel = 4 * i + grp;  // a - (z0-8): block i, row grp
                     const int vr = (4 * (uw_base + i) + (rel & 3)) & (4 * K::NUW - 1);
                     const S *vrow = uw_s + (vr >> 2) * K::UW_SLOT + (vr & 3) * K::UWW + 4 * lane + 4;
@@ -1193,11 +1240,11 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
     }
 }
 
-template <class S, class C, int WAVE, bool BATCH, bool PUNCH>
+template <class S, class C, int WAVE, bool BATCH, bool PUNCH, bool TABLE = false>
 int launch_fused_impl(const Shot<S, C> &s, const Shot<S, C> *shots, const WorkItem *items, const int *item_off,
                       int nblocks, int par, int it, int rec_index, int *err_flag, cudaStream_t st)
 {
-    using K = Cfg<S, C, WAVE>;
+    using K = Cfg<S, C, WAVE, TABLE>;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)nblocks);
     cfg.blockDim = dim3(K::NTH);
@@ -1208,18 +1255,18 @@ int launch_fused_impl(const Shot<S, C> &s, const Shot<S, C> *shots, const WorkIt
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    const cudaError_t e = cudaLaunchKernelEx(&cfg, fused_step<S, C, WAVE, BATCH, PUNCH>, s, shots, items, item_off,
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, fused_step<S, C, WAVE, BATCH, PUNCH, TABLE>, s, shots, items, item_off,
                                              par, it, rec_index, err_flag);
     return e == cudaSuccess ? FD23_OK : FD23_ERR_CUDA;
 }
 
-template <class S, class C, int WAVE, bool PUNCH>
+template <class S, class C, int WAVE, bool PUNCH, bool TABLE = false>
 int prepare_one()
 {
-    using K = Cfg<S, C, WAVE>;
-    const bool ok = cudaFuncSetAttribute(fused_step<S, C, WAVE, false, PUNCH>,
+    using K = Cfg<S, C, WAVE, TABLE>;
+    const bool ok = cudaFuncSetAttribute(fused_step<S, C, WAVE, false, PUNCH, TABLE>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)K::SMEM) == cudaSuccess &&
-                    cudaFuncSetAttribute(fused_step<S, C, WAVE, true, PUNCH>,
+                    cudaFuncSetAttribute(fused_step<S, C, WAVE, true, PUNCH, TABLE>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)K::SMEM) == cudaSuccess;
     return ok ? FD23_OK : FD23_ERR_CUDA;
 }

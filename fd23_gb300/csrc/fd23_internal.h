@@ -93,7 +93,16 @@ struct ShotMaps {
     TmaDesc t[2];   // old stresses of buffer set 0 / 1, box PWW x 4 x NT
     TmaDesc ms;     // stress-update material, box PWW x 4 x NMS
     TmaDesc mv;     // velocity-update material, box PWW x 4 x NMV
+    TmaDesc idx;    // material-table indices (bytes), 2-D [row][column], box kIdxBoxW x 8
 };
+
+// Material table (mktable, PD/material/mktable.cpp): every cell's material
+// tuple (P-SV LAM MU MUA BU BW, SH MUX MUZ BV, storage values) as a one-byte
+// index into a table of at most kTabEntries tuples; entry 0 is the zero tuple
+// of the padding.  The fused sweep copies 8 index rows of kIdxBoxW bytes per
+// iteration (16-byte aligned start, so wider than the point-wise rows).
+constexpr int kTabEntries = 256;
+constexpr int kIdxBoxW = 160;
 
 // Device view of the box of one shot: residual field r and box material,
 // bx*bz each, row-major; `inc` = the incident field of the current step.
@@ -157,6 +166,8 @@ struct alignas(16) Shot {
     const ShotMaps *maps;  // tensor maps of the fused sweep's copies (device memory)
     int cta0, ncta;     // CTAs of the launch working on this shot (receiver gather split)
     Punch punch;        // tile step windows (punch.win == nullptr: none)
+    const unsigned char *midx;  // material-table indices, padded layout (nullptr: no table)
+    const S *mtab;              // table [material array][kTabEntries], storage values
     Box<C> box;         // hybrid box (box.on == 0: none); last, the batched sweep never reads it
 };
 

@@ -58,11 +58,12 @@ int launch_box_post(const Shot<S, C> &s, int par, int fused, int rec_index, cuda
 
 // The same sweep over several shots in one launch: `shots` = device array of
 // shot descriptors; every CTA's items belong to one shot (a WorkPlan).
-// `punch`: some shot carries tile step windows (the sweep with windows runs)
+// `punch`: some shot carries tile step windows (the sweep with windows
+// runs); `table`: the shots carry material tables (all of them)
 template <class S, class C>
 int launch_step_fused_batch(const Shot<S, C> *shots, int wave, const WorkItem *items, const int *item_off,
                             int nblocks, int par, int it, int rec_index, int *err_flag, bool punch,
-                            cudaStream_t st);
+                            bool table, cudaStream_t st);
 
 // The sweep with tile step windows (fd23_fused_punch.cu): one shot (`shots`
 // null, descriptor `s`) or a shot table; called by the two launchers above.
@@ -71,6 +72,19 @@ int launch_step_fused_punch(const Shot<S, C> &s, const Shot<S, C> *shots, int wa
                             const int *item_off, int nblocks, int par, int it, int rec_index, int *err_flag,
                             cudaStream_t st);
 int fused_prepare_punch(int wave, int prec);
+
+// The sweep with material tables, without / with tile step windows
+// (fd23_fused_table.cu, fd23_fused_table_punch.cu); same arguments.
+template <class S, class C>
+int launch_step_fused_table(const Shot<S, C> &s, const Shot<S, C> *shots, int wave, const WorkItem *items,
+                            const int *item_off, int nblocks, int par, int it, int rec_index, int *err_flag,
+                            cudaStream_t st);
+template <class S, class C>
+int launch_step_fused_table_punch(const Shot<S, C> &s, const Shot<S, C> *shots, int wave, const WorkItem *items,
+                                  const int *item_off, int nblocks, int par, int it, int rec_index, int *err_flag,
+                                  cudaStream_t st);
+int fused_prepare_table(int wave, int prec);
+int fused_prepare_table_punch(int wave, int prec);
 
 // one thread waits on an mbarrier nothing completes, with the sweep's bounded
 // wait: sets *err_flag when the wait gives up (about 2 s)

@@ -67,6 +67,12 @@ struct fd23_solver {
     fd23::TuneParams tune;
     // hybrid box: residual field, box material, ring cells, incident field
     // of steps [box_inc_it0, box_inc_it0 + box_inc_n)
+    // material table (device): indices (padded layout, bytes) and the table
+    // [nmat][kTabEntries] of storage values; null when off
+    unsigned char *d_midx = nullptr;
+    void *d_mtab = nullptr;
+    bool table_on = false;
+    int table_n = 0;
     // usepunch tile step windows (device, [nbz][nbx] int2), null when off
     int2 *d_punch = nullptr;
     int punch_nbx = 0, punch_nbz = 0;
@@ -97,6 +103,15 @@ int build_worklist(fd23_solver *s);
 int dispatch_step(fd23_solver *s, int rec_now);
 // copies buffer set `par` (wavefields, memory variables) into the other set
 int mirror_sets(fd23_solver *s, cudaStream_t st);
+// material table from the device material (fd23_table.cpp): FD23_OK, or
+// FD23_ERR_UNSUPPORTED with more distinct tuples than the table holds
+int build_material_table(fd23_solver *s);
+// one nx x nz array between the host (row-major, es bytes per value) and the
+// padded device layout
+int upload_grid(fd23_solver *s, void *dptr, const unsigned char *host, size_t es);
+int download_grid(fd23_solver *s, const void *dptr, unsigned char *host, size_t es);
+void free_material_table(fd23_solver *s);
+int encode_maps(fd23_solver *s);
 
 template <class S, class C>
 Shot<S, C> make_shot(const fd23_solver *s)
@@ -128,6 +143,8 @@ Shot<S, C> make_shot(const fd23_solver *s)
     sh.cta0 = 0;
     sh.ncta = s->nblocks > 0 ? s->nblocks : 1;
     sh.punch = Punch{s->d_punch, s->punch_nbx, s->punch_nbz};
+    sh.midx = s->d_midx;
+    sh.mtab = (const S *)s->d_mtab;
     sh.box.on = s->box_on ? 1 : 0;
     if (s->box_on) {
         sh.box.x0 = s->box_x0;

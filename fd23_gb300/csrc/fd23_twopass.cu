@@ -27,6 +27,14 @@ __device__ __forceinline__ C dplus(const S *p, long long s, C c0, C c1, C c2, C 
     return comb<C>(c0, c1, c2, c3, v(1) - v(0), v(2) - v(-1), v(3) - v(-2), v(4) - v(-3));
 }
 
+// material array m at padded offset o, through the material table when the
+// shot has one (lossless: the table holds the stored values)
+template <class S, class C>
+__device__ __forceinline__ C matv(const Shot<S, C> &s, int m, long long o)
+{
+    return s.midx ? to_c<C>(s.mtab[m * kTabEntries + s.midx[o]]) : to_c<C>(s.mat[m][o]);
+}
+
 template <class C>
 __device__ __forceinline__ long long psi_x_index(int ix, int iz, int nx, int npml)
 {
@@ -57,7 +65,7 @@ __global__ void __launch_bounds__(256) psv_stress_2p(Shot<S, C> s, int it)
     const C uz = dminus<S, C>(U + o, P, c0, c1, c2, c3);
     const C wx = dplus<S, C>(W + o, 1, c0, c1, c2, c3);
     const C wz = dplus<S, C>(W + o, P, c0, c1, c2, c3);
-    const C lam = to_c<C>(s.mat[0][o]), mu = to_c<C>(s.mat[1][o]), mua = to_c<C>(s.mat[2][o]);
+    const C lam = matv<S, C>(s, 0, o), mu = matv<S, C>(s, 1, o), mua = matv<S, C>(s, 2, o);
     const C gam = lam + (C)2 * mu;
     C txx = to_c<C>(Txx[o]), tzz = to_c<C>(Tzz[o]), txz = to_c<C>(Txz[o]);
     const int nx = s.nx, nz = s.nz, npml = s.npml, B = s.cpml_blk;
@@ -123,7 +131,7 @@ __global__ void __launch_bounds__(256) psv_velocity_2p(Shot<S, C> s, int it)
     const C dzTzz = dminus<S, C>(Tzz + o, P, c0, c1, c2, c3);
     const C dxTxz = dminus<S, C>(Txz + o, 1, c0, c1, c2, c3);
     const C dzTxz = dplus<S, C>(Txz + o, P, c0, c1, c2, c3);
-    const C bu = to_c<C>(s.mat[3][o]), bw = to_c<C>(s.mat[4][o]);
+    const C bu = matv<S, C>(s, 3, o), bw = matv<S, C>(s, 4, o);
     C u = to_c<C>(U[o]), w = to_c<C>(W[o]);
     const int nx = s.nx, nz = s.nz, npml = s.npml, B = s.cpml_blk;
     const C *b = s.cpml, *c = s.cpml + B, *k = s.cpml + 2 * B;
@@ -181,7 +189,7 @@ __global__ void __launch_bounds__(256) sh_stress_2p(Shot<S, C> s, int it)
             c3 = Coef<C>::get(ord, 3);
     const C dxV = dplus<S, C>(V + o, 1, c0, c1, c2, c3);
     const C dzV = dminus<S, C>(V + o, P, c0, c1, c2, c3);
-    const C mux = to_c<C>(s.mat[0][o]), muz = to_c<C>(s.mat[1][o]);
+    const C mux = matv<S, C>(s, 0, o), muz = matv<S, C>(s, 1, o);
     const int nx = s.nx, nz = s.nz, npml = s.npml, B = s.cpml_blk;
     const C *b = s.cpml, *c = s.cpml + B, *k = s.cpml + 2 * B;
     C tx = to_c<C>(Tx[o]), tz = to_c<C>(Tz[o]);
@@ -224,7 +232,7 @@ __global__ void __launch_bounds__(256) sh_velocity_2p(Shot<S, C> s, int it)
             c3 = Coef<C>::get(ord, 3);
     const C dxTx = dminus<S, C>(Tx + o, 1, c0, c1, c2, c3);
     const C dzTz = dplus<S, C>(Tz + o, P, c0, c1, c2, c3);
-    const C bv = to_c<C>(s.mat[2][o]);
+    const C bv = matv<S, C>(s, 2, o);
     const int nx = s.nx, nz = s.nz, npml = s.npml, B = s.cpml_blk;
     const C *b = s.cpml, *c = s.cpml + B, *k = s.cpml + 2 * B;
     C v = to_c<C>(V[o]);

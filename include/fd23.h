@@ -196,8 +196,8 @@ int fd23_set_state(fd23_solver *s, const void *buf, size_t bytes, int it0);
  *   FD23_ERR_ORDER for a step it does not cover.
  * fd23_get_box_state / fd23_set_box_state: r as U W Txx Txz Tzz, bx*bz each,
  *   compute type (fd23_box_state_bytes).
- * A box and tile step windows (fd23_set_punch) exclude each other:
- *   FD23_ERR_UNSUPPORTED. */
+ * A box excludes tile step windows (fd23_set_punch) and material tables
+ *   (fd23_set_material_table): FD23_ERR_UNSUPPORTED. */
 int fd23_set_box(fd23_solver *s, int x0, int z0, int bx, int bz, const double *bmat);
 int fd23_set_box_incident(fd23_solver *s, const void *inc, int it0, int nsteps);
 size_t fd23_box_state_bytes(fd23_solver *s);
@@ -304,6 +304,21 @@ int fd23_debug_expire_wait(fd23_solver *s);
  * Runs on `stream` (a cudaStream_t, NULL = default) and waits for it. */
 int fd23_sum_squares_noalloc(int prec, const void *const *fields, int nfields, size_t n,
                              void *stream, double *sum, int *nonfinite);
+
+/* ---- material table (mktable) ----
+ * Replaces MATERIAL::mktable (PD/material/mktable.cpp:43-106; called by
+ * SH/main.cpp:154) and the usetable reads of the sweep kernels
+ * (PD/fd/cu_fd.cu:262-270, SH/fd/cu_fd.cu:117,219).  on = 1 turns the
+ * solver's material into one index byte per cell and a table of the distinct
+ * material tuples (storage values, matched bit for bit, so results are
+ * identical); the sweeps then read one byte per cell instead of 5 (P-SV) or
+ * 3 (SH) material values.  Returns the number of table entries (the zero
+ * tuple of the padding included), FD23_ERR_UNSUPPORTED past 256 entries or
+ * with a hybrid box, FD23_ERR_ORDER before the material.  While on, every
+ * fd23_set_material / fd23_set_model rebuilds the table; one that no longer
+ * fits turns the table off.  on = 0 removes it.  Batches need tables in all
+ * shots or in none. */
+int fd23_set_material_table(fd23_solver *s, int on);
 
 /* ---- usepunch: tile step windows ----
  * Replaces the SLIDE object (PD/slide/slide.h:4-13, PD/slide/cu_slide.cu:6-66)

@@ -220,3 +220,34 @@ def test_narrowed_items_in_bounds(nx, nz, es, wave):
         for it in (0, 7, 31, 90):
             nar = [narrow(nx, nz, items, first, last, it, terms=[(nx // 2, nz // 3)]) for items in ctas]
             audit(nx, nz, es, wave, per_sm=per_sm, ctas=nar, narrowed=True)
+
+
+@pytest.mark.parametrize("nx,nz", SIZES)
+@pytest.mark.parametrize("es,wave", [(4, "psv"), (8, "psv"), (2, "psv"), (4, "sh"), (2, "sh")])
+def test_table_index_box_in_bounds(nx, nz, es, wave):
+    """The material-table form copies, per iteration, 8 index rows (bytes)
+    of kIdxBoxW = 160 from the 16-byte boundary at or before the point-wise
+    copy's start: x is a multiple of 16 bytes, the rows lie inside the
+    padded index array, every thread's 4 index bytes lie inside the box and
+    are 4-byte aligned, and the stage layout stays 128-byte aligned."""
+    IW = 160
+    pitch, rows, origin = layout(nx, nz)
+    lay = smem_layout(es, wave)
+    npml = min(40, nx // 2, nz // 2)
+    pg_ms = lay["pg_ms"]
+    stage = pg_ms + al128(8 * IW)
+    assert pg_ms % 128 == 0 and stage % 128 == 0
+    for items in worklist(nx, nz, npml, 1.0, {8: 1, 4: 3, 2: 2}[es]):
+        for (x0, z0, z1) in items:
+            niter = (z1 - z0) // 4 + 2
+            xs = XPAD + x0 - 4 - lay["pwoff"]
+            xa = xs & ~15
+            assert xa >= 0 and xa % 16 == 0 and xa <= xs
+            for i in (0, niter - 1):
+                yv = ZPAD + z0 - 8 + 4 * i
+                assert yv >= 0 and yv + 8 <= rows
+            for q in (0, 31):
+                ixo = (xs & 15) + lay["pwoff"] + 4 * q
+                assert ixo % 4 == 0 and ixo + 3 < IW
+                # the byte is the cell the point-wise row holds at this lane
+                assert xa + ixo == XPAD + x0 - 4 + 4 * q
