@@ -20,12 +20,17 @@
 // U_sta_file / W_sta_file or nrec ixrec0 izrec0_u izrec0_w idxrec idzrec.
 // Optional: srctype (1 moment, p 'p' dipole; default 1), itrecord (1),
 // restart + nt0, savestate.  Accepted and ignored (no effect on this path):
-// ntsnap itprint gpuid ngpu ord bw usetable src_shift_x src_shift_z
+// ntsnap itprint gpuid ngpu ord bw src_shift_x src_shift_z
 // sourcetime stype.  usepunch=1 (with before, after, timefile) updates
 // every 32 x 16 tile only inside its step window (PN/slide/cu_slide.cu,
 // PN/param/param.cpp usepunch block): the timefile holds nx*nz float travel
 // times (PN, SH), or doubles with prec=f64 (PD, whose windows use the double
-// dt).  Not supported here: usebox=1 (the box is in the C ABI).  Additions: prec (f32, f64, bf16, f16; default f32),
+// dt).  usetable=1 (PN/param/param.cpp:180-181; the SH program's default,
+// SH/main.cpp:154) reads the material through a table of its distinct
+// tuples when they fit (fd23_set_material_table), else prints the
+// reference's "Too many materials" and goes on without.  Not supported
+// here: usebox=1 (the box is in the C ABI).  Additions: prec (f32, f64,
+// bf16, f16; default f32),
 // explosion (1: Mxx = Mzz = 1, the *_exp builds), topabsorb (1: CPML on top,
 // the *_topabsorb builds), device (CUDA ordinal, default 0), dryrun (1: print
 // the resolved set-up and stop before touching the GPU).
@@ -307,6 +312,15 @@ int main(int argc, char **argv)
     rc = fd23_set_model(s, kSH ? nullptr : vp.data(), vs.data(), den.data(), &stab);
     std::printf("stab = %g\n", stab);
     if (rc) return fail("model", rc);
+    // material table (PN/param/param.cpp usetable; the SH program always
+    // tries one, SH/main.cpp:154): index + table form when the distinct
+    // material tuples fit, the material arrays otherwise
+    if (p.num("usetable", kSH ? 1 : 0) != 0) {
+        rc = fd23_set_material_table(s, 1);
+        if (rc == FD23_ERR_UNSUPPORTED) std::printf("Too many materials, abort make table\n");
+        else if (rc < 0) return fail("material table", rc);
+        else std::printf("material table: %d entries\n", rc);
+    }
     double m[3];
     int kind;
     if (kSH) {

@@ -136,6 +136,17 @@ def test_cli_usepunch_equals_api(tmp_path):
     np.testing.assert_array_equal(got, want)
 
 
+def test_cli_usetable_equals_plain(tmp_path):
+    """usetable=1 (the polygon model fits a table) writes the same traces."""
+    _setup(tmp_path)
+    _cli(tmp_path, "nt=40", "output=plain")
+    r = _cli(tmp_path, "nt=40", "output=tab", "usetable=1")
+    assert "material table:" in r.stdout
+    a = np.fromfile(str(tmp_path / "plain_U"), dtype=np.float32)
+    b = np.fromfile(str(tmp_path / "tab_U"), dtype=np.float32)
+    np.testing.assert_array_equal(a, b)
+
+
 @pytest.mark.parametrize("stype", [3, 2])
 def test_sh_program_equals_api(tmp_path, stype):
     _setup(tmp_path)
