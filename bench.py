@@ -347,14 +347,14 @@ def main():
     if args.config == "c5":
         # usepunch: tile step windows from straight-ray travel times at the
         # fastest velocity (never later than the first arrival), opening
-        # PUNCH_BEFORE early and not closing within the run.  The work plan
-        # is the one measured best for this windowed shot (oversubscribed
-        # six times, so the moving active region spreads over the SMs).
+        # PUNCH_BEFORE early and not closing within the run.  The sweep plans
+        # every 128-step phase over the blocks live in it, one wave of CTAs
+        # with the C1 block weights.
         first, last = punch_windows_c5(vp)
         s.set_punch(first, last)
         if args.kernel == "fused":
-            s.set_plan(6.0, 4.0, 3, 6.0)
-            best_plan = {"wx": 6.0, "wz": 4.0, "oversub": 6.0}
+            s.set_plan(6.0, 4.0, 3, 1.0)
+            best_plan = {"wx": 6.0, "wz": 4.0, "oversub": 1.0, "phase_steps": 128}
         punch = {"first": first, "last": last, "active": punch_active_fraction(first, last, nt)}
 
     def shot():

@@ -56,7 +56,7 @@ ABI_FUNCTIONS = [
     "fd23_batch_get_stream", "fd23_batch_set_graph", "fd23_autotune", "fd23_batch_autotune",
     "fd23_batch_get_plan", "fd23_work_plan", "fd23_read_model", "fd23_read_stations",
     "fd23_debug_expire_wait", "fd23_set_plan", "fd23_get_plan", "fd23_punch_tiles", "fd23_punch_windows", "fd23_read_punch", "fd23_set_punch",
-    "fd23_set_material_table",
+    "fd23_set_material_table", "fd23_set_punch_phase",
 ]
 
 
@@ -157,6 +157,7 @@ def lib():
         "fd23_read_punch": ([_C.c_char_p, i, i, i, d, d, d, vp, vp], i),
         "fd23_set_punch": ([vp, vp, vp, i, i], i),
         "fd23_set_material_table": ([vp, i], i),
+        "fd23_set_punch_phase": ([vp, i], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -621,6 +622,10 @@ class Solver:
         if f.size != nbx * nbz or l.size != nbx * nbz:
             nbx = nbz = -1  # let the library reject the sizes
         _check(lib().fd23_set_punch(self._h, _p(f), _p(l), nbx, nbz), "fd23_set_punch")
+
+    def set_punch_phase(self, steps):
+        """Steps per phase plan of the windowed sweep (0: one static plan)."""
+        _check(lib().fd23_set_punch_phase(self._h, steps), "fd23_set_punch_phase")
 
     # -- hybrid box --
     def set_box(self, x0, z0, bx, bz, bmat=None):

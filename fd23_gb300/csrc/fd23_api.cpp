@@ -171,9 +171,21 @@ int step_impl(fd23_solver *s, int rec_now)
     int rc = FD23_OK;
     if (box && (rc = launch_box_pre<S, C>(sh, s->fused ? s->par : 0, s->fused, s->stream))) return rc;
     if (s->fused) {
-        rc = launch_step_fused<S, C>(sh, s->d.wave, s->d_items, s->d_item_off, s->nblocks, s->par, s->it,
-                                     s->pending_rec, s->err_flag, s->stream);
+        const WorkItem *items = s->d_items;
+        const int *off = s->d_item_off;
+        int nblocks = s->nblocks;
+        int slot = -1;
+        if (s->d_punch && s->punch_phase > 0) {
+            if ((rc = phase_plan(s, &slot))) return rc;
+            items = s->phase[slot].items;
+            off = s->phase[slot].off;
+            nblocks = s->phase[slot].nblocks;
+            sh.ncta = nblocks;
+        }
+        rc = launch_step_fused<S, C>(sh, s->d.wave, items, off, nblocks, s->par, s->it, s->pending_rec,
+                                     s->err_flag, s->stream);
         if (rc) return rc;
+        if (slot >= 0) CK(cudaEventRecord(s->phase[slot].done, s->stream));
         s->pending_rec = -1;
         s->par = 1 - s->par;
         if (rec_now && !box) s->pending_rec = s->nrec_steps++;
@@ -325,6 +337,7 @@ int build_worklist(fd23_solver *s)
     if (rc) return rc;
     if ((rc = upload_plan(plan, &s->d_items, &s->d_item_off))) return rc;
     s->nblocks = plan.nblocks;
+    ++s->punch_ver;  // phase plans follow the tuning
     return FD23_OK;
 }
 
@@ -378,6 +391,12 @@ void free_all(fd23_solver *s)
     cudaFree(s->mat_block);
     cudaFree(s->d_maps);
     cudaFree(s->d_punch);
+    for (auto &ph : s->phase) {
+        cudaFree(ph.items);
+        cudaFree(ph.off);
+        cudaFreeHost(ph.host);
+        if (ph.done) cudaEventDestroy(ph.done);
+    }
     cudaFree(s->d_midx);
     cudaFree(s->d_mtab);
     cudaFree(s->cpml);
@@ -680,6 +699,9 @@ int fd23_set_source_terms(fd23_solver *s, int nterms, const int *field, const in
     s->tamp_nt = nt_amp;
     s->h_tfield.assign(field, field + nterms);
     s->h_tamp.assign(amp, amp + na);
+    s->h_tcell.clear();
+    for (int k = 0; k < nterms; ++k) s->h_tcell.push_back(make_int2(ix[k], iz[k]));
+    ++s->punch_ver;
     return upload_source_amps(s);
 }
 

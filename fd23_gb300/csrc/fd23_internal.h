@@ -192,8 +192,10 @@ struct WorkPlan {
     std::vector<int> off, cta0, ncta;
     int nblocks = 0;
 };
+// live (optional): per shot, per 4-row block (strip-major, strip * nzb + zb)
+// whether it is planned at all; without it every block is
 int plan_work(const std::vector<ShotGeom> &shots, int tile_x, int sms, const TuneParams &tp,
-              WorkPlan &plan);
+              WorkPlan &plan, const std::vector<std::vector<unsigned char>> *live = nullptr);
 
 // host builders (fd23_host.cpp)
 int build_psv_material(int nx, int nz, double h, double dt, const double *vp, const double *vs,

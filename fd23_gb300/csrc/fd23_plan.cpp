@@ -6,7 +6,9 @@
 // edge rows).  CTAs are shared out between shots in proportion to their cost,
 // then every shot's blocks are cut, strip-major, into contiguous ranges of
 // equal cost; a range that crosses strips becomes several items.  A CTA never
-// mixes shots, so it keeps one shot descriptor.
+// mixes shots, so it keeps one shot descriptor.  With a live mask only the
+// live blocks are planned (runs of consecutive live blocks of a strip take
+// the place of strips).
 #include <algorithm>
 #include <cmath>
 
@@ -28,15 +30,18 @@ double block_cost(const ShotGeom &g, int tile_x, int strip, int zb, const TunePa
 
 }  // namespace
 
-// Cuts the nb blocks of one shot (cumulative costs c) into n contiguous
-// ranges of near-equal cost, none touching more than 4 strips; false if the
-// last range would need more.
-bool cut_shot(const std::vector<double> &c, long long nb, int nzb, int n, std::vector<long long> &ends)
+// Cuts the nb planned blocks of one shot (cumulative costs c; run_begin[r]
+// = first block of run r, a run being consecutive blocks of one strip) into
+// n contiguous ranges of near-equal cost, none touching more than 4 runs;
+// false if the last range would need more.
+bool cut_shot(const std::vector<double> &c, long long nb, const std::vector<long long> &run_of,
+              const std::vector<long long> &run_begin, int n, std::vector<long long> &ends)
 {
     ends.clear();
     long long b0 = 0;
     for (int q = 0; q < n; ++q) {
-        const long long cap = std::min(nb, (b0 / nzb + 4) * (long long)nzb);  // at most 4 strips
+        const long long r4 = run_of[b0] + 4;
+        const long long cap = r4 < (long long)run_begin.size() ? run_begin[r4] : nb;  // at most 4 runs
         long long b1;
         if (q == n - 1) {
             b1 = nb;
@@ -54,25 +59,40 @@ bool cut_shot(const std::vector<double> &c, long long nb, int nzb, int n, std::v
     return true;
 }
 
-int plan_work(const std::vector<ShotGeom> &shots, int tile_x, int sms, const TuneParams &tp, WorkPlan &plan)
+int plan_work(const std::vector<ShotGeom> &shots, int tile_x, int sms, const TuneParams &tp, WorkPlan &plan,
+              const std::vector<std::vector<unsigned char>> *live)
 {
     const int ns = (int)shots.size();
     if (ns <= 0 || tile_x <= 0 || sms <= 0) return FD23_ERR_ARG;
+    if (live && (int)live->size() != ns) return FD23_ERR_ARG;
+    // planned blocks of every shot (all of them, or the live ones), strip-major,
+    // with their runs and cumulative costs
+    std::vector<std::vector<long long>> blk(ns), run_of(ns), run_begin(ns);
     std::vector<std::vector<double>> cum(ns);
-    std::vector<int> ntx(ns), nzb(ns), nmin(ns);
+    std::vector<int> nzb(ns), nmin(ns);
     std::vector<long long> nbk(ns);
     double total = 0.0;
     long long sum_min = 0;
     for (int k = 0; k < ns; ++k) {
         const ShotGeom &g = shots[k];
-        ntx[k] = (g.nx + tile_x - 1) / tile_x;
+        const int ntx = (g.nx + tile_x - 1) / tile_x;
         nzb[k] = (g.nz + 3) / 4;
-        nbk[k] = (long long)ntx[k] * nzb[k];
-        cum[k].assign((size_t)nbk[k] + 1, 0.0);
-        for (long long b = 0; b < nbk[k]; ++b)
-            cum[k][b + 1] = cum[k][b] + block_cost(g, tile_x, (int)(b / nzb[k]), (int)(b % nzb[k]), tp);
-        total += cum[k][nbk[k]];
-        nmin[k] = (int)std::min<long long>(nbk[k], std::max(1, (ntx[k] + 1) / 2));  // within 4 items
+        const long long all = (long long)ntx * nzb[k];
+        if (live && (long long)(*live)[k].size() != all) return FD23_ERR_ARG;
+        cum[k].assign(1, 0.0);
+        long long prev = -2;
+        for (long long b = 0; b < all; ++b) {
+            if (live && !(*live)[k][b]) continue;
+            if (b != prev + 1 || b % nzb[k] == 0) run_begin[k].push_back((long long)blk[k].size());
+            run_of[k].push_back((long long)run_begin[k].size() - 1);
+            blk[k].push_back(b);
+            cum[k].push_back(cum[k].back() + block_cost(g, tile_x, (int)(b / nzb[k]), (int)(b % nzb[k]), tp));
+            prev = b;
+        }
+        nbk[k] = (long long)blk[k].size();
+        total += cum[k].back();
+        const long long runs = (long long)run_begin[k].size();
+        nmin[k] = (int)std::min<long long>(nbk[k], std::max(1LL, (runs + 1) / 2));  // within 4 items
         sum_min += nmin[k];
     }
     // CTA count: the resident slots times the oversubscription, rounded up to
@@ -125,21 +145,24 @@ int plan_work(const std::vector<ShotGeom> &shots, int tile_x, int sms, const Tun
     plan.ncta.assign(ns, 0);
     std::vector<long long> ends;
     for (int k = 0; k < ns; ++k) {
+        plan.cta0[k] = (int)plan.off.size() - 1;
+        if (nbk[k] == 0) continue;  // nothing to do for this shot
         int n = nc[k];
-        while (!cut_shot(cum[k], nbk[k], nzb[k], n, ends)) {
+        while (!cut_shot(cum[k], nbk[k], run_of[k], run_begin[k], n, ends)) {
             if (n >= nbk[k]) return FD23_ERR_ARG;
             ++n;
         }
-        plan.cta0[k] = (int)plan.off.size() - 1;
         plan.ncta[k] = n;
         long long b0 = 0;
         for (long long b1 : ends) {
             while (b0 < b1) {
-                const int strip = (int)(b0 / nzb[k]);
-                const long long send = (long long)(strip + 1) * nzb[k];
-                const long long e = std::min(b1, send);
-                plan.items.push_back(WorkItem{k, strip * tile_x, (int)(b0 - (long long)strip * nzb[k]) * 4,
-                                              (int)(e - (long long)strip * nzb[k]) * 4});
+                // one item per run inside the range
+                const long long r = run_of[k][b0];
+                const long long rend = r + 1 < (long long)run_begin[k].size() ? run_begin[k][r + 1] : nbk[k];
+                const long long e = std::min(b1, rend);
+                const long long first = blk[k][b0], last = blk[k][e - 1];
+                const int strip = (int)(first / nzb[k]);
+                plan.items.push_back(WorkItem{k, strip * tile_x, (int)(first % nzb[k]) * 4, (int)(last % nzb[k] + 1) * 4});
                 b0 = e;
             }
             plan.off.push_back((int)plan.items.size());

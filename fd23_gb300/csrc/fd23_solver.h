@@ -73,9 +73,30 @@ struct fd23_solver {
     void *d_mtab = nullptr;
     bool table_on = false;
     int table_n = 0;
-    // usepunch tile step windows (device, [nbz][nbx] int2), null when off
+    // usepunch tile step windows (device, [nbz][nbx] int2), null when off,
+    // and their host copy
     int2 *d_punch = nullptr;
     int punch_nbx = 0, punch_nbz = 0;
+    std::vector<int2> h_punch;
+    // With windows the fused sweep runs on phase plans: work lists over the
+    // 4-row blocks live at some step of a phase of punch_phase steps (0: the
+    // static plan), built on the host and kept in a ring of device buffers
+    // (reused once the event of their last launch has completed).
+    struct PhasePlan {
+        fd23::WorkItem *items = nullptr;
+        int *off = nullptr;
+        size_t cap_items = 0, cap_off = 0;
+        void *host = nullptr;  // pinned staging of items + offsets
+        size_t cap_host = 0;
+        int nblocks = 0;
+        long long key = -1;
+        cudaEvent_t done = nullptr;
+    };
+    PhasePlan phase[3];
+    int punch_phase = 128;
+    long long punch_ver = 0;  // bumped when windows, sources or the tuning change
+    int phase_next = 0;
+    std::vector<int2> h_tcell;  // source-term cells (ix, iz)
     bool box_on = false;
     int box_x0 = 0, box_z0 = 0, box_bx = 0, box_bz = 0, box_nsub = 0, box_nring = 0;
     void *box_r[5] = {};
@@ -103,6 +124,8 @@ int build_worklist(fd23_solver *s);
 int dispatch_step(fd23_solver *s, int rec_now);
 // copies buffer set `par` (wavefields, memory variables) into the other set
 int mirror_sets(fd23_solver *s, cudaStream_t st);
+// the phase plan of step s->it (fd23_punch.cpp): slot of s->phase to use
+int phase_plan(fd23_solver *s, int *slot);
 // material table from the device material (fd23_table.cpp): FD23_OK, or
 // FD23_ERR_UNSUPPORTED with more distinct tuples than the table holds
 int build_material_table(fd23_solver *s);

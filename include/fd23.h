@@ -346,6 +346,11 @@ int fd23_punch_windows(const void *times, int elem_bytes, int nx, int nz, double
 int fd23_read_punch(const char *timefile, int elem_bytes, int nx, int nz, double before, double after, double dt,
                     int *first, int *last);
 int fd23_set_punch(fd23_solver *s, const int *first, const int *last, int nbx, int nbz);
+/* With windows the fused sweep of a single solver plans its work per phase
+ * of `steps` steps (default 128) over the 4-row blocks live in that phase, so
+ * every step's work spreads over the whole GPU; 0 keeps the one plan of the
+ * whole grid (batches always do). */
+int fd23_set_punch_phase(fd23_solver *s, int steps);
 
 /* ---- model and station input (host only) ----
  * fd23_read_model: a ".mdl" polygon model (BACK / POLY / DEF commands,
