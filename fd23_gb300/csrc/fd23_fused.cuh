@@ -382,10 +382,12 @@ struct Cfg {
     }
     static constexpr int MAX_ITEMS = 4;
     static constexpr int MAX_TERMS = 16;
-    // CTAs per SM the register budget is built for: three for the 4-byte
-    // forms (shared memory allows three); two for the 16-bit forms, whose
-    // extra conversions run faster with the larger register budget (measured)
-    static constexpr int MINB = sizeof(S) == 8 ? 1 : (sizeof(S) == 2 ? 2 : 3);
+    // CTAs per SM the register budget is built for: three (shared memory
+    // allows three) except FP64 (one); the single-shot P-SV 16-bit sweep is
+    // built for two, which it runs faster with while still fitting three
+    // (measured; the batched and SH 16-bit sweeps would grow past three)
+    template <bool BATCH>
+    static constexpr int minb() { return sizeof(S) == 8 ? 1 : (sizeof(S) == 2 && PSV && !BATCH ? 2 : 3); }
     static constexpr size_t RING_BYTES =
         (((size_t)(UW_ELEMS + PW_ELEMS + TR_ELEMS + TAB_ELEMS) * sizeof(S) + 15) & ~(size_t)15);
     static constexpr size_t SMEM = RING_BYTES + 256 /* 2*(NUW+NPW) barriers */ + MAX_ITEMS * 16 +
@@ -406,7 +408,7 @@ struct ItemInfo {
 // TABLE = true: the shots carry material tables; the material of a cell is
 // its index byte looked up in the CTA's shared-memory copy of the table.
 template <class S, class C, int WAVE, bool BATCH, bool PUNCH, bool TABLE>
-__global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::MINB)
+__global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::template minb<BATCH>())
     fused_step(const __grid_constant__ Shot<S, C> sh_param, const Shot<S, C> *__restrict__ shots,
                const WorkItem *__restrict__ items, const int *__restrict__ item_off, int par, int it,
                int rec_index, int *err_flag)
