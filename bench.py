@@ -342,7 +342,7 @@ def main():
     stream = torch.cuda.ExternalStream(s.stream, device=local)
     # work plan picked by the autotuner on this shot (set-up, not timed)
     tune = s.autotune(10) if args.kernel == "fused" and not args.no_tune and args.config != "c5" else []
-    best_plan = min(tune, key=lambda r: r["ms_per_step"]) if tune else None
+    best_plan = s.plan() if tune else None  # the plan the autotuner kept
     punch = None
     if args.config == "c5":
         # usepunch: tile step windows from straight-ray travel times at the

@@ -382,8 +382,8 @@ class Batch:
         return d
 
     def autotune(self, trial_steps=10):
-        tab = (TuneEntry * 64)()
-        n = _check(lib().fd23_batch_autotune(self._h, trial_steps, _C.cast(tab, _C.c_void_p), 64),
+        tab = (TuneEntry * 128)()
+        n = _check(lib().fd23_batch_autotune(self._h, trial_steps, _C.cast(tab, _C.c_void_p), 128),
                    "fd23_batch_autotune")
         return [tab[k].as_dict() for k in range(n)]
 
@@ -584,8 +584,8 @@ class Solver:
     def autotune(self, trial_steps=10):
         """Time the candidate work plans on this shot and keep the fastest;
         returns the trials as dicts."""
-        tab = (TuneEntry * 64)()
-        n = _check(lib().fd23_autotune(self._h, trial_steps, _C.cast(tab, _C.c_void_p), 64), "fd23_autotune")
+        tab = (TuneEntry * 128)()
+        n = _check(lib().fd23_autotune(self._h, trial_steps, _C.cast(tab, _C.c_void_p), 128), "fd23_autotune")
         return [tab[k].as_dict() for k in range(n)]
 
     def set_plan(self, wx=4.0, wz=3.0, per_sm=3, oversub=1.0):

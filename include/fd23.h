@@ -249,10 +249,12 @@ int fd23_batch_set_graph(fd23_batch *b, int on);
  * an estimated cost (wx for blocks touching the x-CPML, wz for the z-CPML and
  * edge rows, 1 otherwise), cut into equal-cost contiguous ranges for
  * per_sm x SMs x oversub CTAs.  fd23_autotune / fd23_batch_autotune time
- * every candidate plan for trial_steps steps on the live shot(s), restore the
- * wavefields, memory variables and step counters after each trial, and keep
- * the fastest plan.  table (cap entries) receives every trial; returns the
- * number of trials or a negative status. */
+ * every candidate plan (72: wx 2..7, wz 2..5, oversub 1..3) for trial_steps
+ * steps on the live shot(s), then the five fastest for 3 x trial_steps,
+ * restore the wavefields, memory variables and step counters after each
+ * trial, and keep the fastest plan of the second round.  table (cap
+ * entries) receives every trial, the second round last; returns the number
+ * of trials or a negative status. */
 typedef struct {
     double wx, wz;      /* block cost weights */
     int per_sm;         /* resident CTAs per SM */
