@@ -290,7 +290,8 @@ std::vector<TuneParams> candidates()
 }
 
 // Times every candidate for trial_steps steps, then the five fastest again
-// for three times as long (short trials are noisy); keeps the best of those
+// for three times as long (short trials are noisy), then the half-step
+// neighbours of the best weights; keeps the best of the long trials
 // installed.  `apply` installs a plan, `steps` runs k steps without
 // recording on `st`.  The table gets every trial, the second round last.
 template <class Apply, class Steps>
@@ -303,7 +304,7 @@ int autotune_core(const std::vector<fd23_solver *> &ss, cudaStream_t st, int tri
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
-    const std::vector<TuneParams> cand = candidates();
+    std::vector<TuneParams> cand = candidates();
     int best = -1, n = 0;
     std::vector<double> first(cand.size(), 1e300);
     auto trial = [&](size_t i, int k, double *per) -> int {
@@ -335,6 +336,22 @@ int autotune_core(const std::vector<fd23_solver *> &ss, cudaStream_t st, int tri
                 best_ms = per;
             }
         }
+        // third round: the half-step neighbours of the best weights
+        const TuneParams b0 = cand[best];
+        for (double dx : {-0.5, 0.0, 0.5})
+            for (double dz : {-0.5, 0.0, 0.5}) {
+                if ((dx == 0.0 && dz == 0.0) || b0.wx + dx < 1.0 || b0.wz + dz < 1.0 || rc) continue;
+                TuneParams t = b0;
+                t.wx += dx;
+                t.wz += dz;
+                cand.push_back(t);
+                double per = 0.0;
+                rc = trial(cand.size() - 1, 3 * trial_steps, &per);
+                if (!rc && per < best_ms) {
+                    best = (int)cand.size() - 1;
+                    best_ms = per;
+                }
+            }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

@@ -250,9 +250,10 @@ int fd23_batch_set_graph(fd23_batch *b, int on);
  * edge rows, 1 otherwise), cut into equal-cost contiguous ranges for
  * per_sm x SMs x oversub CTAs.  fd23_autotune / fd23_batch_autotune time
  * every candidate plan (72: wx 2..7, wz 2..5, oversub 1..3) for trial_steps
- * steps on the live shot(s), then the five fastest for 3 x trial_steps,
- * restore the wavefields, memory variables and step counters after each
- * trial, and keep the fastest plan of the second round.  table (cap
+ * steps on the live shot(s), then the five fastest and the 8 half-step
+ * neighbours of the best weights for 3 x trial_steps, restore the
+ * wavefields, memory variables and step counters after each trial, and
+ * keep the fastest plan of the long trials.  table (cap
  * entries) receives every trial, the second round last; returns the number
  * of trials or a negative status. */
 typedef struct {
