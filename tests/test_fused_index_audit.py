@@ -1,4 +1,4 @@
-"""CPU audit of every address the fused sweep forms (fd23_gb300/csrc/fd23_fused.cu).
+"""CPU audit of every address the fused sweep forms (fd23_gb300/csrc/fd23_fused.cuh).
 
 Takes the work plans from the library (fd23_work_plan: the planner the
 solver and the batch use), restates the padded layout (make_layout) and the
@@ -48,7 +48,7 @@ def al128(b):
 
 
 def smem_layout(es, wave):
-    """Byte offsets of the ring slots / stage groups (Cfg in fd23_fused.cu)."""
+    """Byte offsets of the ring slots / stage groups (Cfg in fd23_fused.cuh)."""
     nv, nt = (2, 3) if wave == "psv" else (1, 2)
     nms, nmv = (3, 2) if wave == "psv" else (2, 1)
     pwoff = 4 if es == 2 else 0
