@@ -56,7 +56,7 @@ ABI_FUNCTIONS = [
     "fd23_batch_get_stream", "fd23_batch_set_graph", "fd23_autotune", "fd23_batch_autotune",
     "fd23_batch_get_plan", "fd23_work_plan", "fd23_read_model", "fd23_read_stations",
     "fd23_debug_expire_wait", "fd23_set_plan", "fd23_get_plan", "fd23_punch_tiles", "fd23_punch_windows", "fd23_read_punch", "fd23_set_punch",
-    "fd23_set_material_table", "fd23_set_punch_phase",
+    "fd23_set_material_table", "fd23_set_punch_phase", "fd23_work_plan_live",
 ]
 
 
@@ -158,6 +158,7 @@ def lib():
         "fd23_set_punch": ([vp, vp, vp, i, i], i),
         "fd23_set_material_table": ([vp, i], i),
         "fd23_set_punch_phase": ([vp, i], i),
+        "fd23_work_plan_live": ([i, vp, vp, vp, vp, i, vp, vp, vp, i, vp, i], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -320,17 +321,20 @@ def box_material(mat, x0, z0, bx, bz, src_vp, src_vs, src_den, dt, h):
     return m, bm, n
 
 
-def work_plan(grids, sms=152, wx=4.0, wz=3.0, per_sm=3, oversub=1.0):
+def work_plan(grids, sms=152, wx=4.0, wz=3.0, per_sm=3, oversub=1.0, live=None):
     """The fused sweep's work plan for grids [(nx, nz, npml, topabsorb)]:
-    list over CTAs of lists of (shot, x0, z0, z1) items."""
+    list over CTAs of lists of (shot, x0, z0, z1) items.  live: optional
+    per-grid boolean arrays over the 4-row blocks (strip-major) to plan."""
     n = len(grids)
     a = [_np.ascontiguousarray([g[k] for g in grids], dtype=_np.int32) for k in range(4)]
     cap = sum(((g[0] + 119) // 120) * ((g[1] + 3) // 4) for g in grids) * 2 + 16
     items = _np.zeros(4 * cap, _np.int32)
     off = _np.zeros(cap + 1, _np.int32)
     t = TuneEntry(wx, wz, per_sm, oversub, 0.0)
-    nb = _check(lib().fd23_work_plan(n, *[_p(v) for v in a], sms, _C.cast(_C.pointer(t), _C.c_void_p),
-                                     _p(items), cap, _p(off), cap), "fd23_work_plan")
+    lv = None if live is None else _np.ascontiguousarray(_np.concatenate([_np.asarray(m, bool).ravel()
+                                                                           for m in live]), dtype=_np.uint8)
+    nb = _check(lib().fd23_work_plan_live(n, *[_p(v) for v in a], sms, _C.cast(_C.pointer(t), _C.c_void_p),
+                                          _p(lv), _p(items), cap, _p(off), cap), "fd23_work_plan_live")
     it = items.reshape(-1, 4)
     return [[tuple(int(v) for v in it[j]) for j in range(off[c], off[c + 1])] for c in range(nb)]
 

@@ -509,8 +509,9 @@ int fd23_batch_autotune(fd23_batch *b, int trial_steps, fd23_tune_entry *table, 
     return rc < 0 ? rc : (jr ? jr : rc);
 }
 
-int fd23_work_plan(int nshots, const int *nx, const int *nz, const int *npml, const int *topabsorb, int sms,
-                   const fd23_tune_entry *tune, int *items, int cap_items, int *off, int cap_ctas)
+int fd23_work_plan_live(int nshots, const int *nx, const int *nz, const int *npml, const int *topabsorb, int sms,
+                        const fd23_tune_entry *tune, const unsigned char *live, int *items, int cap_items, int *off,
+                        int cap_ctas)
 {
     if (nshots <= 0 || !nx || !nz || !npml || !topabsorb || sms <= 0 || !tune || !items || !off) return FD23_ERR_ARG;
     std::vector<ShotGeom> geo;
@@ -523,8 +524,18 @@ int fd23_work_plan(int nshots, const int *nx, const int *nz, const int *npml, co
     tp.wz = tune->wz;
     tp.per_sm = tune->per_sm;
     tp.oversub = tune->oversub;
+    const int tx = fused_geom(FD23_PSV, FD23_F32).tile_x;
+    std::vector<std::vector<unsigned char>> masks;
+    if (live) {
+        size_t at = 0;
+        for (int k = 0; k < nshots; ++k) {
+            const size_t nb = (size_t)((nx[k] + tx - 1) / tx) * ((nz[k] + 3) / 4);
+            masks.emplace_back(live + at, live + at + nb);
+            at += nb;
+        }
+    }
     WorkPlan plan;
-    const int rc = plan_work(geo, fused_geom(FD23_PSV, FD23_F32).tile_x, sms, tp, plan);
+    const int rc = plan_work(geo, tx, sms, tp, plan, live ? &masks : nullptr);
     if (rc) return rc;
     if ((int)plan.items.size() > cap_items || plan.nblocks + 1 > cap_ctas + 1) return FD23_ERR_ARG;
     for (size_t i = 0; i < plan.items.size(); ++i) {
@@ -535,6 +546,12 @@ int fd23_work_plan(int nshots, const int *nx, const int *nz, const int *npml, co
     }
     for (int c = 0; c <= plan.nblocks; ++c) off[c] = plan.off[c];
     return plan.nblocks;
+}
+
+int fd23_work_plan(int nshots, const int *nx, const int *nz, const int *npml, const int *topabsorb, int sms,
+                   const fd23_tune_entry *tune, int *items, int cap_items, int *off, int cap_ctas)
+{
+    return fd23_work_plan_live(nshots, nx, nz, npml, topabsorb, sms, tune, nullptr, items, cap_items, off, cap_ctas);
 }
 
 int fd23_set_plan(fd23_solver *s, const fd23_tune_entry *tune)

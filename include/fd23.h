@@ -277,6 +277,13 @@ int fd23_get_plan(fd23_solver *s, fd23_tune_entry *current, int *nblocks);
 int fd23_work_plan(int nshots, const int *nx, const int *nz, const int *npml, const int *topabsorb,
                    int sms, const fd23_tune_entry *tune, int *items, int cap_items, int *off,
                    int cap_ctas);
+/* The same over the live 4-row blocks only (the phase plans of the sweep
+ * with tile step windows): live holds, shot after shot, one byte per block
+ * (strip-major: strip * ceil(nz/4) + block, 120-column strips); a shot with
+ * no live block gets no CTA. */
+int fd23_work_plan_live(int nshots, const int *nx, const int *nz, const int *npml, const int *topabsorb,
+                        int sms, const fd23_tune_entry *tune, const unsigned char *live, int *items,
+                        int cap_items, int *off, int cap_ctas);
 
 /* ---- diagnostics ----
  * FP64 energy-norm watchdog over the wavefield: sum of squares of all

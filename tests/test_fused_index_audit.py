@@ -251,3 +251,39 @@ def test_table_index_box_in_bounds(nx, nz, es, wave):
                 assert ixo % 4 == 0 and ixo + 3 < IW
                 # the byte is the cell the point-wise row holds at this lane
                 assert xa + ixo == XPAD + x0 - 4 + 4 * q
+
+
+@pytest.mark.parametrize("nx,nz", [(230, 150), (1000, 500), (4000, 2000), (257, 131)])
+@pytest.mark.parametrize("density", [0.0, 0.05, 0.3, 1.0])
+def test_live_mask_plans(nx, nz, density):
+    """Plans over live blocks (the phase plans of the windowed sweep): every
+    live 4-row block is planned exactly once and nothing else, items stay in
+    one strip on whole blocks, no CTA has more than 4 items, the addresses
+    pass the audit, and an all-live mask gives the ordinary plan."""
+    import numpy as np
+    F = pytest.importorskip("fd23_gb300")
+    try:
+        F.lib()
+    except ImportError as e:
+        pytest.skip(str(e))
+    ntx, nzb = (nx + TX - 1) // TX, (nz + 3) // 4
+    rng = np.random.default_rng(nx + int(100 * density))
+    # live regions shaped like a growing wavefront, plus scattered blocks
+    zz, xx = np.mgrid[0:nzb, 0:ntx]
+    live = (np.hypot((xx - ntx / 2) * 30, zz * 4) < density * 2 * max(nx, nz)) | (rng.random((nzb, ntx)) < density / 10)
+    mask = live.T.ravel()  # strip-major
+    npml = min(40, nx // 2, nz // 2)
+    for ov in (1.0, 3.0):
+        ctas = F.work_plan([(nx, nz, npml, 0)], wx=5.0, wz=4.0, oversub=ov, live=[mask])
+        seen = np.zeros(ntx * nzb, int)
+        for cta in ctas:
+            assert len(cta) <= MAX_ITEMS
+            for (_, x0, z0, z1) in cta:
+                assert x0 % TX == 0 and z0 % 4 == 0 and z1 % 4 == 0 and z1 > z0
+                for zb in range(z0 // 4, z1 // 4):
+                    seen[(x0 // TX) * nzb + zb] += 1
+        np.testing.assert_array_equal(seen, mask.astype(int))
+        if mask.any():
+            audit(nx, nz, 4, "psv", ctas=[[it[1:] for it in c] for c in ctas], narrowed=True)
+    full = F.work_plan([(nx, nz, npml, 0)], wx=5.0, wz=4.0, live=[np.ones(ntx * nzb, bool)])
+    assert full == F.work_plan([(nx, nz, npml, 0)], wx=5.0, wz=4.0)
