@@ -497,6 +497,21 @@ int ensure_sigma(fd23_solver *s)
     return upload_source_amps(s);
 }
 
+// after a new material: the table follows it; with too many distinct tuples
+// it is dropped (as the reference's mktable gives up) and the sweep reads the
+// material arrays
+int material_done(fd23_solver *s)
+{
+    s->have_material = true;
+    if (!s->table_on) return FD23_OK;
+    const int rc = build_material_table(s);
+    if (rc == FD23_ERR_UNSUPPORTED) {
+        free_material_table(s);
+        s->table_on = false;
+        return s->fused ? encode_maps(s) : FD23_OK;
+    }
+    return rc;
+}
 }  // namespace fd23
 
 extern "C" {
@@ -633,26 +648,23 @@ int fd23_set_material(fd23_solver *s, const double *matv)
         if (rc) return rc;
         CK(cudaStreamSynchronize(s->stream));
     }
-    s->have_material = true;
-    if (s->table_on) {
-        // the table follows the material; with too many distinct tuples it
-        // is dropped (as the reference's mktable gives up) and the sweep
-        // reads the material arrays
-        const int rc = build_material_table(s);
-        if (rc == FD23_ERR_UNSUPPORTED) {
-            free_material_table(s);
-            s->table_on = false;
-            return s->fused ? encode_maps(s) : FD23_OK;
-        }
-        if (rc) return rc;
-    }
-    return FD23_OK;
+    return material_done(s);
 }
 
 int fd23_set_model(fd23_solver *s, const double *vp, const double *vs, const double *den, double *stab)
 {
     if (!s || !vs || !den || (s->d.wave == FD23_PSV && !vp)) return FD23_ERR_ARG;
     const size_t n = (size_t)s->d.nx * s->d.nz;
+    if (!scaled_form(s) && (s->d.prec == FD23_F32 || s->d.prec == FD23_F64)) {
+        // built on the device from vp, vs, den: the host builder's arithmetic
+        const double st = material_stab(s->d.wave, vp, vs, n, s->d.h, s->d.dt);
+        if (stab) *stab = st;
+        if (st > 1.0) return FD23_ERR_UNSTABLE;
+        CK(cudaSetDevice(s->d.device));
+        const int rc = build_material_device(s, vp, vs, den);
+        if (rc) return rc;
+        return material_done(s);
+    }
     std::vector<double> m((size_t)s->nmat * n);
     double st = 0.0;
     int rc = s->d.wave == FD23_PSV

@@ -25,7 +25,7 @@ const double kCoef[5][4] = {
 
 static const double kPi = 3.14159265358979;  // PD/param/const.h:26
 
-static double cfl_number(double vmax, double h, double dt)
+double cfl_number(double vmax, double h, double dt)
 {
     // stab = vmax*dt*sum(E)*sqrt(2)/h, PD/material/material.cpp:296-301
     const double esum = kCoef[4][0] + kCoef[4][1] + kCoef[4][2] + kCoef[4][3];
@@ -413,6 +413,20 @@ int box_material(int nx, int nz, double *mat, int x0, int z0, int bx, int bz, do
             bmat[4 * nb + k] = BW;
         }
     return replaced;
+}
+
+}  // namespace fd23
+
+namespace fd23 {
+
+// CFL number of a model: max of vp (P-SV) or vs (SH) through cfl_number, as
+// the builders above
+double material_stab(int wave, const double *vp, const double *vs, size_t n, double h, double dt)
+{
+    const double *v = wave == FD23_PSV ? vp : vs;
+    double vmax = -99999.0;
+    for (size_t k = 0; k < n; ++k) vmax = std::max(vmax, v[k]);
+    return cfl_number(vmax, h, dt);
 }
 
 }  // namespace fd23

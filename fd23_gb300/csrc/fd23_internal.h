@@ -206,6 +206,7 @@ void build_cpml_profile(int npml, double start, int n, double pml_dt, double pml
                         double pml_fc, double *b, double *c, double *k);
 void build_cpml(int wave, int nx, int nz, int npml, double pml_dt, double pml_r, double pml_v,
                 double pml_fc, std::vector<double> &bck);
+double material_stab(int wave, const double *vp, const double *vs, size_t n, double h, double dt);
 void moment_psv(double strike, double dip, double rake, double azimuth, double m[3]);
 void moment_sh(double strike, double dip, double rake, double azimuth, double m[2]);
 int wavelet_gaussian(double dt, int alpha, double *out, int cap);

@@ -135,6 +135,9 @@ int upload_grid(fd23_solver *s, void *dptr, const unsigned char *host, size_t es
 int download_grid(fd23_solver *s, const void *dptr, unsigned char *host, size_t es);
 void free_material_table(fd23_solver *s);
 int encode_maps(fd23_solver *s);
+// the material of vp, vs, den built on the device into the storage arrays
+// (fd23_matgpu.cu; FP32 and FP64 storage, FD23_ERR_UNSUPPORTED otherwise)
+int build_material_device(fd23_solver *s, const double *vp, const double *vs, const double *den);
 
 template <class S, class C>
 Shot<S, C> make_shot(const fd23_solver *s)
