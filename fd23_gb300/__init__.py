@@ -57,6 +57,7 @@ ABI_FUNCTIONS = [
     "fd23_batch_get_plan", "fd23_work_plan", "fd23_read_model", "fd23_read_stations",
     "fd23_debug_expire_wait", "fd23_set_plan", "fd23_get_plan", "fd23_punch_tiles", "fd23_punch_windows", "fd23_read_punch", "fd23_set_punch",
     "fd23_set_material_table", "fd23_set_punch_phase", "fd23_work_plan_live",
+    "fd23_line_source_coefs", "fd23_line_plane_origin", "fd23_line_source_planes", "fd23_set_box_line_source",
 ]
 
 
@@ -73,6 +74,18 @@ class TuneEntry(_C.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class LineDesc(_C.Structure):
+    """fd23_line_desc: planes of the box-source generator."""
+    _fields_ = [("px", _C.c_int), ("pz", _C.c_int), ("ox", _C.c_int), ("oz", _C.c_int),
+                ("h", _C.c_double), ("dt", _C.c_double), ("vp", _C.c_double), ("vs", _C.c_double),
+                ("den", _C.c_double), ("a", _C.c_double * 3), ("sx", _C.c_double), ("sz", _C.c_double)]
+
+
+def line_desc(px, pz, ox, oz, h, dt, vp, vs, den, a, sx=0.25, sz=-0.25):
+    """A LineDesc; a = line_source_coefs(strike, dip, rake, azimuth)."""
+    return LineDesc(px, pz, ox, oz, h, dt, vp, vs, den, (_C.c_double * 3)(*[float(v) for v in a]), sx, sz)
 
 
 class Desc(_C.Structure):
@@ -159,6 +172,10 @@ def lib():
         "fd23_set_material_table": ([vp, i], i),
         "fd23_set_punch_phase": ([vp, i], i),
         "fd23_work_plan_live": ([i, vp, vp, vp, vp, i, vp, vp, vp, i, vp, i], i),
+        "fd23_line_source_coefs": ([d, d, d, d, vp], i),
+        "fd23_line_plane_origin": ([i], i),
+        "fd23_line_source_planes": ([i, _C.POINTER(LineDesc), vp, i, i, i, vp], i),
+        "fd23_set_box_line_source": ([vp, _C.POINTER(LineDesc), vp, i, vp, i, i], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -307,6 +324,29 @@ def box_incident_from_displacement(bx, bz, dt, bmat, u_old, w_old, u_new, w_new)
     a = [_f64(v) for v in (bmat, u_old, w_old, u_new, w_new)]
     _check(lib().fd23_box_incident_from_displacement(bx, bz, dt, *[_p(v) for v in a], _p(out)),
            "fd23_box_incident_from_displacement")
+    return out
+
+
+def line_source_coefs(strike, dip, rake, azimuth):
+    """Radiation coefficients (A1, A2, A3) of the line moment source."""
+    a = _np.zeros(3)
+    _check(lib().fd23_line_source_coefs(strike, dip, rake, azimuth, _p(a)), "fd23_line_source_coefs")
+    return a
+
+
+def line_plane_origin(bw):
+    """Source-relative offset of plane cell (0, 0) of the reference's
+    bw x bw box."""
+    return lib().fd23_line_plane_origin(bw)
+
+
+def line_source_planes(desc, src, it0, nframes, device=0):
+    """Frames it0 .. it0+nframes-1 of the box-source generator on the GPU:
+    array [nframes, 2, pz, px] (U plane, W plane), the source-file layout."""
+    src = _f64(src)
+    out = _np.zeros((nframes, 2, desc.pz, desc.px))
+    _check(lib().fd23_line_source_planes(device, _C.byref(desc), _p(src), len(src), it0, nframes, _p(out)),
+           "fd23_line_source_planes")
     return out
 
 
@@ -650,6 +690,18 @@ class Solver:
                 raise ValueError("set_box_incident: shape %s, expected (nsteps, 5, %d)" % (a.shape, nring))
         _check(lib().fd23_set_box_incident(self._h, _p(a), it0, a.shape[0] if a.ndim == 3 else 0),
                "fd23_set_box_incident")
+
+    def set_box_line_source(self, desc, src, bmat, it0, nsteps):
+        """Incident field of steps it0 .. it0+nsteps-1 generated on the device
+        from the line source desc (planes (bx+8) x (bz+8)); bmat (5, bz, bx)
+        FP64 box material."""
+        src = _f64(src)
+        if self._box is not None:
+            bmat = _sized(_f64(bmat), 5 * self._box[2] * self._box[3], "bmat")
+        else:
+            bmat = _f64(bmat)
+        _check(lib().fd23_set_box_line_source(self._h, _C.byref(desc), _p(src), len(src), _p(bmat), it0, nsteps),
+               "fd23_set_box_line_source")
 
     def get_box_state(self):
         n = lib().fd23_box_state_bytes(self._h) // _np.dtype(self.dtype).itemsize

@@ -32,6 +32,10 @@
  *                                         fd23_box_incident_from_displacement + fd23_set_box_incident
  *   BOX::cu_addsource/cu_subsource, cu_step_stress_r/_velocity_r
  *                                  PD/box/cu_box.cu:55,71; PD/fd/cu_fd.cu:504,523  fd23_run (box set)
+ *   the box-source generator ntde_line (compute_pQpW_mathematica + cu_con)
+ *                                  PD/source/source_line.cpp:196-410,
+ *                                  PD/source/cu_source.cu:2-42  fd23_line_source_planes,
+ *                                                                fd23_set_box_line_source
  *
  * Conventions: every call returns FD23_OK (0) or a negative status and never
  * exits the process; fd23_strerror() names the status.  Host arrays passed in
@@ -223,6 +227,52 @@ int fd23_box_incident_from_displacement(int bx, int bz, double dt, const double 
  * than 1e-4 are set to it in mat too.  Returns the number of such cells. */
 int fd23_box_material(int nx, int nz, double *mat, int x0, int z0, int bx, int bz, double src_vp,
                       double src_vs, double src_den, double dt, double h, double *bmat);
+
+/* ---- box-source generator (the reference's ntde_line program,
+ * PD/source/source_line.cpp:307-410) ----
+ * Displacement planes of a line moment source in a homogeneous full space,
+ * the incident field of the hybrid box.  Plane cell (p, q), p < px, q < pz,
+ * is ox + p, oz + q cells from the source cell; the U plane samples the
+ * point ((ox+p) + 0.5 - sx, (oz+q) - sz) * h, the W plane
+ * ((ox+p) - sx, (oz+q) - 0.5 - sz) * h (x right, z down).  Each sample is
+ * the time derivative of the closed-form 2-D Green's function
+ * (compute_pQpW_mathematica, :196-305; FP64), convolved with the wavelet
+ * src (s(t) dt values, as fd23_set_source takes) in the reference kernel's
+ * order (cu_con, PD/source/cu_source.cu:2-42).  Samples before a point's
+ * P arrival are zero; points within one step's travel of the source give
+ * NaN at t = 0 (0/0), as in the reference, and so NaN in the first
+ * frames after the convolution.
+ * The reference writes frames 0 .. nt-1 of the square box around its
+ * source: px = pz = bw + 8, ox = oz = fd23_line_plane_origin(bw),
+ * sx = 0.25, sz = -0.25, a = fd23_line_source_coefs(strike, dip, rake,
+ * azimuth) (:320-326, theta = azimuth - strike). */
+typedef struct {
+    int px, pz;          /* plane size in cells */
+    int ox, oz;          /* source-relative cell offset of plane cell (0, 0) */
+    double h, dt;
+    double vp, vs, den;  /* the homogeneous medium (srcpvel, srcsvel, srcden) */
+    double a[3];         /* radiation coefficients A1, A2, A3 */
+    double sx, sz;       /* source point inside its cell, in cells */
+} fd23_line_desc;
+int fd23_line_source_coefs(double strike, double dip, double rake, double azimuth, double a[3]);
+int fd23_line_plane_origin(int bw);
+/* Frames it0 .. it0+nframes-1 computed on the GPU `device`, written to the
+ * host buffer out as [frame][U plane, W plane][pz][px] doubles (the layout
+ * of the reference's source file).  FD23_ERR_ARG for sizes <= 0, lsrc < 1
+ * or lsrc > 8192, a non-positive h, dt, vp, vs or den. */
+int fd23_line_source_planes(int device, const fd23_line_desc *d, const double *src, int lsrc, int it0,
+                            int nframes, double *out);
+/* The box's incident field of steps it0 .. it0+nsteps-1 generated on the
+ * device from the line source: frames it0 .. it0+nsteps of the planes the
+ * ring stencils read (px = bx+8, pz = bz+8, plane cell (i+4, j+4) = box
+ * cell (i, j)) followed by the setboxsource step with the box material
+ * bmat (FP64, as for fd23_set_box; LAM, MU, MUA used), in place of a
+ * fd23_set_box_incident upload.  Same values as
+ * fd23_line_source_planes -> fd23_box_incident_from_displacement ->
+ * fd23_set_box_incident.  FD23_ERR_ORDER without a box, FD23_ERR_ARG for
+ * planes of another size. */
+int fd23_set_box_line_source(fd23_solver *s, const fd23_line_desc *d, const double *src, int lsrc,
+                             const double *bmat, int it0, int nsteps);
 
 /* ---- batched shots (no counterpart in the reference, which runs one shot
  * per process, PD/main.cpp:43-183) ----

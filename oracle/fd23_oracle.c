@@ -614,4 +614,164 @@ static inline int or_punch_skip(int nx, int ix, int iz, int it)
 #undef FMA
 #undef SFX
 
+/* ------------------------------------------------------------------------- */
+/* Box-source generator (FP64): the ntde_line program,                        */
+/* PD/source/source_line.cpp:307-410 (main), :196-305                         */
+/* (compute_pQpW_mathematica) and the wavelet convolution cu_con of           */
+/* PD/source/cu_source.cu:2-42.                                               */
+/* ------------------------------------------------------------------------- */
+
+/* Radiation coefficients A1, A2, A3 of a line moment source
+ * (PD/source/source_line.cpp:320-326): theta = azimuth - strike, delta = dip,
+ * lambda = rake, degrees. */
+void or_line_source_coefs(double strike, double dip, double rake, double azimuth, double *a)
+{
+    const double d = dip * OR_PI / 180.0, l = rake * OR_PI / 180.0, th = (azimuth - strike) * OR_PI / 180.0;
+    a[0] = sin(2.0 * th) * cos(l) * sin(d) + 0.5 * cos(2.0 * th) * sin(l) * sin(2.0 * d);
+    a[1] = cos(th) * cos(l) * cos(d) - sin(th) * sin(l) * cos(2.0 * d);
+    a[2] = 0.5 * sin(l) * sin(2.0 * d);
+}
+
+/* Per receiver point (r, z) (metres from the source, z down) and component
+ * (0 = horizontal "Q", 1 = vertical "W"), the time derivative of the 2-D
+ * full-space displacement of the line source is
+ *   v(t) = t^3 (Ta - Tb) k[0] + t (Ta k[1] + Tb k[2]) + (Ta k[3] + Tb k[4]) / t
+ * with Ta = 1/sqrt(1 - (R/(t vp))^2), Tb likewise with vs.  k[] folds the
+ * closed-form polynomials in r and z of the reference expressions
+ * (source_line.cpp:262-299, one table row per radiation term A1, A2, A3 and
+ * per power of t), the radiation coefficients, 1/vp^2, 1/vs^2, 1/vp^4,
+ * 1/vs^4 and G/R^8, G = sqrt(2)/(4 pi^2 den).  Products and sums in the order
+ * written; the CUDA generator evaluates the same sequence. */
+void or_line_source_kcoef(double r, double z, int comp, double vp, double vs, double den, const double *a,
+                          double *k)
+{
+    const double r2 = r * r, z2 = z * z, rz = r * z;
+    const double r4 = r2 * r2, z4 = z2 * z2, r6 = r4 * r2, z6 = z4 * z2, z8 = z4 * z4;
+    const double R2 = r2 + z2, R4 = R2 * R2;
+    const double dif = r2 - z2;
+    const double e4 = r4 - 6.0 * r2 * z2 + z4;                   /* r^4 - 6 r^2 z^2 + z^4 */
+    const double e6 = r6 - 5.0 * r4 * z2 - 5.0 * r2 * z4 + z6;   /* r^6 - 5 r^4 z^2 - 5 r^2 z^4 + z^6 */
+    const double f4 = 3.0 * r4 - 2.0 * r2 * z2 - 5.0 * z4;       /* 3 r^4 - 2 r^2 z^2 - 5 z^4 */
+    double p[3][5]; /* [A term][t^3, t*Ta, t*Tb, Ta/t, Tb/t] */
+    if (comp == 0) {
+        p[0][0] = e4;
+        p[0][1] = 2.0 * (3.0 * r4 * z2 + 2.0 * r2 * z4 - z6);
+        p[0][2] = e6;
+        p[0][3] = R4 * z4;
+        p[0][4] = r2 * R4 * z2;
+        p[1][0] = -8.0 * rz * dif;
+        p[1][1] = 2.0 * rz * f4;
+        p[1][2] = 8.0 * rz * (z4 - r4);
+        p[1][3] = 2.0 * rz * R4 * z2;
+        p[1][4] = rz * R4 * dif;
+        p[2][0] = -3.0 * e4;
+        p[2][1] = 2.0 * (r6 - 8.0 * r4 * z2 - 7.0 * r2 * z4 + 2.0 * z6);
+        p[2][2] = -3.0 * e6;
+        p[2][3] = 2.0 * r6 * z2 + 3.0 * r4 * z4 - z8;
+        p[2][4] = -3.0 * r2 * R4 * z2;
+    } else {
+        p[0][0] = 4.0 * rz * dif;
+        p[0][1] = -rz * f4;
+        p[0][2] = rz * f4;
+        p[0][3] = -rz * R4 * z2;
+        p[0][4] = rz * R4 * z2;
+        p[1][0] = 2.0 * e4;
+        p[1][1] = -2.0 * e6;
+        p[1][2] = r6 - 11.0 * r4 * z2 - 9.0 * r2 * z4 + 3.0 * z6;
+        p[1][3] = -2.0 * r2 * R4 * z2;
+        p[1][4] = R4 * dif * z2;
+        p[2][0] = -12.0 * rz * dif;
+        p[2][1] = rz * (13.0 * r4 + 2.0 * r2 * z2 - 11.0 * z4);
+        p[2][2] = -3.0 * rz * f4;
+        p[2][3] = rz * (z6 - 2.0 * r6 - 3.0 * r4 * z2);
+        p[2][4] = -3.0 * rz * R4 * z2;
+    }
+    const double ivp2 = 1.0 / (vp * vp), ivs2 = 1.0 / (vs * vs);
+    const double G = sqrt(2.0) / (4.0 * OR_PI * OR_PI * den);
+    const double S = G / (R4 * R4);
+    const double w[5] = {S, S * ivp2, S * ivs2, S * (ivp2 * ivp2), S * (ivs2 * ivs2)};
+    for (int j = 0; j < 5; j++) k[j] = (a[0] * p[0][j] + a[1] * p[1][j] + a[2] * p[2][j]) * w[j];
+}
+
+/* The wave factor T(i) at sample i (t = i dt) for travel time R/v
+ * (source_line.cpp:199-222): 0 up to the arrival step n = floor(R/v/dt);
+ * at n+1 the integrated first sample sqrt(b (2 R/(v dt) + b)),
+ * b = (n+1) - R/v/dt + 0.5; afterwards 1/sqrt(1 - (R/(t v))^2). */
+static double or_line_wave(double R, double v, double dt, int i)
+{
+    const double u = R / v / dt;
+    const int n = (int)floor(u);
+    if (i <= n) return 0.0;
+    if (i == n + 1) {
+        const double b = ((double)(n + 1) - u) + 0.5;
+        return sqrt(b * (2.0 * u + b));
+    }
+    const double t = i * dt, q = R / (t * v);
+    return 1.0 / sqrt(1.0 - q * q);
+}
+
+/* One sample of v(t) above; samples before the P arrival step are 0 (the
+ * arrival step itself is evaluated, which at t = 0 gives 0/0 as in the
+ * reference). */
+double or_line_sample(double R, const double *k, double vp, double vs, double dt, int i)
+{
+    const int na = (int)floor(R / vp / dt);
+    if (i < na) return 0.0;
+    const double t = i * dt;
+    const double ta = or_line_wave(R, vp, dt, i), tb = or_line_wave(R, vs, dt, i);
+    const double t3 = (t * t) * t;
+    double v = (t3 * (ta - tb)) * k[0];
+    v = v + t * (ta * k[1] + tb * k[2]);
+    v = v + (ta * k[3] + tb * k[4]) / t;
+    return v;
+}
+
+/* Displacement planes of frames it0 .. it0+nf-1: out[f][comp][q*px + p],
+ * comp 0 = U plane (point ((ox+p)+0.5-sx, (oz+q)-sz) cells from the source),
+ * comp 1 = W plane (point ((ox+p)-sx, (oz+q)-0.5-sz)); both times h.  Each
+ * sample is the causal convolution with the wavelet src[0..lsrc) in the
+ * reference kernel's order: the wavelet padded with zeros to a multiple of
+ * 32 taps, taps taken from the last to the first, one fused multiply-add
+ * each (PD/source/cu_source.cu:2-16; out[k] = sum_j src[j] g[k-j], g = 0
+ * before sample 0).  The reference program writes frames 0 .. nt-1 for the
+ * square box px = pz = bw+8, ox = oz = (bw+1)/2 + 4 + 1 - (bw+8),
+ * sx = 0.25, sz = -0.25.  Returns 0, -1 on bad arguments or memory. */
+int or_line_source_planes(int px, int pz, int ox, int oz, double h, double dt, double vp, double vs, double den,
+                          const double *a, double sx, double sz, const double *src, int lsrc, int it0, int nf,
+                          double *out)
+{
+    if (px <= 0 || pz <= 0 || lsrc <= 0 || it0 < 0 || nf < 0 || !(vp > 0) || !(vs > 0) || !(dt > 0)) return -1;
+    const int ntap = ((lsrc + 31) / 32) * 32;
+    const int ng = it0 + nf; /* samples 0 .. ng-1 of g */
+    double *tap = (double *)calloc((size_t)ntap, sizeof(double));
+    double *g = (double *)malloc(sizeof(double) * (size_t)(ng > 0 ? ng : 1));
+    if (!tap || !g) {
+        free(tap);
+        free(g);
+        return -1;
+    }
+    for (int j = 0; j < lsrc; j++) tap[j] = src[j];
+    const long plane = (long)px * pz;
+    for (int comp = 0; comp < 2; comp++)
+        for (int q = 0; q < pz; q++)
+            for (int p = 0; p < px; p++) {
+                const double x = comp == 0 ? ((ox + p) + 0.5) - sx : (ox + p) - sx;
+                const double zz = comp == 0 ? (oz + q) - sz : ((oz + q) - 0.5) - sz;
+                const double r = x * h, z = zz * h;
+                double k[5];
+                or_line_source_kcoef(r, z, comp, vp, vs, den, a, k);
+                const double R = sqrt(r * r + z * z);
+                for (int i = 0; i < ng; i++) g[i] = or_line_sample(R, k, vp, vs, dt, i);
+                for (int f = 0; f < nf; f++) {
+                    const int it = it0 + f;
+                    double acc = 0.0;
+                    for (int j = ntap - 1; j >= 0; j--) acc = fma(tap[j], it - j >= 0 ? g[it - j] : 0.0, acc);
+                    out[((long)f * 2 + comp) * plane + (long)q * px + p] = acc;
+                }
+            }
+    free(tap);
+    free(g);
+    return 0;
+}
+
 int or_version(void) { return 1; }

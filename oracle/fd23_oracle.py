@@ -55,6 +55,9 @@ def lib():
         for nm in ("or_psv_box_run_f64", "or_psv_box_run_f32"):
             getattr(_lib, nm).argtypes = [i, i, i, i, vp, vp, i, vp, vp, vp, i, i, vp, vp,
                                           i, i, i, vp, vp, i, i, i, i, vp, vp, vp, i]
+        _lib.or_line_source_coefs.argtypes = [d, d, d, d, vp]
+        _lib.or_line_source_coefs.restype = None
+        _lib.or_line_source_planes.argtypes = [i, i, i, i, d, d, d, d, d, vp, d, d, vp, i, i, i, vp]
     return _lib
 
 
@@ -407,6 +410,35 @@ def box_incident_from_displacement(bx, bz, dt, rmat, uo, wo, un, wn):
     out = np.zeros((5, nsub + nadd))
     a = [np.ascontiguousarray(v, dtype=np.float64) for v in (rmat, uo, wo, un, wn)]
     lib().or_box_incident_from_displacement(bx, bz, dt, *[_p(v) for v in a], _p(out))
+    return out
+
+
+def line_source_coefs(strike, dip, rake, azimuth):
+    """Radiation coefficients (A1, A2, A3) of the line moment source
+    (PD/source/source_line.cpp:320-326)."""
+    a = np.zeros(3)
+    lib().or_line_source_coefs(strike, dip, rake, azimuth, _p(a))
+    return a
+
+
+def box_plane_origin(bw):
+    """Source-relative cell offset of plane cell (0, 0) for the reference's
+    square box of width bw (PD/source/source_line.cpp:346-347)."""
+    return (bw + 1) // 2 + 4 + 1 - (bw + 8)
+
+
+def line_source_planes(px, pz, ox, oz, h, dt, vp, vs, den, a, src, it0, nf, sx=0.25, sz=-0.25):
+    """Displacement planes of the box-source generator (ntde_line,
+    PD/source/source_line.cpp:307-410): array [nf, 2, pz, px] of frames
+    it0 .. it0+nf-1 (U plane, W plane), the layout of the reference's source
+    file."""
+    out = np.zeros((nf, 2, pz, px))
+    src = np.ascontiguousarray(src, dtype=np.float64)
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    rc = lib().or_line_source_planes(px, pz, ox, oz, h, dt, vp, vs, den, _p(a), sx, sz, _p(src), len(src),
+                                     it0, nf, _p(out))
+    if rc:
+        raise ValueError("bad line-source arguments")
     return out
 
 
