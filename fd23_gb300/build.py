@@ -57,16 +57,18 @@ def _compile(src, verbose=False):
 CLI_SRC = os.path.join(HERE, "cli", "fd23_psv2d.cpp")
 CLI = os.path.join(LIBDIR, "fd23_psv2d")
 CLI_SH = os.path.join(LIBDIR, "fd23_sh2d")
+CLI_NTDE = os.path.join(LIBDIR, "fd23_ntde_line")
 
 
 def build_cli(force=False):
-    """The parfile programs fd23_psv2d and fd23_sh2d (one source) next to the
-    library, linked to it and finding it through their own directory."""
+    """The parfile programs fd23_psv2d, fd23_sh2d and fd23_ntde_line (one
+    source) next to the library, linked to it and finding it through their
+    own directory."""
     newest = max(os.path.getmtime(p) for p in [CLI_SRC, LIB] + headers())
-    for exe, sh in ((CLI, 0), (CLI_SH, 1)):
+    for exe, flag in ((CLI, "-DFD23_CLI_SH=0"), (CLI_SH, "-DFD23_CLI_SH=1"), (CLI_NTDE, "-DFD23_CLI_NTDE=1")):
         if not force and os.path.exists(exe) and os.path.getmtime(exe) >= newest:
             continue
-        cmd = [_nvcc(), "-x", "c++", "-std=c++17", "-O2", "-DFD23_CLI_SH=%d" % sh, CLI_SRC, "-o", exe,
+        cmd = [_nvcc(), "-x", "c++", "-std=c++17", "-O2", flag, CLI_SRC, "-o", exe,
                "-L" + LIBDIR, "-lfd23", "-Xlinker", "-rpath=$ORIGIN"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

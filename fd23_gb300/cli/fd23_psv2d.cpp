@@ -28,9 +28,21 @@
 // dt).  usetable=1 (PN/param/param.cpp:180-181; the SH program's default,
 // SH/main.cpp:154) reads the material through a table of its distinct
 // tuples when they fit (fd23_set_material_table), else prints the
-// reference's "Too many materials" and goes on without.  Not supported
-// here: usebox=1 (the box is in the C ABI).  Additions: prec (f32, f64,
-// bf16, f16; default f32),
+// reference's "Too many materials" and goes on without.  usebox=1 (P-SV,
+// prec f32 or f64; PD/main.cpp:153-200, PD/box/box.cpp) runs the hybrid
+// box of width bw around (xs, zs) instead of the point source: the box
+// material is the homogeneous srcpvel / srcsvel / srcden
+// (PD/material/material.cpp:39-97, box cells of the model that differ are
+// replaced), and the incident field comes from sourcefile, the
+// displacement planes the box-source generator wrote (fd23_ntde_line or
+// the reference's ntde_line), read frame by frame as the reference reads
+// them (a frame past the end of the file leaves the older buffer in place,
+// PD/box/box.cpp:120-139); boxsource=device (an addition) generates the
+// planes on the GPU from the parfile's source instead of reading the file.
+// zs closer than bw/2+4 to the top or bottom is refused
+// (PD/param/param.cpp:182-185).  Additions: prec (f32, f64,
+// bf16, f16; default f32; f64 reads h and dt as doubles, as the PD
+// programs do, the others round them to float as PN does),
 // explosion (1: Mxx = Mzz = 1, the *_exp builds), topabsorb (1: CPML on top,
 // the *_topabsorb builds), device (CUDA ordinal, default 0), dryrun (1: print
 // the resolved set-up and stop before touching the GPU).
@@ -43,6 +55,13 @@
 // savestate=1 the state file state%06d (step nt0+nt-1); with restart=1 the
 // run starts from state%06d (step nt0-1).  Header words the reference leaves
 // unset are written as zero.
+//
+// Built with FD23_CLI_NTDE=1 it is fd23_ntde_line, the reference's
+// box-source generator (PD/source/source_line.cpp:307-410): from the same
+// parfile (nt h dt srcden srcsvel srcpvel sourcefile bw sourcetime with
+// alpha or trap1-3, strike dip rake azimuth; device optional) it writes
+// sourcefile, nt frames of the (bw+8) x (bw+8) U and W displacement planes
+// as doubles, computed on the GPU (fd23_line_source_planes).
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -59,11 +78,15 @@
 #ifndef FD23_CLI_SH
 #define FD23_CLI_SH 0
 #endif
+#ifndef FD23_CLI_NTDE
+#define FD23_CLI_NTDE 0
+#endif
 
 namespace {
 
 constexpr bool kSH = FD23_CLI_SH != 0;
-const char *kProg = kSH ? "fd23_sh2d" : "fd23_psv2d";
+constexpr bool kNTDE = FD23_CLI_NTDE != 0;
+const char *kProg = kNTDE ? "fd23_ntde_line" : (kSH ? "fd23_sh2d" : "fd23_psv2d");
 
 struct Params {
     std::map<std::string, std::string> kv;
@@ -136,6 +159,130 @@ bool write_file(const std::string &name, const void *p, size_t bytes)
     return f && f.write((const char *)p, (std::streamsize)bytes);
 }
 
+bool report_missing(Params &p)
+{
+    if (p.missing.empty()) return false;
+    std::fprintf(stderr, "%s: missing parameter(s):", kProg);
+    for (auto &m : p.missing) std::fprintf(stderr, " %s", m.c_str());
+    std::fprintf(stderr, "\n");
+    return true;
+}
+
+// the source time function of the PD programs' "sourcetime" keys
+// (PD/param/param.cpp:92-100): s(t)*dt samples, or an empty vector
+std::vector<double> pd_wavelet(Params &p, double dt)
+{
+    const std::string st = p.need("sourcetime");
+    std::vector<double> src(1 << 20);
+    int n = -1;
+    if (!st.empty() && (st[0] == 'G' || st[0] == 'g'))
+        n = fd23_wavelet_gaussian(dt, (int)p.need_num("alpha"), src.data(), (int)src.size());
+    else if (!st.empty() && (st[0] == 'T' || st[0] == 't'))
+        n = fd23_wavelet_trapezoid(dt, p.need_num("trap1"), p.need_num("trap2"), p.need_num("trap3"), src.data(),
+                                   (int)src.size());
+    src.resize(n > 0 ? n : 0);
+    return src;
+}
+
+// the line source of the box-source generator for a bw x bw box around its
+// source (PD/source/source_line.cpp:307-347)
+fd23_line_desc line_desc(int bw, double h, double dt, double vp, double vs, double den, double strike, double dip,
+                         double rake, double azimuth)
+{
+    fd23_line_desc d{};
+    d.px = d.pz = bw + 8;
+    d.ox = d.oz = fd23_line_plane_origin(bw);
+    d.h = h;
+    d.dt = dt;
+    d.vp = vp;
+    d.vs = vs;
+    d.den = den;
+    fd23_line_source_coefs(strike, dip, rake, azimuth, d.a);
+    d.sx = 0.25;  // the generator's fixed source point (source_line.cpp:309-310)
+    d.sz = -0.25;
+    return d;
+}
+
+// fd23_ntde_line: the planes of frames 0 .. nt-1 into sourcefile
+int ntde_main(Params &p)
+{
+    const int nt = (int)p.need_num("nt"), bw = (int)p.need_num("bw");
+    const double h = p.need_num("h"), dt = p.need_num("dt");
+    const double den = p.need_num("srcden"), vs = p.need_num("srcsvel"), vp = p.need_num("srcpvel");
+    const std::string out = p.need("sourcefile");
+    const double strike = p.need_num("strike"), dip = p.need_num("dip"), rake = p.need_num("rake"),
+                 azimuth = p.need_num("azimuth");
+    const std::vector<double> src = pd_wavelet(p, dt);
+    const int device = (int)p.num("device", 0);
+    if (report_missing(p)) return 1;
+    if (src.empty() || nt < 1 || bw < 1) {
+        std::fprintf(stderr, "%s: sourcetime must be Gaussian or Trapezoid; nt and bw positive\n", kProg);
+        return 1;
+    }
+    const fd23_line_desc d = line_desc(bw, h, dt, vp, vs, den, strike, dip, rake, azimuth);
+    const size_t frame = 2 * (size_t)d.px * d.pz;
+    std::ofstream f(out, std::ios::binary);
+    if (!f) {
+        std::fprintf(stderr, "%s: cannot write %s\n", kProg, out.c_str());
+        return 1;
+    }
+    const int chunk = (int)std::max<size_t>(1, ((size_t)64 << 20) / (frame * sizeof(double)));
+    std::vector<double> buf;
+    for (int f0 = 0; f0 < nt; f0 += chunk) {
+        const int nf = std::min(chunk, nt - f0);
+        buf.resize((size_t)nf * frame);
+        const int rc = fd23_line_source_planes(device, &d, src.data(), (int)src.size(), f0, nf, buf.data());
+        if (rc) return fail("planes", rc);
+        if (!f.write((const char *)buf.data(), (std::streamsize)(buf.size() * sizeof(double)))) {
+            std::fprintf(stderr, "%s: cannot write %s\n", kProg, out.c_str());
+            return 1;
+        }
+    }
+    std::printf("finish!\n");
+    return 0;
+}
+
+// The box's incident field of steps 0 .. nt-1 from the planes file, read as
+// BOX::init_box / setboxsource read it (PD/box/box.cpp:106-139): frame 0 at
+// set-up, one frame per step into alternating buffers; a read past the end
+// of the file leaves the buffer as it was.
+int incident_from_file(const std::string &name, int bw, int nt, double dt, const std::vector<double> &bmat,
+                       bool f64, std::vector<unsigned char> &inc)
+{
+    int nsub = 0, nadd = 0;
+    const int nring = fd23_box_ring_size(bw, bw, &nsub, &nadd);
+    if (nring < 0) return nring;
+    const size_t plane = (size_t)(bw + 8) * (bw + 8);
+    std::ifstream f(name, std::ios::binary);
+    if (!f) return FD23_ERR_ARG;
+    std::vector<double> u1(plane), w1(plane), u2(plane), w2(plane), one(5 * (size_t)nring);
+    auto rd = [&](std::vector<double> &v) {
+        if (f) f.read((char *)v.data(), (std::streamsize)(plane * sizeof(double)));
+    };
+    rd(u1);
+    rd(w1);
+    if (!f) return FD23_ERR_ARG;  // not even frame 0
+    const size_t cs = f64 ? 8 : 4;
+    inc.assign((size_t)nt * 5 * nring * cs, 0);
+    bool read_u1 = false;
+    for (int it = 0; it < nt; ++it) {
+        std::vector<double> &un = read_u1 ? u1 : u2, &wn = read_u1 ? w1 : w2;
+        const std::vector<double> &uo = read_u1 ? u2 : u1, &wo = read_u1 ? w2 : w1;
+        rd(un);
+        rd(wn);
+        read_u1 = !read_u1;
+        const int rc = fd23_box_incident_from_displacement(bw, bw, dt, bmat.data(), uo.data(), wo.data(),
+                                                           un.data(), wn.data(), one.data());
+        if (rc < 0) return rc;
+        unsigned char *o = inc.data() + (size_t)it * 5 * nring * cs;
+        for (size_t k = 0; k < one.size(); ++k) {
+            if (f64) reinterpret_cast<double *>(o)[k] = one[k];
+            else reinterpret_cast<float *>(o)[k] = (float)one[k];
+        }
+    }
+    return FD23_OK;
+}
+
 }  // namespace
 
 int main(int argc, char **argv)
@@ -157,14 +304,22 @@ int main(int argc, char **argv)
         std::fprintf(stderr, "usage: %s par=file [key=value ...]\n", kProg);
         return 1;
     }
+    if (kNTDE) return ntde_main(p);
+    const std::string precs = p.str("prec", "f32");
     const int restart = (int)p.num("restart", 0), savestate = (int)p.num("savestate", 0);
     const int nt0 = restart ? (int)p.need_num("nt0") : 0;
     const int nx = (int)p.need_num("nx"), nz = (int)p.need_num("nz"), nt = (int)p.need_num("nt");
-    const float h = (float)p.need_num("h"), dt = (float)p.need_num("dt");
+    // PN reads h and dt as float, PD (prec=f64) as double
+    const bool pd = precs == "f64";
+    const double h = pd ? p.need_num("h") : (double)(float)p.need_num("h");
+    const double dt = pd ? p.need_num("dt") : (double)(float)p.need_num("dt");
+    const float hf = (float)h, dtf = (float)dt;
     const std::string srctype = p.str("srctype", "1");
     const int stype = (int)p.num("stype", 3);
-    const std::string srctime = (kSH && p.has("sourcetime")) || !p.has("srctime") ? p.need(kSH ? "sourcetime" : "srctime")
-                                                                                   : p.str("srctime");
+    // SH and PD name the key sourcetime, PN srctime; either is accepted
+    const std::string srctime = p.has("srctime") && !(kSH && p.has("sourcetime"))
+                                    ? p.str("srctime")
+                                    : (p.has("sourcetime") || kSH ? p.need("sourcetime") : p.need("srctime"));
     double alpha = 0, trap[3] = {0, 0, 0};
     if (!srctime.empty() && (srctime[0] == 'T' || srctime[0] == 't'))
         for (int k = 0; k < 3; ++k) trap[k] = p.need_num("trap" + std::to_string(k + 1));
@@ -188,7 +343,6 @@ int main(int argc, char **argv)
         idz = (int)p.need_num("idzrec");
     }
     const std::string model = p.need("model");
-    const std::string precs = p.str("prec", "f32");
     const int explosion = (int)p.num("explosion", 0), topabsorb = (int)p.num("topabsorb", 0);
     const int device = (int)p.num("device", 0);
     if (!p.missing.empty()) {
@@ -197,9 +351,30 @@ int main(int argc, char **argv)
         std::fprintf(stderr, "\n");
         return 1;
     }
-    if (p.num("usebox", 0) != 0) {
-        std::fprintf(stderr, "%s: ", kProg); std::fprintf(stderr, "usebox is not supported by this program\n");
-        return 1;
+    const int usebox = (int)p.num("usebox", 0);
+    int bw = 0;
+    double srcden = 0, srcsvel = 0, srcpvel = 0;
+    std::string sourcefile;
+    const bool box_device = p.str("boxsource", "file") == "device";
+    if (usebox == 1) {
+        srcden = p.need_num("srcden");
+        srcsvel = p.need_num("srcsvel");
+        srcpvel = p.need_num("srcpvel");
+        bw = (int)p.need_num("bw");
+        if (!box_device) sourcefile = p.need("sourcefile");
+        if (report_missing(p)) return 1;
+        if (kSH || (precs != "f32" && precs != "f64")) {
+            std::fprintf(stderr, "%s: usebox=1 needs the P-SV program with prec f32 or f64\n", kProg);
+            return 1;
+        }
+        if (zs < bw / 2 + 4 || nz - zs < bw / 2 + 4) {
+            std::fprintf(stderr, "%s: zs %d is too near to the boundary\n", kProg, zs);
+            return 1;
+        }
+        if (restart || savestate || p.num("usepunch", 0) != 0 || p.num("usetable", 0) != 0) {
+            std::fprintf(stderr, "%s: usebox=1 runs without restart, savestate, usepunch and usetable\n", kProg);
+            return 1;
+        }
     }
     const int usepunch = (int)p.num("usepunch", 0);
     double before = 0, after = 0;
@@ -277,13 +452,17 @@ int main(int argc, char **argv)
         std::printf("{\"nx\": %d, \"nz\": %d, \"nt\": %d, \"nt0\": %d, \"h\": %.9g, \"dt\": %.9g, \"npml\": %d, "
                     "\"topabsorb\": %d, \"prec\": \"%s\", \"source\": \"%s\", \"xs\": %d, \"zs\": %d, "
                     "\"lsrc\": %d, \"itrecord\": %d, \"traces_u\": %zu, \"traces_w\": %zu, \"model\": \"%s\", "
-                    "\"output\": \"%s\", \"savestate\": %d, \"punch_tiles\": %d, \"punch_first_min\": %d}\n",
+                    "\"output\": \"%s\", \"savestate\": %d, \"punch_tiles\": %d, \"punch_first_min\": %d, "
+                    "\"box\": [%d, %d, %d, %d], \"boxsource\": \"%s\"}\n",
                     nx, nz, nt, nt0, h, dt, npml, topabsorb, precs.c_str(),
                     kSH ? (stype == 2 ? "force" : (stype == 13 ? "moment_p" : "moment"))
                         : (explosion ? "explosion" : (srctype == "1" ? "moment" : "moment_p")),
                     xs, zs, lsrc, itrecord,
                     rxu.size(), rxw.size(), model.c_str(), output.c_str(), savestate, nbx * nbz,
-                    pfirst.empty() ? 0 : *std::min_element(pfirst.begin(), pfirst.end()));
+                    pfirst.empty() ? 0 : *std::min_element(pfirst.begin(), pfirst.end()),
+                    usebox == 1 ? xs + (bw + 1) / 2 + 1 - bw : 0, usebox == 1 ? zs + (bw + 1) / 2 + 1 - bw : 0,
+                    usebox == 1 ? bw : 0, usebox == 1 ? bw : 0,
+                    usebox != 1 ? "none" : (box_device ? "device" : sourcefile.c_str()));
         return 0;
     }
     // model
@@ -309,9 +488,25 @@ int main(int argc, char **argv)
     fd23_solver *s = nullptr;
     if ((rc = fd23_create(&d, &s))) return fail("create", rc);
     double stab = 0;
-    rc = fd23_set_model(s, kSH ? nullptr : vp.data(), vs.data(), den.data(), &stab);
-    std::printf("stab = %g\n", stab);
-    if (rc) return fail("model", rc);
+    std::vector<double> bmat;
+    const int bx0 = xs + (bw + 1) / 2 + 1 - bw, bz0 = zs + (bw + 1) / 2 + 1 - bw;  // PD/box/box.cpp:26-45
+    if (usebox == 1) {
+        // the grid material with the box made homogeneous, and the box's own
+        // (MATERIAL::get_model then BOX::init_box, PD/main.cpp:229-236)
+        std::vector<double> mat(5 * n);
+        rc = fd23_build_material(FD23_PSV, nx, nz, h, dt, vp.data(), vs.data(), den.data(), mat.data(), &stab);
+        std::printf("stab = %g\n", stab);
+        if (rc) return fail("model", rc);
+        bmat.resize(5 * (size_t)bw * bw);
+        rc = fd23_box_material(nx, nz, mat.data(), bx0, bz0, bw, bw, srcpvel, srcsvel, srcden, dt, h, bmat.data());
+        if (rc < 0) return fail("box material", rc);
+        if ((rc = fd23_set_material(s, mat.data()))) return fail("material", rc);
+        if ((rc = fd23_set_box(s, bx0, bz0, bw, bw, bmat.data()))) return fail("box", rc);
+    } else {
+        rc = fd23_set_model(s, kSH ? nullptr : vp.data(), vs.data(), den.data(), &stab);
+        std::printf("stab = %g\n", stab);
+        if (rc) return fail("model", rc);
+    }
     // material table (PN/param/param.cpp usetable; the SH program always
     // tries one, SH/main.cpp:154): index + table form when the distinct
     // material tuples fit, the material arrays otherwise
@@ -330,7 +525,21 @@ int main(int argc, char **argv)
         fd23_moment_psv(strike, dip, rake, azimuth, m);
         kind = explosion ? FD23_SRC_EXPLOSION : (srctype == "1" ? FD23_SRC_MOMENT : FD23_SRC_MOMENT_P);
     }
-    if ((rc = fd23_set_source(s, kind, xs, zs, m, src.data(), lsrc, nt0 + nt))) return fail("source", rc);
+    if (usebox == 1) {
+        // the box is the source (PD/main.cpp:153-200 has no point source)
+        if (box_device) {
+            const fd23_line_desc ld = line_desc(bw, h, dt, srcpvel, srcsvel, srcden, strike, dip, rake, azimuth);
+            if ((rc = fd23_set_box_line_source(s, &ld, src.data(), lsrc, bmat.data(), 0, nt)))
+                return fail("box source", rc);
+        } else {
+            std::vector<unsigned char> inc;
+            if ((rc = incident_from_file(sourcefile, bw, nt, dt, bmat, prec == FD23_F64, inc)))
+                return fail(("sourcefile " + sourcefile).c_str(), rc);
+            if ((rc = fd23_set_box_incident(s, inc.data(), 0, nt))) return fail("box incident", rc);
+        }
+    } else if ((rc = fd23_set_source(s, kind, xs, zs, m, src.data(), lsrc, nt0 + nt))) {
+        return fail("source", rc);
+    }
     if ((rc = fd23_set_receivers(s, 0, rxu.data(), rzu.data(), (int)rxu.size()))) return fail("receivers", rc);
     if (!kSH && (rc = fd23_set_receivers(s, FD23_W, rxw.data(), rzw.data(), (int)rxw.size())))
         return fail("W receivers", rc);
@@ -373,13 +582,13 @@ int main(int argc, char **argv)
             IsisTrace t;
             std::memset(&t, 0, sizeof t);
             const int ixr = (*rx[c])[r], izr = (*rz[c])[r];
-            t.xr = ((float)ixr + shiftx[c]) * h;
-            t.zr = ((float)izr + shiftz[c]) * h;
-            t.xs = (float)xs * h;
-            t.zs = (float)zs * h;
+            t.xr = ((float)ixr + shiftx[c]) * hf;
+            t.zr = ((float)izr + shiftz[c]) * hf;
+            t.xs = (float)xs * hf;
+            t.zs = (float)zs * hf;
             t.nt = ntrec;
-            t.samplerate = dt * (float)itrecord;
-            t.gain = dt / h;
+            t.samplerate = dtf * (float)itrecord;
+            t.gain = dtf / hf;
             t.ampstatic = 1.0f;
             t.srcflagnum = xs;
             t.recflagnum = ixr;

@@ -177,3 +177,38 @@ def test_sh_program_parameters(tmp_path):
     assert run("stype=5", "dryrun=1").returncode == 1
     (tmp_path / "st").write_text("0 10\n0 30\n")
     assert json.loads(run("V_sta_file=st", "dryrun=1").stdout)["traces_u"] == 4
+
+
+NTDE = os.path.join(os.path.dirname(CLI), "fd23_ntde_line")
+
+
+def test_usebox_parameters(tmp_path):
+    """usebox=1: the box around (xs, zs), the reference's boundary check on
+    zs, and the options a box run excludes."""
+    (tmp_path / "run.par").write_text(PAR)
+    box = ["usebox=1", "srcden=2.6", "srcsvel=3.2", "srcpvel=5.5", "sourcefile=pl.bin", "bw=20", "zs=40", "xs=60"]
+    r = _cli(tmp_path, "par=run.par", "dryrun=1", "prec=f64", *box)
+    assert r.returncode == 0, r.stderr
+    d = json.loads(r.stdout)
+    assert d["box"] == [60 + 10 + 1 - 20, 40 + 10 + 1 - 20, 20, 20] and d["boxsource"] == "pl.bin"
+    d = json.loads(_cli(tmp_path, "par=run.par", "dryrun=1", *box, "boxsource=device").stdout)
+    assert d["boxsource"] == "device"
+    r = _cli(tmp_path, "par=run.par", "dryrun=1", *box, "zs=13")  # bw/2 + 4 = 14
+    assert r.returncode == 1 and "too near" in r.stderr
+    r = _cli(tmp_path, "par=run.par", "dryrun=1", *box, "usepunch=1", "before=0", "after=1", "timefile=t")
+    assert r.returncode == 1 and "usebox" in r.stderr
+    r = _cli(tmp_path, "par=run.par", "dryrun=1", *box, "prec=bf16")
+    assert r.returncode == 1 and "usebox" in r.stderr
+    r = _cli(tmp_path, "par=run.par", "dryrun=1", "usebox=1", "bw=20")
+    assert r.returncode == 1 and "missing parameter" in r.stderr and "srcden" in r.stderr
+
+
+def test_ntde_program_parameters(tmp_path):
+    if not os.path.exists(NTDE):
+        pytest.skip("fd23_ntde_line not built")
+    r = subprocess.run([NTDE, "nt=10", "h=1", "dt=0.001"], cwd=str(tmp_path), capture_output=True, text=True)
+    assert r.returncode == 1 and "missing parameter" in r.stderr and "sourcefile" in r.stderr
+    r = subprocess.run([NTDE, "nt=10", "h=1", "dt=0.001", "srcden=2", "srcsvel=2", "srcpvel=3", "bw=8",
+                        "sourcefile=x.bin", "sourcetime=none", "strike=0", "dip=0", "rake=0", "azimuth=0"],
+                       cwd=str(tmp_path), capture_output=True, text=True)
+    assert r.returncode == 1 and "sourcetime" in r.stderr

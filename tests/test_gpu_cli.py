@@ -1,6 +1,8 @@
 """fd23_psv2d on the GPU: the program's trace files equal the same run through
 the API bit for bit (FP32 and FP64), its .isis files carry the reference's
-header layout, and savestate / restart split a run exactly."""
+header layout, and savestate / restart split a run exactly; fd23_ntde_line
+writes the box-source planes and fd23_psv2d usebox=1 runs the hybrid box
+from them."""
 import os
 import struct
 import subprocess
@@ -49,11 +51,12 @@ def _cli(tmp_path, *args):
 
 
 def _api(tmp_path, prec, nt):
-    vp, vs, den = F.read_model(str(tmp_path / "layers.mdl"), 150, 100, np.float32(0.3))
-    s = F.Solver("psv", 150, 100, 12, float(np.float32(0.3)), float(np.float32(0.01)), prec=prec, pml_dt=0.005,
-                 pml_v=30.0, pml_r=1e-11, pml_fc=2.0)
+    # the program reads h and dt as doubles for f64 (PD), as floats otherwise (PN)
+    h, dt = (0.3, 0.01) if prec == "f64" else (float(np.float32(0.3)), float(np.float32(0.01)))
+    vp, vs, den = F.read_model(str(tmp_path / "layers.mdl"), 150, 100, h)
+    s = F.Solver("psv", 150, 100, 12, h, dt, prec=prec, pml_dt=0.005, pml_v=30.0, pml_r=1e-11, pml_fc=2.0)
     s.set_model(vp, vs, den)
-    src = F.wavelet_gaussian(float(np.float32(0.01)), -5)
+    src = F.wavelet_gaussian(dt, -5)
     s.set_source(F.SRC_MOMENT, 75, 20, F.moment_psv(0, 20, 90, 45), src, nt)
     rx, rz = F.receivers_file(str(tmp_path / "st"))
     s.set_receivers(0, rx, rz)
@@ -172,3 +175,107 @@ def test_sh_program_equals_api(tmp_path, stype):
     got = np.fromfile(str(tmp_path / "shr_V"), dtype=np.float32).reshape(nt, len(rx))
     np.testing.assert_array_equal(got, want)
     assert (tmp_path / "shr_V.isis").stat().st_size == len(rx) * (84 + 4 * nt)
+
+
+CLI_NTDE = os.path.join(ROOT, "fd23_gb300", "_lib", "fd23_ntde_line")
+BOX_PAR = """nx=150 nz=100 nt=60 h=0.3 dt=0.01
+sourcetime=Gaussian alpha=-5
+strike=30 dip=60 rake=90 azimuth=45
+xs=110 zs=70
+npml=12 pml_dt=0.005 pml_v=30 pml_fc=2 pml_r=1e-11
+model=layers.mdl ntsnap=100
+U_sta_file=stb W_sta_file=stb
+usebox=1 usepunch=0 ngpu=1 srcden=2.6 srcsvel=3.2 srcpvel=5.5 sourcefile=planes.bin bw=32
+"""
+BOX_STATIONS = [(50, 100), (60, 90), (75, 131), (91, 110), (70, 112), (0, 110)]  # (z, x) near and in the box
+
+
+def _box_api(tmp_path, prec, nt, inc=None, line=None):
+    """The box run of BOX_PAR through the API (h, dt as the program reads them)."""
+    h, dt = (0.3, 0.01) if prec == "f64" else (float(np.float32(0.3)), float(np.float32(0.01)))
+    vp, vs, den = F.read_model(str(tmp_path / "layers.mdl"), 150, 100, h)
+    mat, stab, rc = F.build_material("psv", vp, vs, den, h, dt)
+    assert rc == 0
+    bw, x0, z0 = 32, 110 + 16 + 1 - 32, 70 + 16 + 1 - 32
+    mat, bmat, _ = F.box_material(mat, x0, z0, bw, bw, 5.5, 3.2, 2.6, dt, h)
+    s = F.Solver("psv", 150, 100, 12, h, dt, prec=prec, pml_dt=0.005, pml_v=30.0, pml_r=1e-11, pml_fc=2.0)
+    s.set_material(mat)
+    rx, rz = F.receivers_file(str(tmp_path / "stb"))
+    s.set_receivers(0, rx, rz)
+    s.set_receivers(1, rx, rz)
+    s.set_box(x0, z0, bw, bw, bmat=bmat)
+    if inc is not None:
+        s.set_box_incident(inc(bmat, dt).astype(s.dtype), 0)
+    else:
+        d = F.line_desc(bw + 8, bw + 8, F.line_plane_origin(bw), F.line_plane_origin(bw), h, dt, 5.5, 3.2, 2.6,
+                        F.line_source_coefs(30, 60, 90, 45))
+        s.set_box_line_source(d, F.wavelet_gaussian(dt, -5), bmat, 0, nt)
+    s.run(nt, 1)
+    out = s.seismograms(0), s.seismograms(1), mat, bmat
+    s.close()
+    return out
+
+
+def _file_incident(planes, nt):
+    """BOX::setboxsource over the file's frames: step it reads frame it + 1;
+    past the end of the file the buffer keeps frame it - 1 (the reference's
+    failed read leaves it)."""
+    def inc(bmat, dt):
+        out = []
+        for it in range(nt):
+            new = planes[it + 1] if it + 1 < len(planes) else planes[it - 1]
+            out.append(F.box_incident_from_displacement(32, 32, dt, bmat, planes[it, 0], planes[it, 1], new[0],
+                                                        new[1]))
+        return np.stack(out)
+    return inc
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_ntde_and_usebox_programs(tmp_path, prec):
+    """fd23_ntde_line writes the generator's planes (= the API's, bit for
+    bit); fd23_psv2d usebox=1 reading them equals the API box run with the
+    same incident field (the reference's read order), and for FP64 the
+    oracle's box run; boxsource=device equals it up to the last step, whose
+    frame lies past the file's end."""
+    _setup(tmp_path)
+    if not os.path.exists(CLI_NTDE):
+        pytest.skip("fd23_ntde_line not built")
+    (tmp_path / "run.par").write_text(BOX_PAR)
+    (tmp_path / "stb").write_text("".join("%d %d\n" % zx for zx in BOX_STATIONS))
+    nt = 60
+    r = subprocess.run([CLI_NTDE, "par=run.par"], cwd=str(tmp_path), capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    planes = np.fromfile(str(tmp_path / "planes.bin"), dtype=np.float64).reshape(nt, 2, 40, 40)
+    d = F.line_desc(40, 40, F.line_plane_origin(32), F.line_plane_origin(32), 0.3, 0.01, 5.5, 3.2, 2.6,
+                    F.line_source_coefs(30, 60, 90, 45))
+    np.testing.assert_array_equal(planes, F.line_source_planes(d, F.wavelet_gaussian(0.01, -5), 0, nt))
+    _cli(tmp_path, "output=box", "prec=" + prec)
+    ntr = 2 * len(BOX_STATIONS)
+    dt_ = np.float64 if prec == "f64" else np.float32
+    fu = np.fromfile(str(tmp_path / "box_U"), dtype=dt_).reshape(nt, ntr)
+    fw = np.fromfile(str(tmp_path / "box_W"), dtype=dt_).reshape(nt, ntr)
+    su, sw, mat, bmat = _box_api(tmp_path, prec, nt, inc=_file_incident(planes, nt))
+    np.testing.assert_array_equal(fu, su)
+    np.testing.assert_array_equal(fw, sw)
+    assert np.abs(fu).max() > 0
+    if prec == "f64":
+        from oracle import fd23_oracle as O
+        rx, rz = F.receivers_file(str(tmp_path / "stb"))
+        rec = (rx + rz * 150).astype(np.int64)
+        rf = np.repeat(np.arange(2, dtype=np.int32), len(rec))
+        bck = O.cpml_psv(150, 100, 12, 0.005, 1e-11, 30.0, 2.0)
+        no_source = (np.zeros(0, np.int32), np.zeros(0, np.int64), np.zeros((0, 1)))
+        seis, _, _ = O.psv_box_run("f64", 150, 100, 12, 0, mat, bck, no_source, rf, np.tile(rec, 2), nt,
+                                   (110 + 16 + 1 - 32, 70 + 16 + 1 - 32, 32, 32), bmat,
+                                   _file_incident(planes, nt)(bmat, 0.01))
+        np.testing.assert_array_equal(fu, seis[:, :len(rec)])
+        np.testing.assert_array_equal(fw, seis[:, len(rec):])
+    # the planes generated on the device: the same run but for the last step
+    _cli(tmp_path, "output=dev", "prec=" + prec, "boxsource=device")
+    du = np.fromfile(str(tmp_path / "dev_U"), dtype=dt_).reshape(nt, ntr)
+    if prec == "f64":
+        np.testing.assert_array_equal(du[:-1], fu[:-1])
+    else:  # the f32 program generates with h and dt rounded to float, the file has PD's doubles
+        np.testing.assert_allclose(du[:-1], fu[:-1], rtol=0, atol=1e-5 * np.abs(fu).max())
+    gu, _, _, _ = _box_api(tmp_path, prec, nt, line=True)
+    np.testing.assert_array_equal(du, gu)
