@@ -46,8 +46,19 @@ Windowed workload (--config c5, usepunch): the C1 shot with tile step
   of the live tiles only; accuracy carries the seismogram error against the
   same shot without windows.
 
+Generated-box workload (--config c6, the reference's hybrid use): the C1
+  grid and model, 5000 steps, a 32 x 32 box around a line moment source
+  buried at (2000, 200) (strike 30, dip 60, rake 90, one-sided Gaussian
+  alpha = -20); the box material is the source cell's vp, vs, rho (box
+  cells of the model replaced, as the reference does); the incident field
+  is generated on the device every shot (the box-source generator: FP64
+  Green's functions and wavelet convolution on the ring stencils, then the
+  setboxsource step).  "check" compares a shot against the same shot driven
+  through the host path (generator planes -> setboxsource on the host ->
+  incident upload) bit for bit.
+
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--config c0|c1|c2|c3|c4|c5] [--nt NT] [--prec f32|bf16|f16|f64]
+                  [--config c0|c1|c2|c3|c4|c5|c6] [--nt NT] [--prec f32|bf16|f16|f64]
                   [--kernel fused|twopass]
 """
 import argparse
@@ -69,6 +80,8 @@ NX, NZ, H, DT, NT, NPML, F0 = 4000, 2000, 5.0, 4e-4, 5000, 40, 15.0
 NSTA = 400
 # hybrid-box workload: box origin and size, steps
 BOX_X0, BOX_Z0, BOX_BX, BOX_BZ, NT_BOX = 1000, 10, 2000, 1000, 3000
+# generated-box workload: source cell, box width, mechanism, Gaussian alpha
+LB_XS, LB_ZS, LB_BW, LB_MECH, LB_ALPHA = NX // 2, 200, 32, (30.0, 60.0, 90.0, 0.0), -20
 # batched workload: shots, steps, stations per shot, shots checked against FP64
 NSHOT_B, NT_B, NSTA_B, NCHECK_B = 64, 3000, 200, 6
 
@@ -293,7 +306,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
-    ap.add_argument("--config", default="c1", choices=["c0", "c1", "c2", "c3", "c4", "c5"])
+    ap.add_argument("--config", default="c1", choices=["c0", "c1", "c2", "c3", "c4", "c5", "c6"])
     args = ap.parse_args()
     if args.config == "c3":
         # the large grid: 16000 x 8000, h 2.5 m, dt 2e-4 s, 8000 steps, C1-style model
@@ -323,6 +336,9 @@ def main():
         return
     if args.config == "c4":
         bench_batch(args, F, torch, rank, world, local, dist)
+        return
+    if args.config == "c6":
+        bench_linebox(args, F, torch, rank, world, local, dist)
         return
     if args.config == "c0":
         bench_sh(args, F, torch, rank, world, local, dist)
@@ -635,6 +651,176 @@ def bench_box(args, F, torch, rank, world, local, dist):
             "e2e": e2e}
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline_box(inc)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    s.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def linebox_setup(F, vp, vs, rho):
+    """Material, box and line source of the generated-box workload, built as
+    the reference's PD program builds them (MATERIAL::get_model, then
+    BOX::init_box homogenises the box): FP64 on the host."""
+    mat, stab, rc = F.build_material("psv", vp, vs, rho, H, DT)
+    if rc:
+        raise RuntimeError("generated-box model fails the CFL check (stab %.3f)" % stab)
+    sv = (float(vp[LB_ZS, LB_XS]), float(vs[LB_ZS, LB_XS]), float(rho[LB_ZS, LB_XS]))
+    x0 = LB_XS + (LB_BW + 1) // 2 + 1 - LB_BW
+    z0 = LB_ZS + (LB_BW + 1) // 2 + 1 - LB_BW
+    mat, bmat, _ = F.box_material(mat, x0, z0, LB_BW, LB_BW, sv[0], sv[1], sv[2], DT, H)
+    o = F.line_plane_origin(LB_BW)
+    desc = F.line_desc(LB_BW + 8, LB_BW + 8, o, o, H, DT, sv[0], sv[1], sv[2], F.line_source_coefs(*LB_MECH))
+    return mat, bmat, (x0, z0, LB_BW, LB_BW), desc, sv
+
+
+def cpu_baseline_linebox(budget_s=15.0):
+    """The generated-box shot on the host cores: the oracle's generator for the
+    box planes, setboxsource, and the oracle's box run (FP32, all threads),
+    for as many steps as fit the budget."""
+    import fd23_gb300 as F
+    from oracle import fd23_oracle as O
+    vp, vs, rho = c1_model()
+    mat, bmat, box, desc, sv = linebox_setup(F, vp, vs, rho)
+    bck = O.cpml_psv(NX, NZ, NPML, DT, 1e-11, vp.max() / H, F0)
+    none = (np.zeros(0, np.int32), np.zeros(0, np.int64), np.zeros((0, 1)))
+    rf = np.zeros(NSTA, np.int32)
+    ri = np.arange(200, 200 + 9 * NSTA, 9).astype(np.int64)
+    src = O.gaussian(DT, LB_ALPHA)
+    a = O.line_source_coefs(*LB_MECH)
+
+    def run(steps):
+        t0 = time.perf_counter()
+        pl = O.line_source_planes(desc.px, desc.pz, desc.ox, desc.oz, H, DT, sv[0], sv[1], sv[2], a, src, 0,
+                                  steps + 1)
+        inc = np.stack([O.box_incident_from_displacement(LB_BW, LB_BW, DT, bmat, pl[i, 0], pl[i, 1], pl[i + 1, 0],
+                                                         pl[i + 1, 1]) for i in range(steps)])
+        O.psv_box_run("f32", NX, NZ, NPML, 0, mat, bck, none, rf, ri, steps, box, bmat, inc)
+        return time.perf_counter() - t0
+
+    one = run(8) / 8
+    steps = int(max(4, min(budget_s / max(one, 1e-4), NT)))
+    t_used = run(steps)
+    cores = os.cpu_count() or 1
+    return {"value": NX * NZ * steps / t_used, "unit": "cell-updates/s", "cores": cores, "kind": "port",
+            "sample": "%d steps of the %dx%d grid with the %d-cell generated box (%.1f s): oracle generator + "
+                      "setboxsource + FP32 oracle box run, %d threads" % (steps, NX, NZ, LB_BW, t_used, cores)}
+
+
+def bench_linebox(args, F, torch, rank, world, local, dist):
+    """Generated-box workload: the box's incident field generated on the device
+    inside every timed shot."""
+    nt = args.nt
+    vp, vs, rho = c1_model(seed=1 + rank)
+    mat, bmat, box, desc, sv = linebox_setup(F, vp, vs, rho)
+    src = F.wavelet_gaussian(DT, LB_ALPHA)
+    s = F.Solver("psv", NX, NZ, NPML, H, DT, prec="f32", pml_dt=DT, pml_v=float(vp.max()) / H, pml_r=1e-11,
+                 pml_fc=F0, device=local, kernel=args.kernel)
+    rxu, rzu = F.receivers_line(NSTA, 200, 0, 9, 0)
+    rxw, rzw = F.receivers_line(NSTA, 200, 1, 9, 0)
+
+    def configure():
+        s.set_material(mat)
+        s.set_receivers(0, rxu, rzu)
+        s.set_receivers(1, rxw, rzw)
+        s.set_box(*box, bmat=bmat)
+
+    configure()
+    nring = sum(F.box_ring_size(LB_BW, LB_BW))
+    stream = torch.cuda.ExternalStream(s.stream, device=local)
+
+    def shot():
+        s.reset()
+        s.set_box_line_source(desc, src, bmat, 0, nt)
+        s.run(nt, 1)
+
+    for _ in range(args.warmup):
+        shot()
+    got = s.seismograms(0), s.seismograms(1)
+    # the same shot through the host path: generator planes, setboxsource on
+    # the host, incident upload
+    planes = F.line_source_planes(desc, src, 0, nt + 1, device=local)
+    inc = np.stack([F.box_incident_from_displacement(LB_BW, LB_BW, DT, bmat, planes[i, 0], planes[i, 1],
+                                                     planes[i + 1, 0], planes[i + 1, 1]) for i in range(nt)])
+    s.reset()
+    s.set_box_incident(inc.astype(np.float32), 0)
+    s.run(nt, 1)
+    check = bool(np.array_equal(s.seismograms(0), got[0]) and np.array_equal(s.seismograms(1), got[1]))
+    reached = float(np.abs(got[0]).max())
+    del planes, inc
+    # the generator alone (CUDA events on the solver's stream)
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g0.record(stream)
+    s.set_box_line_source(desc, src, bmat, 0, nt)
+    g1.record(stream)
+    s.sync()
+    gen_ms = g0.elapsed_time(g1)
+    sampler = ClockSampler(local)
+    if rank == 0:
+        sampler.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        shot()
+    e1.record(stream)
+    s.sync()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    clocks = sampler.stop() if rank == 0 else None
+    ms_max = max_over_ranks(ms, dist)
+    value = NX * NZ * nt * args.steps * world / (ms_max * 1e-3)
+
+    e2e = None
+    if not args.no_e2e:
+        times = []
+        seis_bytes = 0
+        for _ in range(max(1, min(args.steps, 2))):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            m2, b2, _, _, _ = linebox_setup(F, vp, vs, rho)
+            s.set_material(m2)
+            s.set_box(*box, bmat=b2)
+            shot()
+            su, sw = s.seismograms(0), s.seismograms(1)
+            times.append(time.perf_counter() - t0)
+            seis_bytes = su.nbytes + sw.nbytes
+        e2e = {"value": NX * NZ * nt / statistics.mean(times) * world, "unit": "cell-updates/s",
+               "h2d_bytes_per_step": mat.nbytes + bmat.nbytes + src.nbytes, "d2h_bytes_per_step": seis_bytes,
+               "note": "per step = one whole shot: FP64 material and box material built on the host (as the "
+                       "reference does), uploaded, incident generated on the device, the run, seismograms"}
+    hbm, peak_kind = load_peaks()
+    per_step_ms = ms_max / (args.steps * nt)
+    ab = alg_bytes(NX, NZ, NPML, 4) + box_alg_bytes(LB_BW, LB_BW, nring, 4)
+    achieved = ab / (per_step_ms * 1e-3) / 1e9
+    line = {"metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "psv_4000x2000_5000steps_box32_linesource_c6", "nx": NX, "nz": NZ,
+                       "nt": nt, "box": list(box), "ring_cells": nring, "source": [LB_XS, LB_ZS],
+                       "mechanism": list(LB_MECH), "alpha": LB_ALPHA, "box_material": list(sv),
+                       "kernel": args.kernel,
+                       "cells_counted": "grid cells nx*nz per step (the box's residual field is extra work)",
+                       "l2": "inputs larger than L2", "parallelism": "replicas x%d" % world},
+            "check": {"seismograms_bit_exact_vs_host_generated_incident": check, "max_abs_u": reached},
+            "generator": {"ms_per_shot": gen_ms, "frames": nt + 1,
+                          "share_of_shot": gen_ms / (ms_max / args.steps)},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "traffic": None, "peak_source": peak_kind,
+                         "scope": "whole step: sweep + box kernels (the generator is in the time)",
+                         "alg_bytes_per_launch": ab, "launch_ms": per_step_ms},
+            # per step the sweep and the two one-CTA box kernels of a small box;
+            # per shot the generator's points, Green's function, convolution
+            # and incident kernels (one frame chunk)
+            "gpu_launches": args.steps * (nt * 3 + 4),
+            "clocks": clocks,
+            "e2e": e2e}
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline_linebox()
     if rank == 0:
         print(json.dumps(line), flush=True)
     s.close()

@@ -7,6 +7,11 @@
 // 4 .. n-5).  Here a box is any rectangle of at least 16 x 16 cells; the
 // residual updates cover cells 4 .. n-5 of the box (the outer 4 are the sub
 // ring, rewritten from g before every read), with one thread per cell.
+// Boxes whose interior and rings fit eight passes of a 1024-thread CTA (the
+// reference's own boxes, up to 32 cells, among them) run each half of the
+// box step as one CTA launched as a programmatic dependent of the kernel
+// before it: two small launches per step instead of four, their launch
+// latency under the sweep's tail.
 //
 // Stress exchange around the fused sweep: the residual stress update writes
 // g = r + s into the old-stress slot of every add-ring cell, and the sweep
@@ -37,34 +42,37 @@ __device__ __forceinline__ C dplus_r(const C *p, long long s)
 // ring exchange of fields F0 .. F1-1 on buffer set `par`, ring positions
 // [0, qend) (qend = nsub: the sub ring only)
 template <class S, class C, int F0, int F1>
-__global__ void __launch_bounds__(256) box_ring_kernel(Shot<S, C> s, int par, int qend)
+__device__ __forceinline__ void ring_cell(const Shot<S, C> &s, int par, int q)
 {
     const Box<C> &b = s.box;
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < qend; q += gridDim.x * blockDim.x) {
-        const int2 c = b.cells[q];
-        const long long g = s.origin + (long long)(b.z0 + c.y) * s.pitch + (b.x0 + c.x);
-        const long long r = (long long)c.y * b.bx + c.x;
-        const bool add = q >= b.nsub;
+    const int2 c = b.cells[q];
+    const long long g = s.origin + (long long)(b.z0 + c.y) * s.pitch + (b.x0 + c.x);
+    const long long r = (long long)c.y * b.bx + c.x;
+    const bool add = q >= b.nsub;
 #pragma unroll
-        for (int f = F0; f < F1; ++f) {
-            S *G = par ? s.f[1][f] : s.f[0][f];
-            const C sv = b.inc[(long long)f * b.nring + q];
-            if (add) G[g] = to_s<S>(b.r[f][r] + sv);
-            else b.r[f][r] = to_c<C>(G[g]) - sv;
-        }
+    for (int f = F0; f < F1; ++f) {
+        S *G = par ? s.f[1][f] : s.f[0][f];
+        const C sv = b.inc[(long long)f * b.nring + q];
+        if (add) G[g] = to_s<S>(b.r[f][r] + sv);
+        else b.r[f][r] = to_c<C>(G[g]) - sv;
     }
 }
 
-// residual stress update, cells 4 .. n-5 of the box; the accumulation order
-// is that of the main update (x terms, then z terms).  On add-ring cells it
-// also stores g = r + s into the grid stresses of buffer set `par` (the
-// fused sweep's old-stress slot); add_g = 0 skips that.
+template <class S, class C, int F0, int F1>
+__global__ void __launch_bounds__(256) box_ring_kernel(Shot<S, C> s, int par, int qend)
+{
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < qend; q += gridDim.x * blockDim.x)
+        ring_cell<S, C, F0, F1>(s, par, q);
+}
+
+// residual stress update of box cell (ix, iz), 4 <= ix, iz < n-4; the
+// accumulation order is that of the main update (x terms, then z terms).
+// On add-ring cells it also stores g = r + s into the grid stresses of
+// buffer set `par` (the fused sweep's old-stress slot); add_g = 0 skips that.
 template <class S, class C>
-__global__ void __launch_bounds__(256) box_stress_r(Shot<S, C> s, int par, int add_g)
+__device__ __forceinline__ void stress_r_cell(const Shot<S, C> &s, int par, int add_g, int ix, int iz)
 {
     const Box<C> &b = s.box;
-    const int ix = 4 + blockIdx.x * 32 + threadIdx.x, iz = 4 + blockIdx.y * 8 + threadIdx.y;
-    if (ix >= b.bx - 4 || iz >= b.bz - 4) return;
     const long long o = (long long)iz * b.bx + ix, P = b.bx;
     const C ux = dminus_r<C>(b.r[0] + o, 1), uz = dminus_r<C>(b.r[0] + o, P);
     const C wx = dplus_r<C>(b.r[1] + o, 1), wz = dplus_r<C>(b.r[1] + o, P);
@@ -94,25 +102,32 @@ __global__ void __launch_bounds__(256) box_stress_r(Shot<S, C> s, int par, int a
     }
 }
 
-// receivers of this step's output (buffer set `par`, before the next ring
-// exchange rewrites the add ring), then the residual velocity update
 template <class S, class C>
-__global__ void __launch_bounds__(256) box_velocity_r(Shot<S, C> s, int par, int rec_index)
+__global__ void __launch_bounds__(256) box_stress_r(Shot<S, C> s, int par, int add_g)
 {
-    if (rec_index >= 0) {
-        const int nthr = gridDim.x * gridDim.y * blockDim.x * blockDim.y;
-        const int t0 = (blockIdx.y * gridDim.x + blockIdx.x) * (blockDim.x * blockDim.y) +
-                       threadIdx.y * blockDim.x + threadIdx.x;
-#pragma unroll
-        for (int c = 0; c < 5; ++c) {
-            const S *F = par ? s.f[1][c] : s.f[0][c];
-            for (int i = t0; i < s.nrec[c]; i += nthr)
-                s.seis[c][(long long)rec_index * s.nrec[c] + i] = to_c<C>(F[s.rec[c][i]]);
-        }
-    }
-    const Box<C> &b = s.box;
     const int ix = 4 + blockIdx.x * 32 + threadIdx.x, iz = 4 + blockIdx.y * 8 + threadIdx.y;
-    if (ix >= b.bx - 4 || iz >= b.bz - 4) return;
+    if (ix >= s.box.bx - 4 || iz >= s.box.bz - 4) return;
+    stress_r_cell<S, C>(s, par, add_g, ix, iz);
+}
+
+// receivers of this step's output (buffer set `par`, before the next ring
+// exchange rewrites the add ring): thread t of nthr
+template <class S, class C>
+__device__ __forceinline__ void box_receivers(const Shot<S, C> &s, int par, int rec_index, int t0, int nthr)
+{
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+        const S *F = par ? s.f[1][c] : s.f[0][c];
+        for (int i = t0; i < s.nrec[c]; i += nthr)
+            s.seis[c][(long long)rec_index * s.nrec[c] + i] = to_c<C>(F[s.rec[c][i]]);
+    }
+}
+
+// residual velocity update of box cell (ix, iz)
+template <class S, class C>
+__device__ __forceinline__ void velocity_r_cell(const Shot<S, C> &s, int ix, int iz)
+{
+    const Box<C> &b = s.box;
     const long long o = (long long)iz * b.bx + ix, P = b.bx;
     const C dxTxx = dplus_r<C>(b.r[2] + o, 1), dzTzz = dminus_r<C>(b.r[4] + o, P);
     const C dxTxz = dminus_r<C>(b.r[3] + o, 1), dzTxz = dplus_r<C>(b.r[3] + o, P);
@@ -124,6 +139,84 @@ __global__ void __launch_bounds__(256) box_velocity_r(Shot<S, C> s, int par, int
     w = fmaC<C>(bw, dzTzz, w);
     b.r[0][o] = u;
     b.r[1][o] = w;
+}
+
+template <class S, class C>
+__global__ void __launch_bounds__(256) box_velocity_r(Shot<S, C> s, int par, int rec_index)
+{
+    if (rec_index >= 0) {
+        const int nthr = gridDim.x * gridDim.y * blockDim.x * blockDim.y;
+        const int t0 = (blockIdx.y * gridDim.x + blockIdx.x) * (blockDim.x * blockDim.y) +
+                       threadIdx.y * blockDim.x + threadIdx.x;
+        box_receivers<S, C>(s, par, rec_index, t0, nthr);
+    }
+    const int ix = 4 + blockIdx.x * 32 + threadIdx.x, iz = 4 + blockIdx.y * 8 + threadIdx.y;
+    if (ix >= s.box.bx - 4 || iz >= s.box.bz - 4) return;
+    velocity_r_cell<S, C>(s, ix, iz);
+}
+
+// Small boxes: each half of the box step in one CTA, the ring exchange and
+// the residual update it feeds separated by a barrier instead of a kernel
+// boundary, launched as programmatic dependents so their launch overlaps
+// the sweep.  Each waits for its predecessor (griddepcontrol.wait) before
+// it touches memory and lets its successor launch at once (the successor
+// waits for this grid's completion in turn).
+constexpr int kSmallThreads = 1024;
+
+// before the sweep: ring U, W (sub: r = g - s, add: g = r + s), then the
+// residual stress update (+ g = r + s on the add ring for the fused sweep)
+template <class S, class C>
+__global__ void __launch_bounds__(kSmallThreads, 1) box_small_pre(Shot<S, C> s, int par, int add_g)
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    const Box<C> &b = s.box;
+    const int t = threadIdx.x;
+    for (int q = t; q < b.nring; q += kSmallThreads) ring_cell<S, C, 0, 2>(s, par, q);
+    __syncthreads();
+    const int w = b.bx - 8, n = w * (b.bz - 8);
+    for (int k = t; k < n; k += kSmallThreads) stress_r_cell<S, C>(s, par, add_g, 4 + k % w, 4 + k / w);
+}
+
+// after the sweep: sub-ring stresses r = g - s (fused sweep only; the
+// two-pass sweep did the whole exchange), then this step's receivers and
+// the residual velocity update
+template <class S, class C>
+__global__ void __launch_bounds__(kSmallThreads, 1) box_small_post(Shot<S, C> s, int par, int sub_t, int rec_index)
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    const Box<C> &b = s.box;
+    const int t = threadIdx.x;
+    if (sub_t) {
+        for (int q = t; q < b.nsub; q += kSmallThreads) ring_cell<S, C, 2, 5>(s, par, q);
+        __syncthreads();
+    }
+    if (rec_index >= 0) box_receivers<S, C>(s, par, rec_index, t, kSmallThreads);
+    const int w = b.bx - 8, n = w * (b.bz - 8);
+    for (int k = t; k < n; k += kSmallThreads) velocity_r_cell<S, C>(s, 4 + k % w, 4 + k / w);
+}
+
+// boxes whose interior and rings each fit a few passes of one CTA
+template <class C>
+inline bool small_box(const Box<C> &b)
+{
+    return (long long)(b.bx - 8) * (b.bz - 8) <= 8 * kSmallThreads && b.nring <= 8 * kSmallThreads;
+}
+
+template <class K, class... Args>
+int launch_pdl(K kernel, cudaStream_t st, Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(1);
+    cfg.blockDim = dim3(kSmallThreads);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...) == cudaSuccess ? FD23_OK : FD23_ERR_CUDA;
 }
 
 inline dim3 interior_grid(int bx, int bz) { return dim3((unsigned)((bx - 8 + 31) / 32), (unsigned)((bz - 8 + 7) / 8)); }
@@ -143,6 +236,7 @@ int launch_box_ring(const Shot<S, C> &s, int par, int which, cudaStream_t st)
 template <class S, class C>
 int launch_box_pre(const Shot<S, C> &s, int par, int fused, cudaStream_t st)
 {
+    if (fused && small_box(s.box)) return launch_pdl(box_small_pre<S, C>, st, s, par, fused);
     const int rc = launch_box_ring<S, C>(s, par, 0, st);
     if (rc) return rc;
     box_stress_r<S, C><<<interior_grid(s.box.bx, s.box.bz), dim3(32, 8), 0, st>>>(s, par, fused);
@@ -152,6 +246,7 @@ int launch_box_pre(const Shot<S, C> &s, int par, int fused, cudaStream_t st)
 template <class S, class C>
 int launch_box_post(const Shot<S, C> &s, int par, int fused, int rec_index, cudaStream_t st)
 {
+    if (fused && small_box(s.box)) return launch_pdl(box_small_post<S, C>, st, s, par, fused, rec_index);
     if (fused)  // sub-ring stresses r = g - s (the two-pass sweep did the whole exchange)
         box_ring_kernel<S, C, 2, 5><<<ring_blocks(s.box.nsub), 256, 0, st>>>(s, par, s.box.nsub);
     box_velocity_r<S, C><<<interior_grid(s.box.bx, s.box.bz), dim3(32, 8), 0, st>>>(s, par, rec_index);
