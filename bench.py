@@ -26,8 +26,10 @@ SH workload (--config c0): 800 x 400 SH grid, h=10 m, dt=1e-3 s, 2000 steps,
   two layers (vs 2000 / 3000 m/s, rho 2200 / 2500, interface at iz=200),
   10 Hz Ricker line force on V at (400, 20), 20-cell CPML, free surface, 200
   surface receivers.  The 10 MB working set stays in L2 within a shot, so the
-  step is launch- and latency-bound; the run is captured in a CUDA graph (a
-  one-shot batch) and L2 is flushed between timed shots.
+  step is launch- and latency-bound; the run is the fused sweep captured in a
+  CUDA graph (a one-shot batch), or with --kernel persist one cooperative
+  launch per shot (grid barriers between the update phases).  L2 is flushed
+  between timed shots.
 
 Batched workload (--config c4): 64 shots with seeded grid sizes nx in
   [1000, 4000], nz in [500, 2000] (not tile multiples), h=5 m, dt=4e-4 s,
@@ -301,13 +303,16 @@ def main():
     ap.add_argument("--impl", default="ours")
     ap.add_argument("--nt", type=int, default=NT)
     ap.add_argument("--prec", default="f32")
-    ap.add_argument("--kernel", default="fused")
+    ap.add_argument("--kernel", default=None, choices=["fused", "twopass", "persist"],
+                    help="default fused; persist: a run in one cooperative launch (small grids)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--config", default="c1", choices=["c0", "c1", "c2", "c3", "c4", "c5", "c6"])
     args = ap.parse_args()
+    if args.kernel is None:
+        args.kernel = "fused"
     if args.config == "c3":
         # the large grid: 16000 x 8000, h 2.5 m, dt 2e-4 s, 8000 steps, C1-style model
         NX, NZ, H, DT, NT = 16000, 8000, 2.5, 2e-4, 8000
@@ -843,24 +848,37 @@ def sh_model():
 def bench_sh(args, F, torch, rank, world, local, dist):
     nt = min(args.nt, SH_NT)
     vs, rho = sh_model()
+    # persistent: the whole shot in one cooperative launch (grid barriers
+    # between the update phases); fused: the fused sweep in a CUDA graph
+    persist = args.kernel == "persist"
     s = F.Solver("sh", SH_NX, SH_NZ, SH_NPML, SH_H, SH_DT, prec=args.prec, pml_dt=SH_DT,
-                 pml_v=float(vs.max()) / SH_H, pml_r=1e-11, pml_fc=SH_F0, device=local, kernel="fused")
+                 pml_v=float(vs.max()) / SH_H, pml_r=1e-11, pml_fc=SH_F0, device=local,
+                 kernel="persist" if persist else "fused")
     s.set_model(None, vs, rho)
     src = F.wavelet_ricker(SH_DT, SH_F0)
     s.set_source(F.SRC_FORCE, SH_NX // 2, 20, np.array([1.0, 0.0]), src, nt)
     rx, rz = F.receivers_line(SH_NSTA // 2, 2, 0, 4, 0)
     s.set_receivers(0, rx, rz)
-    b = F.Batch([s])
-    stream = torch.cuda.ExternalStream(b.stream, device=local)
+    b = None if persist else F.Batch([s])
+    stream = torch.cuda.ExternalStream(s.stream if persist else b.stream, device=local)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda:%d" % local)
 
     def shot():
         s.reset()
-        b.run(nt, 1)
+        if persist:
+            s.run(nt, 1)
+        else:
+            b.run(nt, 1)
+
+    def sync():
+        if persist:
+            s.sync()
+        else:
+            b.sync()
 
     for _ in range(args.warmup):
         shot()
-    b.sync()
+    sync()
     sampler = ClockSampler(local)
     if rank == 0:
         sampler.start()
@@ -874,7 +892,7 @@ def bench_sh(args, F, torch, rank, world, local, dist):
         e0.record(stream)
         shot()
         e1.record(stream)
-        b.sync()
+        sync()
         ms += e0.elapsed_time(e1)
     clocks = sampler.stop() if rank == 0 else None
     ms_max = max_over_ranks(ms, dist)
@@ -905,14 +923,15 @@ def bench_sh(args, F, torch, rank, world, local, dist):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.prec,
             "data": "synthetic",
             "config": {"workload": "sh_800x400_2000steps_c0", "nx": SH_NX, "nz": SH_NZ, "nt": nt,
-                       "source": "10 Hz Ricker line force", "traces": SH_NSTA, "graph": "one-shot batch",
+                       "source": "10 Hz Ricker line force", "traces": SH_NSTA,
+                       "kernel": "persistent cooperative launch per shot" if persist else "fused sweep, one-shot batch graph",
                        "l2": "working set (about 10 MB) L2-resident within a shot; L2 flushed between "
                              "timed shots", "parallelism": "replicas x%d" % world},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": None, "peak_source": peak_kind,
                          "note": "L2-resident working set: the HBM fraction is not meaningful here",
                          "alg_bytes_per_launch": ab, "launch_ms": per_launch_ms},
-            "gpu_launches": args.steps * (nt + 1), "clocks": clocks, "e2e": e2e}
+            "gpu_launches": args.steps * (1 if persist else nt + 1), "clocks": clocks, "e2e": e2e}
     if rank == 0 and not args.no_cpu:
         from oracle import fd23_oracle as O
         mat, _, _ = O.sh_material(vs, rho, SH_H, SH_DT)
@@ -929,7 +948,8 @@ def bench_sh(args, F, torch, rank, world, local, dist):
                                 "sample": "400 steps of the SH grid (%.1f s), FP32 oracle, all threads" % tt}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    b.close()
+    if b is not None:
+        b.close()
     s.close()
     if dist:
         dist.barrier()
@@ -1004,9 +1024,15 @@ def bench_batch(args, F, torch, rank, world, local, dist):
             s.reset()
         b.run(nt, 1)
 
+    def sync():
+        if persist:
+            s.sync()
+        else:
+            b.sync()
+
     for _ in range(args.warmup):
         shot()
-    b.sync()
+    sync()
     sampler = ClockSampler(local)
     if rank == 0:
         sampler.start()

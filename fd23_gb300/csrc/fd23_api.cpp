@@ -221,6 +221,24 @@ int dispatch_step(fd23_solver *s, int rec_now)
         default: return step_impl<float, float>(s, rec_now);
     }
 }
+int dispatch_persist(fd23_solver *s, int nsteps, int itrecord, int any_rec)
+{
+    switch (s->d.prec) {
+        case FD23_F64:
+            return launch_persist<double, double>(make_shot<double, double>(s), s->d.wave, s->it, nsteps, itrecord,
+                                                  s->nrec_steps, any_rec, s->d_bar, s->err_flag, s->stream);
+        case FD23_BF16:
+            return launch_persist<__nv_bfloat16, float>(make_shot<__nv_bfloat16, float>(s), s->d.wave, s->it, nsteps,
+                                                        itrecord, s->nrec_steps, any_rec, s->d_bar, s->err_flag,
+                                                        s->stream);
+        case FD23_F16:
+            return launch_persist<__half, float>(make_shot<__half, float>(s), s->d.wave, s->it, nsteps, itrecord,
+                                                 s->nrec_steps, any_rec, s->d_bar, s->err_flag, s->stream);
+        default:
+            return launch_persist<float, float>(make_shot<float, float>(s), s->d.wave, s->it, nsteps, itrecord,
+                                                s->nrec_steps, any_rec, s->d_bar, s->err_flag, s->stream);
+    }
+}
 int dispatch_flush(fd23_solver *s)
 {
     switch (s->d.prec) {
@@ -401,6 +419,7 @@ void free_all(fd23_solver *s)
     cudaFree(s->d_mtab);
     cudaFree(s->cpml);
     cudaFree(s->err_flag);
+    cudaFree(s->d_bar);
     cudaFree(s->norm_buf);
     cudaFree(s->d_terms);
     cudaFree(s->d_tamp);
@@ -544,7 +563,7 @@ int fd23_create(const fd23_desc *desc, fd23_solver **out)
     if (d.nx < 2 || d.nz < 2 || d.npml < 0 || 2 * d.npml > d.nx || 2 * d.npml > d.nz) return FD23_ERR_ARG;
     if ((long long)d.nx * d.nz > (1LL << 31)) return FD23_ERR_ARG;
     if (!(d.h > 0) || !(d.dt > 0)) return FD23_ERR_ARG;
-    if (d.kernel < FD23_KERNEL_AUTO || d.kernel > FD23_KERNEL_TWOPASS) return FD23_ERR_ARG;
+    if (d.kernel < FD23_KERNEL_AUTO || d.kernel > FD23_KERNEL_PERSIST) return FD23_ERR_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || d.device < 0 || d.device >= ndev) {
         cudaGetLastError();
@@ -559,7 +578,8 @@ int fd23_create(const fd23_desc *desc, fd23_solver **out)
     s->npsi = d.wave == FD23_PSV ? 8 : 4;
     s->es = storage_size(d.prec);
     s->cs = compute_size(d.prec);
-    s->fused = d.kernel != FD23_KERNEL_TWOPASS;
+    s->fused = d.kernel == FD23_KERNEL_AUTO || d.kernel == FD23_KERNEL_FUSED;
+    s->persist = d.kernel == FD23_KERNEL_PERSIST;
     if (const char *v = getenv("FD23_COST_XPML")) s->tune.wx = atof(v);
     if (const char *v = getenv("FD23_COST_ZPML")) s->tune.wz = atof(v);
     const FusedGeom g = fused_geom(d.wave, d.prec);
@@ -591,6 +611,7 @@ int fd23_create(const fd23_desc *desc, fd23_solver **out)
     if ((rc = dev_alloc(&s->cpml, bck.size() * s->cs))) return fail(rc);
     if ((rc = upload_cpml(s, bck))) return fail(rc);
     if ((rc = dev_alloc((void **)&s->err_flag, sizeof(int)))) return fail(rc);
+    if (s->persist && (rc = dev_alloc((void **)&s->d_bar, 2 * sizeof(unsigned)))) return fail(rc);
     if ((rc = dev_alloc((void **)&s->norm_buf, 2 * sizeof(double)))) return fail(rc);
     if (s->fused) {
         if ((rc = fused_prepare(d.wave, d.prec))) return fail(rc);
@@ -798,6 +819,15 @@ int fd23_run(fd23_solver *s, int nsteps, int itrecord)
     if (any_rec) {
         int rc = ensure_record_capacity(s, s->nrec_steps + nrec_new);
         if (rc) return rc;
+    }
+    if (s->persist && !s->box_on) {
+        // the whole run in one cooperative launch
+        if (nsteps == 0) return FD23_OK;
+        const int rc = dispatch_persist(s, nsteps, itrecord, any_rec);
+        if (rc) return rc;
+        s->it += nsteps;
+        if (any_rec) s->nrec_steps += nrec_new;
+        return FD23_OK;
     }
     for (int k = 0; k < nsteps; ++k) {
         const int rec_now = any_rec && (s->it % itrecord == 0);

@@ -24,6 +24,8 @@ struct fd23_solver {
     fd23::Layout L;
     cudaStream_t stream = nullptr;
     int fused = 1;
+    bool persist = false;     // FD23_KERNEL_PERSIST: a run is one cooperative launch
+    unsigned *d_bar = nullptr;  // its grid barrier (count, generation)
     void *fld[2][5] = {};   // wavefields; those of one buffer set are one allocation
     void *mat[5] = {};      // material arrays, one allocation
     void *fld_block[2] = {};

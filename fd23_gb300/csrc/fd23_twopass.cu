@@ -6,6 +6,8 @@
 // padded layout, for any nx, nz.  The fused single-pass sweep
 // (fd23_fused_psv.cu) is the fast path; this one is the cross-check and the
 // fallback for forms the fused sweep does not cover.
+#include <algorithm>
+
 #include "fd23_device.cuh"
 #include "fd23_kernels.h"
 
@@ -50,10 +52,8 @@ __device__ __forceinline__ long long psi_z_index(int ix, int iz, int nx, int nz,
 
 // ----------------------------- P-SV ---------------------------------------
 template <class S, class C>
-__global__ void __launch_bounds__(256) psv_stress_2p(Shot<S, C> s, int it)
+__device__ __forceinline__ void psv_stress_cell(const Shot<S, C> &s, int it, int ix, int iz)
 {
-    const int ix = blockIdx.x * 32 + threadIdx.x, iz = blockIdx.y * 8 + threadIdx.y;
-    if (ix >= s.nx || iz >= s.nz) return;
     if (!punch_active(s.punch, ix, iz, it)) return;  // outside the tile's step window
     const long long o = s.origin + (long long)iz * s.pitch + ix, P = s.pitch;
     const S *U = s.f[0][0], *W = s.f[0][1];
@@ -116,10 +116,8 @@ __global__ void __launch_bounds__(256) psv_stress_2p(Shot<S, C> s, int it)
 }
 
 template <class S, class C>
-__global__ void __launch_bounds__(256) psv_velocity_2p(Shot<S, C> s, int it)
+__device__ __forceinline__ void psv_velocity_cell(const Shot<S, C> &s, int it, int ix, int iz)
 {
-    const int ix = blockIdx.x * 32 + threadIdx.x, iz = blockIdx.y * 8 + threadIdx.y;
-    if (ix >= s.nx || iz >= s.nz) return;
     if (!punch_active(s.punch, ix, iz, it)) return;  // outside the tile's step window
     const long long o = s.origin + (long long)iz * s.pitch + ix, P = s.pitch;
     S *U = s.f[0][0], *W = s.f[0][1];
@@ -174,10 +172,8 @@ __global__ void __launch_bounds__(256) psv_velocity_2p(Shot<S, C> s, int it)
 
 // ------------------------------ SH ----------------------------------------
 template <class S, class C>
-__global__ void __launch_bounds__(256) sh_stress_2p(Shot<S, C> s, int it)
+__device__ __forceinline__ void sh_stress_cell(const Shot<S, C> &s, int it, int ix, int iz)
 {
-    const int ix = blockIdx.x * 32 + threadIdx.x, iz = blockIdx.y * 8 + threadIdx.y;
-    if (ix >= s.nx || iz >= s.nz) return;
     if (!punch_active(s.punch, ix, iz, it)) return;  // outside the tile's step window
     // cells skipped by the reference, SH/fd/cu_fd.cu:140
     if (ix == 0 || ix >= s.nx - 1 || iz >= s.nz - 1) return;
@@ -218,11 +214,13 @@ __global__ void __launch_bounds__(256) sh_stress_2p(Shot<S, C> s, int it)
     Tz[o] = to_s<S>(tz);
 }
 
-template <class S, class C>
-__global__ void __launch_bounds__(256) sh_velocity_2p(Shot<S, C> s, int it)
+// IMG (the persistent form): the free-surface image Tz(x,0) = -Tz(x,1) of
+// this step has not been stored yet; the cells whose z stencil reaches row 0
+// read the image value in its place, and the cell of row 0 stores it (the
+// same values the two-pass order gives: image first, then the update)
+template <class S, class C, bool IMG = false>
+__device__ __forceinline__ void sh_velocity_cell(const Shot<S, C> &s, int it, int ix, int iz)
 {
-    const int ix = blockIdx.x * 32 + threadIdx.x, iz = blockIdx.y * 8 + threadIdx.y;
-    if (ix >= s.nx || iz >= s.nz) return;
     if (!punch_active(s.punch, ix, iz, it)) return;  // outside the tile's step window
     const long long o = s.origin + (long long)iz * s.pitch + ix, P = s.pitch;
     S *V = s.f[0][0];
@@ -231,7 +229,16 @@ __global__ void __launch_bounds__(256) sh_velocity_2p(Shot<S, C> s, int it)
     const C c0 = Coef<C>::get(ord, 0), c1 = Coef<C>::get(ord, 1), c2 = Coef<C>::get(ord, 2),
             c3 = Coef<C>::get(ord, 3);
     const C dxTx = dminus<S, C>(Tx + o, 1, c0, c1, c2, c3);
-    const C dzTz = dplus<S, C>(Tz + o, P, c0, c1, c2, c3);
+    C dzTz;
+    if (IMG && iz <= 3 && punch_active(s.punch, ix, 0, it)) {
+        const long long o0 = s.origin + ix;
+        const S img = to_s<S>(-to_c<C>(Tz[o0 + P]));
+        if (iz == 0) s.f[0][2][o0] = img;
+        auto v = [&](int j) { return iz + j == 0 ? to_c<C>(img) : to_c<C>(Tz[o + j * P]); };
+        dzTz = comb<C>(c0, c1, c2, c3, v(1) - v(0), v(2) - v(-1), v(3) - v(-2), v(4) - v(-3));
+    } else {
+        dzTz = dplus<S, C>(Tz + o, P, c0, c1, c2, c3);
+    }
     const C bv = matv<S, C>(s, 2, o);
     const int nx = s.nx, nz = s.nz, npml = s.npml, B = s.cpml_blk;
     const C *b = s.cpml, *c = s.cpml + B, *k = s.cpml + 2 * B;
@@ -257,6 +264,32 @@ __global__ void __launch_bounds__(256) sh_velocity_2p(Shot<S, C> s, int it)
         v = fmaC<C>(bv, dzTz, v);
     }
     V[o] = to_s<S>(v);
+}
+
+// one thread per cell
+template <class S, class C>
+__global__ void __launch_bounds__(256) psv_stress_2p(Shot<S, C> s, int it)
+{
+    const int ix = blockIdx.x * 32 + threadIdx.x, iz = blockIdx.y * 8 + threadIdx.y;
+    if (ix < s.nx && iz < s.nz) psv_stress_cell<S, C>(s, it, ix, iz);
+}
+template <class S, class C>
+__global__ void __launch_bounds__(256) psv_velocity_2p(Shot<S, C> s, int it)
+{
+    const int ix = blockIdx.x * 32 + threadIdx.x, iz = blockIdx.y * 8 + threadIdx.y;
+    if (ix < s.nx && iz < s.nz) psv_velocity_cell<S, C>(s, it, ix, iz);
+}
+template <class S, class C>
+__global__ void __launch_bounds__(256) sh_stress_2p(Shot<S, C> s, int it)
+{
+    const int ix = blockIdx.x * 32 + threadIdx.x, iz = blockIdx.y * 8 + threadIdx.y;
+    if (ix < s.nx && iz < s.nz) sh_stress_cell<S, C>(s, it, ix, iz);
+}
+template <class S, class C>
+__global__ void __launch_bounds__(256) sh_velocity_2p(Shot<S, C> s, int it)
+{
+    const int ix = blockIdx.x * 32 + threadIdx.x, iz = blockIdx.y * 8 + threadIdx.y;
+    if (ix < s.nx && iz < s.nz) sh_velocity_cell<S, C>(s, it, ix, iz);
 }
 
 // Point-source injection after the stress update (terms in order, one thread),
@@ -285,7 +318,159 @@ __global__ void post_stress_2p(Shot<S, C> s, int it, int sh_image)
     }
 }
 
+// ---------------- persistent form for small grids ----------------
+// A grid whose fields sit in L2 steps in a few microseconds of work, less
+// than one launch of either sweep costs.  Here one cooperative launch runs
+// many steps: every phase of the two-pass update (stress, then velocity) is
+// a loop over all cells by all threads of the grid, phases separated by a
+// grid-wide barrier, with the two-pass kernels' per-cell code and the same
+// in-place updates, so results are those of the two-pass sweep bit for bit.
+
+// Grid barrier (all blocks co-resident: cooperative launch).  Block leaders
+// arrive on a counter with an acquire-release add (so the last one has seen
+// every other block's writes); the last resets the counter and releases the
+// next generation, which the others wait for with acquire loads.  Every wait
+// is bounded: past the limit, or when another block has given up, the block
+// sets err = 3 and the caller abandons the launch (the host reports a
+// timeout).
+constexpr int kBarSpin = 1 << 24;
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ bool grid_barrier(unsigned *bar, int *err)
+{
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned *count = bar, *gen = bar + 1;
+        unsigned g, old;
+        asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(g) : "l"(gen) : "memory");
+        asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(count) : "memory");
+        int good = 1;
+        if (old + 1u == gridDim.x) {
+            asm volatile("st.relaxed.gpu.global.u32 [%0], 0;" ::"l"(count) : "memory");
+            asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(gen), "r"(g + 1u) : "memory");
+        } else {
+            for (int i = 0; ld_acquire_u32(gen) == g; ++i) {
+                if (i >= kBarSpin || ((i & 1023) == 1023 && *(volatile int *)err)) {
+                    good = 0;
+                    atomicCAS(err, 0, 3);
+                    break;
+                }
+            }
+        }
+        ok = good;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+template <class S, class C>
+__device__ __forceinline__ void persist_record(const Shot<S, C> &s, int row, int t, int nthr)
+{
+#pragma unroll
+    for (int comp = 0; comp < 5; ++comp) {
+        const int n = s.nrec[comp];
+        for (int i = t; i < n; i += nthr) s.seis[comp][(long long)row * n + i] = to_c<C>(s.f[0][comp][s.rec[comp][i]]);
+    }
+}
+
+// point-source terms on fields [f0, f1) at step it, each by the thread that
+// owns its cell in the phase loops (cell c = iz*nx + ix is thread c % nthr),
+// in list order
+template <class S, class C>
+__device__ __forceinline__ void persist_terms(const Shot<S, C> &s, int it, int f0, int f1, int t, int nthr)
+{
+    if (it >= s.tamp_nt) return;
+    for (int k = 0; k < s.nterms; ++k) {
+        const int4 tm = s.terms[k];
+        if (tm.x < f0 || tm.x >= f1 || ((long long)tm.z * s.nx + tm.y) % nthr != t) continue;
+        S *F = s.f[0][tm.x];
+        const long long o = s.origin + (long long)tm.z * s.pitch + tm.y;
+        F[o] = to_s<S>(to_c<C>(F[o]) + s.tamp[(long long)k * s.tamp_nt + it]);
+    }
+}
+
+// steps it0 .. it0+nsteps-1; record rows from rec_row on the steps with
+// it % itrecord == 0 (any_rec); rec_sep: some receivers are on stress fields,
+// so the gather gets its own phase (else it runs during the next stress
+// phase, which leaves the velocities alone)
+template <class S, class C, int WAVE>
+__global__ void __launch_bounds__(1024, 1) persist_steps(Shot<S, C> s, int it0, int nsteps, int itrecord, int rec_row,
+                                                     int any_rec, int rec_sep, unsigned *bar, int *err)
+{
+    const int nthr = gridDim.x * blockDim.x, t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nx = s.nx;
+    const long long ncell = (long long)nx * s.nz;
+    const int nvel = WAVE == FD23_PSV ? 2 : 1;  // velocity fields come first
+    int pending = -1;
+    for (int k = 0; k < nsteps; ++k) {
+        const int it = it0 + k;
+        if (pending >= 0) persist_record<S, C>(s, pending, t, nthr);
+        pending = -1;
+        for (long long c = t; c < ncell; c += nthr) {
+            const int iz = (int)(c / nx), ix = (int)(c - (long long)iz * nx);
+            if (WAVE == FD23_PSV) psv_stress_cell<S, C>(s, it, ix, iz);
+            else sh_stress_cell<S, C>(s, it, ix, iz);
+        }
+        persist_terms<S, C>(s, it, nvel, 5, t, nthr);
+        if (!grid_barrier(bar, err)) return;
+        // SH: the free-surface stress image Tz(x,0) = -Tz(x,1) after the
+        // source (SH/fd/cu_fd.cu:226; post_stress_2p) is taken inside the
+        // velocity update (IMG), which saves a barrier
+        persist_terms<S, C>(s, it, 0, nvel, t, nthr);
+        for (long long c = t; c < ncell; c += nthr) {
+            const int iz = (int)(c / nx), ix = (int)(c - (long long)iz * nx);
+            if (WAVE == FD23_PSV) psv_velocity_cell<S, C>(s, it, ix, iz);
+            else sh_velocity_cell<S, C, true>(s, it, ix, iz);
+        }
+        if (!grid_barrier(bar, err)) return;
+        if (any_rec && it % itrecord == 0) {
+            if (rec_sep) {
+                persist_record<S, C>(s, rec_row, t, nthr);
+                if (!grid_barrier(bar, err)) return;
+            } else {
+                pending = rec_row;
+            }
+            ++rec_row;
+        }
+    }
+    if (pending >= 0) persist_record<S, C>(s, pending, t, nthr);
+}
+
 }  // namespace
+
+template <class S, class C>
+int launch_persist(const Shot<S, C> &s, int wave, int it0, int nsteps, int itrecord, int rec_row, int any_rec,
+                   unsigned *bar, int *err, cudaStream_t st)
+{
+    void (*k)(Shot<S, C>, int, int, int, int, int, int, unsigned *, int *) =
+        wave == FD23_PSV ? persist_steps<S, C, FD23_PSV> : persist_steps<S, C, FD23_SH>;
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 1024, 0) != cudaSuccess || per_sm < 1) {
+        cudaGetLastError();
+        return FD23_ERR_CUDA;
+    }
+    const long long cells = (long long)s.nx * s.nz;
+    const int blocks = (int)std::max<long long>(1, std::min<long long>((long long)sms * per_sm, (cells + 1023) / 1024));
+    int rec_sep = 0;
+    for (int c = (wave == FD23_PSV ? 2 : 1); c < 5; ++c) rec_sep |= s.nrec[c] > 0;
+    if (cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), st) != cudaSuccess) return FD23_ERR_CUDA;
+    void *args[] = {(void *)&s, &it0, &nsteps, &itrecord, &rec_row, &any_rec, &rec_sep, &bar, &err};
+    const cudaError_t e = cudaLaunchCooperativeKernel((const void *)k, dim3(blocks), dim3(1024), args, 0, st);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return FD23_ERR_CUDA;
+    }
+    return FD23_OK;
+}
 
 template <class S, class C>
 __global__ void record_kernel(Shot<S, C> s, int par, int rec_index)
@@ -369,7 +554,9 @@ int launch_norm2(const Shot<S, C> &s, int par, int nfields, long long elems, dou
 #define FD23_INST(S, C)                                                                    \
     template int launch_step_twopass<S, C>(const Shot<S, C> &, int, int, cudaStream_t);   \
     template int launch_norm2<S, C>(const Shot<S, C> &, int, int, long long, double *, cudaStream_t); \
-    template int launch_record<S, C>(const Shot<S, C> &, int, int, cudaStream_t);
+    template int launch_record<S, C>(const Shot<S, C> &, int, int, cudaStream_t);                 \
+    template int launch_persist<S, C>(const Shot<S, C> &, int, int, int, int, int, int, unsigned *, int *, \
+                                      cudaStream_t);
 FD23_INST(float, float)
 FD23_INST(double, double)
 FD23_INST(__nv_bfloat16, float)

@@ -70,8 +70,13 @@ enum fd23_wave { FD23_PSV = 0, FD23_SH = 1 };
 /* storage/arithmetic forms.  F32 and F64 store and compute in that type;
  * BF16 and F16 store wavefields and material in 16 bits and compute in FP32. */
 enum fd23_prec { FD23_F32 = 0, FD23_F64 = 1, FD23_BF16 = 2, FD23_F16 = 3 };
-/* kernel choice: AUTO picks the fused single-pass sweep */
-enum fd23_kernel { FD23_KERNEL_AUTO = 0, FD23_KERNEL_FUSED = 1, FD23_KERNEL_TWOPASS = 2 };
+/* kernel choice: AUTO picks the fused single-pass sweep.  PERSIST (an
+ * addition for small grids whose fields sit in L2, where a launch per step
+ * costs more than the step's work) runs a whole fd23_run in one cooperative
+ * launch of the two-pass updates, grid barriers between the phases; results
+ * equal TWOPASS bit for bit.  A PERSIST solver with a box steps like TWOPASS;
+ * batches take FUSED solvers only. */
+enum fd23_kernel { FD23_KERNEL_AUTO = 0, FD23_KERNEL_FUSED = 1, FD23_KERNEL_TWOPASS = 2, FD23_KERNEL_PERSIST = 3 };
 /* field ids (source terms, receivers, state) */
 enum fd23_psv_field { FD23_U = 0, FD23_W = 1, FD23_TXX = 2, FD23_TXZ = 3, FD23_TZZ = 4 };
 enum fd23_sh_field { FD23_V = 0, FD23_TX = 1, FD23_TZ = 2 };
