@@ -7,11 +7,11 @@
 // 4 .. n-5).  Here a box is any rectangle of at least 16 x 16 cells; the
 // residual updates cover cells 4 .. n-5 of the box (the outer 4 are the sub
 // ring, rewritten from g before every read), with one thread per cell.
-// Boxes whose interior and rings fit eight passes of a 1024-thread CTA (the
-// reference's own boxes, up to 32 cells, among them) run each half of the
-// box step as one CTA launched as a programmatic dependent of the kernel
-// before it: two small launches per step instead of four, their launch
-// latency under the sweep's tail.
+// Every box kernel launches as a programmatic dependent of the kernel before
+// it, so its launch latency hides under that kernel's tail.  Boxes whose
+// interior and rings fit eight passes of a 1024-thread CTA (the reference's
+// own boxes, up to 32 cells, among them) run each half of the box step as
+// one CTA: two small launches per step instead of four.
 //
 // Stress exchange around the fused sweep: the residual stress update writes
 // g = r + s into the old-stress slot of every add-ring cell, and the sweep
@@ -58,9 +58,20 @@ __device__ __forceinline__ void ring_cell(const Shot<S, C> &s, int par, int q)
     }
 }
 
+// Every box kernel may run as a programmatic dependent of the kernel before
+// it: it waits for that kernel (griddepcontrol.wait) before touching memory
+// and lets its own successor launch at once (the successor waits in turn).
+// Launched without the attribute, both instructions are no-ops.
+__device__ __forceinline__ void pdl_enter()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 template <class S, class C, int F0, int F1>
 __global__ void __launch_bounds__(256) box_ring_kernel(Shot<S, C> s, int par, int qend)
 {
+    pdl_enter();
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < qend; q += gridDim.x * blockDim.x)
         ring_cell<S, C, F0, F1>(s, par, q);
 }
@@ -105,6 +116,7 @@ __device__ __forceinline__ void stress_r_cell(const Shot<S, C> &s, int par, int 
 template <class S, class C>
 __global__ void __launch_bounds__(256) box_stress_r(Shot<S, C> s, int par, int add_g)
 {
+    pdl_enter();
     const int ix = 4 + blockIdx.x * 32 + threadIdx.x, iz = 4 + blockIdx.y * 8 + threadIdx.y;
     if (ix >= s.box.bx - 4 || iz >= s.box.bz - 4) return;
     stress_r_cell<S, C>(s, par, add_g, ix, iz);
@@ -144,6 +156,7 @@ __device__ __forceinline__ void velocity_r_cell(const Shot<S, C> &s, int ix, int
 template <class S, class C>
 __global__ void __launch_bounds__(256) box_velocity_r(Shot<S, C> s, int par, int rec_index)
 {
+    pdl_enter();
     if (rec_index >= 0) {
         const int nthr = gridDim.x * gridDim.y * blockDim.x * blockDim.y;
         const int t0 = (blockIdx.y * gridDim.x + blockIdx.x) * (blockDim.x * blockDim.y) +
@@ -168,8 +181,7 @@ constexpr int kSmallThreads = 1024;
 template <class S, class C>
 __global__ void __launch_bounds__(kSmallThreads, 1) box_small_pre(Shot<S, C> s, int par, int add_g)
 {
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    pdl_enter();
     const Box<C> &b = s.box;
     const int t = threadIdx.x;
     for (int q = t; q < b.nring; q += kSmallThreads) ring_cell<S, C, 0, 2>(s, par, q);
@@ -184,8 +196,7 @@ __global__ void __launch_bounds__(kSmallThreads, 1) box_small_pre(Shot<S, C> s, 
 template <class S, class C>
 __global__ void __launch_bounds__(kSmallThreads, 1) box_small_post(Shot<S, C> s, int par, int sub_t, int rec_index)
 {
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    pdl_enter();
     const Box<C> &b = s.box;
     const int t = threadIdx.x;
     if (sub_t) {
@@ -205,11 +216,11 @@ inline bool small_box(const Box<C> &b)
 }
 
 template <class K, class... Args>
-int launch_pdl(K kernel, cudaStream_t st, Args... args)
+int launch_pdl(K kernel, dim3 grid, dim3 block, cudaStream_t st, Args... args)
 {
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(1);
-    cfg.blockDim = dim3(kSmallThreads);
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -228,29 +239,31 @@ template <class S, class C>
 int launch_box_ring(const Shot<S, C> &s, int par, int which, cudaStream_t st)
 {
     const int n = s.box.nring;
-    if (which == 0) box_ring_kernel<S, C, 0, 2><<<ring_blocks(n), 256, 0, st>>>(s, par, n);
-    else box_ring_kernel<S, C, 2, 5><<<ring_blocks(n), 256, 0, st>>>(s, par, n);
-    return cudaPeekAtLastError() == cudaSuccess ? FD23_OK : FD23_ERR_CUDA;
+    if (which == 0) return launch_pdl(box_ring_kernel<S, C, 0, 2>, dim3(ring_blocks(n)), dim3(256), st, s, par, n);
+    return launch_pdl(box_ring_kernel<S, C, 2, 5>, dim3(ring_blocks(n)), dim3(256), st, s, par, n);
 }
 
 template <class S, class C>
 int launch_box_pre(const Shot<S, C> &s, int par, int fused, cudaStream_t st)
 {
-    if (fused && small_box(s.box)) return launch_pdl(box_small_pre<S, C>, st, s, par, fused);
+    if (fused && small_box(s.box))
+        return launch_pdl(box_small_pre<S, C>, dim3(1), dim3(kSmallThreads), st, s, par, fused);
     const int rc = launch_box_ring<S, C>(s, par, 0, st);
     if (rc) return rc;
-    box_stress_r<S, C><<<interior_grid(s.box.bx, s.box.bz), dim3(32, 8), 0, st>>>(s, par, fused);
-    return cudaPeekAtLastError() == cudaSuccess ? FD23_OK : FD23_ERR_CUDA;
+    return launch_pdl(box_stress_r<S, C>, interior_grid(s.box.bx, s.box.bz), dim3(32, 8), st, s, par, fused);
 }
 
 template <class S, class C>
 int launch_box_post(const Shot<S, C> &s, int par, int fused, int rec_index, cudaStream_t st)
 {
-    if (fused && small_box(s.box)) return launch_pdl(box_small_post<S, C>, st, s, par, fused, rec_index);
-    if (fused)  // sub-ring stresses r = g - s (the two-pass sweep did the whole exchange)
-        box_ring_kernel<S, C, 2, 5><<<ring_blocks(s.box.nsub), 256, 0, st>>>(s, par, s.box.nsub);
-    box_velocity_r<S, C><<<interior_grid(s.box.bx, s.box.bz), dim3(32, 8), 0, st>>>(s, par, rec_index);
-    return cudaPeekAtLastError() == cudaSuccess ? FD23_OK : FD23_ERR_CUDA;
+    if (fused && small_box(s.box))
+        return launch_pdl(box_small_post<S, C>, dim3(1), dim3(kSmallThreads), st, s, par, fused, rec_index);
+    if (fused) {  // sub-ring stresses r = g - s (the two-pass sweep did the whole exchange)
+        const int rc = launch_pdl(box_ring_kernel<S, C, 2, 5>, dim3(ring_blocks(s.box.nsub)), dim3(256), st, s, par,
+                                  s.box.nsub);
+        if (rc) return rc;
+    }
+    return launch_pdl(box_velocity_r<S, C>, interior_grid(s.box.bx, s.box.bz), dim3(32, 8), st, s, par, rec_index);
 }
 
 #define FD23_INST(S, C)                                                                  \
