@@ -745,7 +745,10 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                     }
                 } else {
                     // ---- general cells: edges (reduced order), CPML, free surface, outside ----
-                    // memory variables first, so their load latency overlaps the derivatives
+                    // memory variables first, so their load latency overlaps the derivatives.
+                    // The CPML coefficients are read through the read-only path
+                    // (__ldg): written once at set-up, so their loads may move
+                    // ahead of this thread's memory-variable stores.
                     C psx[2][4], psz[2][4];
 #pragma unroll
                     for (int e = 0; e < 4; ++e) {
@@ -831,12 +834,12 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                             C txx = told[0][e], txz = told[1][e], tzz = told[2][e];
                             // x chain, PD/fd/cu_fd.cu:303-326
                             if (xp) {
-                                const C pu = fmaC<C>(cp[2 * nx + ix], psx[0][e], cp[B + 2 * nx + ix] * ux);
-                                const C t = fmaC<C>(ux, cp[2 * B + 2 * nx + ix], pu);
+                                const C pu = fmaC<C>(__ldg(cp + (2 * nx + ix)), psx[0][e], __ldg(cp + (B + 2 * nx + ix)) * ux);
+                                const C t = fmaC<C>(ux, __ldg(cp + (2 * B + 2 * nx + ix)), pu);
                                 txx = fmaC<C>(gam, t, txx);
                                 tzz = fmaC<C>(lam, t, tzz);
-                                const C pw = fmaC<C>(cp[3 * nx + ix], psx[1][e], cp[B + 3 * nx + ix] * wx);
-                                txz = fmaC<C>(mua, fmaC<C>(wx, cp[2 * B + 3 * nx + ix], pw), txz);
+                                const C pw = fmaC<C>(__ldg(cp + (3 * nx + ix)), psx[1][e], __ldg(cp + (B + 3 * nx + ix)) * wx);
+                                txz = fmaC<C>(mua, fmaC<C>(wx, __ldg(cp + (2 * B + 3 * nx + ix)), pw), txz);
                                 if (own) { pwr[2][px] = pu; pwr[3][px] = pw; }
                             } else if (j != 0) {
                                 txx = fmaC<C>(gam, ux, txx);
@@ -846,12 +849,12 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                             // z chain, :328-355
                             if (zp) {
                                 const int zb = 4 * nx;
-                                const C pw = fmaC<C>(cp[zb + 3 * nz + j], psz[0][e], cp[B + zb + 3 * nz + j] * wz);
-                                const C t = fmaC<C>(wz, cp[2 * B + zb + 3 * nz + j], pw);
+                                const C pw = fmaC<C>(__ldg(cp + (zb + 3 * nz + j)), psz[0][e], __ldg(cp + (B + zb + 3 * nz + j)) * wz);
+                                const C t = fmaC<C>(wz, __ldg(cp + (2 * B + zb + 3 * nz + j)), pw);
                                 txx = fmaC<C>(lam, t, txx);
                                 tzz = fmaC<C>(gam, t, tzz);
-                                const C pu = fmaC<C>(cp[zb + 2 * nz + j], psz[1][e], cp[B + zb + 2 * nz + j] * uz);
-                                txz = fmaC<C>(mua, fmaC<C>(uz, cp[2 * B + zb + 2 * nz + j], pu), txz);
+                                const C pu = fmaC<C>(__ldg(cp + (zb + 2 * nz + j)), psz[1][e], __ldg(cp + (B + zb + 2 * nz + j)) * uz);
+                                txz = fmaC<C>(mua, fmaC<C>(uz, __ldg(cp + (2 * B + zb + 2 * nz + j)), pu), txz);
                                 if (own) { pwr[7][pz] = pw; pwr[6][pz] = pu; }
                             } else if (j == 0) {
                                 txx = fmaC<C>((C)2 * mu, ux, txx);
@@ -876,17 +879,17 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                             const C mux = ms[0][e], muz = ms[1][e];
                             C tx = told[0][e], tz = told[1][e];
                             if (xp) {
-                                const C a = fmaC<C>(cp[nx + ix], psx[0][e], cp[B + nx + ix] * dxv);
+                                const C a = fmaC<C>(__ldg(cp + (nx + ix)), psx[0][e], __ldg(cp + (B + nx + ix)) * dxv);
                                 if (own) pwr[1][px] = a;
-                                tx = fmaC<C>(mux, fmaC<C>(dxv, cp[2 * B + nx + ix], a), tx);
+                                tx = fmaC<C>(mux, fmaC<C>(dxv, __ldg(cp + (2 * B + nx + ix)), a), tx);
                             } else {
                                 tx = fmaC<C>(mux, dxv, tx);
                             }
                             if (zp) {
                                 const int zb = 2 * nx;
-                                const C a = fmaC<C>(cp[zb + nz + j], psz[0][e], cp[B + zb + nz + j] * dzv);
+                                const C a = fmaC<C>(__ldg(cp + (zb + nz + j)), psz[0][e], __ldg(cp + (B + zb + nz + j)) * dzv);
                                 if (own) pwr[3][pz] = a;
-                                tz = fmaC<C>(muz, fmaC<C>(dzv, cp[2 * B + zb + nz + j], a), tz);
+                                tz = fmaC<C>(muz, fmaC<C>(dzv, __ldg(cp + (2 * B + zb + nz + j)), a), tz);
                             } else {
                                 tz = fmaC<C>(muz, dzv, tz);
                             }
@@ -1156,12 +1159,12 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                                 C u = vold[0][e], w = vold[1][e];
                                 // x chain, PD/fd/cu_fd.cu:455-474
                                 if (xp) {
-                                    const C pa = fmaC<C>(cp[ix], psx[0][e], cp[B + ix] * dxTxx);
+                                    const C pa = fmaC<C>(__ldg(cp + (ix)), psx[0][e], __ldg(cp + (B + ix)) * dxTxx);
                                     pwr[0][px] = pa;
-                                    u = fmaC<C>(bu, fmaC<C>(dxTxx, cp[2 * B + ix], pa), u);
-                                    const C pb = fmaC<C>(cp[nx + ix], psx[1][e], cp[B + nx + ix] * dxTxz);
+                                    u = fmaC<C>(bu, fmaC<C>(dxTxx, __ldg(cp + (2 * B + ix)), pa), u);
+                                    const C pb = fmaC<C>(__ldg(cp + (nx + ix)), psx[1][e], __ldg(cp + (B + nx + ix)) * dxTxz);
                                     pwr[1][px] = pb;
-                                    w = fmaC<C>(bw, fmaC<C>(dxTxz, cp[2 * B + nx + ix], pb), w);
+                                    w = fmaC<C>(bw, fmaC<C>(dxTxz, __ldg(cp + (2 * B + nx + ix)), pb), w);
                                 } else if (a != 0) {
                                     u = fmaC<C>(bu, dxTxx, u);
                                     w = fmaC<C>(bw, dxTxz, w);
@@ -1169,12 +1172,12 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                                 // z chain, :476-499
                                 if (zp) {
                                     const int zb = 4 * nx;
-                                    const C pa = fmaC<C>(cp[zb + nz + a], psz[0][e], cp[B + zb + nz + a] * dzTxz);
-                                    const C pb = fmaC<C>(cp[zb + a], psz[1][e], cp[B + zb + a] * dzTzz);
+                                    const C pa = fmaC<C>(__ldg(cp + (zb + nz + a)), psz[0][e], __ldg(cp + (B + zb + nz + a)) * dzTxz);
+                                    const C pb = fmaC<C>(__ldg(cp + (zb + a)), psz[1][e], __ldg(cp + (B + zb + a)) * dzTzz);
                                     pwr[5][pz] = pa;
                                     pwr[4][pz] = pb;
-                                    u = fmaC<C>(bu, fmaC<C>(dzTxz, cp[2 * B + zb + nz + a], pa), u);
-                                    w = fmaC<C>(bw, fmaC<C>(dzTzz, cp[2 * B + zb + a], pb), w);
+                                    u = fmaC<C>(bu, fmaC<C>(dzTxz, __ldg(cp + (2 * B + zb + nz + a)), pa), u);
+                                    w = fmaC<C>(bw, fmaC<C>(dzTzz, __ldg(cp + (2 * B + zb + a)), pb), w);
                                 } else if (a == 0) {
                                     u = fmaC<C>(bu, dxTxx + dzTxz, u);
                                     w = (C)0;
@@ -1189,17 +1192,17 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                                 const C bv = mv[0][e];
                                 C v = vold[0][e];
                                 if (xp) {
-                                    const C pa = fmaC<C>(cp[ix], psx[0][e], cp[B + ix] * dxT);
+                                    const C pa = fmaC<C>(__ldg(cp + (ix)), psx[0][e], __ldg(cp + (B + ix)) * dxT);
                                     pwr[0][px] = pa;
-                                    v = fmaC<C>(bv, fmaC<C>(dxT, cp[2 * B + ix], pa), v);
+                                    v = fmaC<C>(bv, fmaC<C>(dxT, __ldg(cp + (2 * B + ix)), pa), v);
                                 } else {
                                     v = fmaC<C>(bv, dxT, v);
                                 }
                                 if (zp) {
                                     const int zb = 2 * nx;
-                                    const C pa = fmaC<C>(cp[zb + a], psz[0][e], cp[B + zb + a] * dzT);
+                                    const C pa = fmaC<C>(__ldg(cp + (zb + a)), psz[0][e], __ldg(cp + (B + zb + a)) * dzT);
                                     pwr[2][pz] = pa;
-                                    v = fmaC<C>(bv, fmaC<C>(dzT, cp[2 * B + zb + a], pa), v);
+                                    v = fmaC<C>(bv, fmaC<C>(dzT, __ldg(cp + (2 * B + zb + a)), pa), v);
                                 } else {
                                     v = fmaC<C>(bv, dzT, v);
                                 }
