@@ -743,6 +743,62 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                         P::fma(P::from(ms[0]), P::from(dx), P::from(told[0])).to(tnew[0]);
                         P::fma(P::from(ms[1]), dmz4p<S, C>(urow, 0), P::from(told[1])).to(tnew[1]);
                     }
+                } else if (PSV && xfast && j >= 4 && j <= nz - 5) {
+                    // x-interior cells of a z-CPML row (8th order everywhere): the
+                    // interior's packed differences, then the general path's chains
+                    // with the z memory variables (coefficients uniform in the row)
+                    if constexpr (PSV) {
+                        constexpr C c0 = Coef4<C>::c0, c1 = Coef4<C>::c1, c2 = Coef4<C>::c2, c3 = Coef4<C>::c3;
+                        const bool top = j < npml && sh.topabsorb;
+                        const long long pz0 = top ? (long long)j * nx + x : (long long)(npml + nz - 1 - j) * nx + x;
+                        C psw[4], psu[4];
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) {
+                            psw[e] = prd[7][pz0 + e];
+                            psu[e] = prd[6][pz0 + e];
+                        }
+                        C h[12], ux[4], wx[4], uz[4], wz[4];
+                        ld12<S, C>(urow[4], h);
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) ux[e] = dmx<C>(h, e, c0, c1, c2, c3);
+                        ld12<S, C>(urow[4] + K::UWF, h);
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) wx[e] = dpx<C>(h, e, c0, c1, c2, c3);
+                        dmz4p<S, C>(urow, 0).to(uz);
+                        dpz4p<S, C>(urow, K::UWF).to(wz);
+                        const int zb = 4 * nx;
+                        const C bW = __ldg(cp + (zb + 3 * nz + j)), cW = __ldg(cp + (B + zb + 3 * nz + j)),
+                                kW = __ldg(cp + (2 * B + zb + 3 * nz + j));
+                        const C bU = __ldg(cp + (zb + 2 * nz + j)), cU = __ldg(cp + (B + zb + 2 * nz + j)),
+                                kU = __ldg(cp + (2 * B + zb + 2 * nz + j));
+                        const bool own_row = j >= I.z0 && j < I.z1;
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) {
+                            C pw = psw[e], pu = psu[e];
+                            if (act) {
+                                const C lam = ms[0][e], mu = ms[1][e], mua = ms[2][e];
+                                const C gam = lam + (C)2 * mu;
+                                C txx = told[0][e], txz = told[1][e], tzz = told[2][e];
+                                txx = fmaC<C>(gam, ux[e], txx);
+                                tzz = fmaC<C>(lam, ux[e], tzz);
+                                txz = fmaC<C>(mua, wx[e], txz);
+                                pw = fmaC<C>(bW, psw[e], cW * wz[e]);
+                                const C t = fmaC<C>(wz[e], kW, pw);
+                                txx = fmaC<C>(lam, t, txx);
+                                tzz = fmaC<C>(gam, t, tzz);
+                                pu = fmaC<C>(bU, psu[e], cU * uz[e]);
+                                txz = fmaC<C>(mua, fmaC<C>(uz[e], kU, pu), txz);
+                                tnew[0][e] = txx;
+                                tnew[1][e] = txz;
+                                tnew[2][e] = tzz;
+                            }
+                            const int ix = x + e;
+                            if (own_row && ix >= I.x0 && ix < I.x0 + K::TX) {
+                                pwr[7][pz0 + e] = pw;
+                                pwr[6][pz0 + e] = pu;
+                            }
+                        }
+                    }
                 } else {
                     // ---- general cells: edges (reduced order), CPML, free surface, outside ----
                     // memory variables first, so their load latency overlaps the derivatives.
@@ -1070,6 +1126,53 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                             for (int e = 0; e < 4; ++e) dx[e] = dmx<C>(h, e, c0, c1, c2, c3);
                             const P t = P::fma(bv, P::from(dx), P::from(vold[0]));
                             P::fma(bv, dpz4p<S, C>(trow, K::SW), t).to(vnew[0]);  // d/dz Tz
+                        }
+                    } else if (PSV && xfast && a >= 4 && a <= nz - 5) {
+                        // x-interior cells of a z-CPML row, as in the stress update
+                        if constexpr (PSV) {
+                            constexpr C c0 = Coef4<C>::c0, c1 = Coef4<C>::c1, c2 = Coef4<C>::c2, c3 = Coef4<C>::c3;
+                            const bool top = a < npml && sh.topabsorb;
+                            const long long pz0 = top ? (long long)a * nx + x : (long long)(npml + nz - 1 - a) * nx + x;
+                            C psa[4], psb[4];
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) {
+                                psa[e] = prd[5][pz0 + e];
+                                psb[e] = prd[4][pz0 + e];
+                            }
+                            C h[12], dxTxx[4], dxTxz[4], dzTxz[4], dzTzz[4];
+                            ld12<S, C>(trow[4], h);  // Txx
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) dxTxx[e] = dpx<C>(h, e, c0, c1, c2, c3);
+                            ld12<S, C>(trow[4] + K::SW, h);  // Txz
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) dxTxz[e] = dmx<C>(h, e, c0, c1, c2, c3);
+                            dpz4p<S, C>(trow, K::SW).to(dzTxz);
+                            dmz4p<S, C>(trow, 2 * K::SW).to(dzTzz);
+                            const int zb = 4 * nx;
+                            const C bA = __ldg(cp + (zb + nz + a)), cA = __ldg(cp + (B + zb + nz + a)),
+                                    kA = __ldg(cp + (2 * B + zb + nz + a));
+                            const C bB = __ldg(cp + (zb + a)), cB = __ldg(cp + (B + zb + a)),
+                                    kB = __ldg(cp + (2 * B + zb + a));
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) {
+                                C pa = psa[e], pb = psb[e];
+                                vnew[0][e] = vold[0][e];
+                                vnew[1][e] = vold[1][e];
+                                if (vact) {
+                                    const C bu = mv[0][e], bw = mv[1][e];
+                                    C u = vold[0][e], w = vold[1][e];
+                                    u = fmaC<C>(bu, dxTxx[e], u);
+                                    w = fmaC<C>(bw, dxTxz[e], w);
+                                    pa = fmaC<C>(bA, psa[e], cA * dzTxz[e]);
+                                    pb = fmaC<C>(bB, psb[e], cB * dzTzz[e]);
+                                    u = fmaC<C>(bu, fmaC<C>(dzTxz[e], kA, pa), u);
+                                    w = fmaC<C>(bw, fmaC<C>(dzTzz[e], kB, pb), w);
+                                    vnew[0][e] = u;
+                                    vnew[1][e] = w;
+                                }
+                                pwr[5][pz0 + e] = pa;
+                                pwr[4][pz0 + e] = pb;
+                            }
                         }
                     } else {
                         C psx[2][4], psz[2][4];
