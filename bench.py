@@ -9,8 +9,9 @@ Workload (one bench "step" = one whole shot from a zero wavefield):
 
 value: cell-updates/s with the model already resident in HBM (CUDA events on
        the solver's stream around K whole shots).
-e2e:   the same metric through the public API with host buffers: material
-       build + host->device upload, the shot, device->host seismograms.
+e2e:   the same metric through the public API with host buffers in pinned
+       memory: model upload + material build, the shot, device->host
+       seismograms into caller-owned buffers.
 roofline: the fused sweep kernel against the measured HBM copy bandwidth.
 cpu_baseline: the oracle's restatement of the reference update loop on the
        host cores, on a bounded sample of the same grid.
@@ -146,6 +147,19 @@ def box_alg_bytes(bx, bz, nring, es):
     interior cells, and per ring cell the incident field (5 values) and the
     exchange (read r or g, write g or r, for 5 fields)."""
     return 20 * es * (bx - 8) * (bz - 8) + 15 * es * nring
+
+
+def pinned_copy(torch, a):
+    """a copied into page-locked host memory (a numpy view of it)."""
+    t = torch.empty(a.shape, dtype=torch.from_numpy(np.empty(0, a.dtype)).dtype, pin_memory=True)
+    out = t.numpy()
+    out[...] = a
+    return out
+
+
+def pinned_like(torch, a):
+    """A zeroed page-locked host array of a's shape and type."""
+    return pinned_copy(torch, np.zeros_like(a))
 
 
 def max_over_ranks(ms, dist):
@@ -442,14 +456,17 @@ def main():
     if not args.no_e2e:
         es = {"f32": 4, "f64": 8, "bf16": 2, "f16": 2}[args.prec]
         cs = 8 if args.prec == "f64" else 4
+        # inputs and results in pinned host memory (set up before the timed shots)
+        hvp, hvs, hrho = (pinned_copy(torch, a) for a in (vp, vs, rho))
+        hsu, hsw = (pinned_like(torch, s.seismograms(f)) for f in (0, 1))
         times = []
         seis_bytes = 0
         for _ in range(max(1, min(args.steps, 2))):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            s.set_model(vp, vs, rho)
+            s.set_model(hvp, hvs, hrho)
             shot()
-            su, sw = s.seismograms(0), s.seismograms(1)
+            su, sw = s.seismograms(0, hsu), s.seismograms(1, hsw)
             times.append(time.perf_counter() - t0)
             seis_bytes = su.nbytes + sw.nbytes
         # FP32 / FP64: vp, vs, rho go up as doubles and the material is built
@@ -616,16 +633,18 @@ def bench_box(args, F, torch, rank, world, local, dist):
 
     e2e = None
     if not args.no_e2e:
+        hvp, hvs, hrho = (pinned_copy(torch, a) for a in (vp, vs, rho))
+        hsu, hsw = (pinned_like(torch, s.seismograms(f)) for f in (0, 1))
         times = []
         seis_bytes = 0
         for _ in range(max(1, min(args.steps, 2))):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            s.set_model(vp, vs, rho)
+            s.set_model(hvp, hvs, hrho)
             s.set_box(BOX_X0, BOX_Z0, BOX_BX, BOX_BZ)
             s.set_box_incident(inc, 0)
             shot()
-            su, sw = s.seismograms(0), s.seismograms(1)
+            su, sw = s.seismograms(0, hsu), s.seismograms(1, hsw)
             times.append(time.perf_counter() - t0)
             seis_bytes = su.nbytes + sw.nbytes
         e2e = {"value": NX * NZ * nt / statistics.mean(times) * world, "unit": "cell-updates/s",
@@ -781,6 +800,7 @@ def bench_linebox(args, F, torch, rank, world, local, dist):
 
     e2e = None
     if not args.no_e2e:
+        hsu, hsw = (pinned_like(torch, s.seismograms(f)) for f in (0, 1))
         times = []
         seis_bytes = 0
         for _ in range(max(1, min(args.steps, 2))):
@@ -790,7 +810,7 @@ def bench_linebox(args, F, torch, rank, world, local, dist):
             s.set_material(m2)
             s.set_box(*box, bmat=b2)
             shot()
-            su, sw = s.seismograms(0), s.seismograms(1)
+            su, sw = s.seismograms(0, hsu), s.seismograms(1, hsw)
             times.append(time.perf_counter() - t0)
             seis_bytes = su.nbytes + sw.nbytes
         e2e = {"value": NX * NZ * nt / statistics.mean(times) * world, "unit": "cell-updates/s",
@@ -900,13 +920,15 @@ def bench_sh(args, F, torch, rank, world, local, dist):
     value = cells * nt * args.steps * world / (ms_max * 1e-3)
     e2e = None
     if not args.no_e2e:
+        hvs, hrho = (pinned_copy(torch, a) for a in (vs, rho))
+        hout = pinned_like(torch, s.seismograms(0))
         times = []
         for _ in range(max(1, min(args.steps, 2))):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            s.set_model(None, vs, rho)
+            s.set_model(None, hvs, hrho)
             shot()
-            out = s.seismograms(0)
+            out = s.seismograms(0, hout)
             times.append(time.perf_counter() - t0)
         es = {"f32": 4, "f64": 8, "bf16": 2, "f16": 2}[args.prec]
         # FP32 / FP64: vs and rho as doubles (material built on the device)
@@ -1025,10 +1047,7 @@ def bench_batch(args, F, torch, rank, world, local, dist):
         b.run(nt, 1)
 
     def sync():
-        if persist:
-            s.sync()
-        else:
-            b.sync()
+        b.sync()
 
     for _ in range(args.warmup):
         shot()
@@ -1094,14 +1113,16 @@ def bench_batch(args, F, torch, rank, world, local, dist):
 
     e2e = None
     if not args.no_e2e:
+        hmodels = [tuple(pinned_copy(torch, a) for a in m) for m in models]
+        hout = [(pinned_like(torch, s.seismograms(0)), pinned_like(torch, s.seismograms(1))) for s in solvers]
         times = []
         for _ in range(max(1, min(args.steps, 2))):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            for s, m in zip(solvers, models):
+            for s, m in zip(solvers, hmodels):
                 s.set_model(*m)
             shot()
-            out = [(s.seismograms(0), s.seismograms(1)) for s in solvers]
+            out = [(s.seismograms(0, hu), s.seismograms(1, hw)) for s, (hu, hw) in zip(solvers, hout)]
             times.append(time.perf_counter() - t0)
         es = {"f32": 4, "f64": 8, "bf16": 2, "f16": 2}[prec]
         e2e = {"value": cells * nt / statistics.mean(times) * world, "unit": "cell-updates/s",

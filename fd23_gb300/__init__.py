@@ -601,11 +601,19 @@ class Solver:
         _check(lib().fd23_get_step(self._h, _C.byref(it)), "fd23_get_step")
         return it.value
 
-    def seismograms(self, field):
+    def seismograms(self, field, out=None):
+        """[record rows, traces] of one field.  out: a caller-owned C-contiguous
+        array of that shape and the compute type (e.g. pinned host memory) to
+        copy into instead of a new array."""
         n = self._nrec.get(field, 0)
         nr = _C.c_int(0)
         _check(lib().fd23_get_seismograms(self._h, field, None, 0, _C.byref(nr)), "seismograms")
-        out = _np.zeros((nr.value, n), dtype=self.dtype)
+        if out is None:
+            out = _np.zeros((nr.value, n), dtype=self.dtype)
+        elif (out.shape != (nr.value, n) or out.dtype != _np.dtype(self.dtype) or
+              not out.flags["C_CONTIGUOUS"]):
+            raise ValueError("seismograms: out must be C-contiguous %s of shape %s"
+                             % (_np.dtype(self.dtype).name, (nr.value, n)))
         _check(lib().fd23_get_seismograms(self._h, field, _p(out), out.nbytes, _C.byref(nr)),
                "seismograms")
         return out
