@@ -109,6 +109,8 @@ def c1_model(nx=NX, nz=NZ, seed=1):
 
 
 PUNCH_BEFORE, PUNCH_AFTER = 0.02, 10.0
+# block weights (x-CPML, z-CPML) of the windowed workload's phase plans
+C5_PLAN = (6.0, 4.0)
 
 
 def punch_windows_c5(vp):
@@ -324,6 +326,8 @@ def main():
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--config", default="c1", choices=["c0", "c1", "c2", "c3", "c4", "c5", "c6"])
+    ap.add_argument("--plan", default=None, type=lambda v: tuple(float(x) for x in v.split(",")),
+                    help="c5: x-CPML,z-CPML block weights of the phase plans")
     args = ap.parse_args()
     if args.kernel is None:
         args.kernel = "fused"
@@ -388,8 +392,9 @@ def main():
         first, last = punch_windows_c5(vp)
         s.set_punch(first, last)
         if args.kernel == "fused":
-            s.set_plan(6.0, 4.0, 3, 1.0)
-            best_plan = {"wx": 6.0, "wz": 4.0, "oversub": 1.0, "phase_steps": 128}
+            wx, wz = C5_PLAN if args.plan is None else args.plan
+            s.set_plan(wx, wz, 3, 1.0)
+            best_plan = {"wx": wx, "wz": wz, "oversub": 1.0, "phase_steps": 128}
         punch = {"first": first, "last": last, "active": punch_active_fraction(first, last, nt)}
 
     def shot():

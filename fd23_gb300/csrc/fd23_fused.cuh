@@ -743,7 +743,7 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                         P::fma(P::from(ms[0]), P::from(dx), P::from(told[0])).to(tnew[0]);
                         P::fma(P::from(ms[1]), dmz4p<S, C>(urow, 0), P::from(told[1])).to(tnew[1]);
                     }
-                } else if (PSV && xfast && j >= 4 && j <= nz - 5) {
+                } else if (PSV && !PUNCH && xfast && j >= 4 && j <= nz - 5) {
                     // x-interior cells of a z-CPML row (8th order everywhere): the
                     // interior's packed differences, then the general path's chains
                     // with the z memory variables (coefficients uniform in the row)
@@ -1127,7 +1127,7 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                             const P t = P::fma(bv, P::from(dx), P::from(vold[0]));
                             P::fma(bv, dpz4p<S, C>(trow, K::SW), t).to(vnew[0]);  // d/dz Tz
                         }
-                    } else if (PSV && xfast && a >= 4 && a <= nz - 5) {
+                    } else if (PSV && !PUNCH && xfast && a >= 4 && a <= nz - 5) {
                         // x-interior cells of a z-CPML row, as in the stress update
                         if constexpr (PSV) {
                             constexpr C c0 = Coef4<C>::c0, c1 = Coef4<C>::c1, c2 = Coef4<C>::c2, c3 = Coef4<C>::c3;
