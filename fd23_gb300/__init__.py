@@ -59,6 +59,7 @@ ABI_FUNCTIONS = [
     "fd23_debug_expire_wait", "fd23_set_plan", "fd23_get_plan", "fd23_punch_tiles", "fd23_punch_windows", "fd23_read_punch", "fd23_set_punch",
     "fd23_set_material_table", "fd23_set_punch_phase", "fd23_work_plan_live",
     "fd23_line_source_coefs", "fd23_line_plane_origin", "fd23_line_source_planes", "fd23_set_box_line_source",
+    "fd23_debug_persist_barrier",
 ]
 
 
@@ -164,6 +165,7 @@ def lib():
         "fd23_read_model": ([_C.c_char_p, i, i, d, vp, vp, vp], i),
         "fd23_read_stations": ([_C.c_char_p, vp, vp, i], i),
         "fd23_debug_expire_wait": ([vp], i),
+        "fd23_debug_persist_barrier": ([vp], i),
         "fd23_set_plan": ([vp, vp], i),
         "fd23_get_plan": ([vp, vp, _C.POINTER(i)], i),
         "fd23_punch_tiles": ([i, i, _C.POINTER(i), _C.POINTER(i)], i),

@@ -999,6 +999,27 @@ int fd23_debug_expire_wait(fd23_solver *s)
     return launch_wait_probe(s->err_flag, s->stream);
 }
 
+int fd23_debug_persist_barrier(fd23_solver *s)
+{
+    if (!s) return FD23_ERR_ARG;
+    if (!s->persist || !s->have_material) return FD23_ERR_ORDER;
+    CK(cudaSetDevice(s->d.device));
+    switch (s->d.prec) {
+        case FD23_F64:
+            return launch_persist<double, double>(make_shot<double, double>(s), s->d.wave, s->it, 1, 1, 0, 0,
+                                                  s->d_bar, s->err_flag, s->stream, true);
+        case FD23_BF16:
+            return launch_persist<__nv_bfloat16, float>(make_shot<__nv_bfloat16, float>(s), s->d.wave, s->it, 1, 1, 0,
+                                                        0, s->d_bar, s->err_flag, s->stream, true);
+        case FD23_F16:
+            return launch_persist<__half, float>(make_shot<__half, float>(s), s->d.wave, s->it, 1, 1, 0, 0, s->d_bar,
+                                                 s->err_flag, s->stream, true);
+        default:
+            return launch_persist<float, float>(make_shot<float, float>(s), s->d.wave, s->it, 1, 1, 0, 0, s->d_bar,
+                                                s->err_flag, s->stream, true);
+    }
+}
+
 // ---- hybrid box ----
 int fd23_set_box(fd23_solver *s, int x0, int z0, int bx, int bz, const double *bmat)
 {

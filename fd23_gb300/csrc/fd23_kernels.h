@@ -15,10 +15,12 @@ int launch_step_twopass(const Shot<S, C> &s, int wave, int it, cudaStream_t st);
 // steps it0 .. it0+nsteps-1 of the two-pass updates in one cooperative
 // launch (small grids; buffer set 0 in place), grid barriers between the
 // phases; record rows from rec_row on the steps with it % itrecord == 0
-// (any_rec); bar: two zeroed words of device memory, err: the error flag
+// (any_rec); bar: two zeroed words of device memory, err: the error flag;
+// unreachable_barrier: the failure-path check (the first barrier waits for
+// one arrival more than the grid has and gives up after a short limit)
 template <class S, class C>
 int launch_persist(const Shot<S, C> &s, int wave, int it0, int nsteps, int itrecord, int rec_row, int any_rec,
-                   unsigned *bar, int *err, cudaStream_t st);
+                   unsigned *bar, int *err, cudaStream_t st, bool unreachable_barrier = false);
 
 // receiver gather from buffer set `par` into record row `rec_index`
 template <class S, class C>

@@ -342,7 +342,10 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p)
     return v;
 }
 
-__device__ bool grid_barrier(unsigned *bar, int *err)
+// spin: the wait's iteration limit; extra: arrivals beyond the grid's
+// blocks the barrier waits for (0; 1 only in the failure-path check, where
+// nothing completes it)
+__device__ bool grid_barrier(unsigned *bar, int *err, int spin, int extra)
 {
     __shared__ int ok;
     __syncthreads();
@@ -352,12 +355,12 @@ __device__ bool grid_barrier(unsigned *bar, int *err)
         asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(g) : "l"(gen) : "memory");
         asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(count) : "memory");
         int good = 1;
-        if (old + 1u == gridDim.x) {
+        if (old + 1u == gridDim.x + (unsigned)extra) {
             asm volatile("st.relaxed.gpu.global.u32 [%0], 0;" ::"l"(count) : "memory");
             asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(gen), "r"(g + 1u) : "memory");
         } else {
             for (int i = 0; ld_acquire_u32(gen) == g; ++i) {
-                if (i >= kBarSpin || ((i & 1023) == 1023 && *(volatile int *)err)) {
+                if (i >= spin || ((i & 1023) == 1023 && *(volatile int *)err)) {
                     good = 0;
                     atomicCAS(err, 0, 3);
                     break;
@@ -402,8 +405,11 @@ __device__ __forceinline__ void persist_terms(const Shot<S, C> &s, int it, int f
 // phase, which leaves the velocities alone)
 template <class S, class C, int WAVE>
 __global__ void __launch_bounds__(1024, 1) persist_steps(Shot<S, C> s, int it0, int nsteps, int itrecord, int rec_row,
-                                                     int any_rec, int rec_sep, unsigned *bar, int *err)
+                                                     int any_rec, int rec_sep, unsigned *bar, int *err, int spin,
+                                                     int extra)
 {
+    // a raised error flag stands the run down before it touches anything
+    if (*(volatile int *)err) return;
     const int nthr = gridDim.x * blockDim.x, t = blockIdx.x * blockDim.x + threadIdx.x;
     const int nx = s.nx;
     const long long ncell = (long long)nx * s.nz;
@@ -419,7 +425,7 @@ __global__ void __launch_bounds__(1024, 1) persist_steps(Shot<S, C> s, int it0, 
             else sh_stress_cell<S, C>(s, it, ix, iz);
         }
         persist_terms<S, C>(s, it, nvel, 5, t, nthr);
-        if (!grid_barrier(bar, err)) return;
+        if (!grid_barrier(bar, err, spin, extra)) return;
         // SH: the free-surface stress image Tz(x,0) = -Tz(x,1) after the
         // source (SH/fd/cu_fd.cu:226; post_stress_2p) is taken inside the
         // velocity update (IMG), which saves a barrier
@@ -429,11 +435,11 @@ __global__ void __launch_bounds__(1024, 1) persist_steps(Shot<S, C> s, int it0, 
             if (WAVE == FD23_PSV) psv_velocity_cell<S, C>(s, it, ix, iz);
             else sh_velocity_cell<S, C, true>(s, it, ix, iz);
         }
-        if (!grid_barrier(bar, err)) return;
+        if (!grid_barrier(bar, err, spin, extra)) return;
         if (any_rec && it % itrecord == 0) {
             if (rec_sep) {
                 persist_record<S, C>(s, rec_row, t, nthr);
-                if (!grid_barrier(bar, err)) return;
+                if (!grid_barrier(bar, err, spin, extra)) return;
             } else {
                 pending = rec_row;
             }
@@ -447,10 +453,15 @@ __global__ void __launch_bounds__(1024, 1) persist_steps(Shot<S, C> s, int it0, 
 
 template <class S, class C>
 int launch_persist(const Shot<S, C> &s, int wave, int it0, int nsteps, int itrecord, int rec_row, int any_rec,
-                   unsigned *bar, int *err, cudaStream_t st)
+                   unsigned *bar, int *err, cudaStream_t st, bool unreachable_barrier)
 {
-    void (*k)(Shot<S, C>, int, int, int, int, int, int, unsigned *, int *) =
+    void (*k)(Shot<S, C>, int, int, int, int, int, int, unsigned *, int *, int, int) =
         wave == FD23_PSV ? persist_steps<S, C, FD23_PSV> : persist_steps<S, C, FD23_SH>;
+    int spin = kBarSpin, extra = 0;
+    if (unreachable_barrier) {
+        spin = 1 << 14;  // about 10 ms
+        extra = 1;
+    }
     int dev = 0, sms = 0, per_sm = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
@@ -463,7 +474,7 @@ int launch_persist(const Shot<S, C> &s, int wave, int it0, int nsteps, int itrec
     int rec_sep = 0;
     for (int c = (wave == FD23_PSV ? 2 : 1); c < 5; ++c) rec_sep |= s.nrec[c] > 0;
     if (cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), st) != cudaSuccess) return FD23_ERR_CUDA;
-    void *args[] = {(void *)&s, &it0, &nsteps, &itrecord, &rec_row, &any_rec, &rec_sep, &bar, &err};
+    void *args[] = {(void *)&s, &it0, &nsteps, &itrecord, &rec_row, &any_rec, &rec_sep, &bar, &err, &spin, &extra};
     const cudaError_t e = cudaLaunchCooperativeKernel((const void *)k, dim3(blocks), dim3(1024), args, 0, st);
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -556,7 +567,7 @@ int launch_norm2(const Shot<S, C> &s, int par, int nfields, long long elems, dou
     template int launch_norm2<S, C>(const Shot<S, C> &, int, int, long long, double *, cudaStream_t); \
     template int launch_record<S, C>(const Shot<S, C> &, int, int, cudaStream_t);                 \
     template int launch_persist<S, C>(const Shot<S, C> &, int, int, int, int, int, int, unsigned *, int *, \
-                                      cudaStream_t);
+                                      cudaStream_t, bool);
 FD23_INST(float, float)
 FD23_INST(double, double)
 FD23_INST(__nv_bfloat16, float)

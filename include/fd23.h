@@ -353,6 +353,14 @@ int fd23_field_norm2(fd23_solver *s, double *norm2);
  * return at once, and fd23_reset clears the flag.  For tests of the failure
  * handling; it faults nothing and leaves the GPU usable. */
 int fd23_debug_expire_wait(fd23_solver *s);
+/* The same check for a FD23_KERNEL_PERSIST solver: one step of its
+ * cooperative launch whose first grid barrier waits for one block more than
+ * the launch has.  Every block's bounded wait gives up after about 10 ms and
+ * raises the error flag: fd23_sync returns FD23_ERR_TIMEOUT, later runs
+ * return at once, and fd23_reset clears the flag (the stress update of that
+ * step has run, so the wavefields need the reset too).  FD23_ERR_ORDER for
+ * other solvers or before the material. */
+int fd23_debug_persist_barrier(fd23_solver *s);
 
 /* ---- allocation-free watchdog ----
  * No counterpart in the reference.  For callers that cannot allocate device
