@@ -654,6 +654,7 @@ def bench_box(args, F, torch, rank, world, local, dist):
             seis_bytes = su.nbytes + sw.nbytes
         e2e = {"value": NX * NZ * nt / statistics.mean(times) * world, "unit": "cell-updates/s",
                "h2d_bytes_per_step": 3 * NX * NZ * 8 + inc.nbytes, "d2h_bytes_per_step": seis_bytes,
+               "shot_ms": [round(t * 1e3, 1) for t in times],
                "note": "per step = one whole box shot; the incident field is uploaded from pinned "
                        "host memory inside the timed region"}
     hbm, peak_kind = load_peaks()
