@@ -743,10 +743,35 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                         P::fma(P::from(ms[0]), P::from(dx), P::from(told[0])).to(tnew[0]);
                         P::fma(P::from(ms[1]), dmz4p<S, C>(urow, 0), P::from(told[1])).to(tnew[1]);
                     }
-                } else if (PSV && !PUNCH && xfast && j >= 4 && j <= nz - 5) {
+                } else if (!PUNCH && xfast && j >= 4 && j <= nz - 5) {
                     // x-interior cells of a z-CPML row (8th order everywhere): the
                     // interior's packed differences, then the general path's chains
                     // with the z memory variables (coefficients uniform in the row)
+                    if constexpr (!PSV) {
+                        constexpr C c0 = Coef4<C>::c0, c1 = Coef4<C>::c1, c2 = Coef4<C>::c2, c3 = Coef4<C>::c3;
+                        const bool top = j < npml && sh.topabsorb;
+                        const long long pz0 = top ? (long long)j * nx + x : (long long)(npml + nz - 1 - j) * nx + x;
+                        C psv[4];
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) psv[e] = prd[3][pz0 + e];
+                        C h[12], dxv[4], dzv[4];
+                        ld12<S, C>(urow[4], h);
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) dxv[e] = dpx<C>(h, e, c0, c1, c2, c3);
+                        dmz4p<S, C>(urow, 0).to(dzv);
+                        const int zb = 2 * nx;
+                        const C bZ = __ldg(cp + (zb + nz + j)), cZ = __ldg(cp + (B + zb + nz + j)),
+                                kZ = __ldg(cp + (2 * B + zb + nz + j));
+                        const bool own_row = j >= I.z0 && j < I.z1;
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) {
+                            const C a = fmaC<C>(bZ, psv[e], cZ * dzv[e]);
+                            tnew[0][e] = fmaC<C>(ms[0][e], dxv[e], told[0][e]);
+                            tnew[1][e] = fmaC<C>(ms[1][e], fmaC<C>(dzv[e], kZ, a), told[1][e]);
+                            const int ix = x + e;
+                            if (own_row && ix >= I.x0 && ix < I.x0 + K::TX) pwr[3][pz0 + e] = a;
+                        }
+                    }
                     if constexpr (PSV) {
                         constexpr C c0 = Coef4<C>::c0, c1 = Coef4<C>::c1, c2 = Coef4<C>::c2, c3 = Coef4<C>::c3;
                         const bool top = j < npml && sh.topabsorb;
@@ -1127,8 +1152,32 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                             const P t = P::fma(bv, P::from(dx), P::from(vold[0]));
                             P::fma(bv, dpz4p<S, C>(trow, K::SW), t).to(vnew[0]);  // d/dz Tz
                         }
-                    } else if (PSV && !PUNCH && xfast && a >= 4 && a <= nz - 5) {
+                    } else if (!PUNCH && xfast && a >= 4 && a <= nz - 5) {
                         // x-interior cells of a z-CPML row, as in the stress update
+                        if constexpr (!PSV) {
+                            constexpr C c0 = Coef4<C>::c0, c1 = Coef4<C>::c1, c2 = Coef4<C>::c2, c3 = Coef4<C>::c3;
+                            const bool top = a < npml && sh.topabsorb;
+                            const long long pz0 = top ? (long long)a * nx + x : (long long)(npml + nz - 1 - a) * nx + x;
+                            C pst[4];
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) pst[e] = prd[2][pz0 + e];
+                            C h[12], dxT[4], dzT[4];
+                            ld12<S, C>(trow[4], h);  // Tx
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) dxT[e] = dmx<C>(h, e, c0, c1, c2, c3);
+                            dpz4p<S, C>(trow, K::SW).to(dzT);  // d/dz Tz
+                            const int zb = 2 * nx;
+                            const C bT = __ldg(cp + (zb + a)), cT = __ldg(cp + (B + zb + a)),
+                                    kT = __ldg(cp + (2 * B + zb + a));
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) {
+                                const C bv = mv[0][e];
+                                const C pa = fmaC<C>(bT, pst[e], cT * dzT[e]);
+                                const C v = fmaC<C>(bv, dxT[e], vold[0][e]);
+                                vnew[0][e] = fmaC<C>(bv, fmaC<C>(dzT[e], kT, pa), v);
+                                pwr[2][pz0 + e] = pa;
+                            }
+                        }
                         if constexpr (PSV) {
                             constexpr C c0 = Coef4<C>::c0, c1 = Coef4<C>::c1, c2 = Coef4<C>::c2, c3 = Coef4<C>::c3;
                             const bool top = a < npml && sh.topabsorb;
