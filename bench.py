@@ -474,9 +474,9 @@ def main():
             su, sw = s.seismograms(0, hsu), s.seismograms(1, hsw)
             times.append(time.perf_counter() - t0)
             seis_bytes = su.nbytes + sw.nbytes
-        # FP32 / FP64: vp, vs, rho go up as doubles and the material is built
-        # on the device; the 16-bit forms upload the 5 scaled material arrays
-        model_bytes = 3 * NX * NZ * 8 if args.prec in ("f32", "f64") else 5 * NX * NZ * es
+        # vp, vs, rho go up as doubles; the material is built (and for the
+        # 16-bit forms scaled and rounded) on the device
+        model_bytes = 3 * NX * NZ * 8
         e2e = {"value": NX * NZ * nt / statistics.mean(times) * world, "unit": "cell-updates/s",
                "h2d_bytes_per_step": model_bytes + 2 * nt * cs,
                "d2h_bytes_per_step": seis_bytes}
@@ -937,8 +937,8 @@ def bench_sh(args, F, torch, rank, world, local, dist):
             out = s.seismograms(0, hout)
             times.append(time.perf_counter() - t0)
         es = {"f32": 4, "f64": 8, "bf16": 2, "f16": 2}[args.prec]
-        # FP32 / FP64: vs and rho as doubles (material built on the device)
-        up = 2 * cells * 8 if args.prec in ("f32", "f64") else 3 * cells * es
+        # vs and rho as doubles (material built on the device)
+        up = 2 * cells * 8
         e2e = {"value": cells * nt / statistics.mean(times) * world, "unit": "cell-updates/s",
                "h2d_bytes_per_step": up, "d2h_bytes_per_step": int(out.nbytes)}
     hbm, peak_kind = load_peaks()
@@ -1132,7 +1132,7 @@ def bench_batch(args, F, torch, rank, world, local, dist):
             times.append(time.perf_counter() - t0)
         es = {"f32": 4, "f64": 8, "bf16": 2, "f16": 2}[prec]
         e2e = {"value": cells * nt / statistics.mean(times) * world, "unit": "cell-updates/s",
-               "h2d_bytes_per_step": (3 * cells * 8 if prec in ("f32", "f64") else 5 * cells * es),
+               "h2d_bytes_per_step": 3 * cells * 8,
                "d2h_bytes_per_step": sum(a.nbytes + w.nbytes for a, w in out),
                "note": "per step = one whole batch of shots: material build + upload, the run, seismograms"}
     hbm, peak_kind = load_peaks()

@@ -676,24 +676,15 @@ int fd23_set_model(fd23_solver *s, const double *vp, const double *vs, const dou
 {
     if (!s || !vs || !den || (s->d.wave == FD23_PSV && !vp)) return FD23_ERR_ARG;
     const size_t n = (size_t)s->d.nx * s->d.nz;
-    if (!scaled_form(s) && (s->d.prec == FD23_F32 || s->d.prec == FD23_F64)) {
-        // built on the device from vp, vs, den: the host builder's arithmetic
-        const double st = material_stab(s->d.wave, vp, vs, n, s->d.h, s->d.dt);
-        if (stab) *stab = st;
-        if (st > 1.0) return FD23_ERR_UNSTABLE;
-        CK(cudaSetDevice(s->d.device));
-        const int rc = build_material_device(s, vp, vs, den);
-        if (rc) return rc;
-        return material_done(s);
-    }
-    std::vector<double> m((size_t)s->nmat * n);
-    double st = 0.0;
-    int rc = s->d.wave == FD23_PSV
-                 ? build_psv_material(s->d.nx, s->d.nz, s->d.h, s->d.dt, vp, vs, den, m.data(), &st)
-                 : build_sh_material(s->d.nx, s->d.nz, s->d.h, s->d.dt, vs, den, m.data(), &st);
+    // built on the device from vp, vs, den: the host builder's arithmetic
+    // (and for the 16-bit forms fd23_set_material's scaling and rounding)
+    const double st = material_stab(s->d.wave, vp, vs, n, s->d.h, s->d.dt);
     if (stab) *stab = st;
+    if (st > 1.0) return FD23_ERR_UNSTABLE;
+    CK(cudaSetDevice(s->d.device));
+    const int rc = build_material_device(s, vp, vs, den);
     if (rc) return rc;
-    return fd23_set_material(s, m.data());
+    return material_done(s);
 }
 
 int fd23_set_cpml(fd23_solver *s, const double *bckp)

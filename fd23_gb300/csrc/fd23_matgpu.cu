@@ -4,7 +4,14 @@
 // same operation order and no contraction, so the stored material is bit for
 // bit the host builder's rounded to the storage type.  fd23_set_model uses
 // it so that a shot's set-up uploads vp, vs, density once instead of
-// building five arrays on one host core.
+// building five arrays on one host core.  The 16-bit forms add their
+// power-of-two scale kappa (chosen from the maxima of the two material
+// groups, the first time) and the host conversion's rounding: the scaled
+// double to float, then to 16 bits, each to nearest even.
+#include <cmath>
+#include <cstring>
+#include <type_traits>
+
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -38,18 +45,90 @@ __global__ void psv_mu_lam(int nx, int nz, const double *vp, const double *vs, c
     }
 }
 
+// What the material kernels do with each dt/h-scaled value x of array m
+// (the first nms arrays feed the stress update, the rest the velocity update):
+//   kStore:  storage element (S)x, FP32 / FP64 storage;
+//   kMax:    the largest |x| of each group, for the 16-bit forms' power-of-two
+//            scale kappa (fd23_set_material's choice);
+//   kScaled: 16-bit storage element of x * f (f = kappa or 1/kappa, exact),
+//            rounded to float and then to 16 bits, as the host conversion does.
+enum { kStore = 0, kMax = 1, kScaled = 2 };
+
 template <class S>
 __device__ __forceinline__ S store(double v)
 {
     return (S)v;
 }
+template <>
+__device__ __forceinline__ __half store<__half>(double v)
+{
+    return __float2half_rn((float)v);
+}
+template <>
+__device__ __forceinline__ __nv_bfloat16 store<__nv_bfloat16>(double v)
+{
+    return __float2bfloat16_rn((float)v);
+}
+
+struct MatOut {
+    long long origin;
+    int pitch;
+    double fs, fv;                 // kScaled factors of the stress / velocity group
+    unsigned long long *maxbits;   // kMax: [2] bit patterns of the group maxima
+};
+
+template <class S, int MODE>
+struct MatSink {
+    const MatOut &o;
+    double ms = 0.0, mv = 0.0;
+    __device__ MatSink(const MatOut &out) : o(out) {}
+    __device__ __forceinline__ void put(S *a, long long k, int nx, bool stress, double x)
+    {
+        if constexpr (MODE == kMax) {
+            const double ax = fabs(x);
+            if (stress) ms = ax > ms ? ax : ms;
+            else mv = ax > mv ? ax : mv;
+        } else {
+            const int iz = (int)(k / nx), ix = (int)(k % nx);
+            const long long i = o.origin + (long long)iz * o.pitch + ix;
+            a[i] = MODE == kScaled ? store<S>(x * (stress ? o.fs : o.fv)) : store<S>(x);
+        }
+    }
+    // block-wide maxima into maxbits (non-negative doubles order as their bits)
+    __device__ __forceinline__ void finish()
+    {
+        if constexpr (MODE == kMax) {
+            __shared__ double red[2][32];
+            double a = ms, b = mv;
+            for (int d = 16; d > 0; d >>= 1) {
+                a = fmax(a, __shfl_xor_sync(0xffffffffu, a, d));
+                b = fmax(b, __shfl_xor_sync(0xffffffffu, b, d));
+            }
+            const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+            if (lane == 0) {
+                red[0][w] = a;
+                red[1][w] = b;
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                for (int i = 1; i < (int)(blockDim.x >> 5); ++i) {
+                    a = fmax(a, red[0][i]);
+                    b = fmax(b, red[1][i]);
+                }
+                atomicMax(o.maxbits, (unsigned long long)__double_as_longlong(a));
+                atomicMax(o.maxbits + 1, (unsigned long long)__double_as_longlong(b));
+            }
+        }
+    }
+};
 
 // pass 2: BU, BW, MUA (harmonic average of the 4 MU around the node), the
 // free-surface row, the dt/h factor; written to the padded storage arrays
-template <class S>
+template <class S, int MODE = kStore>
 __global__ void psv_rest(int nx, int nz, const double *den, const double *mu, const double *lam, double fac,
-                         long long origin, int pitch, S *LAM, S *MU, S *MUA, S *BU, S *BW)
+                         MatOut out, S *LAM, S *MU, S *MUA, S *BU, S *BW)
 {
+    MatSink<S, MODE> sink(out);
     const long long n = (long long)nx * nz;
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
         const int iz = (int)(k / nx), ix = (int)(k % nx);
@@ -71,44 +150,44 @@ __global__ void psv_rest(int nx, int nz, const double *den, const double *mu, co
             l = 0.0;
             m = 0.5 * m;
         }
-        const long long o = origin + (long long)iz * pitch + ix;
-        LAM[o] = store<S>(l * fac);
-        MU[o] = store<S>(m * fac);
-        MUA[o] = store<S>(mua * fac);
-        BU[o] = store<S>(bu * fac);
-        BW[o] = store<S>(bw * fac);
+        sink.put(LAM, k, nx, true, l * fac);
+        sink.put(MU, k, nx, true, m * fac);
+        sink.put(MUA, k, nx, true, mua * fac);
+        sink.put(BU, k, nx, false, bu * fac);
+        sink.put(BW, k, nx, false, bw * fac);
     }
+    sink.finish();
 }
 
 // SH: MUX, MUZ (harmonic means with the next cell and the cell above), BV
-template <class S>
-__global__ void sh_all(int nx, int nz, const double *vs, const double *den, double fac, long long origin, int pitch,
-                       S *MUX, S *MUZ, S *BV)
+template <class S, int MODE = kStore>
+__global__ void sh_all(int nx, int nz, const double *vs, const double *den, double fac, MatOut out, S *MUX, S *MUZ,
+                       S *BV)
 {
+    MatSink<S, MODE> sink(out);
     const long long n = (long long)nx * nz;
     auto shear = [&](long long k) { return vs[k] * vs[k] * den[k]; };
     auto harm = [](double a, double b) { return 2.0 * a * b / dmax(a + b, 1e-10); };
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
-        const int iz = (int)(k / nx), ix = (int)(k % nx);
         const double m1 = shear(k);
         const double mux = harm(m1, (k + 1 < n) ? shear(k + 1) : m1);
         const double muz = harm(m1, (k - nx >= 0) ? shear(k - nx) : m1);
         const double bv = 1.0 / den[k];
-        const long long o = origin + (long long)iz * pitch + ix;
-        MUX[o] = store<S>(mux * fac);
-        MUZ[o] = store<S>(muz * fac);
-        BV[o] = store<S>(bv * fac);
+        sink.put(MUX, k, nx, true, mux * fac);
+        sink.put(MUZ, k, nx, true, muz * fac);
+        sink.put(BV, k, nx, false, bv * fac);
     }
+    sink.finish();
 }
 
-template <class S>
+template <class S, bool SCALED>
 int build_on_device(fd23_solver *s, const double *vp, const double *vs, const double *den)
 {
     const int nx = s->d.nx, nz = s->d.nz;
     const size_t n = (size_t)nx * nz, bytes = n * sizeof(double);
     const int nin = s->d.wave == FD23_PSV ? 3 : 2;
     double *buf = nullptr;  // inputs, then MU and LAM (P-SV)
-    int rc = dev_alloc((void **)&buf, (nin + 2) * bytes);
+    int rc = dev_alloc((void **)&buf, (nin + 2) * bytes + 2 * sizeof(unsigned long long));
     if (rc) return rc;
     double *dvp = buf, *dvs = buf + (nin == 3 ? n : 0), *dden = buf + (nin - 1) * n;
     double *dmu = buf + nin * n, *dlam = dmu + n;
@@ -118,16 +197,56 @@ int build_on_device(fd23_solver *s, const double *vp, const double *vs, const do
     if (e == cudaSuccess) e = cudaMemcpyAsync(dden, den, bytes, cudaMemcpyHostToDevice, s->stream);
     const double fac = s->d.dt / s->d.h;  // as the host builders: dt / h, then value * fac
     const unsigned blocks = (unsigned)std::min<size_t>((n + 255) / 256, 152 * 32);
-    if (e == cudaSuccess) {
-        S *const *mm = reinterpret_cast<S *const *>(s->mat);
-        if (s->d.wave == FD23_PSV) {
-            psv_mu_lam<<<blocks, 256, 0, s->stream>>>(nx, nz, dvp, dvs, dden, dmu, dlam);
-            psv_rest<S><<<blocks, 256, 0, s->stream>>>(nx, nz, dden, dmu, dlam, fac, s->L.origin, s->L.pitch, mm[0],
-                                                       mm[1], mm[2], mm[3], mm[4]);
-        } else {
-            sh_all<S><<<blocks, 256, 0, s->stream>>>(nx, nz, dvs, dden, fac, s->L.origin, s->L.pitch, mm[0], mm[1],
-                                                     mm[2]);
+    S *const *mm = reinterpret_cast<S *const *>(s->mat);
+    MatOut out{s->L.origin, s->L.pitch, 1.0, 1.0, reinterpret_cast<unsigned long long *>(dmu)};
+    auto launch = [&](auto mode) {
+        constexpr int M = decltype(mode)::value;
+        if (s->d.wave == FD23_PSV)
+            psv_rest<S, M><<<blocks, 256, 0, s->stream>>>(nx, nz, dden, dmu, dlam, fac, out, mm[0], mm[1], mm[2],
+                                                          mm[3], mm[4]);
+        else
+            sh_all<S, M><<<blocks, 256, 0, s->stream>>>(nx, nz, dvs, dden, fac, out, mm[0], mm[1], mm[2]);
+    };
+    if (e == cudaSuccess && s->d.wave == FD23_PSV) {
+        psv_mu_lam<<<blocks, 256, 0, s->stream>>>(nx, nz, dvp, dvs, dden, dmu, dlam);
+        e = cudaGetLastError();
+    }
+    if constexpr (SCALED) {
+        // kappa from the largest stress-update and velocity-update values, the
+        // first time (fd23_set_material's rule); the maxima go to a scratch
+        // pair after the inputs and MU, LAM
+        unsigned long long *dmax = reinterpret_cast<unsigned long long *>(dlam + n);
+        out.maxbits = dmax;
+        if (e == cudaSuccess && !s->kappa_set) {
+            e = cudaMemsetAsync(dmax, 0, 2 * sizeof(unsigned long long), s->stream);
+            if (e == cudaSuccess) {
+                launch(std::integral_constant<int, kMax>());
+                e = cudaGetLastError();
+            }
+            unsigned long long hb[2] = {0, 0};
+            if (e == cudaSuccess) e = cudaMemcpyAsync(hb, dmax, sizeof(hb), cudaMemcpyDeviceToHost, s->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+            if (e == cudaSuccess) {
+                double ms, mv;
+                std::memcpy(&ms, &hb[0], 8);
+                std::memcpy(&mv, &hb[1], 8);
+                s->kappa = (ms > 0 && mv > 0) ? pow2_round(std::sqrt(mv / ms)) : 1.0;
+                s->kappa_set = true;
+                const int rc = upload_source_amps(s);
+                if (rc) {
+                    cudaFree(buf);
+                    return rc;
+                }
+            }
         }
+        out.fs = s->kappa;
+        out.fv = 1.0 / s->kappa;
+        if (e == cudaSuccess) {
+            launch(std::integral_constant<int, kScaled>());
+            e = cudaGetLastError();
+        }
+    } else if (e == cudaSuccess) {
+        launch(std::integral_constant<int, kStore>());
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
@@ -139,9 +258,12 @@ int build_on_device(fd23_solver *s, const double *vp, const double *vs, const do
 
 int build_material_device(fd23_solver *s, const double *vp, const double *vs, const double *den)
 {
-    if (s->d.prec == FD23_F64) return build_on_device<double>(s, vp, vs, den);
-    if (s->d.prec == FD23_F32) return build_on_device<float>(s, vp, vs, den);
-    return FD23_ERR_UNSUPPORTED;  // the 16-bit forms scale their material first (host path)
+    switch (s->d.prec) {
+        case FD23_F64: return build_on_device<double, false>(s, vp, vs, den);
+        case FD23_F32: return build_on_device<float, false>(s, vp, vs, den);
+        case FD23_F16: return build_on_device<__half, true>(s, vp, vs, den);
+        default: return build_on_device<__nv_bfloat16, true>(s, vp, vs, den);
+    }
 }
 
 }  // namespace fd23

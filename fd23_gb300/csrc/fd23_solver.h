@@ -140,6 +140,10 @@ int encode_maps(fd23_solver *s);
 // the material of vp, vs, den built on the device into the storage arrays
 // (fd23_matgpu.cu; FP32 and FP64 storage, FD23_ERR_UNSUPPORTED otherwise)
 int build_material_device(fd23_solver *s, const double *vp, const double *vs, const double *den);
+// 16-bit forms: the power-of-two scale of a value, the source amplitudes in
+// the scaled units (once kappa is known)
+double pow2_round(double v);
+int upload_source_amps(fd23_solver *s);
 
 template <class S, class C>
 Shot<S, C> make_shot(const fd23_solver *s)
