@@ -109,11 +109,14 @@ const char *fd23_strerror(int status);
 int fd23_version(void);
 
 /* ---- model / material ----
- * fd23_set_model: vp, vs, den rasters (nx*nz, FP64).  Builds the staggered,
- * dt/h-scaled material in FP64 on the host with every edge rule of
+ * fd23_set_model: vp, vs, den rasters (nx*nz, FP64).  Runs the CFL check,
+ * stores *stab, uploads the rasters and builds the staggered, dt/h-scaled
+ * material on the device in FP64 with every edge rule of
  * MATERIAL::get_model (PD/material/material.cpp:156-306; SH:
- * SH/material/material.cpp:75-125), runs the CFL check, stores *stab and
- * uploads.  vp is unused for SH and may be NULL.
+ * SH/material/material.cpp:75-125), in the host builder's operation order
+ * (fd23_build_material gives the same values).  The 16-bit forms then scale
+ * and round it as fd23_set_material does.  vp is unused for SH and may be
+ * NULL.
  * fd23_set_material: already-built arrays, FP64, concatenated
  * (P-SV: LAM, MU, MUA, BU, BW; SH: MUX, MUZ, BV), each nx*nz. */
 int fd23_set_model(fd23_solver *s, const double *vp, const double *vs, const double *den,
