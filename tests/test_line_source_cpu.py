@@ -147,3 +147,17 @@ def test_product_host_helpers_match_oracle():
     with pytest.raises(F.Fd23Error) as e:
         F.line_source_planes(d, np.ones(8193), 0, 4)
     assert e.value.status == F.ERR_ARG
+
+
+def test_late_arrivals_are_zero():
+    """Points whose P arrival falls after the last frame are zero (the
+    reference writes past its arrays there); frames that end just after an
+    arrival carry it."""
+    a = O.line_source_coefs(30, 50, 70, 10)
+    src = O.gaussian(4e-4, -6)
+    h, dt, vp = 5.0, 4e-4, 3000.0
+    # a plane 40 .. 47 cells right of the source: R/vp/dt >= 166 steps
+    far = O.line_source_planes(8, 4, 40, -2, h, dt, vp, 1700.0, 2.5, a, src, 0, 150)
+    assert not np.any(far)
+    late = O.line_source_planes(8, 4, 40, -2, h, dt, vp, 1700.0, 2.5, a, src, 0, 260)
+    assert np.any(late[200:]) and not np.any(late[:150])
