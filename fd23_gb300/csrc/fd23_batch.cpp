@@ -269,11 +269,10 @@ int snapshot_restore(const std::vector<fd23_solver *> &ss, cudaStream_t st, cons
     return FD23_OK;
 }
 
-// block cost weights x waves of CTAs (the plan rounds the CTA count up to
-// whole waves of the resident slots)
 // block cost weights (x-CPML 2..7, z-CPML and edge rows 2..5) x waves of
-// CTAs 1..3: the step time is a bumpy function of the cut, so the grid is
-// fine (on the 4000 x 2000 P-SV grid weights 5 / 4 beat 6 / 4 by 6 %)
+// CTAs 1..3 (the plan rounds the CTA count up to whole waves of the resident
+// slots): the step time is a bumpy function of the cut, so the grid is fine
+// (on the 4000 x 2000 P-SV grid weights 5 / 4 beat 6 / 4 by 6 %)
 std::vector<TuneParams> candidates()
 {
     std::vector<TuneParams> c;
