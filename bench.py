@@ -296,14 +296,20 @@ def run_reference_arm(args, rank, world):
           "sample": "%d samples of %d consecutive time steps of the %dx%d grid (%.1f s), FP32 "
                     "oracle restatement of the reference update loop, %d threads" % (
                         args.steps, m, NX, NZ, t, cores)}
+    sample_ms = t / args.steps * 1e3
     line = {"impl": "reference", "metric": "cell-updates/s", "value": value,
             "unit": "cell-updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": NX * NZ * NT / value * 1e3, "higher_is_better": True,
+            "ms_per_step": sample_ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "psv_4000x2000_5000steps_c1", "nx": NX, "nz": NZ, "nt": NT,
-                       "note": "ms_per_step = one whole 5000-step shot extrapolated from the "
-                               "timed samples; the reference's own sources are not on the GPU "
-                               "host, so its update loop runs as the oracle restatement"},
+            "config": {"workload": "psv_%dx%d_%dsteps_c1" % (NX, NZ, NT), "nx": NX, "nz": NZ, "nt": NT,
+                       "h_m": H, "dt_s": DT, "npml": NPML, "source": "15 Hz Ricker explosion",
+                       "traces": 4 * NSTA, "prec": "f32",
+                       "parallelism": "host cores x%d" % cores},
+            "note": "one bench step = one sample of %d consecutive time steps of the shot "
+                    "(ms_per_step is that sample's measured time); shot_ms_extrapolated = one "
+                    "whole %d-step shot at the measured rate.  The reference's own sources are "
+                    "not on the GPU host, so its update loop runs as the oracle restatement" % (m, NT),
+            "shot_ms_extrapolated": NX * NZ * NT / value * 1e3,
             "cpu_baseline": cb,
             "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}

@@ -48,7 +48,7 @@ ABI_FUNCTIONS = [
     "fd23_set_material", "fd23_set_cpml", "fd23_set_source", "fd23_set_source_terms",
     "fd23_wavelet_gaussian", "fd23_wavelet_trapezoid", "fd23_wavelet_ricker", "fd23_moment_psv",
     "fd23_moment_sh", "fd23_set_receivers", "fd23_receivers_line", "fd23_run", "fd23_sync",
-    "fd23_get_seismograms", "fd23_reset", "fd23_get_stream", "fd23_get_step", "fd23_state_bytes", "fd23_get_state",
+    "fd23_get_seismograms", "fd23_reset", "fd23_get_stream", "fd23_get_step", "fd23_get_field_device", "fd23_state_bytes", "fd23_get_state",
     "fd23_set_state", "fd23_field_norm2", "fd23_build_material", "fd23_build_cpml",
     "fd23_build_source_terms", "fd23_sum_squares_noalloc", "fd23_set_box", "fd23_set_box_incident",
     "fd23_box_state_bytes", "fd23_get_box_state", "fd23_set_box_state", "fd23_box_ring_size",
@@ -134,6 +134,7 @@ def lib():
         "fd23_reset": ([vp], i),
         "fd23_get_stream": ([vp, _C.POINTER(vp)], i),
         "fd23_get_step": ([vp, _C.POINTER(i)], i),
+        "fd23_get_field_device": ([vp, i, _C.POINTER(vp), _C.POINTER(sz)], i),
         "fd23_state_bytes": ([vp], sz),
         "fd23_get_state": ([vp, vp, sz], i),
         "fd23_set_state": ([vp, vp, sz, i], i),
@@ -596,6 +597,22 @@ class Solver:
         p = _C.c_void_p()
         _check(lib().fd23_get_stream(self._h, _C.byref(p)), "fd23_get_stream")
         return p.value or 0
+
+    def field_ptrs(self):
+        """Device addresses of the stored wavefields the solver currently
+        reads (padded layout, storage type), valid until the next run."""
+        out = []
+        for f in range(5 if self.wave == PSV else 3):
+            p, n = _C.c_void_p(), _C.c_size_t(0)
+            _check(lib().fd23_get_field_device(self._h, f, _C.byref(p), _C.byref(n)), "fd23_get_field_device")
+            out.append(p.value or 0)
+        return out
+
+    def stored_elems(self):
+        """Stored elements of one wavefield (nx*nz cells plus zero padding)."""
+        p, n = _C.c_void_p(), _C.c_size_t(0)
+        _check(lib().fd23_get_field_device(self._h, 0, _C.byref(p), _C.byref(n)), "fd23_get_field_device")
+        return n.value
 
     @property
     def step(self):

@@ -846,6 +846,14 @@ int fd23_get_stream(fd23_solver *s, void **stream)
     return FD23_OK;
 }
 
+int fd23_get_field_device(fd23_solver *s, int field, void **dev_ptr, size_t *elems)
+{
+    if (!s || !dev_ptr || !elems || field < 0 || field >= s->nfld) return FD23_ERR_ARG;
+    *dev_ptr = s->fld[s->par][field];
+    *elems = s->L.elems();
+    return FD23_OK;
+}
+
 int fd23_get_step(fd23_solver *s, int *it)
 {
     if (!s || !it) return FD23_ERR_ARG;

@@ -1,17 +1,25 @@
 // Allocation-free variant of the FP64 energy watchdog (fd23_field_norm2).
 //
-// Some callers cannot allocate device memory: code that runs while a CUDA
-// stream is being captured into a graph (cudaMalloc is not allowed there),
-// and programs whose device memory belongs to another allocator (a framework's
-// caching allocator, a memory pool sized at start-up).  For them this entry
-// point takes the arrays to reduce as caller-owned device pointers, writes its
-// results to caller-owned host memory, and keeps its partial sums in a fixed
-// file-scope device array instead of allocating: it calls no cudaMalloc,
-// cudaFree or allocating library routine.
+// Some callers cannot allocate device memory: programs whose device memory
+// belongs to another allocator (a framework's caching allocator, a memory
+// pool sized at start-up, an embedding host that forbids cudaMalloc outside
+// its own arena).  For them this entry point takes the arrays to reduce as
+// caller-owned device pointers, writes its results to caller-owned host
+// memory, and keeps its partial sums in a fixed file-scope device array
+// instead of allocating: it calls no cudaMalloc, cudaFree or allocating
+// library routine.
+//
+// The call waits for its stream to finish (it reads the sum back to the
+// host), so it cannot run on a stream that is being captured into a graph:
+// on a capturing stream it returns FD23_ERR_UNSUPPORTED at once, without
+// touching the stream, and the capture stays valid.
 //
 // Limits and sharing:
 //   * at most FD23_NOALLOC_MAX_FIELDS (8) arrays per call; more is rejected
 //     with FD23_ERR_ARG;
+//   * every array must be device memory of the current device (checked with
+//     cudaPointerGetAttributes, which allocates nothing), and the stream must
+//     belong to that device;
 //   * the scratch (FD23_NOALLOC_BLOCKS partial sums and flags, 16 KiB) is held
 //     by every GPU that loads the library until the process exits;
 //   * every call shares that one scratch array and leaves its contents
@@ -20,8 +28,7 @@
 //     host threads at the same time) race on it and must be serialized by the
 //     caller;
 //   * the first call on a device resolves the scratch's device address for
-//     that device (cudaGetSymbolAddress); make that first call before any
-//     stream capture starts.
+//     that device (cudaGetSymbolAddress).
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -136,6 +143,22 @@ int scratch_for_current_device(double **out)
     return FD23_OK;
 }
 
+// FD23_OK when every pointer is device (or managed) memory of device `dev`
+int check_pointers(const FieldPtrs &fp, int nfields, int dev)
+{
+    for (int k = 0; k < nfields; ++k) {
+        if (!fp.p[k]) continue;  // n == 0: nothing is read
+        cudaPointerAttributes a{};
+        if (cudaPointerGetAttributes(&a, fp.p[k]) != cudaSuccess) {
+            cudaGetLastError();
+            return FD23_ERR_ARG;
+        }
+        if ((a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged) || a.device != dev)
+            return FD23_ERR_ARG;
+    }
+    return FD23_OK;
+}
+
 }  // namespace
 
 extern "C" int fd23_sum_squares_noalloc(int prec, const void *const *fields, int nfields, size_t n,
@@ -144,15 +167,37 @@ extern "C" int fd23_sum_squares_noalloc(int prec, const void *const *fields, int
     if (!fields || !sum || !nonfinite || nfields <= 0 || prec < FD23_F32 || prec > FD23_F16)
         return FD23_ERR_ARG;
     if (nfields > kMaxFields) return FD23_ERR_ARG;  // beyond the fixed scratch
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // the call ends with a stream synchronize, which a capturing stream
+    // refuses (and the refusal would invalidate the capture): decline first
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) {
+        cudaGetLastError();
+        return FD23_ERR_UNSUPPORTED;
+    }
+    if (cap != cudaStreamCaptureStatusNone) return FD23_ERR_UNSUPPORTED;
     FieldPtrs fp{};
     for (int k = 0; k < nfields; ++k) {
         if (!fields[k] && n > 0) return FD23_ERR_ARG;
-        fp.p[k] = fields[k];
+        fp.p[k] = n > 0 ? fields[k] : nullptr;
+    }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return FD23_ERR_CUDA;
+    }
+    int rc = check_pointers(fp, nfields, dev);
+    if (rc) return rc;
+    if (st) {
+        int sdev = -1;
+        if (cudaStreamGetDevice(st, &sdev) != cudaSuccess) {
+            cudaGetLastError();
+            return FD23_ERR_ARG;
+        }
+        if (sdev != dev) return FD23_ERR_ARG;
     }
     double *scratch = nullptr;
-    int rc = scratch_for_current_device(&scratch);
-    if (rc) return rc;
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if ((rc = scratch_for_current_device(&scratch))) return rc;
     const long long nn = (long long)n;
     switch (prec) {
         case FD23_F64: partial_sums<double><<<kBlocks, kThreads, 0, st>>>(fp, nfields, nn, scratch); break;
@@ -160,7 +205,10 @@ extern "C" int fd23_sum_squares_noalloc(int prec, const void *const *fields, int
         case FD23_F16: partial_sums<__half><<<kBlocks, kThreads, 0, st>>>(fp, nfields, nn, scratch); break;
         default: partial_sums<float><<<kBlocks, kThreads, 0, st>>>(fp, nfields, nn, scratch);
     }
+    // a rejected launch must not let the previous call's result through
+    if (cudaGetLastError() != cudaSuccess) return FD23_ERR_CUDA;
     final_sum<<<1, kBlocks, 0, st>>>(scratch);
+    if (cudaGetLastError() != cudaSuccess) return FD23_ERR_CUDA;
     double h[2];
     if (cudaMemcpyAsync(h, scratch + 2 * kBlocks, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess) {

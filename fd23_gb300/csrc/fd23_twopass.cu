@@ -4,7 +4,7 @@
 // versa, so in-place updates are race free).  This is the simple GPU form of
 // the reference kernels (PD/fd/cu_fd.cu:209-501, SH/fd/cu_fd.cu:77-288) on the
 // padded layout, for any nx, nz.  The fused single-pass sweep
-// (fd23_fused_psv.cu) is the fast path; this one is the cross-check and the
+// (fd23_fused.cuh, instantiated by fd23_fused*.cu) is the fast path; this one is the cross-check and the
 // fallback for forms the fused sweep does not cover.
 #include <algorithm>
 

@@ -174,6 +174,14 @@ int fd23_get_seismograms(fd23_solver *s, int field, void *out, size_t out_bytes,
 int fd23_reset(fd23_solver *s);
 /* the cudaStream_t every launch of this solver goes to (for event timing) */
 int fd23_get_stream(fd23_solver *s, void **stream);
+/* device address of wavefield `field` (storage order, FD23_U ..) in the
+ * buffer set the solver currently reads, and its stored element count: the
+ * padded layout, nx*nz cells plus zero padding, of the storage type (for the
+ * 16-bit forms the stored values carry the solver's power-of-two scales).
+ * Valid until the next run; for zero-copy reads such as
+ * fd23_sum_squares_noalloc.  No counterpart in the reference (its FIELD
+ * members are public device pointers, PD/field/field.h). */
+int fd23_get_field_device(fd23_solver *s, int field, void **dev_ptr, size_t *elems);
 int fd23_get_step(fd23_solver *s, int *it);
 
 /* ---- state (restart) ----
@@ -367,17 +375,19 @@ int fd23_debug_persist_barrier(fd23_solver *s);
 
 /* ---- allocation-free watchdog ----
  * No counterpart in the reference.  For callers that cannot allocate device
- * memory (code running inside a CUDA stream capture, programs whose device
- * memory belongs to another allocator): sums the squares of nfields
- * caller-owned device arrays of n elements each (element type prec) in FP64
- * into *sum and sets *nonfinite when any value is NaN or Inf -- the same
- * quantity fd23_field_norm2 computes for a solver -- without allocating.
- * Its partial sums live in a fixed 16 KiB file-scope device array that every
- * GPU loading the library keeps until exit.  At most 8 arrays per call (more
- * returns FD23_ERR_ARG).  The first call on a device looks up that array's
- * address for the device: make it before any stream capture.  All calls
- * share the array, so calls that overlap on the GPU race; serialize them.
- * Runs on `stream` (a cudaStream_t, NULL = default) and waits for it. */
+ * memory (programs whose device memory belongs to another allocator: a
+ * framework's caching allocator, a pool sized at start-up): sums the squares
+ * of nfields caller-owned device arrays of n elements each (element type
+ * prec) in FP64 into *sum and sets *nonfinite when any value is NaN or Inf
+ * -- the same quantity fd23_field_norm2 computes for a solver -- without
+ * allocating.  Its partial sums live in a fixed 16 KiB file-scope device
+ * array that every GPU loading the library keeps until exit.  At most 8
+ * arrays per call (more returns FD23_ERR_ARG); every array must be device
+ * memory of the current device and `stream` (a cudaStream_t, NULL = default)
+ * must belong to it (FD23_ERR_ARG otherwise).  The call waits for its stream,
+ * so it cannot run on a stream that is being captured: there it returns
+ * FD23_ERR_UNSUPPORTED without touching the stream.  All calls share the
+ * scratch array, so calls that overlap on the GPU race; serialize them. */
 int fd23_sum_squares_noalloc(int prec, const void *const *fields, int nfields, size_t n,
                              void *stream, double *sum, int *nonfinite);
 

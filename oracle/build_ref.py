@@ -6,7 +6,7 @@ sources where they lie (``PSV/psv_clean_double/source/source_line.cpp``,
 ``source/waveform.cpp``, ``param/param.cpp`` and ``getpar/getpar.cpp``, the
 last as C) with ``g++``/``gcc`` directly, plus ``oracle/ref_convolve.cpp``
 (a CPU restatement of the one CUDA kernel the program calls), into
-``oracle/_ref/ntde_line``.  Only ``tests/golden/gen_line_source.py`` and the
+``oracle/_ref/ntde_line``.  Only ``tests/golden/make_line_source.py`` and the
 reference-pin tests run it; nothing ships with the product.  Without the
 reference sources (e.g. on a machine that only has this repository) the
 build is skipped and returns None.
@@ -23,7 +23,9 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_ref")
-REF_ROOT = os.environ.get("FD23_REFERENCE_ROOT", "/root/reference")
+# The read-only reference checkout this recipe compiles from (the one place
+# the repository names it); FD23_REFERENCE_ROOT points elsewhere.
+REF_ROOT = os.environ.get("FD23_REFERENCE_ROOT") or "/root/reference"
 PD = os.path.join(REF_ROOT, "PSV", "psv_clean_double")
 NTDE = os.path.join(OUT_DIR, "ntde_line")
 

@@ -57,4 +57,7 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("FD23_REFERENCE_ROOT")
+    if not root:
+        sys.exit("usage: make_golden.py /path/to/fd23 (or set FD23_REFERENCE_ROOT)")
+    main(root)
