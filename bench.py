@@ -325,8 +325,9 @@ def main():
     ap.add_argument("--impl", default="ours")
     ap.add_argument("--nt", type=int, default=NT)
     ap.add_argument("--prec", default="f32")
-    ap.add_argument("--kernel", default=None, choices=["fused", "twopass", "persist"],
-                    help="default fused; persist: a run in one cooperative launch (small grids)")
+    ap.add_argument("--kernel", default=None, choices=["fused", "twopass", "persist", "fused2"],
+                    help="default fused; persist: a run in one cooperative launch (small grids); "
+                         "fused2: two time steps per launch (P-SV FP32)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
@@ -489,7 +490,11 @@ def main():
 
     hbm, peak_kind = load_peaks()
     es = {"f32": 4, "f64": 8, "bf16": 2, "f16": 2}[args.prec]
-    per_launch_ms = ms_max / (args.steps * nt)
+    # the two-step sweep advances two steps per launch and moves the same
+    # compulsory bytes per launch (each field read and written once, the
+    # material and the memory variables once) as a one-step launch
+    launches = nt // 2 + nt % 2 if args.kernel == "fused2" else nt
+    per_launch_ms = ms_max / (args.steps * launches)
     ab = alg_bytes(NX, NZ, NPML, es)
     if punch is not None:
         ab = ab * punch["active"]  # only the cells of tiles the windows leave live move
@@ -497,7 +502,7 @@ def main():
     traffic = None
     tfile = os.path.join(ROOT, "profiles", "traffic_per_cell.json")
     if os.path.exists(tfile):
-        tb = json.load(open(tfile)).get("fused_psv_%s" % args.prec)
+        tb = json.load(open(tfile)).get("%s_psv_%s" % ("fused2" if args.kernel == "fused2" else "fused", args.prec))
         if tb:
             traffic = tb * NX * NZ
     line = {"metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": world,
@@ -516,7 +521,7 @@ def main():
                          "peak_source": peak_kind,
                          "alg_bytes_per_launch": ab,
                          "launch_ms": per_launch_ms},
-            "gpu_launches": args.steps * (nt + 1),
+            "gpu_launches": args.steps * (launches + 1),
             "clocks": clocks,
             "e2e": e2e}
     if best_plan:

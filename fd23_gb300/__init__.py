@@ -28,7 +28,7 @@ LIB_PATH = _os.environ.get("FD23_LIB") or _os.path.join(_HERE, "_lib", "libfd23.
 
 PSV, SH = 0, 1
 F32, F64, BF16, F16 = 0, 1, 2, 3
-KERNEL_AUTO, KERNEL_FUSED, KERNEL_TWOPASS, KERNEL_PERSIST = 0, 1, 2, 3
+KERNEL_AUTO, KERNEL_FUSED, KERNEL_TWOPASS, KERNEL_PERSIST, KERNEL_FUSED2 = 0, 1, 2, 3, 4
 U, W, TXX, TXZ, TZZ = 0, 1, 2, 3, 4
 V, TX, TZ = 0, 1, 2
 SRC_EXPLOSION, SRC_FORCE, SRC_MOMENT, SRC_MOMENT_P = 1, 2, 3, 13
@@ -39,8 +39,8 @@ _WAVES = {"psv": PSV, "sh": SH, PSV: PSV, SH: SH}
 _PRECS = {"f32": F32, "fp32": F32, "f64": F64, "fp64": F64, "bf16": BF16, "f16": F16,
           "fp16": F16, F32: F32, F64: F64, BF16: BF16, F16: F16}
 _KERNELS = {"auto": KERNEL_AUTO, "fused": KERNEL_FUSED, "twopass": KERNEL_TWOPASS, "persist": KERNEL_PERSIST,
-            KERNEL_AUTO: KERNEL_AUTO, KERNEL_FUSED: KERNEL_FUSED, KERNEL_TWOPASS: KERNEL_TWOPASS,
-            KERNEL_PERSIST: KERNEL_PERSIST}
+            "fused2": KERNEL_FUSED2, KERNEL_AUTO: KERNEL_AUTO, KERNEL_FUSED: KERNEL_FUSED,
+            KERNEL_TWOPASS: KERNEL_TWOPASS, KERNEL_PERSIST: KERNEL_PERSIST, KERNEL_FUSED2: KERNEL_FUSED2}
 
 # every function the C ABI exports (checked against include/fd23.h by the tests)
 ABI_FUNCTIONS = [

@@ -20,8 +20,8 @@
 // U_sta_file / W_sta_file or nrec ixrec0 izrec0_u izrec0_w idxrec idzrec.
 // Optional: srctype (1 moment, p 'p' dipole; default 1), itrecord (1),
 // restart + nt0, savestate.  Accepted and ignored (no effect on this path):
-// ntsnap itprint gpuid ngpu ord bw src_shift_x src_shift_z
-// sourcetime stype.  usepunch=1 (with before, after, timefile) updates
+// ntsnap itprint gpuid ngpu ord bw sourcetime stype; src_shift_x and
+// src_shift_z (default 0.25, -0.25) only enter the FP64 trace headers.  usepunch=1 (with before, after, timefile) updates
 // every 32 x 16 tile only inside its step window (PN/slide/cu_slide.cu,
 // PN/param/param.cpp usepunch block): the timefile holds nx*nz float travel
 // times (PN, SH), or doubles with prec=f64 (PD, whose windows use the double
@@ -54,7 +54,11 @@
 // receiver (U positions shifted +0.5 cell in x, W -0.5 cell in z); with
 // savestate=1 the state file state%06d (step nt0+nt-1); with restart=1 the
 // run starts from state%06d (step nt0-1).  Header words the reference leaves
-// unset are written as zero.
+// unset are written as zero.  With prec=f64 the trace files are the FP64
+// program's (PD/record/isis.cpp:8-58): <output>_U.db.isis and
+// <output>_W.db.isis, a 136-byte double header and the double trace per
+// receiver, the source position shifted by src_shift_x / src_shift_z cells,
+// user[1] = bw (0 without the box), user[2] = 123456789.
 //
 // Built with FD23_CLI_NTDE=1 it is fd23_ntde_line, the reference's
 // box-source generator (PD/source/source_line.cpp:307-410): from the same
@@ -146,6 +150,22 @@ struct IsisTrace {
     int user[4];
 };
 static_assert(sizeof(IsisTrace) == 84, "isis trace header is 84 bytes");
+
+// 136-byte trace header of the FP64 program's trace files
+// (PD/record/isis.h:7-26): the same words in double, with the natural
+// alignment padding after nt and after status
+struct IsisTraceDb {
+    double xs, ys, zs;
+    double xr, yr, zr;
+    double t0;
+    int nt;
+    double samplerate;
+    int srcflagnum, recflagnum, status;
+    double gain, dtstatic, ampstatic;
+    unsigned short recorder, chan, scomp, rcomp;
+    int user[4];
+};
+static_assert(sizeof(IsisTraceDb) == 136, "FP64 isis trace header is 136 bytes");
 
 int fail(const char *what, int rc)
 {
@@ -327,6 +347,7 @@ int main(int argc, char **argv)
     const double strike = p.need_num("strike"), dip = p.need_num("dip"), rake = p.need_num("rake"),
                  azimuth = p.need_num("azimuth");
     const int xs = (int)p.need_num("xs"), zs = (int)p.need_num("zs");
+    const double src_shift_x = p.num("src_shift_x", 0.25), src_shift_z = p.num("src_shift_z", -0.25);
     const int npml = (int)p.need_num("npml");
     const double pml_dt = p.need_num("pml_dt"), pml_v = p.need_num("pml_v"), pml_r = p.need_num("pml_r"),
                  pml_fc = p.need_num("pml_fc");
@@ -574,8 +595,39 @@ int main(int argc, char **argv)
             std::fprintf(stderr, "%s: ", kProg); std::fprintf(stderr, "cannot write %s\n", name.c_str());
             return 1;
         }
-        // .isis: one header + trace per receiver, float samples
         const int ntrec = std::min(nrs, nt / itrecord);
+        if (prec == FD23_F64) {
+            // .db.isis: one 136-byte double header + double trace per receiver
+            std::ofstream f(name + ".db.isis", std::ios::binary);
+            std::vector<double> tr((size_t)ntrec);
+            const double dshiftx[2] = {kSH ? 0.0 : 0.5, 0.0}, dshiftz[2] = {0.0, -0.5};
+            for (size_t r = 0; r < ntr; ++r) {
+                IsisTraceDb t;
+                std::memset(&t, 0, sizeof t);
+                const int ixr = (*rx[c])[r], izr = (*rz[c])[r];
+                t.xr = (ixr + dshiftx[c]) * h;
+                t.zr = (izr + dshiftz[c]) * h;
+                t.xs = (double)(xs + src_shift_x) * h;
+                t.zs = (double)(zs + src_shift_z) * h;
+                t.nt = ntrec;
+                t.samplerate = dt * (double)itrecord;
+                t.gain = dt / h;
+                t.ampstatic = 1.0;
+                t.srcflagnum = xs;
+                t.recflagnum = ixr;
+                t.user[1] = usebox == 1 ? bw : 0;
+                t.user[2] = 123456789;
+                for (int k = 0; k < ntrec; ++k) tr[k] = reinterpret_cast<const double *>(raw.data())[(size_t)k * ntr + r];
+                f.write((const char *)&t, sizeof t);
+                f.write((const char *)tr.data(), (std::streamsize)(tr.size() * sizeof(double)));
+            }
+            if (!f) {
+                std::fprintf(stderr, "%s: ", kProg); std::fprintf(stderr, "cannot write %s.db.isis\n", name.c_str());
+                return 1;
+            }
+            continue;
+        }
+        // .isis: one header + trace per receiver, float samples
         std::ofstream f(name + ".isis", std::ios::binary);
         std::vector<float> tr((size_t)ntrec);
         for (size_t r = 0; r < ntr; ++r) {

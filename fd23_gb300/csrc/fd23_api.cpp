@@ -157,6 +157,25 @@ int download_grid(fd23_solver *s, const void *dptr, unsigned char *host, size_t 
     return FD23_OK;
 }
 
+// Two time steps (it, it+1) in one launch of the two-step sweep.  The
+// pending record row (the previous launch's last step) is gathered on the
+// way, step it is recorded inside the launch, step it+1 becomes pending.
+int step2_impl(fd23_solver *s, int rec_now, int rec_next)
+{
+    Shot<float, float> sh = make_shot<float, float>(s);
+    sh.cta0 = 0;
+    sh.ncta = s->nblocks2;
+    const int rec_mid = rec_now ? s->nrec_steps++ : -1;
+    const int rc = launch_step_fused2<float>(sh, s->d_items2, s->d_item_off2, s->nblocks2, s->par, s->it,
+                                             s->pending_rec, rec_mid, s->err_flag, s->stream);
+    if (rc) return rc;
+    s->pending_rec = -1;
+    s->par = 1 - s->par;
+    s->it += 2;
+    if (rec_next) s->pending_rec = s->nrec_steps++;
+    return FD23_OK;
+}
+
 // One time step.  Without a box the fused sweep gathers the previous step's
 // receivers on its way; with a box the step is
 //   ring(U,W) | residual stress (+ add-ring g) | sweep | sub-ring r |
@@ -253,7 +272,8 @@ int dispatch_flush(fd23_solver *s)
 // the wavefield block of each buffer set and of the material block, with the
 // box shapes the sweep copies (fused_boxes).  Coordinates of a copy are
 // padded-array positions, so every box the sweep asks for lies inside.
-int encode_maps(fd23_solver *s)
+// the driver's cuTensorMapEncodeTiled (null when unavailable)
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
 {
     static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
     if (!encode) {
@@ -263,10 +283,63 @@ int encode_maps(fd23_solver *s)
                 cudaSuccess ||
             q != cudaDriverEntryPointSuccess || !fn) {
             cudaGetLastError();
-            return FD23_ERR_CUDA;
+            return nullptr;
         }
         encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
     }
+    return encode;
+}
+
+// Tensor maps of the two-step sweep (FP32 wavefields and material): the same
+// views as encode_maps with its boxes (fused2_boxes).
+int encode_maps2(fd23_solver *s)
+{
+    PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+    if (!encode) return FD23_ERR_CUDA;
+    const Fused2Boxes bx = fused2_boxes(false);
+    const Layout &L = s->L;
+    auto make = [&](TmaDesc &m, void *base, int nfields, int w, int nf, size_t es,
+                    CUtensorMapDataType dt) -> int {
+        const cuuint64_t dims[3] = {(cuuint64_t)L.pitch, (cuuint64_t)L.rows, (cuuint64_t)nfields};
+        const cuuint64_t strides[2] = {(cuuint64_t)L.pitch * es, (cuuint64_t)L.elems() * es};
+        const cuuint32_t box[3] = {(cuuint32_t)w, 4u, (cuuint32_t)nf};
+        const cuuint32_t estr[3] = {1u, 1u, 1u};
+        const CUresult r = encode(reinterpret_cast<CUtensorMap *>(&m), dt, 3, base, dims, strides, box, estr,
+                                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                  CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        return r == CUDA_SUCCESS ? FD23_OK : FD23_ERR_CUDA;
+    };
+    // U W rows of bx.uww (> 256) columns: a 4-D view [field][row][column / 8][8]
+    // whose box {8, uww / 8, 4, 2} lands as [2][4][uww] in shared memory
+    auto make_groups = [&](TmaDesc &m, void *base, int nfields, int w, int nf) -> int {
+        const cuuint64_t dims[4] = {8u, (cuuint64_t)L.pitch / 8, (cuuint64_t)L.rows, (cuuint64_t)nfields};
+        const cuuint64_t strides[3] = {32u, (cuuint64_t)L.pitch * 4, (cuuint64_t)L.elems() * 4};
+        const cuuint32_t box[4] = {8u, (cuuint32_t)(w / 8), 4u, (cuuint32_t)nf};
+        const cuuint32_t estr[4] = {1u, 1u, 1u, 1u};
+        const CUresult r = encode(reinterpret_cast<CUtensorMap *>(&m), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dims,
+                                  strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                  CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        return r == CUDA_SUCCESS ? FD23_OK : FD23_ERR_CUDA;
+    };
+    if (L.pitch % 8 != 0 || bx.uww % 8 != 0) return FD23_ERR_UNSUPPORTED;
+    ShotMaps2 h{};
+    int rc = FD23_OK;
+    for (int b = 0; b < 2 && !rc; ++b) {
+        rc = make_groups(h.uw[b], s->fld_block[b], s->nfld, bx.uww, 2);
+        if (!rc) rc = make(h.t[b], s->fld_block[b], s->nfld, bx.pww, 3, 4, CU_TENSOR_MAP_DATA_TYPE_FLOAT32);
+    }
+    if (!rc) rc = make(h.ms, s->mat_block, s->nmat, bx.mww, 3, 4, CU_TENSOR_MAP_DATA_TYPE_FLOAT32);
+    if (!rc) rc = make(h.mv, s->mat_block, s->nmat, bx.mww, 2, 4, CU_TENSOR_MAP_DATA_TYPE_FLOAT32);
+    if (rc) return rc;
+    if (!s->d_maps2 && (rc = dev_alloc((void **)&s->d_maps2, sizeof(ShotMaps2)))) return rc;
+    CK(cudaMemcpy(s->d_maps2, &h, sizeof(ShotMaps2), cudaMemcpyHostToDevice));
+    return FD23_OK;
+}
+
+int encode_maps(fd23_solver *s)
+{
+    PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+    if (!encode) return FD23_ERR_CUDA;
     const FusedBoxes bx = fused_boxes(s->d.wave, s->d.prec);
     CUtensorMapDataType dt = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
     if (s->d.prec == FD23_F64) dt = CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
@@ -359,6 +432,68 @@ int build_worklist(fd23_solver *s)
     return FD23_OK;
 }
 
+// Work plan of the two-step sweep: strips of kFused2TileX output columns,
+// one CTA per SM (its shared memory allows one).
+int build_worklist2(fd23_solver *s)
+{
+    int sms = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->d.device));
+    TuneParams tp = s->tune;
+    tp.per_sm = 1;
+    WorkPlan plan;
+    const std::vector<ShotGeom> geo{ShotGeom{s->d.nx, s->d.nz, s->d.npml, s->d.topabsorb}};
+    int rc = plan_work(geo, kFused2TileX, sms, tp, plan);
+    if (rc) return rc;
+    cudaFree(s->d_items2);
+    cudaFree(s->d_item_off2);
+    s->d_items2 = nullptr;
+    s->d_item_off2 = nullptr;
+    if ((rc = upload_plan(plan, &s->d_items2, &s->d_item_off2))) return rc;
+    s->nblocks2 = plan.nblocks;
+    s->h_items2 = plan.items;
+    s->h_item_off2 = plan.off;
+    s->rec2_dirty = true;
+    return FD23_OK;
+}
+
+// Receivers of every work item of the two-step plan (the cells it owns:
+// columns [x0, x0+kFused2TileX), rows [z0, z1)), velocity fields first, then
+// stresses, each sorted by row: entries (field, ix, iz, receiver).
+int build_rec2(fd23_solver *s)
+{
+    const int ni = (int)s->h_items2.size();
+    std::vector<int4> list;
+    std::vector<int> off;
+    off.reserve(2 * (size_t)ni + 1);
+    for (int k = 0; k < ni; ++k) {
+        const WorkItem &w = s->h_items2[k];
+        for (int part = 0; part < 2; ++part) {
+            off.push_back((int)list.size());
+            const size_t first = list.size();
+            for (int c = part == 0 ? 0 : 2; c < (part == 0 ? 2 : s->nfld); ++c)
+                for (int r = 0; r < s->nrec[c] && r < (int)s->h_rx[c].size(); ++r) {
+                    const int ix = s->h_rx[c][r], iz = s->h_rz[c][r];
+                    if (ix >= w.x0 && ix < w.x0 + kFused2TileX && iz >= w.z0 && iz < w.z1)
+                        list.push_back(make_int4(c, ix, iz, r));
+                }
+            std::stable_sort(list.begin() + first, list.end(),
+                             [](const int4 &a, const int4 &b) { return a.z < b.z; });
+        }
+    }
+    off.push_back((int)list.size());
+    cudaFree(s->d_rec2);
+    cudaFree(s->d_rec2_off);
+    s->d_rec2 = nullptr;
+    s->d_rec2_off = nullptr;
+    int rc = dev_alloc((void **)&s->d_rec2, std::max<size_t>(1, list.size()) * sizeof(int4));
+    if (rc) return rc;
+    if ((rc = dev_alloc((void **)&s->d_rec2_off, off.size() * sizeof(int)))) return rc;
+    if (!list.empty()) CK(cudaMemcpy(s->d_rec2, list.data(), list.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s->d_rec2_off, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice));
+    s->rec2_dirty = false;
+    return FD23_OK;
+}
+
 int upload_cpml(fd23_solver *s, const std::vector<double> &bck)
 {
     std::vector<unsigned char> tmp(bck.size() * s->cs);
@@ -431,6 +566,12 @@ void free_all(fd23_solver *s)
     cudaFree(s->box_inc);
     cudaFree(s->d_items);
     cudaFree(s->d_item_off);
+    cudaFree(s->d_items2);
+    cudaFree(s->d_item_off2);
+    cudaFree(s->d_maps2);
+    for (int p = 0; p < 8; ++p) cudaFree(s->psi_mid[p]);
+    cudaFree(s->d_rec2);
+    cudaFree(s->d_rec2_off);
     if (s->stream) cudaStreamDestroy(s->stream);
 }
 
@@ -563,7 +704,8 @@ int fd23_create(const fd23_desc *desc, fd23_solver **out)
     if (d.nx < 2 || d.nz < 2 || d.npml < 0 || 2 * d.npml > d.nx || 2 * d.npml > d.nz) return FD23_ERR_ARG;
     if ((long long)d.nx * d.nz > (1LL << 31)) return FD23_ERR_ARG;
     if (!(d.h > 0) || !(d.dt > 0)) return FD23_ERR_ARG;
-    if (d.kernel < FD23_KERNEL_AUTO || d.kernel > FD23_KERNEL_PERSIST) return FD23_ERR_ARG;
+    if (d.kernel < FD23_KERNEL_AUTO || d.kernel > FD23_KERNEL_FUSED2) return FD23_ERR_ARG;
+    if (d.kernel == FD23_KERNEL_FUSED2 && (d.wave != FD23_PSV || d.prec != FD23_F32)) return FD23_ERR_UNSUPPORTED;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || d.device < 0 || d.device >= ndev) {
         cudaGetLastError();
@@ -578,7 +720,8 @@ int fd23_create(const fd23_desc *desc, fd23_solver **out)
     s->npsi = d.wave == FD23_PSV ? 8 : 4;
     s->es = storage_size(d.prec);
     s->cs = compute_size(d.prec);
-    s->fused = d.kernel == FD23_KERNEL_AUTO || d.kernel == FD23_KERNEL_FUSED;
+    s->fused = d.kernel == FD23_KERNEL_AUTO || d.kernel == FD23_KERNEL_FUSED || d.kernel == FD23_KERNEL_FUSED2;
+    s->fused2 = d.kernel == FD23_KERNEL_FUSED2;
     s->persist = d.kernel == FD23_KERNEL_PERSIST;
     if (const char *v = getenv("FD23_COST_XPML")) s->tune.wx = atof(v);
     if (const char *v = getenv("FD23_COST_ZPML")) s->tune.wz = atof(v);
@@ -617,6 +760,13 @@ int fd23_create(const fd23_desc *desc, fd23_solver **out)
         if ((rc = fused_prepare(d.wave, d.prec))) return fail(rc);
         if ((rc = build_worklist(s))) return fail(rc);
         if ((rc = encode_maps(s))) return fail(rc);
+    }
+    if (s->fused2) {
+        for (int p = 0; p < s->npsi; ++p)
+            if ((rc = dev_alloc(&s->psi_mid[p], std::max<size_t>(1, s->psi_elems[p]) * s->cs))) return fail(rc);
+        if ((rc = fused2_prepare(false))) return fail(rc);
+        if ((rc = build_worklist2(s))) return fail(rc);
+        if ((rc = encode_maps2(s))) return fail(rc);
     }
     if ((rc = zero_state(s))) return fail(rc);
     if (cudaStreamSynchronize(s->stream) != cudaSuccess) return fail(FD23_ERR_CUDA);
@@ -762,6 +912,9 @@ int fd23_set_receivers(fd23_solver *s, int field, const int *rx, const int *rz, 
         if (rx[i] < 0 || rx[i] >= s->d.nx || rz[i] < 0 || rz[i] >= s->d.nz) return FD23_ERR_ARG;
         off[i] = s->L.origin + (long long)rz[i] * s->L.pitch + rx[i];
     }
+    s->h_rx[field].assign(rx, rx + n);
+    s->h_rz[field].assign(rz, rz + n);
+    s->rec2_dirty = true;
     cudaFree(s->d_rec[field]);
     cudaFree(s->d_seis[field]);
     s->d_rec[field] = nullptr;
@@ -820,10 +973,23 @@ int fd23_run(fd23_solver *s, int nsteps, int itrecord)
         if (any_rec) s->nrec_steps += nrec_new;
         return FD23_OK;
     }
-    for (int k = 0; k < nsteps; ++k) {
+    const bool two = s->fused2 && !s->box_on && !s->d_punch && !s->d_midx;
+    if (two && any_rec && s->rec2_dirty) {
+        int rc = build_rec2(s);
+        if (rc) return rc;
+    }
+    for (int k = 0; k < nsteps;) {
         const int rec_now = any_rec && (s->it % itrecord == 0);
+        if (two && nsteps - k >= 2) {
+            const int rec_next = any_rec && ((s->it + 1) % itrecord == 0);
+            int rc = step2_impl(s, rec_now, rec_next);
+            if (rc) return rc;
+            k += 2;
+            continue;
+        }
         int rc = dispatch_step(s, rec_now);
         if (rc) return rc;
+        ++k;
     }
     return dispatch_flush(s);
 }

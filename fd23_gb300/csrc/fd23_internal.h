@@ -96,6 +96,15 @@ struct ShotMaps {
     TmaDesc idx;    // material-table indices (bytes), 2-D [row][column], box kIdxBoxW x 8
 };
 
+// Tensor maps of the two-step sweep (fd23_fused2.cu): the same 3-D views with
+// its wider boxes (input rows of 264 columns, point-wise rows of 256).
+struct ShotMaps2 {
+    TmaDesc uw[2];  // U W of buffer set 0 / 1, box 264 x 4 x 2
+    TmaDesc t[2];   // stresses of buffer set 0 / 1, box 256 x 4 x 3
+    TmaDesc ms;     // stress-update material, box (256 or 264) x 4 x 3
+    TmaDesc mv;     // velocity-update material, box (256 or 264) x 4 x 2
+};
+
 // Material table (mktable, PD/material/mktable.cpp): every cell's material
 // tuple (P-SV LAM MU MUA BU BW, SH MUX MUZ BV, storage values) as a one-byte
 // index into a table of at most kTabEntries tuples; entry 0 is the zero tuple
@@ -168,6 +177,16 @@ struct alignas(16) Shot {
     Punch punch;        // tile step windows (punch.win == nullptr: none)
     const unsigned char *midx;  // material-table indices, padded layout (nullptr: no table)
     const S *mtab;              // table [material array][kTabEntries], storage values
+    // two-step sweep only: its tensor maps, the memory variables of the
+    // step in between (written and read within one launch), and the
+    // receivers each work item records at that step: entries (field, ix, iz,
+    // receiver) sorted by iz, velocity entries of item k in
+    // [rec2_off[2k], rec2_off[2k+1]), stress entries up to rec2_off[2k+2]
+    const ShotMaps2 *maps2;
+    const void *mat16[5];  // FP16 copies of the material (null: the sweep reads `mat`)
+    C *psim[8];
+    const int4 *rec2;
+    const int *rec2_off;
     Box<C> box;         // hybrid box (box.on == 0: none); last, the batched sweep never reads it
 };
 

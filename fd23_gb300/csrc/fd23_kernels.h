@@ -96,6 +96,25 @@ int launch_step_fused_table_punch(const Shot<S, C> &s, const Shot<S, C> *shots, 
 int fused_prepare_table(int wave, int prec);
 int fused_prepare_table_punch(int wave, int prec);
 
+// Two-step fused sweep (fd23_fused2.cu; P-SV, FP32 wavefields): one launch
+// advances every cell two full time steps, it and it+1, reading buffer set
+// `par` and writing `1-par`; the memory variables of step it+1 go to
+// s.psim.  `rec_index` >= 0 gathers the receivers of the previous step from
+// buffer set `par` on the way (as the one-step sweep does); `rec_mid` >= 0
+// records step it (the step in between) into that record row.
+// half_material: the material is read from FP16 copies (s.maps2 views them).
+constexpr int kFused2TileX = 232;  // output columns per strip
+template <class M>
+int launch_step_fused2(const Shot<float, float> &s, const WorkItem *items, const int *item_off, int nblocks,
+                       int par, int it, int rec_index, int rec_mid, int *err_flag, cudaStream_t st);
+int fused2_prepare(bool half_material);        // once per device before the first launch
+size_t fused2_smem_bytes(bool half_material);  // dynamic shared memory of one CTA
+// copy shapes of the two-step sweep (for its tensor maps)
+struct Fused2Boxes {
+    int uww, pww, mww;
+};
+Fused2Boxes fused2_boxes(bool half_material);
+
 // one thread waits on an mbarrier nothing completes, with the sweep's bounded
 // wait: sets *err_flag when the wait gives up (about 2 s)
 int launch_wait_probe(int *err_flag, cudaStream_t st);

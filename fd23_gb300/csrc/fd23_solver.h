@@ -99,6 +99,22 @@ struct fd23_solver {
     long long punch_ver = 0;  // bumped when windows, sources or the tuning change
     int phase_next = 0;
     std::vector<int2> h_tcell;  // source-term cells (ix, iz)
+    // two-step sweep (FD23_KERNEL_FUSED2): its work plan and tensor maps, the
+    // memory variables of the step in between, the per-item receiver lists
+    // of that step (rebuilt when receivers change), host copies of the
+    // receiver positions
+    bool fused2 = false;
+    fd23::WorkItem *d_items2 = nullptr;
+    int *d_item_off2 = nullptr;
+    int nblocks2 = 0;
+    std::vector<fd23::WorkItem> h_items2;
+    std::vector<int> h_item_off2;
+    fd23::ShotMaps2 *d_maps2 = nullptr;
+    void *psi_mid[8] = {};
+    int4 *d_rec2 = nullptr;
+    int *d_rec2_off = nullptr;
+    bool rec2_dirty = true;
+    std::vector<int> h_rx[5], h_rz[5];
     bool box_on = false;
     int box_x0 = 0, box_z0 = 0, box_bx = 0, box_bz = 0, box_nsub = 0, box_nring = 0;
     void *box_r[5] = {};
@@ -177,6 +193,11 @@ Shot<S, C> make_shot(const fd23_solver *s)
     sh.punch = Punch{s->d_punch, s->punch_nbx, s->punch_nbz};
     sh.midx = s->d_midx;
     sh.mtab = (const S *)s->d_mtab;
+    sh.maps2 = s->d_maps2;
+    for (int m = 0; m < 5; ++m) sh.mat16[m] = nullptr;
+    for (int p = 0; p < 8; ++p) sh.psim[p] = (C *)s->psi_mid[p];
+    sh.rec2 = s->d_rec2;
+    sh.rec2_off = s->d_rec2_off;
     sh.box.on = s->box_on ? 1 : 0;
     if (s->box_on) {
         sh.box.x0 = s->box_x0;

@@ -75,8 +75,18 @@ enum fd23_prec { FD23_F32 = 0, FD23_F64 = 1, FD23_BF16 = 2, FD23_F16 = 3 };
  * costs more than the step's work) runs a whole fd23_run in one cooperative
  * launch of the two-pass updates, grid barriers between the phases; results
  * equal TWOPASS bit for bit.  A PERSIST solver with a box steps like TWOPASS;
- * batches take FUSED solvers only. */
-enum fd23_kernel { FD23_KERNEL_AUTO = 0, FD23_KERNEL_FUSED = 1, FD23_KERNEL_TWOPASS = 2, FD23_KERNEL_PERSIST = 3 };
+ * batches take FUSED solvers only.  FUSED2 (P-SV, F32 only; an addition)
+ * advances two time steps per launch of a fused sweep that reads and writes
+ * every wavefield once per two steps; results equal FUSED bit for bit.  An
+ * odd step, and runs with a box, tile windows or a material table, use the
+ * one-step sweep. */
+enum fd23_kernel {
+    FD23_KERNEL_AUTO = 0,
+    FD23_KERNEL_FUSED = 1,
+    FD23_KERNEL_TWOPASS = 2,
+    FD23_KERNEL_PERSIST = 3,
+    FD23_KERNEL_FUSED2 = 4
+};
 /* field ids (source terms, receivers, state) */
 enum fd23_psv_field { FD23_U = 0, FD23_W = 1, FD23_TXX = 2, FD23_TXZ = 3, FD23_TZZ = 4 };
 enum fd23_sh_field { FD23_V = 0, FD23_TX = 1, FD23_TZ = 2 };

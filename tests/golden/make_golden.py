@@ -11,6 +11,11 @@ lists, model files) and writes:
                         with its station list and .mdl text
   psv_fp32_restart.npz  PSV/clean_nobox/TEST/tt/state000000, state000001,
                         state000499, state000999 (FP32 96x96 restart states)
+  isis_headers.npz      the trace headers (bytes) of PSV/psv_clean_double/test/
+                        0_U.isis, 0_W.isis (36 x 136-byte FP64 headers) and of
+                        PSV/t/clean_nobox/TEST/output_U.isis (400 x 84-byte
+                        FP32 headers); the traces themselves are the
+                        seismograms above
 
 The parameters of each run are stored next to the data.  Two of them differ
 from the parfiles committed in the reference and were recovered from the data
@@ -44,6 +49,15 @@ def main(ref):
                              strike=0.0, dip=20.0, rake=90.0, azimuth=45.0, alpha=-5, stype=3,
                              npml=32, pml_r=1e-11, pml_dt=0.005, pml_v=30.0, pml_fc=2.0,
                              topabsorb=0, itrecord=1))))
+    hdr = {}
+    for c in ("U", "W"):
+        raw = open(os.path.join(pd, "0_%s.isis" % c), "rb").read()
+        step = 136 + 8 * 2001
+        hdr["fp64_" + c] = np.frombuffer(raw, dtype=np.uint8).reshape(36, step)[:, :136].copy()
+    raw = open(os.path.join(ref, "PSV", "t", "clean_nobox", "TEST", "output_U.isis"), "rb").read()
+    step = 84 + 4 * 2000
+    hdr["fp32_U"] = np.frombuffer(raw, dtype=np.uint8).reshape(400, step)[:, :84].copy()
+    np.savez_compressed(os.path.join(HERE, "isis_headers.npz"), **hdr)
     tt = os.path.join(ref, "PSV", "clean_nobox", "TEST", "tt")
     states = {}
     for i in (0, 1, 499, 999):
