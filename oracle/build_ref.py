@@ -1,6 +1,17 @@
 """Build recipe for the reference programs used as checkers -- TEST
 INFRASTRUCTURE ONLY.
 
+Two kinds of checker are built, both from the reference's own sources:
+
+* ``oracle/_ref/ntde_line``, the box-source generator (below);
+* ``oracle/_ref/ref_setup_pn``, ``ref_setup_sh``, ``ref_setup_pd``: the
+  harness ``oracle/ref_setup_harness.cpp`` linked with the host set-up code
+  of the FP32 P-SV program (``PSV/clean_nobox``: material, cpml, model), the
+  SH program (``SH``: the same plus ``fd/fd.cpp``'s host step) and the FP64
+  P-SV program (``PSV/psv_clean_double``: the same plus ``box/box.cpp``,
+  ``field/field.cpp`` and ``fd/fd.cpp``'s residual updates).  Only
+  ``tests/golden/make_ref_pins.py`` runs them.
+
 Compiles the reference's box-source generator ``ntde_line`` from its own
 sources where they lie (``PSV/psv_clean_double/source/source_line.cpp``,
 ``source/waveform.cpp``, ``param/param.cpp`` and ``getpar/getpar.cpp``, the
@@ -41,7 +52,41 @@ def sources():
     }
 
 
+# harness programs: name -> (program root, -D macro, program sources)
+HARNESS = {
+    "ref_setup_pn": (os.path.join("PSV", "clean_nobox"), "REF_PN",
+                     ["material/material.cpp", "cpml/cpml.cpp", "model/model.cpp", "model/util.cpp"]),
+    "ref_setup_sh": ("SH", "REF_SH",
+                     ["material/material.cpp", "cpml/cpml.cpp", "model/model.cpp", "model/util.cpp",
+                      "fd/fd.cpp"]),
+    "ref_setup_pd": (os.path.join("PSV", "psv_clean_double"), "REF_PD",
+                     ["material/material.cpp", "cpml/cpml.cpp", "model/model.cpp", "model/util.cpp",
+                      "fd/fd.cpp", "box/box.cpp", "field/field.cpp"]),
+}
+
+
+def build_harness(force=False):
+    """The three set-up harnesses; {name: path}, or None without the
+    reference sources."""
+    harness = os.path.join(HERE, "ref_setup_harness.cpp")
+    out = {}
+    for name, (sub, macro, files) in HARNESS.items():
+        root = os.path.join(REF_ROOT, sub)
+        srcs = [os.path.join(root, f) for f in files]
+        if not all(os.path.exists(p) for p in srcs):
+            return None
+        os.makedirs(OUT_DIR, exist_ok=True)
+        exe = os.path.join(OUT_DIR, name)
+        if force or not os.path.exists(exe) or any(
+                os.path.getmtime(p) > os.path.getmtime(exe) for p in srcs + [harness]):
+            subprocess.check_call(["g++", "-std=c++11", "-O2", "-w", "-ffp-contract=off", "-D" + macro,
+                                   "-I" + root, "-o", exe, harness] + srcs + ["-lm"])
+        out[name] = exe
+    return out
+
+
 def build(force=False):
+    build_harness(force)
     src = sources()
     if not all(os.path.exists(p) for p in src.values()):
         return None

@@ -614,6 +614,25 @@ static inline int or_punch_skip(int nx, int ix, int iz, int it)
 #undef FMA
 #undef SFX
 
+/* FP32 with every multiply-add rounded twice (a product, then a sum): what a
+ * build without multiply-add contraction computes, e.g. the reference's FP32
+ * program built for device debugging (nvcc -G; PSV/clean_nobox/Makefile).
+ * Used to test whether the reference's FP32 restart states
+ * (PSV/clean_nobox/TEST/tt) came from such a build; -ffp-contract=off keeps
+ * the two roundings. */
+static inline float or_mul_add_f(float a, float b, float c)
+{
+    const float p = a * b;
+    return p + c;
+}
+#define REAL float
+#define FMA or_mul_add_f
+#define SFX f32nf
+#include "fd23_oracle_step.inc"
+#undef REAL
+#undef FMA
+#undef SFX
+
 /* ------------------------------------------------------------------------- */
 /* Box-source generator (FP64): the ntde_line program,                        */
 /* PD/source/source_line.cpp:307-410 (main), :196-305                         */

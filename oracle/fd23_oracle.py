@@ -40,10 +40,10 @@ def lib():
         _lib.or_sh_source_terms.argtypes = [i, i, i, i, vp, d, d, vp, i, i, vp, vp, vp]
         _lib.or_mdl_raster.argtypes = [i, i, d, i, vp, vp, vp, vp, vp, vp, vp, vp, vp]
         _lib.or_mdl_raster.restype = None
-        for nm in ("or_psv_run_f64", "or_psv_run_f32"):
+        for nm in ("or_psv_run_f64", "or_psv_run_f32", "or_psv_run_f32nf"):
             getattr(_lib, nm).argtypes = [i, i, i, i, vp, vp, i, vp, vp, vp, i, i, vp, i, vp,
                                           i, i, i, vp, vp, vp, i]
-        for nm in ("or_sh_run_f64", "or_sh_run_f32"):
+        for nm in ("or_sh_run_f64", "or_sh_run_f32", "or_sh_run_f32nf"):
             getattr(_lib, nm).argtypes = [i, i, i, i, vp, vp, i, vp, vp, vp, i, i, vp,
                                           i, i, i, vp, vp, i]
         _lib.or_set_punch.argtypes = [vp, vp, i]
@@ -52,6 +52,7 @@ def lib():
         _lib.or_box_rings.argtypes = [i, i, i, i, i, vp, vp, vp, vp]
         _lib.or_box_incident_from_displacement.argtypes = [i, i, d, vp, vp, vp, vp, vp, vp]
         _lib.or_box_material.argtypes = [i, i, vp, i, i, i, i, d, d, d, d, d, vp]
+        _lib.or_box_residual_step_f64.argtypes = [i, i, vp, vp]
         for nm in ("or_psv_box_run_f64", "or_psv_box_run_f32"):
             getattr(_lib, nm).argtypes = [i, i, i, i, vp, vp, i, vp, vp, vp, i, i, vp, vp,
                                           i, i, i, vp, vp, i, i, i, i, vp, vp, vp, i]
@@ -292,13 +293,14 @@ class _Punch:
 
 def psv_run(prec, nx, nz, npml, topabsorb, mat, bck, terms, rec_u, rec_w, nt, itrecord=1, it0=0,
             state=None, nthreads=0, punch=None):
-    """Run nt steps of the P-SV oracle.  prec 'f64' or 'f32'.  mat (5,nz,nx)
+    """Run nt steps of the P-SV oracle.  prec 'f64', 'f32' or 'f32nf' (FP32
+    with every multiply-add rounded twice, no fused multiply-add).  mat (5,nz,nx)
     and bck (3, 4nx+4nz) FP64 arrays are rounded to prec.  terms = (field,
     idx, amp[nterms, nt_amp]) with absolute step indexing.  rec_* = flat
     indices.  punch = tile step windows (first, last), [nbz*nbx] each, or
     None.  Returns (seis_u, seis_w, state)."""
     dt_ = np.float64 if prec == "f64" else np.float32
-    fn = lib().or_psv_run_f64 if prec == "f64" else lib().or_psv_run_f32
+    fn = getattr(lib(), "or_psv_run_" + prec)
     mat_r = np.ascontiguousarray(mat, dtype=dt_)
     bck_r = np.ascontiguousarray(bck, dtype=dt_)
     field, idx, amp = terms
@@ -325,7 +327,7 @@ def psv_run(prec, nx, nz, npml, topabsorb, mat, bck, terms, rec_u, rec_w, nt, it
 def sh_run(prec, nx, nz, npml, topabsorb, mat, bck, terms, rec, nt, itrecord=1, it0=0, state=None,
            nthreads=0, punch=None):
     dt_ = np.float64 if prec == "f64" else np.float32
-    fn = lib().or_sh_run_f64 if prec == "f64" else lib().or_sh_run_f32
+    fn = getattr(lib(), "or_sh_run_" + prec)
     mat_r = np.ascontiguousarray(mat, dtype=dt_)
     bck_r = np.ascontiguousarray(bck, dtype=dt_)
     field, idx, amp = terms
@@ -484,6 +486,18 @@ def psv_box_run(prec, nx, nz, npml, topabsorb, mat, bck, terms, rec_field, rec_i
     if rc < 0:
         raise ValueError("bad box")
     return seis, state, rstate
+
+
+def box_residual_step(rmat, r):
+    """One residual step (stress then velocity) of a box residual field
+    r = [U W Txx Txz Tzz] of shape (5, bz, bx) in the box material rmat
+    (5, bz, bx), FP64: the update the box run applies between its ring
+    exchanges (PD/fd/fd.cpp:63-91, 208-234).  Returns the new field."""
+    rm = np.ascontiguousarray(rmat, dtype=np.float64)
+    out = np.ascontiguousarray(r, dtype=np.float64).copy()
+    bz, bx = out.shape[1], out.shape[2]
+    lib().or_box_residual_step_f64(bx, bz, _p(rm), _p(out))
+    return out
 
 
 def psv_ring_history(prec, nx, nz, npml, topabsorb, mat, bck, terms, nt, box, it0=0, state=None):
