@@ -166,8 +166,8 @@ int step2_impl(fd23_solver *s, int rec_now, int rec_next)
     sh.cta0 = 0;
     sh.ncta = s->nblocks2;
     const int rec_mid = rec_now ? s->nrec_steps++ : -1;
-    const int rc = launch_step_fused2<float>(sh, s->d_items2, s->d_item_off2, s->nblocks2, s->par, s->it,
-                                             s->pending_rec, rec_mid, s->err_flag, s->stream);
+    const int rc = launch_step_fused2<float>(sh, s->f2_width, s->d_items2, s->d_item_off2, s->nblocks2, s->par,
+                                             s->it, s->pending_rec, rec_mid, s->err_flag, s->stream);
     if (rc) return rc;
     s->pending_rec = -1;
     s->par = 1 - s->par;
@@ -296,7 +296,7 @@ int encode_maps2(fd23_solver *s)
 {
     PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
     if (!encode) return FD23_ERR_CUDA;
-    const Fused2Boxes bx = fused2_boxes(false);
+    const Fused2Boxes bx = fused2_boxes(false, s->f2_width);
     const Layout &L = s->L;
     auto make = [&](TmaDesc &m, void *base, int nfields, int w, int nf, size_t es,
                     CUtensorMapDataType dt) -> int {
@@ -309,8 +309,9 @@ int encode_maps2(fd23_solver *s)
                                   CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         return r == CUDA_SUCCESS ? FD23_OK : FD23_ERR_CUDA;
     };
-    // U W rows of bx.uww (> 256) columns: a 4-D view [field][row][column / 8][8]
-    // whose box {8, uww / 8, 4, 2} lands as [2][4][uww] in shared memory
+    // U, W rows of bx.uww columns (more than a box dimension's 256 for the
+    // wide strips): a 4-D view [field][row][column / 8][8] whose box
+    // {8, uww / 8, 4, 1} lands as [4][uww] in shared memory
     auto make_groups = [&](TmaDesc &m, void *base, int nfields, int w, int nf) -> int {
         const cuuint64_t dims[4] = {8u, (cuuint64_t)L.pitch / 8, (cuuint64_t)L.rows, (cuuint64_t)nfields};
         const cuuint64_t strides[3] = {32u, (cuuint64_t)L.pitch * 4, (cuuint64_t)L.elems() * 4};
@@ -325,7 +326,7 @@ int encode_maps2(fd23_solver *s)
     ShotMaps2 h{};
     int rc = FD23_OK;
     for (int b = 0; b < 2 && !rc; ++b) {
-        rc = make_groups(h.uw[b], s->fld_block[b], s->nfld, bx.uww, 2);
+        rc = make_groups(h.uw[b], s->fld_block[b], s->nfld, bx.uww, 1);
         if (!rc) rc = make(h.t[b], s->fld_block[b], s->nfld, bx.pww, 3, 4, CU_TENSOR_MAP_DATA_TYPE_FLOAT32);
     }
     if (!rc) rc = make(h.ms, s->mat_block, s->nmat, bx.mww, 3, 4, CU_TENSOR_MAP_DATA_TYPE_FLOAT32);
@@ -439,10 +440,10 @@ int build_worklist2(fd23_solver *s)
     int sms = 0;
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->d.device));
     TuneParams tp = s->tune;
-    tp.per_sm = 1;
+    tp.per_sm = fused2_per_sm(s->f2_width);
     WorkPlan plan;
     const std::vector<ShotGeom> geo{ShotGeom{s->d.nx, s->d.nz, s->d.npml, s->d.topabsorb}};
-    int rc = plan_work(geo, kFused2TileX, sms, tp, plan);
+    int rc = plan_work(geo, fused2_tile_x(s->f2_width), sms, tp, plan);
     if (rc) return rc;
     cudaFree(s->d_items2);
     cudaFree(s->d_item_off2);
@@ -457,11 +458,12 @@ int build_worklist2(fd23_solver *s)
 }
 
 // Receivers of every work item of the two-step plan (the cells it owns:
-// columns [x0, x0+kFused2TileX), rows [z0, z1)), velocity fields first, then
+// columns [x0, x0+fused2_tile_x), rows [z0, z1)), velocity fields first, then
 // stresses, each sorted by row: entries (field, ix, iz, receiver).
 int build_rec2(fd23_solver *s)
 {
     const int ni = (int)s->h_items2.size();
+    const int tx = fused2_tile_x(s->f2_width);
     std::vector<int4> list;
     std::vector<int> off;
     off.reserve(2 * (size_t)ni + 1);
@@ -473,7 +475,7 @@ int build_rec2(fd23_solver *s)
             for (int c = part == 0 ? 0 : 2; c < (part == 0 ? 2 : s->nfld); ++c)
                 for (int r = 0; r < s->nrec[c] && r < (int)s->h_rx[c].size(); ++r) {
                     const int ix = s->h_rx[c][r], iz = s->h_rz[c][r];
-                    if (ix >= w.x0 && ix < w.x0 + kFused2TileX && iz >= w.z0 && iz < w.z1)
+                    if (ix >= w.x0 && ix < w.x0 + tx && iz >= w.z0 && iz < w.z1)
                         list.push_back(make_int4(c, ix, iz, r));
                 }
             std::stable_sort(list.begin() + first, list.end(),
@@ -764,7 +766,9 @@ int fd23_create(const fd23_desc *desc, fd23_solver **out)
     if (s->fused2) {
         for (int p = 0; p < s->npsi; ++p)
             if ((rc = dev_alloc(&s->psi_mid[p], std::max<size_t>(1, s->psi_elems[p]) * s->cs))) return fail(rc);
-        if ((rc = fused2_prepare(false))) return fail(rc);
+        s->f2_width = 256;
+        if (const char *v = getenv("FD23_FUSED2_WIDTH")) s->f2_width = atoi(v) == 128 ? 128 : 256;
+        if ((rc = fused2_prepare(false, s->f2_width))) return fail(rc);
         if ((rc = build_worklist2(s))) return fail(rc);
         if ((rc = encode_maps2(s))) return fail(rc);
     }

@@ -63,21 +63,25 @@ __device__ __forceinline__ void tma_load_4d(void *dst, const void *map, int c0, 
         : "memory");
 }
 
-template <class M>
+template <class M, int W>
 struct Cfg2 {
-    static constexpr int NCW = 8;              // compute warps: 4 rows x 2 column halves
+    static constexpr int NCWX = W / 128;       // compute warps per row
+    static constexpr int NCW = 4 * NCWX;       // compute warps: 4 rows x NCWX column parts
     static constexpr int NCT = 32 * NCW;       // compute threads
     static constexpr int NTH = NCT + 32;       // + one producer warp
-    static constexpr int W1 = 256;             // columns of S1 = ring row width
+    static constexpr int NTR = W / 4;          // column groups (threads) per row
+    static constexpr int MINB = 256 / W;       // CTAs per SM the registers are budgeted for
+    static constexpr int W1 = W;               // columns of S1 = ring row width
     static constexpr int TX = W1 - 24;         // output columns per strip
-    static constexpr int UWW = W1 + 8;         // input rows: columns x0-16 .. x0+247
+    static constexpr int UWW = W1 + 8;         // input rows: columns x0-16 .. x0+W1-9
     static constexpr int MOFF = sizeof(M) == 2 ? 4 : 0;  // 16-byte aligned copy starts
     static constexpr int MWW = W1 + 2 * MOFF;  // material rows
     static constexpr int NUW = 4, NPW = 2, NR = 3;
     static constexpr int MAX_ITEMS = 4, MAX_TERMS = 16;
     static constexpr int al128(int b) { return (b + 127) / 128 * 128; }
-    static constexpr int UW_SLOT = 2 * 4 * UWW;  // floats: [U W][4 rows][UWW]
-    static constexpr int UWF = 4 * UWW;          // W's offset in a slot
+    // U and W inputs in two rings of 4 * NUW rows (a power of two) with a
+    // uniform row stride, so a row's address is one mask and one multiply
+    static constexpr int UW_RING = 4 * NUW * UWW;  // floats per input ring
     static constexpr int TOLD_B = 3 * 4 * W1 * 4;                   // [Txx Txz Tzz][4 rows][W1] floats
     static constexpr int MS_B = al128(3 * 4 * MWW * (int)sizeof(M));  // [LAM MU MUA][4][MWW]
     static constexpr int MV_B = al128(2 * 4 * MWW * (int)sizeof(M));  // [BU BW][4][MWW]
@@ -85,7 +89,7 @@ struct Cfg2 {
     static constexpr int TR_ROW = 3 * W1;  // floats per stress-ring row: [Txx Txz Tzz][W1]
     static constexpr int VR_ROW = 2 * W1;  // velocity-ring row: [U W][W1]
     static constexpr int OFF_UW = 0;
-    static constexpr int OFF_PW = OFF_UW + NUW * UW_SLOT * 4;
+    static constexpr int OFF_PW = OFF_UW + 2 * UW_RING * 4;
     static constexpr int OFF_TR = OFF_PW + NPW * STAGE_B;
     static constexpr int OFF_VR = OFF_TR + NR * 4 * TR_ROW * 4;
     static constexpr int OFF_T2 = OFF_VR + NR * 4 * VR_ROW * 4;
@@ -93,12 +97,21 @@ struct Cfg2 {
     static constexpr int OFF_INFO = OFF_BAR + 128;
     static constexpr int OFF_TL = OFF_INFO + MAX_ITEMS * 16;
     static constexpr size_t SMEM = (size_t)OFF_TL + MAX_ITEMS * MAX_TERMS * 16;
-    static constexpr uint32_t UW_TX = (uint32_t)(UW_SLOT * 4);
+    static constexpr uint32_t UW_TX = (uint32_t)(2 * 4 * UWW * 4);
     static constexpr uint32_t PW_TX = (uint32_t)(TOLD_B + 5 * 4 * MWW * sizeof(M));
+    static_assert(W == 128 || W == 256, "strip widths");
+    static_assert((4 * UWW * 4) % 128 == 0, "input slots land 128-byte aligned");
     static_assert(OFF_PW % 128 == 0 && STAGE_B % 128 == 0 && OFF_TR % 128 == 0, "copy destinations");
     static_assert(2 * (NUW + NPW) * 8 <= 128, "barrier space");
     static_assert(UWW % 8 == 0 && (kXPad - 16) % 8 == 0 && TX % 8 == 0, "input copies start on 8-column groups");
 };
+
+// ring row (rb + d) of a ring of 12 rows, rb in [0, 12): no division
+__device__ __forceinline__ int ring12(int rb, int d)
+{
+    const int r = rb + d;
+    return r >= 12 ? r - 12 : r;
+}
 
 // P-SV stress update of cells x .. x+3 of row j (PD/fd/cu_fd.cu:209-358).
 // ur[d]: U at row j-4+d (d = 0..8) at this thread's first cell; W at
@@ -512,12 +525,12 @@ __device__ __forceinline__ void add_terms(const Shot<float, float> &sh, const in
     }
 }
 
-template <class M>
-__global__ void __launch_bounds__(Cfg2<M>::NTH, 1)
+template <class M, int W>
+__global__ void __launch_bounds__(Cfg2<M, W>::NTH, Cfg2<M, W>::MINB)
     fused2_step(const __grid_constant__ Shot<float, float> sh, const WorkItem *__restrict__ items,
                 const int *__restrict__ item_off, int par, int it, int rec_index, int rec_mid, int *err_flag)
 {
-    using K = Cfg2<M>;
+    using K = Cfg2<M, W>;
     using C = float;
     constexpr int W1 = K::W1;
     if (err_flag && *(volatile int *)err_flag) return;
@@ -526,7 +539,7 @@ __global__ void __launch_bounds__(Cfg2<M>::NTH, 1)
         if (threadIdx.x == 0 && err_flag) atomicExch(err_flag, 2);
         return;
     }
-    float *uw_s = reinterpret_cast<float *>(smem_raw + K::OFF_UW);
+    float *uw_s = reinterpret_cast<float *>(smem_raw + K::OFF_UW);  // U ring, then W ring
     unsigned char *pw_b = smem_raw + K::OFF_PW;
     float *tr_s = reinterpret_cast<float *>(smem_raw + K::OFF_TR);
     float *vr_s = reinterpret_cast<float *>(smem_raw + K::OFF_VR);
@@ -542,7 +555,7 @@ __global__ void __launch_bounds__(Cfg2<M>::NTH, 1)
     const int ibeg = item_off[blockIdx.x], iend = item_off[blockIdx.x + 1];
     const int nitems = min(iend - ibeg, K::MAX_ITEMS);
     const int nx = sh.nx, nz = sh.nz, pitch = sh.pitch;
-    const long long origin = sh.origin;
+    const int origin = (int)sh.origin;  // padded arrays hold fewer than 2^31 elements
 
     // ---- per-item set-up: geometry and the source terms inside its S1 region ----
     if (tid < nitems) {
@@ -580,7 +593,8 @@ __global__ void __launch_bounds__(Cfg2<M>::NTH, 1)
     // ======================= producer warp =======================
     if (warp == K::NCW) {
         const ShotMaps2 *maps = sh.maps2;
-        // input block e -> item k, block b (rows z0-16+4b .. +3)
+        // input block e -> item k, block b (rows z0-16+4b .. +3), into rows
+        // 4*(e % NUW) .. +3 of the U ring and of the W ring
         auto issue_uw = [=](int e) {
             int k = 0, base = 0;
             while (k < nitems - 1 && e >= base + info[k].niter + 2) {
@@ -591,10 +605,12 @@ __global__ void __launch_bounds__(Cfg2<M>::NTH, 1)
             const int slot = e % K::NUW;
             const int r0 = I.z0 - 16 + 4 * (e - base);
             if (lane == 0) {
-                // rows of 264 columns (a box dimension holds at most 256): the map
-                // views the columns as [column / 8][8], the copy starts on a group
+                // rows wider than a box dimension's 256 elements: the map views
+                // the columns as [column / 8][8], the copy starts on a group
                 mbar_arrive_expect_tx(&full_uw[slot], K::UW_TX);
-                tma_load_4d(uw_s + slot * K::UW_SLOT, &maps->uw[par], 0, (kXPad + I.x0 - 16) / 8, kZPad + r0, 0,
+                const int gx = (kXPad + I.x0 - 16) / 8;
+                tma_load_4d(uw_s + slot * 4 * K::UWW, &maps->uw[par], 0, gx, kZPad + r0, FD23_U, &full_uw[slot]);
+                tma_load_4d(uw_s + K::UW_RING + slot * 4 * K::UWW, &maps->uw[par], 0, gx, kZPad + r0, FD23_W,
                             &full_uw[slot]);
             }
         };
@@ -671,8 +687,14 @@ __global__ void __launch_bounds__(Cfg2<M>::NTH, 1)
     }
 
     const int g = warp & 3;                   // row of the 4-row block
-    const int t = 32 * (warp >> 2) + lane;    // column group 0..63
-    const bool v1_t = t >= 1 && t <= 62, s2_t = t >= 2 && t <= 61, v2_t = t >= 3 && t <= 60;
+    const int t = 32 * (warp >> 2) + lane;    // column group 0 .. NTR-1
+    constexpr int NTR = K::NTR;
+    const bool v1_t = t >= 1 && t <= NTR - 2, s2_t = t >= 2 && t <= NTR - 3, v2_t = t >= 3 && t <= NTR - 4;
+    // this thread's column in the input rings and in the 12-row rings
+    const float *const u_col = uw_s + 4 + 4 * t;
+    float *const tr_col = tr_s + 4 * t;
+    float *const vr_col = vr_s + 4 * t;
+    float *const t2_col = t2_s + 4 * t;
     float *const *psi_rd = sh.psi[par];
     float *const *psi_wr = sh.psi[1 - par];
     float *const *psi_mid = sh.psim;
@@ -703,12 +725,17 @@ __global__ void __launch_bounds__(Cfg2<M>::NTH, 1)
             ce = __ldg(sh.rec2_off + 2 * kk + 2);
         }
         const int cs0 = cs;  // end of the velocity entries
-        for (int i = 0; i < I.niter; ++i, ++gflat) {
+        // 12-row ring rows (block b, row r) = (4b + r) mod 12: rb = row of
+        // (block i-2, row g), wb = row of (block i, row g); advanced by 4 per
+        // iteration
+        int rb = (12 - 8 + g) % 12, wb = g;
+        for (int i = 0; i < I.niter; ++i, ++gflat, rb = ring12(rb, 4), wb = ring12(wb, 4)) {
             for (; ok && uw_ready <= uw_base + i + 2; ++uw_ready)
                 ok = mbar_wait_bounded(&full_uw[uw_ready % K::NUW], (uint32_t)((uw_ready / K::NUW) & 1), err_flag);
             if (ok) ok = mbar_wait_bounded(&full_pw[gflat % K::NPW], (uint32_t)((gflat / K::NPW) & 1), err_flag);
             const unsigned char *stg = pw_b + (gflat % K::NPW) * K::STAGE_B;
             const float *told_s = reinterpret_cast<const float *>(stg);
+            const int ub = (4 * (uw_base + i) + g) & (4 * K::NUW - 1);  // input ring row of (block i, row g)
             const M *ms_s = reinterpret_cast<const M *>(stg + K::TOLD_B);
             const M *mv_s = reinterpret_cast<const M *>(stg + K::TOLD_B + K::MS_B);
             const int j1 = I.z0 - 12 + 4 * i + g, a1 = j1 - 4, j2 = j1 - 8, a2 = j1 - 12;
@@ -719,12 +746,12 @@ __global__ void __launch_bounds__(Cfg2<M>::NTH, 1)
 #pragma unroll
             for (int e = 0; e < 4; ++e) ms2[0][e] = ms2[1][e] = ms2[2][e] = mv2[0][e] = mv2[1][e] = 0.f;
             if (s2_on && s2_t && xin && j2 >= 0 && j2 < nz) {
-                const long long o = origin + (long long)j2 * pitch + x;
+                const int o = origin + j2 * pitch + x;
 #pragma unroll
                 for (int m = 0; m < 3; ++m) ldg_mat4<M>(gmat[m] + o, ms2[m]);
             }
             if (v2_on && v2_t && xin && a2 >= 0 && a2 < nz) {
-                const long long o = origin + (long long)a2 * pitch + x;
+                const int o = origin + a2 * pitch + x;
 #pragma unroll
                 for (int m = 0; m < 2; ++m) ldg_mat4<M>(gmat[3 + m] + o, mv2[m]);
             }
@@ -733,10 +760,7 @@ __global__ void __launch_bounds__(Cfg2<M>::NTH, 1)
             {
                 const float *ur[9];
 #pragma unroll
-                for (int d = 0; d < 9; ++d) {
-                    const int q = g + d;
-                    ur[d] = uw_s + ((uw_base + i + (q >> 2)) & (K::NUW - 1)) * K::UW_SLOT + (q & 3) * K::UWW + 4 + 4 * t;
-                }
+                for (int d = 0; d < 9; ++d) ur[d] = u_col + ((ub + d) & (4 * K::NUW - 1)) * K::UWW;
                 float tnew[3][4];
                 if (j1 < 0 || j1 >= nz || !xin) {
 #pragma unroll
@@ -749,7 +773,7 @@ __global__ void __launch_bounds__(Cfg2<M>::NTH, 1)
                     for (int f = 0; f < 3; ++f) Vec4<float, float>::ld(told_s + (f * 4 + g) * W1 + 4 * t, told[f]);
 #pragma unroll
                     for (int m = 0; m < 3; ++m) ld_mat4<M>(ms_s + (m * 4 + g) * K::MWW + K::MOFF + 4 * t, ms[m]);
-                    stress4<K::UWF>(sh, psi_rd, psi_mid, j1, x, xfast, ur, told, ms, [](int) { return true; }, tnew);
+                    stress4<K::UW_RING>(sh, psi_rd, psi_mid, j1, x, xfast, ur, told, ms, [](int) { return true; }, tnew);
                     add_terms(sh, tl, ntl, j1, x, it, tnew);
                     // stress receivers of step it
                     if (cs < ce && j1 >= I.z0 && j1 < I.z1) {
@@ -769,7 +793,7 @@ __global__ void __launch_bounds__(Cfg2<M>::NTH, 1)
                         }
                     }
                 }
-                float *dst = tr_s + ((i % 3) * 4 + g) * K::TR_ROW + 4 * t;
+                float *dst = tr_col + wb * K::TR_ROW;
 #pragma unroll
                 for (int f = 0; f < 3; ++f) Vec4<float, float>::st(dst + f * W1, tnew[f]);
             }
@@ -785,14 +809,11 @@ __global__ void __launch_bounds__(Cfg2<M>::NTH, 1)
                 } else {
                     const float *tr[9];
 #pragma unroll
-                    for (int d = 0; d < 9; ++d) {
-                        const int q = g + d;
-                        tr[d] = tr_s + (((i - 2 + (q >> 2)) % 3) * 4 + (q & 3)) * K::TR_ROW + 4 * t;
-                    }
-                    const float *vo = uw_s + ((uw_base + i) & (K::NUW - 1)) * K::UW_SLOT + g * K::UWW + 4 + 4 * t;
+                    for (int d = 0; d < 9; ++d) tr[d] = tr_col + ring12(rb, d) * K::TR_ROW;
+                    const float *vo = u_col + ub * K::UWW;
                     float vold[2][4], mv[2][4];
                     Vec4<float, float>::ld(vo, vold[0]);
-                    Vec4<float, float>::ld(vo + K::UWF, vold[1]);
+                    Vec4<float, float>::ld(vo + K::UW_RING, vold[1]);
 #pragma unroll
                     for (int m = 0; m < 2; ++m) ld_mat4<M>(mv_s + (m * 4 + g) * K::MWW + K::MOFF + 4 * t, mv[m]);
                     velocity4<W1>(sh, psi_rd, psi_mid, a1, x, xfast, tr, vold, mv, [](int) { return true; }, vnew);
@@ -812,7 +833,7 @@ __global__ void __launch_bounds__(Cfg2<M>::NTH, 1)
                         }
                     }
                 }
-                float *dst = vr_s + ((i % 3) * 4 + g) * K::VR_ROW + 4 * t;
+                float *dst = vr_col + wb * K::VR_ROW;
                 Vec4<float, float>::st(dst, vnew[0]);
                 Vec4<float, float>::st(dst + W1, vnew[1]);
             }
@@ -840,11 +861,8 @@ __global__ void __launch_bounds__(Cfg2<M>::NTH, 1)
                 } else {
                     const float *vr[9];
 #pragma unroll
-                    for (int d = 0; d < 9; ++d) {
-                        const int q = g + d;
-                        vr[d] = vr_s + (((i - 2 + (q >> 2)) % 3) * 4 + (q & 3)) * K::VR_ROW + 4 * t;
-                    }
-                    const float *to = tr_s + (((i - 2) % 3) * 4 + g) * K::TR_ROW + 4 * t;
+                    for (int d = 0; d < 9; ++d) vr[d] = vr_col + ring12(rb, d) * K::VR_ROW;
+                    const float *to = tr_col + rb * K::TR_ROW;
                     float told[3][4];
 #pragma unroll
                     for (int f = 0; f < 3; ++f) Vec4<float, float>::ld(to + f * W1, told[f]);
@@ -853,7 +871,7 @@ __global__ void __launch_bounds__(Cfg2<M>::NTH, 1)
                                 [=](int ix) { return orow && ix >= ox0 && ix < ox1; }, tnew);
                     add_terms(sh, tl, ntl, j2, x, it + 1, tnew);
                     if (orow && v2_t) {
-                        const long long o = origin + (long long)j2 * pitch + x;
+                        const int o = origin + j2 * pitch + x;
                         if (x + 3 < nx) {
 #pragma unroll
                             for (int f = 0; f < 3; ++f) Vec4<float, float>::st(wr[FD23_TXX + f] + o, tnew[f]);
@@ -866,7 +884,7 @@ __global__ void __launch_bounds__(Cfg2<M>::NTH, 1)
                         }
                     }
                 }
-                float *dst = t2_s + ((i % 3) * 4 + g) * K::TR_ROW + 4 * t;
+                float *dst = t2_col + wb * K::TR_ROW;
 #pragma unroll
                 for (int f = 0; f < 3; ++f) Vec4<float, float>::st(dst + f * W1, tnew[f]);
             }
@@ -877,17 +895,14 @@ __global__ void __launch_bounds__(Cfg2<M>::NTH, 1)
             if (v2_on && v2_t && a2 >= I.z0 && a2 < I.z1 && a2 < nz && x < nx) {
                 const float *tr[9];
 #pragma unroll
-                for (int d = 0; d < 9; ++d) {
-                    const int q = g + d;
-                    tr[d] = t2_s + (((i - 2 + (q >> 2)) % 3) * 4 + (q & 3)) * K::TR_ROW + 4 * t;
-                }
-                const float *vo = vr_s + (((i - 2) % 3) * 4 + g) * K::VR_ROW + 4 * t;
+                for (int d = 0; d < 9; ++d) tr[d] = t2_col + ring12(rb, d) * K::TR_ROW;
+                const float *vo = vr_col + rb * K::VR_ROW;
                 float vold[2][4], vnew[2][4];
                 Vec4<float, float>::ld(vo, vold[0]);
                 Vec4<float, float>::ld(vo + W1, vold[1]);
                 velocity4<W1>(sh, psi_mid, psi_wr, a2, x, xfast, tr, vold, mv2,
                               [=](int ix) { return ix >= ox0 && ix < ox1; }, vnew);
-                const long long o = origin + (long long)a2 * pitch + x;
+                const int o = origin + a2 * pitch + x;
                 if (x + 3 < nx) {
                     Vec4<float, float>::st(wr[FD23_U] + o, vnew[0]);
                     Vec4<float, float>::st(wr[FD23_W] + o, vnew[1]);
@@ -905,24 +920,21 @@ __global__ void __launch_bounds__(Cfg2<M>::NTH, 1)
     }
 }
 
-template <class M>
+template <class M, int W>
 int prepare2()
 {
-    using K = Cfg2<M>;
-    return cudaFuncSetAttribute(fused2_step<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)K::SMEM) ==
+    using K = Cfg2<M, W>;
+    return cudaFuncSetAttribute(fused2_step<M, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)K::SMEM) ==
                    cudaSuccess
                ? FD23_OK
                : FD23_ERR_CUDA;
 }
 
-}  // namespace
-
-template <class M>
-int launch_step_fused2(const Shot<float, float> &s, const WorkItem *items, const int *item_off, int nblocks, int par,
-                       int it, int rec_index, int rec_mid, int *err_flag, cudaStream_t st)
+template <class M, int W>
+int launch2(const Shot<float, float> &s, const WorkItem *items, const int *item_off, int nblocks, int par, int it,
+            int rec_index, int rec_mid, int *err_flag, cudaStream_t st)
 {
-    using K = Cfg2<M>;
-    static_assert(K::TX == kFused2TileX, "strip width");
+    using K = Cfg2<M, W>;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)nblocks);
     cfg.blockDim = dim3(K::NTH);
@@ -934,29 +946,42 @@ int launch_step_fused2(const Shot<float, float> &s, const WorkItem *items, const
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     const cudaError_t e =
-        cudaLaunchKernelEx(&cfg, fused2_step<M>, s, items, item_off, par, it, rec_index, rec_mid, err_flag);
+        cudaLaunchKernelEx(&cfg, fused2_step<M, W>, s, items, item_off, par, it, rec_index, rec_mid, err_flag);
     return e == cudaSuccess ? FD23_OK : FD23_ERR_CUDA;
 }
 
-int fused2_prepare(bool half_material)
+}  // namespace
+
+template <class M>
+int launch_step_fused2(const Shot<float, float> &s, int width, const WorkItem *items, const int *item_off,
+                       int nblocks, int par, int it, int rec_index, int rec_mid, int *err_flag, cudaStream_t st)
 {
-    return half_material ? prepare2<__half>() : prepare2<float>();
+    return width == 128 ? launch2<M, 128>(s, items, item_off, nblocks, par, it, rec_index, rec_mid, err_flag, st)
+                        : launch2<M, 256>(s, items, item_off, nblocks, par, it, rec_index, rec_mid, err_flag, st);
 }
 
-size_t fused2_smem_bytes(bool half_material)
+int fused2_prepare(bool half_material, int width)
 {
-    return half_material ? Cfg2<__half>::SMEM : Cfg2<float>::SMEM;
+    if (width == 128) return half_material ? prepare2<__half, 128>() : prepare2<float, 128>();
+    return half_material ? prepare2<__half, 256>() : prepare2<float, 256>();
 }
 
-Fused2Boxes fused2_boxes(bool half_material)
+int fused2_tile_x(int width) { return width == 128 ? Cfg2<float, 128>::TX : Cfg2<float, 256>::TX; }
+
+int fused2_per_sm(int width) { return width == 128 ? Cfg2<float, 128>::MINB : Cfg2<float, 256>::MINB; }
+
+Fused2Boxes fused2_boxes(bool half_material, int width)
 {
-    return half_material ? Fused2Boxes{Cfg2<__half>::UWW, Cfg2<__half>::W1, Cfg2<__half>::MWW}
-                         : Fused2Boxes{Cfg2<float>::UWW, Cfg2<float>::W1, Cfg2<float>::MWW};
+    if (width == 128)
+        return half_material ? Fused2Boxes{Cfg2<__half, 128>::UWW, Cfg2<__half, 128>::W1, Cfg2<__half, 128>::MWW}
+                             : Fused2Boxes{Cfg2<float, 128>::UWW, Cfg2<float, 128>::W1, Cfg2<float, 128>::MWW};
+    return half_material ? Fused2Boxes{Cfg2<__half, 256>::UWW, Cfg2<__half, 256>::W1, Cfg2<__half, 256>::MWW}
+                         : Fused2Boxes{Cfg2<float, 256>::UWW, Cfg2<float, 256>::W1, Cfg2<float, 256>::MWW};
 }
 
-template int launch_step_fused2<float>(const Shot<float, float> &, const WorkItem *, const int *, int, int, int, int,
-                                       int, int *, cudaStream_t);
-template int launch_step_fused2<__half>(const Shot<float, float> &, const WorkItem *, const int *, int, int, int, int,
-                                        int, int *, cudaStream_t);
+template int launch_step_fused2<float>(const Shot<float, float> &, int, const WorkItem *, const int *, int, int, int,
+                                       int, int, int *, cudaStream_t);
+template int launch_step_fused2<__half>(const Shot<float, float> &, int, const WorkItem *, const int *, int, int, int,
+                                        int, int, int *, cudaStream_t);
 
 }  // namespace fd23

@@ -101,19 +101,21 @@ int fused_prepare_table_punch(int wave, int prec);
 // `par` and writing `1-par`; the memory variables of step it+1 go to
 // s.psim.  `rec_index` >= 0 gathers the receivers of the previous step from
 // buffer set `par` on the way (as the one-step sweep does); `rec_mid` >= 0
-// records step it (the step in between) into that record row.
+// records step it (the step in between) into that record row.  `width`:
+// strip width of the CTA's first stress update, 256 (one CTA per SM) or 128
+// (two); the output strips are fused2_tile_x(width) columns wide.
 // half_material: the material is read from FP16 copies (s.maps2 views them).
-constexpr int kFused2TileX = 232;  // output columns per strip
 template <class M>
-int launch_step_fused2(const Shot<float, float> &s, const WorkItem *items, const int *item_off, int nblocks,
-                       int par, int it, int rec_index, int rec_mid, int *err_flag, cudaStream_t st);
-int fused2_prepare(bool half_material);        // once per device before the first launch
-size_t fused2_smem_bytes(bool half_material);  // dynamic shared memory of one CTA
+int launch_step_fused2(const Shot<float, float> &s, int width, const WorkItem *items, const int *item_off,
+                       int nblocks, int par, int it, int rec_index, int rec_mid, int *err_flag, cudaStream_t st);
+int fused2_prepare(bool half_material, int width);  // once per device before the first launch
+int fused2_tile_x(int width);                       // output columns per strip
+int fused2_per_sm(int width);                       // CTAs per SM
 // copy shapes of the two-step sweep (for its tensor maps)
 struct Fused2Boxes {
     int uww, pww, mww;
 };
-Fused2Boxes fused2_boxes(bool half_material);
+Fused2Boxes fused2_boxes(bool half_material, int width);
 
 // one thread waits on an mbarrier nothing completes, with the sweep's bounded
 // wait: sets *err_flag when the wait gives up (about 2 s)

@@ -104,6 +104,7 @@ struct fd23_solver {
     // of that step (rebuilt when receivers change), host copies of the
     // receiver positions
     bool fused2 = false;
+    int f2_width = 256;  // strip width of the two-step sweep's CTAs (256 or 128)
     fd23::WorkItem *d_items2 = nullptr;
     int *d_item_off2 = nullptr;
     int nblocks2 = 0;

@@ -24,8 +24,7 @@ import pytest
 
 XPAD = ZPAD = 8
 TX1 = 120                  # one-step strips (they size the layout)
-W1, TX = 256, 232          # two-step sweep: ring row width, output columns
-UWW = W1 + 8
+WIDTHS = (256, 128)        # two-step sweep: ring row width W1; output columns W1 - 24
 NUW, NPW, NR = 4, 2, 3
 
 GRIDS = [(96, 64, 12), (250, 130, 12), (257, 131, 16), (300, 200, 12), (130, 97, 12), (700, 90, 12),
@@ -45,14 +44,15 @@ def al128(b):
     return (b + 127) // 128 * 128
 
 
-def smem(es_mat):
+def smem(es_mat, W1):
+    uww = W1 + 8
     moff = 4 if es_mat == 2 else 0
     mww = W1 + 2 * moff
-    uw_slot = 2 * 4 * UWW * 4
+    uw_slot = 4 * uww * 4          # 4 rows of one field: U and W rings of NUW slots each
     told = 3 * 4 * W1 * 4
     ms_b, mv_b = al128(3 * 4 * mww * es_mat), al128(2 * 4 * mww * es_mat)
     stage = told + ms_b + mv_b
-    off_pw = NUW * uw_slot
+    off_pw = 2 * NUW * uw_slot
     off_tr = off_pw + NPW * stage
     off_vr = off_tr + NR * 4 * 3 * W1 * 4
     off_t2 = off_vr + NR * 4 * 2 * W1 * 4
@@ -62,14 +62,18 @@ def smem(es_mat):
                 off_pw=off_pw, off_tr=off_tr, off_vr=off_vr, off_t2=off_t2, total=total)
 
 
+@pytest.mark.parametrize("W1", WIDTHS)
 @pytest.mark.parametrize("es_mat", [4, 2])
-def test_shared_memory_regions(es_mat):
-    m = smem(es_mat)
-    assert m["total"] <= 227 * 1024
+def test_shared_memory_regions(es_mat, W1):
+    m = smem(es_mat, W1)
+    UWW = W1 + 8
+    per_sm = 256 // W1
+    # the CTAs per SM the launch bounds promise fit in 228 KB (1 KB reserved per CTA)
+    assert per_sm * (m["total"] + 1024) <= 228 * 1024
     for k in ("off_pw", "off_tr", "off_vr", "off_t2", "stage", "uw_slot"):
         assert m[k] % 128 == 0, k
     assert (m["told"] + m["ms_b"]) % 128 == 0
-    # box dimensions: input {8, 33, 4, 2}; stresses {256, 4, 3}; material {mww, 4, 3|2}
+    # box dimensions: input {8, UWW/8, 4, 1}; stresses {W1, 4, 3}; material {mww, 4, 3|2}
     assert UWW % 8 == 0 and UWW // 8 <= 256
     assert W1 <= 256
     if es_mat == 4:
@@ -77,20 +81,27 @@ def test_shared_memory_regions(es_mat):
     # bytes a stage's copies deliver equal the stage's expect_tx
     assert m["told"] + 5 * 4 * m["mww"] * es_mat <= m["stage"]
     # ring reads: ld12 reads p-4 .. p+7 of a row, p = 4t (rings) or 4 + 4t (input rows)
-    for lo, hi in ((1, 62), (2, 61), (3, 60)):       # V1, S2, V2 read rings
+    ntr = W1 // 4
+    for lo, hi in ((1, ntr - 2), (2, ntr - 3), (3, ntr - 4)):  # V1, S2, V2 read rings
         assert 4 * lo - 4 >= 0 and 4 * hi + 7 < W1
-    assert 4 * 63 + 4 + 7 < UWW and 0 + 4 - 4 >= 0  # S1 reads input rows
-    # writes: S1 all 64 groups, V1 / S2 their ranges, all inside a ring row
-    assert 4 * 63 + 3 < W1
-    # material rows in a stage: offset moff + 4t, t <= 63
-    assert m["moff"] + 4 * 63 + 3 < m["mww"]
+    assert 4 * (ntr - 1) + 4 + 7 < UWW and 0 + 4 - 4 >= 0  # S1 reads input rows
+    # writes: S1 all groups, V1 / S2 their ranges, all inside a ring row
+    assert 4 * (ntr - 1) + 3 < W1
+    # material rows in a stage: offset moff + 4t
+    assert m["moff"] + 4 * (ntr - 1) + 3 < m["mww"]
+    # 12-row ring rows: rb + d with rb < 12, d <= 8 wraps at most once
+    assert all((rb + d if rb + d < 12 else rb + d - 12) < 12 for rb in range(12) for d in range(9))
 
 
+@pytest.mark.parametrize("W1", WIDTHS)
 @pytest.mark.parametrize("nx,nz,npml", GRIDS)
-def test_global_addresses(nx, nz, npml):
+def test_global_addresses(nx, nz, npml, W1):
     pitch, rows, origin = layout(nx, nz)
     elems = pitch * rows
-    assert pitch % 32 == 0
+    assert pitch % 32 == 0 and pitch % 8 == 0
+    assert elems < 2 ** 31  # 32-bit element offsets
+    TX = W1 - 24
+    ntr = W1 // 4
     nstrip = (nx + TX - 1) // TX
     for s in range(nstrip):
         x0 = s * TX
@@ -100,7 +111,7 @@ def test_global_addresses(nx, nz, npml):
         # stress / material copies: 16-byte x starts for FP32, 8-column starts for FP16
         assert ((XPAD + x0 - 12) * 4) % 16 == 0
         assert (XPAD + x0 - 12 - 4) % 8 == 0
-        for t_lo, t_hi in ((2, 61), (3, 60)):
+        for t_lo, t_hi in ((2, ntr - 3), (3, ntr - 4)):
             for t in (t_lo, t_hi):
                 x = x0 - 12 + 4 * t
                 if not (x + 3 >= 0 and x < nx):

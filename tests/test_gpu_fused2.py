@@ -7,7 +7,8 @@ of every step (the step in between is recorded inside the launch), the full
 state (wavefields and every memory variable), over grids that are not tile
 multiples, free-surface and absorbing tops, every P-SV source kind, the
 fluid-layer edge rules, odd step counts (the last step runs the one-step
-sweep), record decimation, split runs, restarts and stress receivers.
+sweep), record decimation, split runs, restarts and stress receivers, for
+both strip widths.
 """
 import numpy as np
 import pytest
@@ -16,6 +17,14 @@ from tests.fd23_cases import Case
 
 pytestmark = pytest.mark.gpu
 
+
+@pytest.fixture(params=[256, 128], autouse=True)
+def width(request, monkeypatch):
+    """both strip widths of the sweep: 256 columns (one CTA per SM) and 128
+    (two); read when a solver is created"""
+    monkeypatch.setenv("FD23_FUSED2_WIDTH", str(request.param))
+    return request.param
+
 PSV_CASES = [
     dict(nx=96, nz=64, kind=3),
     dict(nx=250, nz=130, kind=3, topabsorb=1),
@@ -23,6 +32,7 @@ PSV_CASES = [
     dict(nx=300, nz=200, kind=1, fluid=True),
     dict(nx=130, nz=97, kind=3, zs=1, xs=5),  # source next to the surface and the edge
     dict(nx=700, nz=90, kind=3, xs=463, zs=40),  # source on a strip boundary (232-column strips)
+    dict(nx=420, nz=77, kind=3, xs=207, zs=30),  # source on a strip boundary (104-column strips)
 ]
 
 
