@@ -29,7 +29,8 @@ def _receivers(c, extra_x, extra_z):
 
 @pytest.mark.parametrize("prec", ["f32", "f64"])
 @pytest.mark.parametrize("kernel", ["fused", "twopass"])
-@pytest.mark.parametrize("box", [(70, 30, 64, 56), (20, 14, 130, 101)])  # one-CTA and column-blocked kernels
+# one-CTA kernels (small boxes), multi-CTA kernels (odd and even widths)
+@pytest.mark.parametrize("box", [(70, 30, 64, 56), (20, 14, 130, 101), (16, 12, 128, 100)])
 def test_box_parity_with_oracle(prec, kernel, box):
     """Box driven by the ring field of a run in another model (so the residual
     field is far from zero), with the grid's own point source outside the box
