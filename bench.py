@@ -331,6 +331,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--bands", type=int, choices=(0, 1), default=None,
+                    help="with --no-tune: the default block weights, cut strip after strip (0) or banded (1)")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--config", default="c1", choices=["c0", "c1", "c2", "c3", "c4", "c5", "c6"])
     ap.add_argument("--plan", default=None, type=lambda v: tuple(float(x) for x in v.split(",")),
@@ -389,6 +391,9 @@ def main():
     # work plan picked by the autotuner on this shot (set-up, not timed)
     tune = s.autotune(10) if args.kernel == "fused" and not args.no_tune and args.config != "c5" else []
     best_plan = s.plan() if tune else None  # the plan the autotuner kept
+    if args.kernel == "fused" and args.no_tune and args.bands is not None and args.config != "c5":
+        s.set_plan(4.0, 3.0, 3, 1.0, bands=args.bands)
+        best_plan = s.plan()
     punch = None
     if args.config == "c5":
         # usepunch: tile step windows from straight-ray travel times at the
@@ -502,7 +507,10 @@ def main():
     traffic = None
     tfile = os.path.join(ROOT, "profiles", "traffic_per_cell.json")
     if os.path.exists(tfile):
-        tb = json.load(open(tfile)).get("%s_psv_%s" % ("fused2" if args.kernel == "fused2" else "fused", args.prec))
+        key = "%s_psv_%s" % ("fused2" if args.kernel == "fused2" else "fused", args.prec)
+        if best_plan and best_plan.get("bands"):
+            key += "_bands1"  # the banded plan re-reads less (shared halo lines hit in L2)
+        tb = json.load(open(tfile)).get(key)
         if tb:
             traffic = tb * NX * NZ
     line = {"metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": world,
@@ -526,7 +534,12 @@ def main():
             "e2e": e2e}
     if best_plan:
         line["config"]["plan"] = {"wx": best_plan["wx"], "wz": best_plan["wz"], "oversub": best_plan["oversub"],
-                                  "autotune_trials": len(tune)}
+                                  "bands": best_plan.get("bands", 0), "autotune_trials": len(tune)}
+        if tune:
+            # fastest trial of each way of cutting (ms per step)
+            line["config"]["plan"]["best_trial_ms"] = {
+                "bands%d" % b: min((t["ms_per_step"] for t in tune if t["bands"] == b), default=None)
+                for b in (0, 1)}
     if accuracy:
         line["accuracy"] = accuracy
     if punch is not None:

@@ -71,7 +71,7 @@ class Fd23Error(RuntimeError):
 
 
 class TuneEntry(_C.Structure):
-    _fields_ = [("wx", _C.c_double), ("wz", _C.c_double), ("per_sm", _C.c_int),
+    _fields_ = [("wx", _C.c_double), ("wz", _C.c_double), ("per_sm", _C.c_int), ("bands", _C.c_int),
                 ("oversub", _C.c_double), ("ms_per_step", _C.c_double)]
 
     def as_dict(self):
@@ -365,16 +365,17 @@ def box_material(mat, x0, z0, bx, bz, src_vp, src_vs, src_den, dt, h):
     return m, bm, n
 
 
-def work_plan(grids, sms=152, wx=4.0, wz=3.0, per_sm=3, oversub=1.0, live=None):
+def work_plan(grids, sms=152, wx=4.0, wz=3.0, per_sm=3, oversub=1.0, live=None, bands=1):
     """The fused sweep's work plan for grids [(nx, nz, npml, topabsorb)]:
     list over CTAs of lists of (shot, x0, z0, z1) items.  live: optional
-    per-grid boolean arrays over the 4-row blocks (strip-major) to plan."""
+    per-grid boolean arrays over the 4-row blocks (strip-major) to plan;
+    bands=1: every strip cut on its own (fd23_tune_entry.bands)."""
     n = len(grids)
     a = [_np.ascontiguousarray([g[k] for g in grids], dtype=_np.int32) for k in range(4)]
     cap = sum(((g[0] + 119) // 120) * ((g[1] + 3) // 4) for g in grids) * 2 + 16
     items = _np.zeros(4 * cap, _np.int32)
     off = _np.zeros(cap + 1, _np.int32)
-    t = TuneEntry(wx, wz, per_sm, oversub, 0.0)
+    t = TuneEntry(wx=wx, wz=wz, per_sm=per_sm, bands=bands, oversub=oversub)
     lv = None if live is None else _np.ascontiguousarray(_np.concatenate([_np.asarray(m, bool).ravel()
                                                                            for m in live]), dtype=_np.uint8)
     nb = _check(lib().fd23_work_plan_live(n, *[_p(v) for v in a], sms, _C.cast(_C.pointer(t), _C.c_void_p),
@@ -430,10 +431,10 @@ class Batch:
         return d
 
     def autotune(self, trial_steps=10):
-        tab = (TuneEntry * 128)()
-        n = _check(lib().fd23_batch_autotune(self._h, trial_steps, _C.cast(tab, _C.c_void_p), 128),
+        tab = (TuneEntry * 256)()
+        n = _check(lib().fd23_batch_autotune(self._h, trial_steps, _C.cast(tab, _C.c_void_p), 256),
                    "fd23_batch_autotune")
-        return [tab[k].as_dict() for k in range(n)]
+        return [tab[k].as_dict() for k in range(min(n, 256))]
 
 
 def receivers_line(nsta, ix0, iz0, idx, idz):
@@ -656,13 +657,13 @@ class Solver:
     def autotune(self, trial_steps=10):
         """Time the candidate work plans on this shot and keep the fastest;
         returns the trials as dicts."""
-        tab = (TuneEntry * 128)()
-        n = _check(lib().fd23_autotune(self._h, trial_steps, _C.cast(tab, _C.c_void_p), 128), "fd23_autotune")
-        return [tab[k].as_dict() for k in range(n)]
+        tab = (TuneEntry * 256)()
+        n = _check(lib().fd23_autotune(self._h, trial_steps, _C.cast(tab, _C.c_void_p), 256), "fd23_autotune")
+        return [tab[k].as_dict() for k in range(min(n, 256))]
 
-    def set_plan(self, wx=4.0, wz=3.0, per_sm=3, oversub=1.0):
+    def set_plan(self, wx=4.0, wz=3.0, per_sm=3, oversub=1.0, bands=1):
         """Install a work plan without timing it (fd23_set_plan)."""
-        t = TuneEntry(wx, wz, per_sm, oversub, 0.0)
+        t = TuneEntry(wx=wx, wz=wz, per_sm=per_sm, bands=bands, oversub=oversub)
         _check(lib().fd23_set_plan(self._h, _C.cast(_C.pointer(t), _C.c_void_p)), "fd23_set_plan")
 
     def plan(self):

@@ -271,20 +271,23 @@ int snapshot_restore(const std::vector<fd23_solver *> &ss, cudaStream_t st, cons
 
 // block cost weights (x-CPML 2..7, z-CPML and edge rows 2..5) x waves of
 // CTAs 1..3 (the plan rounds the CTA count up to whole waves of the resident
-// slots): the step time is a bumpy function of the cut, so the grid is fine
-// (on the 4000 x 2000 P-SV grid weights 5 / 4 beat 6 / 4 by 6 %)
+// slots) x the two ways of cutting (strip after strip, or banded): the step
+// time is a bumpy function of the cut, so the grid is fine (on the
+// 4000 x 2000 P-SV grid weights 5 / 4 beat 6 / 4 by 6 %)
 std::vector<TuneParams> candidates()
 {
     std::vector<TuneParams> c;
-    for (double ov : {1.0, 2.0, 3.0})
-        for (double wx : {2.0, 3.0, 4.0, 5.0, 6.0, 7.0})
-            for (double wz : {2.0, 3.0, 4.0, 5.0}) {
-                TuneParams t;
-                t.wx = wx;
-                t.wz = wz;
-                t.oversub = ov;
-                c.push_back(t);
-            }
+    for (int bands : {0, 1})
+        for (double ov : {1.0, 2.0, 3.0})
+            for (double wx : {2.0, 3.0, 4.0, 5.0, 6.0, 7.0})
+                for (double wz : {2.0, 3.0, 4.0, 5.0}) {
+                    TuneParams t;
+                    t.wx = wx;
+                    t.wz = wz;
+                    t.oversub = ov;
+                    t.bands = bands;
+                    c.push_back(t);
+                }
     return c;
 }
 
@@ -317,7 +320,7 @@ int autotune_core(const std::vector<fd23_solver *> &ss, cudaStream_t st, int tri
         float ms = 0.f;
         CK(cudaEventElapsedTime(&ms, e0, e1));
         *per = ms / k;
-        if (table && n < cap) table[n] = fd23_tune_entry{cand[i].wx, cand[i].wz, cand[i].per_sm, cand[i].oversub, *per};
+        if (table && n < cap) table[n] = fd23_tune_entry{cand[i].wx, cand[i].wz, cand[i].per_sm, cand[i].bands, cand[i].oversub, *per};
         ++n;
         return snapshot_restore(ss, st, sn);
     };
@@ -455,7 +458,7 @@ int fd23_batch_set_graph(fd23_batch *b, int on)
 int fd23_batch_get_plan(fd23_batch *b, fd23_tune_entry *cur, int *nblocks)
 {
     if (!b) return FD23_ERR_ARG;
-    if (cur) *cur = fd23_tune_entry{b->tune.wx, b->tune.wz, b->tune.per_sm, b->tune.oversub, 0.0};
+    if (cur) *cur = fd23_tune_entry{b->tune.wx, b->tune.wz, b->tune.per_sm, b->tune.bands, b->tune.oversub, 0.0};
     if (nblocks) *nblocks = b->plan.nblocks;
     return FD23_OK;
 }
@@ -523,6 +526,7 @@ int fd23_work_plan_live(int nshots, const int *nx, const int *nz, const int *npm
     tp.wz = tune->wz;
     tp.per_sm = tune->per_sm;
     tp.oversub = tune->oversub;
+    tp.bands = tune->bands;
     const int tx = fused_geom(FD23_PSV, FD23_F32).tile_x;
     std::vector<std::vector<unsigned char>> masks;
     if (live) {
@@ -556,19 +560,19 @@ int fd23_work_plan(int nshots, const int *nx, const int *nz, const int *npml, co
 int fd23_set_plan(fd23_solver *s, const fd23_tune_entry *tune)
 {
     if (!s || !tune || !(tune->wx > 0) || !(tune->wz > 0) || tune->per_sm < 1 || !(tune->oversub >= 1.0) ||
-        tune->oversub > 64.0)
+        tune->oversub > 64.0 || (tune->bands != 0 && tune->bands != 1))
         return FD23_ERR_ARG;
     if (!s->fused) return FD23_ERR_UNSUPPORTED;
     CK(cudaSetDevice(s->d.device));
     CK(cudaStreamSynchronize(s->stream));  // the old work list may still be in use
-    s->tune = TuneParams{tune->wx, tune->wz, tune->per_sm, tune->oversub};
+    s->tune = TuneParams{tune->wx, tune->wz, tune->per_sm, tune->oversub, tune->bands};
     return build_worklist(s);
 }
 
 int fd23_get_plan(fd23_solver *s, fd23_tune_entry *cur, int *nblocks)
 {
     if (!s) return FD23_ERR_ARG;
-    if (cur) *cur = fd23_tune_entry{s->tune.wx, s->tune.wz, s->tune.per_sm, s->tune.oversub, 0.0};
+    if (cur) *cur = fd23_tune_entry{s->tune.wx, s->tune.wz, s->tune.per_sm, s->tune.bands, s->tune.oversub, 0.0};
     if (nblocks) *nblocks = s->nblocks;
     return FD23_OK;
 }

@@ -205,6 +205,7 @@ struct TuneParams {
     double wx = 4.0, wz = 3.0;  // relative cost of 4-row blocks touching the x / z CPML
     int per_sm = 3;             // CTAs resident per SM the plan is sized for
     double oversub = 1.0;       // CTAs launched per resident slot
+    int bands = 1;              // cut every strip on its own (plan_work)
 };
 struct WorkPlan {
     std::vector<WorkItem> items;

@@ -28,6 +28,53 @@ double block_cost(const ShotGeom &g, int tile_x, int strip, int zb, const TunePa
     return xp ? tp.wx : (zp ? tp.wz : 1.0);
 }
 
+// Banded cut of one shot (every block planned) for n CTAs: every strip is
+// cut on its own into ranges of equal cost, each strip getting the fewest
+// CTAs that keep its ranges at or below the largest per-CTA cost of the best
+// split (CTAs handed out one at a time to the strip with the costliest
+// ranges).  Strips of the same cost profile (all the interior strips) get the
+// same row boundaries, so neighbouring strips sweep the same rows at the same
+// time and the columns their copies share are still in L2 for the second
+// reader.  False (nothing added) when there are fewer CTAs than strips.
+bool cut_bands(const std::vector<double> &c, int shot, int ntx, int nzb, int tile_x, int n, WorkPlan &plan)
+{
+    if (n < ntx) return false;
+    std::vector<double> cost(ntx);
+    for (int s = 0; s < ntx; ++s) cost[s] = c[(size_t)(s + 1) * nzb] - c[(size_t)s * nzb];
+    std::vector<int> ns(ntx, 1);
+    for (int left = n - ntx; left > 0; --left) {
+        int w = -1;
+        for (int s = 0; s < ntx; ++s)
+            if (ns[s] < nzb && (w < 0 || cost[s] * ns[w] > cost[w] * ns[s])) w = s;
+        if (w < 0) break;
+        ++ns[w];
+    }
+    double m = 0.0;
+    for (int s = 0; s < ntx; ++s) m = std::max(m, cost[s] / ns[s]);
+    for (int s = 0; s < ntx; ++s) {
+        int k = 1;
+        while (k < ns[s] && cost[s] / k > m * (1.0 + 1e-12)) ++k;
+        ns[s] = k;
+    }
+    for (int s = 0; s < ntx; ++s) {
+        const size_t a = (size_t)s * nzb;
+        long long b0 = 0;
+        for (int q = 0; q < ns[s]; ++q) {
+            long long b1 = nzb;
+            if (q < ns[s] - 1) {
+                const double target = c[a] + cost[s] * (double)(q + 1) / (double)ns[s];
+                b1 = (long long)(std::lower_bound(c.begin() + a + b0 + 1, c.begin() + a + nzb, target) - (c.begin() + a));
+                b1 = std::max(b1, b0 + 1);
+                b1 = std::min(b1, (long long)nzb - (ns[s] - 1 - q));
+            }
+            plan.items.push_back(WorkItem{shot, s * tile_x, (int)b0 * 4, (int)b1 * 4});
+            plan.off.push_back((int)plan.items.size());
+            b0 = b1;
+        }
+    }
+    return true;
+}
+
 }  // namespace
 
 // Cuts the nb planned blocks of one shot (cumulative costs c; run_begin[r]
@@ -147,6 +194,10 @@ int plan_work(const std::vector<ShotGeom> &shots, int tile_x, int sms, const Tun
     for (int k = 0; k < ns; ++k) {
         plan.cta0[k] = (int)plan.off.size() - 1;
         if (nbk[k] == 0) continue;  // nothing to do for this shot
+        if (tp.bands && !live && cut_bands(cum[k], k, (shots[k].nx + tile_x - 1) / tile_x, nzb[k], tile_x, nc[k], plan)) {
+            plan.ncta[k] = (int)plan.off.size() - 1 - plan.cta0[k];
+            continue;
+        }
         int n = nc[k];
         while (!cut_shot(cum[k], nbk[k], run_of[k], run_begin[k], n, ends)) {
             if (n >= nbk[k]) return FD23_ERR_ARG;

@@ -324,9 +324,10 @@ int fd23_batch_set_graph(fd23_batch *b, int on);
  * The fused sweep's work plan: 4-row blocks of 120-column strips, weighted by
  * an estimated cost (wx for blocks touching the x-CPML, wz for the z-CPML and
  * edge rows, 1 otherwise), cut into equal-cost contiguous ranges for
- * per_sm x SMs x oversub CTAs.  fd23_autotune / fd23_batch_autotune time
- * every candidate plan (72: wx 2..7, wz 2..5, oversub 1..3) for trial_steps
- * steps on the live shot(s), then the five fastest and the 8 half-step
+ * per_sm x SMs x oversub CTAs (bands = 0), or strip by strip (bands = 1).
+ * fd23_autotune / fd23_batch_autotune time every candidate plan (144: wx
+ * 2..7, wz 2..5, oversub 1..3, bands 0..1) for trial_steps steps on the live
+ * shot(s), then the five fastest and the 8 half-step
  * neighbours of the best weights for 3 x trial_steps, restore the
  * wavefields, memory variables and step counters after each trial, and
  * keep the fastest plan of the long trials.  table (cap
@@ -335,6 +336,10 @@ int fd23_batch_set_graph(fd23_batch *b, int on);
 typedef struct {
     double wx, wz;      /* block cost weights */
     int per_sm;         /* resident CTAs per SM */
+    int bands;          /* 0: ranges cut strip after strip; 1: every strip cut
+                         * on its own, at the same rows as the strips of the
+                         * same cost (single-shot plans of one wave or more
+                         * CTAs than strips; others fall back to 0) */
     double oversub;     /* CTAs launched per resident slot */
     double ms_per_step; /* measured (0 for the current plan) */
 } fd23_tune_entry;

@@ -34,13 +34,14 @@ def layout(nx, nz):
     return pitch, rows, ZPAD * pitch + XPAD
 
 
-def worklist(nx, nz, npml, oversub=1.0, per_sm=3):
+def worklist(nx, nz, npml, oversub=1.0, per_sm=3, bands=0):
     F = pytest.importorskip("fd23_gb300")
     try:
         F.lib()
     except ImportError as e:
         pytest.skip(str(e))
-    return [[it[1:] for it in cta] for cta in F.work_plan([(nx, nz, npml, 0)], per_sm=per_sm, oversub=oversub)]
+    return [[it[1:] for it in cta]
+            for cta in F.work_plan([(nx, nz, npml, 0)], per_sm=per_sm, oversub=oversub, bands=bands)]
 
 
 def al128(b):
@@ -69,7 +70,7 @@ def box_ok(x, y, z, w, nf, pitch, rows, nfields, es):
     assert w <= 256 and nf <= 256
 
 
-def audit(nx, nz, es, wave, per_sm=3, oversub=1.0, ctas=None, narrowed=False):
+def audit(nx, nz, es, wave, per_sm=3, oversub=1.0, ctas=None, narrowed=False, bands=0):
     pitch, rows, origin = layout(nx, nz)
     npml = min(40, nx // 2, nz // 2)
     elems = pitch * rows
@@ -85,7 +86,7 @@ def audit(nx, nz, es, wave, per_sm=3, oversub=1.0, ctas=None, narrowed=False):
     pww = SW + 2 * pwoff
     assert (pitch * es) % 16 == 0
     if ctas is None:
-        ctas = worklist(nx, nz, npml, oversub, per_sm)
+        ctas = worklist(nx, nz, npml, oversub, per_sm, bands)
     covered = set()
     for items in ctas:
         assert (0 if narrowed else 1) <= len(items) <= MAX_ITEMS
@@ -146,10 +147,11 @@ SIZES = [(96, 96), (96, 64), (250, 130), (257, 131), (500, 300), (1000, 1000), (
 @pytest.mark.parametrize("es,wave", [(4, "psv"), (8, "psv"), (2, "psv"), (4, "sh"), (2, "sh")])
 def test_fused_addresses_in_bounds(nx, nz, es, wave):
     per_sm = {8: 1, 4: 3, 2: 2}[es]  # the register budget each storage width is built for
-    audit(nx, nz, es, wave, per_sm=per_sm)
-    if es == 2:  # and three, should the runtime report three resident CTAs
-        audit(nx, nz, es, wave, per_sm=3)
-    audit(nx, nz, es, wave, per_sm=per_sm, oversub=3.0)
+    for bands in (0, 1):  # strip-major and banded plans
+        audit(nx, nz, es, wave, per_sm=per_sm, bands=bands)
+        if es == 2:  # and three, should the runtime report three resident CTAs
+            audit(nx, nz, es, wave, per_sm=3, bands=bands)
+        audit(nx, nz, es, wave, per_sm=per_sm, oversub=3.0, bands=bands)
 
 
 def test_batch_plan_in_bounds():
@@ -166,8 +168,10 @@ def test_batch_plan_in_bounds():
     grids = [(d["nx"], d["nz"], 40, 0) for d in bench.batch_shots()]
     for wx, wz in ((1.0, 1.0), (2.5, 1.5), (4.0, 3.0), (6.0, 4.0), (4.0, 2.0), (3.0, 3.0)):
         for ov in (1.0, 2.0, 3.0):
-            ctas = F.work_plan(grids, wx=wx, wz=wz, oversub=ov)
+            ctas = F.work_plan(grids, wx=wx, wz=wz, oversub=ov, bands=0)
             assert len(ctas) % 456 == 0
+            # banded: shots with fewer CTAs than strips keep the strip-major cut
+            assert len(F.work_plan(grids, wx=wx, wz=wz, oversub=ov, bands=1)) <= len(ctas)
             per_shot = {}
             for cta in ctas:
                 shots = {it[0] for it in cta}
@@ -286,4 +290,40 @@ def test_live_mask_plans(nx, nz, density):
         if mask.any():
             audit(nx, nz, 4, "psv", ctas=[[it[1:] for it in c] for c in ctas], narrowed=True)
     full = F.work_plan([(nx, nz, npml, 0)], wx=5.0, wz=4.0, live=[np.ones(ntx * nzb, bool)])
-    assert full == F.work_plan([(nx, nz, npml, 0)], wx=5.0, wz=4.0)
+    assert full == F.work_plan([(nx, nz, npml, 0)], wx=5.0, wz=4.0, bands=0)
+
+
+@pytest.mark.parametrize("nx,nz,npml", [(4000, 2000, 40), (16000, 8000, 40), (800, 400, 20), (1000, 1000, 20),
+                                        (257, 131, 12)])
+@pytest.mark.parametrize("ov", [1.0, 3.0])
+def test_banded_plan_covers_grid_with_shared_row_cuts(nx, nz, npml, ov):
+    """Banded plans (fd23_tune_entry.bands = 1): one item per CTA, every
+    4-row block of the grid exactly once, no more CTAs than the strip-major
+    plan, and every interior strip cut at the same rows (the x-CPML strips
+    have their own cut); their copies pass the audit."""
+    F = pytest.importorskip("fd23_gb300")
+    try:
+        F.lib()
+    except ImportError as e:
+        pytest.skip(str(e))
+    ref = F.work_plan([(nx, nz, npml, 0)], wx=5.0, wz=2.5, oversub=ov, bands=0)
+    ctas = F.work_plan([(nx, nz, npml, 0)], wx=5.0, wz=2.5, oversub=ov, bands=1)
+    ntx = (nx + TX - 1) // TX
+    if len(ref) < ntx:  # fewer CTAs than strips: the strip-major plan
+        assert ctas == ref
+        return
+    assert len(ctas) <= len(ref)
+    cuts = {}
+    for cta in ctas:
+        assert len(cta) == 1
+        (_, x0, z0, z1), = cta
+        cuts.setdefault(x0, []).append((z0, z1))
+    assert sorted(cuts) == [TX * s for s in range(ntx)]
+    nzb = (nz + 3) // 4
+    for x0, c in cuts.items():
+        c.sort()
+        assert c[0][0] == 0 and c[-1][1] == 4 * nzb
+        assert all(a[1] == b[0] for a, b in zip(c, c[1:]))
+    interior = [x0 for x0 in cuts if x0 - 4 >= max(npml, 4) and x0 + TX + 4 <= min(nx - npml, nx - 4)]
+    assert len({tuple(cuts[x0]) for x0 in interior}) <= 1
+    audit(nx, nz, 4, "psv", ctas=[[it[1:] for it in cta] for cta in ctas])

@@ -44,3 +44,33 @@ def test_fused_equals_oracle_benchmark_cpml():
     for a, b in zip(seis, seis_o):
         np.testing.assert_array_equal(a, b)
     np.testing.assert_array_equal(st, st_o)
+
+
+@pytest.mark.parametrize("prec", ["f32", "f16"])
+def test_banded_plan_keeps_results(prec):
+    """The banded work plan (every strip cut on its own) at the benchmark
+    size gives bit for bit the strip-major plan's wavefields and seismograms;
+    at the 1000 x 500 cut, the oracle's FP32 run."""
+    c = Case("psv", 4000, 2000, npml=40, h=0.005, dt=4e-4, nt=120, seed=14, xs=2000, zs=20,
+             wavelet=("ricker", 25.0))
+    out = {}
+    for bands in (0, 1):
+        s = c.solver(prec, "fused")
+        s.set_plan(5.0, 2.5, 3, 1.0, bands=bands)
+        assert s.plan()["bands"] == bands
+        s.run(c.nt, 1)
+        out[bands] = [s.seismograms(0), s.seismograms(1), s.get_state()]
+        s.close()
+    for a, b in zip(out[0], out[1]):
+        np.testing.assert_array_equal(a, b)
+    if prec == "f32":
+        c = Case("psv", 1000, 500, npml=40, h=0.005, dt=4e-4, nt=150, seed=15, xs=500, zs=20,
+                 wavelet=("ricker", 25.0))
+        seis_o, st_o = c.oracle("f32")
+        s = c.solver("f32", "fused")
+        s.set_plan(4.0, 3.0, 3, 2.0, bands=1)
+        s.run(c.nt, 1)
+        np.testing.assert_array_equal(s.seismograms(0), seis_o[0])
+        np.testing.assert_array_equal(s.seismograms(1), seis_o[1])
+        np.testing.assert_array_equal(s.get_state(), st_o)
+        s.close()
