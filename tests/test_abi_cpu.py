@@ -30,6 +30,17 @@ def test_library_exports_every_declared_function():
     assert sorted(F.ABI_FUNCTIONS) == names
 
 
+def test_tune_entry_layout():
+    """fd23_tune_entry: bands fills the padding after per_sm, so the struct
+    keeps the size and offsets it had without it (40 bytes, oversub at 24)."""
+    import ctypes
+    assert ctypes.sizeof(F.TuneEntry) == 40
+    assert F.TuneEntry.per_sm.offset == 16 and F.TuneEntry.bands.offset == 20
+    assert F.TuneEntry.oversub.offset == 24 and F.TuneEntry.ms_per_step.offset == 32
+    t = F.TuneEntry()
+    assert t.bands == 0  # zero-filled: the strip-major cut
+
+
 def test_create_without_gpu_fails_cleanly():
     try:
         import torch
