@@ -391,7 +391,7 @@ def main():
     # work plan picked by the autotuner on this shot (set-up, not timed)
     tune = s.autotune(10) if args.kernel == "fused" and not args.no_tune and args.config != "c5" else []
     best_plan = s.plan() if tune else None  # the plan the autotuner kept
-    if args.kernel == "fused" and args.no_tune and args.bands is not None and args.config != "c5":
+    if args.kernel in ("fused", "fused2") and args.no_tune and args.bands is not None and args.config != "c5":
         s.set_plan(4.0, 3.0, 3, 1.0, bands=args.bands)
         best_plan = s.plan()
     punch = None

@@ -441,6 +441,9 @@ int build_worklist2(fd23_solver *s)
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->d.device));
     TuneParams tp = s->tune;
     tp.per_sm = fused2_per_sm(s->f2_width);
+    // strip-major: measured faster for this sweep (C1: 5.44e10 cell-updates/s
+    // against 5.00e10 with the banded cut)
+    tp.bands = 0;
     WorkPlan plan;
     const std::vector<ShotGeom> geo{ShotGeom{s->d.nx, s->d.nz, s->d.npml, s->d.topabsorb}};
     int rc = plan_work(geo, fused2_tile_x(s->f2_width), sms, tp, plan);

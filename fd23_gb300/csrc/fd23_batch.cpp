@@ -566,7 +566,10 @@ int fd23_set_plan(fd23_solver *s, const fd23_tune_entry *tune)
     CK(cudaSetDevice(s->d.device));
     CK(cudaStreamSynchronize(s->stream));  // the old work list may still be in use
     s->tune = TuneParams{tune->wx, tune->wz, tune->per_sm, tune->oversub, tune->bands};
-    return build_worklist(s);
+    int rc = build_worklist(s);
+    // the two-step sweep's plan takes the same weights and cut (its own CTAs per SM)
+    if (!rc && s->fused2) rc = build_worklist2(s);
+    return rc;
 }
 
 int fd23_get_plan(fd23_solver *s, fd23_tune_entry *cur, int *nblocks)

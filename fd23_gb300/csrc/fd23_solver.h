@@ -140,6 +140,7 @@ int zero_state(fd23_solver *s);
 int fused_per_sm(int device, int wave, int prec);
 int upload_plan(const WorkPlan &plan, WorkItem **d_items, int **d_off);
 int build_worklist(fd23_solver *s);
+int build_worklist2(fd23_solver *s);
 int dispatch_step(fd23_solver *s, int rec_now);
 // copies buffer set `par` (wavefields, memory variables) into the other set
 int mirror_sets(fd23_solver *s, cudaStream_t st);
