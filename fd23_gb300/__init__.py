@@ -55,7 +55,7 @@ ABI_FUNCTIONS = [
     "fd23_box_ring_index", "fd23_box_ring_cells", "fd23_box_incident_from_displacement",
     "fd23_box_material", "fd23_batch_create", "fd23_batch_destroy", "fd23_batch_run", "fd23_batch_sync",
     "fd23_batch_get_stream", "fd23_batch_set_graph", "fd23_autotune", "fd23_batch_autotune",
-    "fd23_batch_get_plan", "fd23_work_plan", "fd23_read_model", "fd23_read_stations",
+    "fd23_batch_get_plan", "fd23_batch_set_plan", "fd23_work_plan", "fd23_read_model", "fd23_read_stations",
     "fd23_debug_expire_wait", "fd23_set_plan", "fd23_get_plan", "fd23_punch_tiles", "fd23_punch_windows", "fd23_read_punch", "fd23_set_punch",
     "fd23_set_material_table", "fd23_set_punch_phase", "fd23_work_plan_live",
     "fd23_line_source_coefs", "fd23_line_plane_origin", "fd23_line_source_planes", "fd23_set_box_line_source",
@@ -159,6 +159,7 @@ def lib():
         "fd23_batch_sync": ([vp], i),
         "fd23_batch_get_stream": ([vp, _C.POINTER(vp)], i),
         "fd23_batch_set_graph": ([vp, i], i),
+        "fd23_batch_set_plan": ([vp, vp], i),
         "fd23_autotune": ([vp, i, vp, i], i),
         "fd23_batch_autotune": ([vp, i, vp, i], i),
         "fd23_batch_get_plan": ([vp, vp, _C.POINTER(i)], i),
@@ -429,6 +430,11 @@ class Batch:
         d = e.as_dict()
         d["nblocks"] = nb.value
         return d
+
+    def set_plan(self, wx=4.0, wz=3.0, per_sm=3, oversub=1.0, bands=1):
+        """Install a work plan for the batch without timing it (fd23_batch_set_plan)."""
+        t = TuneEntry(wx=wx, wz=wz, per_sm=per_sm, bands=bands, oversub=oversub)
+        _check(lib().fd23_batch_set_plan(self._h, _C.cast(_C.pointer(t), _C.c_void_p)), "fd23_batch_set_plan")
 
     def autotune(self, trial_steps=10):
         tab = (TuneEntry * 256)()

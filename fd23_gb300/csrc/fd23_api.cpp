@@ -385,7 +385,7 @@ int encode_maps(fd23_solver *s)
 
 // CTAs per SM the fused sweep can keep resident (shared memory bound, at most
 // the 3 its register budget is built for)
-int fused_per_sm(int device, int wave, int prec)
+int fused_per_sm(int device, int wave, int prec, bool batch)
 {
     // registers and shared memory both bound the residency: ask the runtime
     // (after fused_prepare has raised the dynamic shared-memory limit)
@@ -397,7 +397,7 @@ int fused_per_sm(int device, int wave, int prec)
             return 1;
         }
     }
-    return std::max(1, std::min(3, fused_occupancy(wave, prec)));
+    return std::max(1, std::min(3, fused_occupancy(wave, prec, batch)));
 }
 
 int upload_plan(const WorkPlan &plan, WorkItem **d_items, int **d_off)
@@ -442,8 +442,9 @@ int build_worklist2(fd23_solver *s)
     TuneParams tp = s->tune;
     tp.per_sm = fused2_per_sm(s->f2_width);
     // strip-major: measured faster for this sweep (C1: 5.44e10 cell-updates/s
-    // against 5.00e10 with the banded cut)
+    // against 5.00e10 with the banded cut); strips from column 0
     tp.bands = 0;
+    tp.shift = 0;
     WorkPlan plan;
     const std::vector<ShotGeom> geo{ShotGeom{s->d.nx, s->d.nz, s->d.npml, s->d.topabsorb}};
     int rc = plan_work(geo, fused2_tile_x(s->f2_width), sms, tp, plan);

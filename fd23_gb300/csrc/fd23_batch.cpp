@@ -52,7 +52,7 @@ int batch_plan(fd23_batch *b, const TuneParams &tp)
     int sms = 0;
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
     TuneParams t = tp;
-    t.per_sm = std::min(t.per_sm, fused_per_sm(b->device, b->wave, b->prec));
+    t.per_sm = std::min(t.per_sm, fused_per_sm(b->device, b->wave, b->prec, true));
     WorkPlan plan;
     int rc = plan_work(geo, fused_geom(b->wave, b->prec).tile_x, sms, t, plan);
     if (rc) return rc;
@@ -455,6 +455,17 @@ int fd23_batch_set_graph(fd23_batch *b, int on)
     return FD23_OK;
 }
 
+int fd23_batch_set_plan(fd23_batch *b, const fd23_tune_entry *tune)
+{
+    if (!b || !tune || !(tune->wx > 0) || !(tune->wz > 0) || tune->per_sm < 1 || !(tune->oversub >= 1.0) ||
+        tune->oversub > 64.0 || (tune->bands != 0 && tune->bands != 1))
+        return FD23_ERR_ARG;
+    CK(cudaSetDevice(b->device));
+    CK(cudaStreamSynchronize(b->stream));  // the old work list may still be in use
+    TuneParams t{tune->wx, tune->wz, tune->per_sm, tune->oversub, tune->bands};
+    return batch_plan(b, t);
+}
+
 int fd23_batch_get_plan(fd23_batch *b, fd23_tune_entry *cur, int *nblocks)
 {
     if (!b) return FD23_ERR_ARG;
@@ -565,7 +576,9 @@ int fd23_set_plan(fd23_solver *s, const fd23_tune_entry *tune)
     if (!s->fused) return FD23_ERR_UNSUPPORTED;
     CK(cudaSetDevice(s->d.device));
     CK(cudaStreamSynchronize(s->stream));  // the old work list may still be in use
-    s->tune = TuneParams{tune->wx, tune->wz, tune->per_sm, tune->oversub, tune->bands};
+    TuneParams t{tune->wx, tune->wz, tune->per_sm, tune->oversub, tune->bands};
+    t.shift = s->tune.shift;
+    s->tune = t;
     int rc = build_worklist(s);
     // the two-step sweep's plan takes the same weights and cut (its own CTAs per SM)
     if (!rc && s->fused2) rc = build_worklist2(s);

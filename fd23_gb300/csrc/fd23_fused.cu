@@ -124,33 +124,34 @@ int fused_prepare(int wave, int prec)
 }
 
 template <class S, class C, int WAVE>
-int occupancy_one()
+int occupancy_one(bool batch)
 {
     using K = Cfg<S, C, WAVE>;
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fused_step<S, C, WAVE, false, false, false>, K::NTH, K::SMEM) !=
-        cudaSuccess) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &n, batch ? fused_step<S, C, WAVE, true, false, false> : fused_step<S, C, WAVE, false, false, false>,
+            K::NTH, K::SMEM) != cudaSuccess) {
         cudaGetLastError();
         return 1;
     }
     return n > 0 ? n : 1;
 }
 
-int fused_occupancy(int wave, int prec)
+int fused_occupancy(int wave, int prec, bool batch)
 {
     if (wave == FD23_PSV) {
         switch (prec) {
-            case FD23_F64: return occupancy_one<double, double, FD23_PSV>();
-            case FD23_BF16: return occupancy_one<__nv_bfloat16, float, FD23_PSV>();
-            case FD23_F16: return occupancy_one<__half, float, FD23_PSV>();
-            default: return occupancy_one<float, float, FD23_PSV>();
+            case FD23_F64: return occupancy_one<double, double, FD23_PSV>(batch);
+            case FD23_BF16: return occupancy_one<__nv_bfloat16, float, FD23_PSV>(batch);
+            case FD23_F16: return occupancy_one<__half, float, FD23_PSV>(batch);
+            default: return occupancy_one<float, float, FD23_PSV>(batch);
         }
     }
     switch (prec) {
-        case FD23_F64: return occupancy_one<double, double, FD23_SH>();
-        case FD23_BF16: return occupancy_one<__nv_bfloat16, float, FD23_SH>();
-        case FD23_F16: return occupancy_one<__half, float, FD23_SH>();
-        default: return occupancy_one<float, float, FD23_SH>();
+        case FD23_F64: return occupancy_one<double, double, FD23_SH>(batch);
+        case FD23_BF16: return occupancy_one<__nv_bfloat16, float, FD23_SH>(batch);
+        case FD23_F16: return occupancy_one<__half, float, FD23_SH>(batch);
+        default: return occupancy_one<float, float, FD23_SH>(batch);
     }
 }
 

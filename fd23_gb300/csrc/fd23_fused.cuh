@@ -47,6 +47,7 @@
 // the two compile in parallel.
 #pragma once
 #include <climits>
+#include <cstddef>
 #include <cstdio>
 #include <type_traits>
 
@@ -441,13 +442,17 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
 
     const Shot<S, C> *shp;
     if constexpr (BATCH) {
-        __shared__ Shot<S, C> sh_s;
-        static_assert(sizeof(Shot<S, C>) % 16 == 0, "shot descriptor copied as 16-byte words");
+        // the descriptor up to the fields only single shots use (the two-step
+        // sweep's, the box), as 16-byte words: three CTAs per SM still fit
+        using ShotT = Shot<S, C>;
+        constexpr int kHead = (int)((offsetof(ShotT, maps2) + 15) / 16 * 16);
+        static_assert(kHead <= (int)sizeof(ShotT) && sizeof(ShotT) % 16 == 0, "descriptor head");
+        __shared__ alignas(16) unsigned char sh_head[kHead];
         const int4 *src = reinterpret_cast<const int4 *>(shots + items[ibeg].shot);
-        int4 *dst = reinterpret_cast<int4 *>(&sh_s);
-        for (int w = tid; w < (int)(sizeof(Shot<S, C>) / 16); w += K::NTH) dst[w] = src[w];
+        int4 *dst = reinterpret_cast<int4 *>(sh_head);
+        for (int w = tid; w < kHead / 16; w += K::NTH) dst[w] = src[w];
         __syncthreads();
-        shp = &sh_s;
+        shp = reinterpret_cast<const Shot<S, C> *>(sh_head);
     } else {
         shp = &sh_param;
     }
@@ -500,7 +505,7 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
             for (int k = 0; k < nitems; ++k) {
                 const ItemInfo I = info[k];
                 const int tz0 = I.z0 / kPunchTZ, tz1 = (min(I.z1, nz) - 1) / kPunchTZ;
-                const int tx0 = I.x0 / kPunchTX, tx1 = (min(I.x0 + K::TX, nx) - 1) / kPunchTX;
+                const int tx0 = max(I.x0, 0) / kPunchTX, tx1 = (min(I.x0 + K::TX, nx) - 1) / kPunchTX;
                 for (int tz = tz0 + tid; tz <= tz1; tz += K::NTH) {
                     bool live = false;
                     for (int tx = tx0; tx <= tx1; ++tx) live |= !punch_steady(__ldg(&pu.win[tz * pu.nbx + tx]), it);
@@ -668,7 +673,9 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
         const int ntl = tcount[k];
         const int4 *tl = tlist + k * K::MAX_TERMS;
         const int x = I.x0 - 4 + 4 * lane;  // first of this thread's 4 cells
-        const bool own_x = lane >= 1 && lane <= 30;
+        // lanes 1 .. 30 own their cells (0 and 31: halo); a strip whose origin
+        // lies left of column 0 owns no cells there (x is a multiple of 4)
+        const bool own_x = lane >= 1 && lane <= 30 && x >= 0;
         // byte offset of this thread's 4 cells in a row of the index box
         const int ixo = ((kXPad + I.x0 - 4 - K::PWOFF) & 15) + K::PWOFF + 4 * lane;
         // the 4 cells are interior (8th order), outside the x-CPML and inside the grid
@@ -1013,7 +1020,7 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                 // the residual stress update before this launch (every column:
                 // halo columns feed the velocity stencil too).  Shared-memory
                 // copies only: the old stresses are still in the point-wise stage.
-                if constexpr (PSV && std::is_same<S, C>::value) {
+                if constexpr (PSV && std::is_same<S, C>::value && !BATCH) {  // batches have no box
                     const int aj = j - sh.box.z0 - 4, ai0 = x - sh.box.x0 - 4;
                     const int aw = sh.box.bx - 8, ah = sh.box.bz - 8;
                     if (sh.box.on && aj >= 0 && aj < ah && ai0 + 3 >= 0 && ai0 < aw &&

@@ -187,7 +187,8 @@ struct alignas(16) Shot {
     C *psim[8];
     const int4 *rec2;
     const int *rec2_off;
-    Box<C> box;         // hybrid box (box.on == 0: none); last, the batched sweep never reads it
+    Box<C> box;         // hybrid box (box.on == 0: none); single shots only
+    // (the batched sweep copies and reads the fields before maps2 only)
 };
 
 // Work list entry of the fused sweep: one x-strip of one shot, rows [z0, z1)
@@ -200,12 +201,14 @@ struct WorkItem {
 // on by CTAs [cta0[k], cta0[k] + ncta[k]).
 struct ShotGeom {
     int nx, nz, npml, topabsorb;
+    int xoff = 0;  // first strip's first column (plan_work sets it: a multiple of 8 in (-tile_x, 0])
 };
 struct TuneParams {
     double wx = 4.0, wz = 3.0;  // relative cost of 4-row blocks touching the x / z CPML
     int per_sm = 3;             // CTAs resident per SM the plan is sized for
     double oversub = 1.0;       // CTAs launched per resident slot
     int bands = 1;              // cut every strip on its own (plan_work)
+    int shift = 1;              // let plan_work move the strips' origin left of column 0
 };
 struct WorkPlan {
     std::vector<WorkItem> items;

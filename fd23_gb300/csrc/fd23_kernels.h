@@ -41,7 +41,7 @@ struct FusedBoxes {
 FusedBoxes fused_boxes(int wave, int prec);
 int fused_prepare(int wave, int prec);       // once per device before the first launch
 size_t fused_smem_bytes(int wave, int prec); // dynamic shared memory of one CTA
-int fused_occupancy(int wave, int prec);     // resident CTAs per SM (current device)
+int fused_occupancy(int wave, int prec, bool batch);  // resident CTAs per SM (current device)
 
 // One time step of every work item: reads buffer set `par`, writes `1-par`.
 // `rec_index` >= 0 gathers the receivers of the previous step from buffer set

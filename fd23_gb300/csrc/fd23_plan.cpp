@@ -1,6 +1,7 @@
 // Work plans of the fused sweep (host side).
 //
-// A shot is cut into strips of tile_x output columns and 4-row blocks.  Every
+// A shot is cut into strips of tile_x output columns (from an origin at or
+// left of column 0, best_xoff) and 4-row blocks.  Every
 // block gets an estimated cost (blocks that touch the CPML run the general
 // per-cell path and cost more: wx for the x-CPML, wz for the z-CPML and the
 // edge rows).  CTAs are shared out between shots in proportion to their cost,
@@ -11,6 +12,7 @@
 // the place of strips).
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 
 #include "fd23_internal.h"
 
@@ -18,14 +20,55 @@ namespace fd23 {
 
 namespace {
 
+// strip `strip` of a shot runs the CPML / reduced-order path in its x range
+// (its 4-column stress halos included)
+bool strip_xp(const ShotGeom &g, int tile_x, int strip)
+{
+    const int x0 = g.xoff + strip * tile_x;
+    return (x0 - 4 < std::max(g.npml, 4)) || (x0 + tile_x + 4 > std::min(g.nx - g.npml, g.nx - 4));
+}
+
+// cost of block row zb of a strip clear of the x-CPML
+double row_cost(const ShotGeom &g, int zb, const TuneParams &tp)
+{
+    const int r0 = 4 * zb, r1 = r0 + 3;
+    const bool zp = (r1 >= std::min(g.nz - g.npml, g.nz - 4)) || r0 < 4 || (g.topabsorb && r0 < g.npml);
+    return zp ? tp.wz : 1.0;
+}
+
 // cost of block (strip, zb) of a shot
 double block_cost(const ShotGeom &g, int tile_x, int strip, int zb, const TuneParams &tp)
 {
-    const int x0 = strip * tile_x;
-    const bool xp = (x0 - 4 < std::max(g.npml, 4)) || (x0 + tile_x + 4 > std::min(g.nx - g.npml, g.nx - 4));
-    const int r0 = 4 * zb, r1 = r0 + 3;
-    const bool zp = (r1 >= std::min(g.nz - g.npml, g.nz - 4)) || r0 < 4 || (g.topabsorb && r0 < g.npml);
-    return xp ? tp.wx : (zp ? tp.wz : 1.0);
+    return strip_xp(g, tile_x, strip) ? tp.wx : row_cost(g, zb, tp);
+}
+
+int strips_of(const ShotGeom &g, int tile_x) { return (g.nx - g.xoff + tile_x - 1) / tile_x; }
+
+// Strip origin of a shot: the multiple of 8 in (-tile_x, 0] whose strips
+// cost least in total (ties: the one nearest 0).  Moving the origin left
+// can put both x-CPML zones and their 4-column halos into fewer strips: on
+// the 4000-column grid with a 40-cell CPML, origin 0 makes three strips run
+// the CPML path (0, 32 and 33, strip 32 through its halo only), origin -40
+// two.  Copies that start left of column -8 read zeros, as the padding
+// columns hold.
+int best_xoff(ShotGeom g, int tile_x, const TuneParams &tp)
+{
+    const int nzb = (g.nz + 3) / 4;
+    double interior = 0.0;
+    for (int zb = 0; zb < nzb; ++zb) interior += row_cost(g, zb, tp);
+    int best = 0;
+    double best_cost = 0.0;
+    for (int xo = 0; xo > -tile_x; xo -= 8) {
+        g.xoff = xo;
+        double cost = 0.0;
+        const int ntx = strips_of(g, tile_x);
+        for (int s = 0; s < ntx; ++s) cost += strip_xp(g, tile_x, s) ? tp.wx * nzb : interior;
+        if (xo == 0 || cost < best_cost - 1e-9) {
+            best = xo;
+            best_cost = cost;
+        }
+    }
+    return best;
 }
 
 // Banded cut of one shot (every block planned) for n CTAs: every strip is
@@ -36,7 +79,7 @@ double block_cost(const ShotGeom &g, int tile_x, int strip, int zb, const TunePa
 // same row boundaries, so neighbouring strips sweep the same rows at the same
 // time and the columns their copies share are still in L2 for the second
 // reader.  False (nothing added) when there are fewer CTAs than strips.
-bool cut_bands(const std::vector<double> &c, int shot, int ntx, int nzb, int tile_x, int n, WorkPlan &plan)
+bool cut_bands(const std::vector<double> &c, int shot, int xoff, int ntx, int nzb, int tile_x, int n, WorkPlan &plan)
 {
     if (n < ntx) return false;
     std::vector<double> cost(ntx);
@@ -67,7 +110,7 @@ bool cut_bands(const std::vector<double> &c, int shot, int ntx, int nzb, int til
                 b1 = std::max(b1, b0 + 1);
                 b1 = std::min(b1, (long long)nzb - (ns[s] - 1 - q));
             }
-            plan.items.push_back(WorkItem{shot, s * tile_x, (int)b0 * 4, (int)b1 * 4});
+            plan.items.push_back(WorkItem{shot, xoff + s * tile_x, (int)b0 * 4, (int)b1 * 4});
             plan.off.push_back((int)plan.items.size());
             b0 = b1;
         }
@@ -120,9 +163,18 @@ int plan_work(const std::vector<ShotGeom> &shots, int tile_x, int sms, const Tun
     std::vector<long long> nbk(ns);
     double total = 0.0;
     long long sum_min = 0;
+    // strip origins: planned over every block, the cheapest; with a live mask
+    // (laid out over strips from column 0) at column 0
+    // (FD23_STRIP_SHIFT=0 in the environment keeps every origin at column 0)
+    static const bool no_shift = [] {
+        const char *v = std::getenv("FD23_STRIP_SHIFT");
+        return v && std::atoi(v) == 0;
+    }();
+    std::vector<ShotGeom> geo(shots);
+    for (auto &g : geo) g.xoff = (!live && tp.shift && !no_shift) ? best_xoff(g, tile_x, tp) : 0;
     for (int k = 0; k < ns; ++k) {
-        const ShotGeom &g = shots[k];
-        const int ntx = (g.nx + tile_x - 1) / tile_x;
+        const ShotGeom &g = geo[k];
+        const int ntx = strips_of(g, tile_x);
         nzb[k] = (g.nz + 3) / 4;
         const long long all = (long long)ntx * nzb[k];
         if (live && (long long)(*live)[k].size() != all) return FD23_ERR_ARG;
@@ -194,7 +246,8 @@ int plan_work(const std::vector<ShotGeom> &shots, int tile_x, int sms, const Tun
     for (int k = 0; k < ns; ++k) {
         plan.cta0[k] = (int)plan.off.size() - 1;
         if (nbk[k] == 0) continue;  // nothing to do for this shot
-        if (tp.bands && !live && cut_bands(cum[k], k, (shots[k].nx + tile_x - 1) / tile_x, nzb[k], tile_x, nc[k], plan)) {
+        if (tp.bands && !live &&
+            cut_bands(cum[k], k, geo[k].xoff, strips_of(geo[k], tile_x), nzb[k], tile_x, nc[k], plan)) {
             plan.ncta[k] = (int)plan.off.size() - 1 - plan.cta0[k];
             continue;
         }
@@ -213,7 +266,8 @@ int plan_work(const std::vector<ShotGeom> &shots, int tile_x, int sms, const Tun
                 const long long e = std::min(b1, rend);
                 const long long first = blk[k][b0], last = blk[k][e - 1];
                 const int strip = (int)(first / nzb[k]);
-                plan.items.push_back(WorkItem{k, strip * tile_x, (int)(first % nzb[k]) * 4, (int)(last % nzb[k] + 1) * 4});
+                plan.items.push_back(
+                    WorkItem{k, geo[k].xoff + strip * tile_x, (int)(first % nzb[k]) * 4, (int)(last % nzb[k] + 1) * 4});
                 b0 = e;
             }
             plan.off.push_back((int)plan.items.size());

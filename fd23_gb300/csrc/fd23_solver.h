@@ -137,7 +137,7 @@ int ensure_sigma(fd23_solver *s);
 int ensure_record_capacity(fd23_solver *s, int need);
 int dispatch_flush(fd23_solver *s);
 int zero_state(fd23_solver *s);
-int fused_per_sm(int device, int wave, int prec);
+int fused_per_sm(int device, int wave, int prec, bool batch = false);
 int upload_plan(const WorkPlan &plan, WorkItem **d_items, int **d_off);
 int build_worklist(fd23_solver *s);
 int build_worklist2(fd23_solver *s);

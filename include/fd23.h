@@ -346,6 +346,9 @@ typedef struct {
 int fd23_autotune(fd23_solver *s, int trial_steps, fd23_tune_entry *table, int cap);
 int fd23_batch_autotune(fd23_batch *b, int trial_steps, fd23_tune_entry *table, int cap);
 int fd23_batch_get_plan(fd23_batch *b, fd23_tune_entry *current, int *nblocks);
+/* fd23_batch_set_plan installs a plan for the batch without timing it (the
+ * arguments of fd23_set_plan). */
+int fd23_batch_set_plan(fd23_batch *b, const fd23_tune_entry *tune);
 /* fd23_set_plan installs a plan without timing it (ms_per_step ignored;
  * per_sm is capped at the residency the device reports; oversub in
  * [1, 64]); fd23_get_plan reports the current one and its CTA count. */
@@ -354,14 +357,17 @@ int fd23_get_plan(fd23_solver *s, fd23_tune_entry *current, int *nblocks);
 /* The work plan for nshots grids under the given parameters (host only, for
  * inspection and tests): items receives 4 ints per item (shot, x0, z0, z1:
  * 120 columns from x0, rows [z0, z1)), off[c] .. off[c+1] indexes the items of
- * CTA c (off needs cap_ctas + 1 entries).  Returns the CTA count. */
+ * CTA c (off needs cap_ctas + 1 entries).  Returns the CTA count.  A shot's
+ * strips start at a column xoff, a multiple of 8 in (-120, 0], chosen so that
+ * the x-CPML zones fall into the fewest strips (x0 = xoff + 120 k; columns
+ * left of 0 are outside the grid). */
 int fd23_work_plan(int nshots, const int *nx, const int *nz, const int *npml, const int *topabsorb,
                    int sms, const fd23_tune_entry *tune, int *items, int cap_items, int *off,
                    int cap_ctas);
 /* The same over the live 4-row blocks only (the phase plans of the sweep
  * with tile step windows): live holds, shot after shot, one byte per block
- * (strip-major: strip * ceil(nz/4) + block, 120-column strips); a shot with
- * no live block gets no CTA. */
+ * (strip-major: strip * ceil(nz/4) + block, 120-column strips from column 0);
+ * a shot with no live block gets no CTA. */
 int fd23_work_plan_live(int nshots, const int *nx, const int *nz, const int *npml, const int *topabsorb,
                         int sms, const fd23_tune_entry *tune, const unsigned char *live, int *items,
                         int cap_items, int *off, int cap_ctas);

@@ -63,7 +63,10 @@ def smem_layout(es, wave):
 
 
 def box_ok(x, y, z, w, nf, pitch, rows, nfields, es):
-    assert x >= 0 and x + w <= pitch, (x, w, pitch)
+    # a copy may start left of the array (strips whose origin lies left of
+    # column 0) or end past its last column: those elements read as zero,
+    # as the padding columns hold; it must overlap the array
+    assert x + w > 0 and x < pitch, (x, w, pitch)
     assert y >= 0 and y + 4 <= rows, (y, rows)
     assert z >= 0 and z + nf <= nfields
     assert (x * es) % 16 == 0 and (w * es) % 16 == 0
@@ -88,6 +91,10 @@ def audit(nx, nz, es, wave, per_sm=3, oversub=1.0, ctas=None, narrowed=False, ba
     if ctas is None:
         ctas = worklist(nx, nz, npml, oversub, per_sm, bands)
     covered = set()
+    # strip origin: a multiple of 8 in (-TX, 0], congruent to every x0 mod TX
+    r = min(x0 for items in ctas for (x0, _, _) in items) % TX if any(ctas) else 0
+    xoff = r - TX if r else 0
+    assert -TX < xoff <= 0 and xoff % 8 == 0
     for items in ctas:
         assert (0 if narrowed else 1) <= len(items) <= MAX_ITEMS
         for (x0, z0, z1) in items:
@@ -96,7 +103,7 @@ def audit(nx, nz, es, wave, per_sm=3, oversub=1.0, ctas=None, narrowed=False, ba
                 assert key not in covered  # every block exactly once
                 covered.add(key)
         for (x0, z0, z1) in items:
-            assert x0 % TX == 0 and z0 % 4 == 0 and z1 % 4 == 0 and z1 > z0
+            assert (x0 - xoff) % TX == 0 and z0 % 4 == 0 and z1 % 4 == 0 and z1 > z0
             niter = (z1 - z0) // 4 + 2
             # stencil-input copies: blocks 0 .. niter+1, rows z0-8+4b .. +3
             for b in (0, niter + 1):
@@ -121,13 +128,13 @@ def audit(nx, nz, es, wave, per_sm=3, oversub=1.0, ctas=None, narrowed=False, ba
                         assert pwoff + 4 * q + 3 < pww
                         assert 4 * q + 3 < SW  # stress ring write
                         x = x0 - 4 + 4 * q
-                        if 0 <= j < nz and z0 <= j < z1 and 1 <= q <= 30 and x < nx:
+                        if 0 <= j < nz and z0 <= j < z1 and 1 <= q <= 30 and 0 <= x < nx:
                             o = origin + j * pitch + x
                             assert 0 <= o and o + 3 < elems
                             assert ((XPAD + x) * es) % min(16, 4 * es) == 0
                         # velocity phase
                         a = z0 - 8 + 4 * i + g
-                        if a >= z0 and a < nz and 1 <= q <= 30 and x < nx:
+                        if a >= z0 and a < nz and 1 <= q <= 30 and 0 <= x < nx:
                             assert i >= 2
                             blk = (a - (z0 - 8)) // 4
                             assert blk == i
@@ -197,7 +204,7 @@ def narrow(nx, nz, items, first, last, it, terms=()):
     out = []
     for (x0, z0, z1) in items:
         rows = [tz for tz in range(z0 // 16, (min(z1, nz) - 1) // 16 + 1)
-                if any(not steady(tz * nbx + tx) for tx in range(x0 // 32, (min(x0 + TX, nx) - 1) // 32 + 1))]
+                if any(not steady(tz * nbx + tx) for tx in range(max(x0, 0) // 32, (min(x0 + TX, nx) - 1) // 32 + 1))]
         rows += [tz // 16 for (tx, tz) in terms if x0 <= tx < x0 + TX and z0 <= tz < z1]
         if not rows:
             continue
@@ -233,7 +240,10 @@ def test_table_index_box_in_bounds(nx, nz, es, wave):
     of kIdxBoxW = 160 from the 16-byte boundary at or before the point-wise
     copy's start: x is a multiple of 16 bytes, the rows lie inside the
     padded index array, every thread's 4 index bytes lie inside the box and
-    are 4-byte aligned, and the stage layout stays 128-byte aligned."""
+    are 4-byte aligned, and the stage layout stays 128-byte aligned.  Index
+    bytes of columns left of the array (strips whose origin lies left of
+    column 0) read as index 0: those cells are outside the grid, their
+    results are never stored."""
     IW = 160
     pitch, rows, origin = layout(nx, nz)
     lay = smem_layout(es, wave)
@@ -246,7 +256,8 @@ def test_table_index_box_in_bounds(nx, nz, es, wave):
             niter = (z1 - z0) // 4 + 2
             xs = XPAD + x0 - 4 - lay["pwoff"]
             xa = xs & ~15
-            assert xa >= 0 and xa % 16 == 0 and xa <= xs
+            # left of the array (a strip origin left of column 0) the copy reads zeros
+            assert xa + IW > 0 and xa % 16 == 0 and xa <= xs
             for i in (0, niter - 1):
                 yv = ZPAD + z0 - 8 + 4 * i
                 assert yv >= 0 and yv + 8 <= rows
@@ -290,7 +301,13 @@ def test_live_mask_plans(nx, nz, density):
         if mask.any():
             audit(nx, nz, 4, "psv", ctas=[[it[1:] for it in c] for c in ctas], narrowed=True)
     full = F.work_plan([(nx, nz, npml, 0)], wx=5.0, wz=4.0, live=[np.ones(ntx * nzb, bool)])
-    assert full == F.work_plan([(nx, nz, npml, 0)], wx=5.0, wz=4.0, bands=0)
+    plain = F.work_plan([(nx, nz, npml, 0)], wx=5.0, wz=4.0, bands=0)
+    # masks are laid out over strips from column 0; the ordinary plan may move
+    # its origin left (then only the block coverage is the same)
+    if min(it[1] for cta in plain for it in cta) == 0:
+        assert full == plain
+    else:
+        assert all(it[1] % TX == 0 for cta in full for it in cta)
 
 
 @pytest.mark.parametrize("nx,nz,npml", [(4000, 2000, 40), (16000, 8000, 40), (800, 400, 20), (1000, 1000, 20),
@@ -308,8 +325,7 @@ def test_banded_plan_covers_grid_with_shared_row_cuts(nx, nz, npml, ov):
         pytest.skip(str(e))
     ref = F.work_plan([(nx, nz, npml, 0)], wx=5.0, wz=2.5, oversub=ov, bands=0)
     ctas = F.work_plan([(nx, nz, npml, 0)], wx=5.0, wz=2.5, oversub=ov, bands=1)
-    ntx = (nx + TX - 1) // TX
-    if len(ref) < ntx:  # fewer CTAs than strips: the strip-major plan
+    if len(ref) < len({it[1] for cta in ref for it in cta}):  # fewer CTAs than strips: strip-major
         assert ctas == ref
         return
     assert len(ctas) <= len(ref)
@@ -318,7 +334,10 @@ def test_banded_plan_covers_grid_with_shared_row_cuts(nx, nz, npml, ov):
         assert len(cta) == 1
         (_, x0, z0, z1), = cta
         cuts.setdefault(x0, []).append((z0, z1))
-    assert sorted(cuts) == [TX * s for s in range(ntx)]
+    xoff = min(cuts)
+    assert -TX < xoff <= 0 and xoff % 8 == 0
+    ntx = (nx - xoff + TX - 1) // TX
+    assert sorted(cuts) == [xoff + TX * s for s in range(ntx)]
     nzb = (nz + 3) // 4
     for x0, c in cuts.items():
         c.sort()
@@ -327,3 +346,38 @@ def test_banded_plan_covers_grid_with_shared_row_cuts(nx, nz, npml, ov):
     interior = [x0 for x0 in cuts if x0 - 4 >= max(npml, 4) and x0 + TX + 4 <= min(nx - npml, nx - 4)]
     assert len({tuple(cuts[x0]) for x0 in interior}) <= 1
     audit(nx, nz, 4, "psv", ctas=[[it[1:] for it in cta] for cta in ctas])
+
+
+def _xp_strips(nx, npml, x0s):
+    """strips whose 128 stress columns reach the x-CPML or the reduced-order
+    edge columns (the planner's x-CPML strips)"""
+    return [x0 for x0 in x0s if x0 - 4 < max(npml, 4) or x0 + TX + 4 > min(nx - npml, nx - 4)]
+
+
+@pytest.mark.parametrize("nx,nz,npml,want_xp", [(4000, 2000, 40, 2), (16000, 8000, 40, 2), (2000, 1000, 40, 2),
+                                                 (800, 400, 20, 2)])
+def test_strip_origin_puts_the_cpml_into_fewest_strips(nx, nz, npml, want_xp):
+    """The planner moves the strips' origin left of column 0 (a multiple of
+    8 above -120) when that puts the x-CPML zones and their halos into fewer
+    strips: on the 4000-column grid with a 40-cell CPML, two CPML strips
+    (origin 0 gives three: 0, 32 and 33)."""
+    F = pytest.importorskip("fd23_gb300")
+    try:
+        F.lib()
+    except ImportError as e:
+        pytest.skip(str(e))
+    for bands in (0, 1):
+        ctas = F.work_plan([(nx, nz, npml, 0)], wx=5.0, wz=2.5, bands=bands)
+        x0s = sorted({it[1] for cta in ctas for it in cta})
+        xoff = x0s[0]
+        assert -TX < xoff <= 0 and xoff % 8 == 0
+        assert x0s == [xoff + TX * s for s in range(len(x0s))] and x0s[-1] + TX >= nx
+        assert len(_xp_strips(nx, npml, x0s)) == want_xp
+        # no origin puts the CPML into fewer strips
+        for xo in range(0, -TX, -8):
+            cand = [xo + TX * s for s in range((nx - xo + TX - 1) // TX)]
+            assert len(_xp_strips(nx, npml, cand)) >= want_xp
+    if (nx, npml) == (4000, 40):
+        import numpy as np
+        ref = F.work_plan([(nx, nz, npml, 0)], wx=5.0, wz=2.5, bands=0, live=[np.ones(34 * ((nz + 3) // 4), bool)])
+        assert len(_xp_strips(nx, npml, sorted({it[1] for cta in ref for it in cta}))) == 3
