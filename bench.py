@@ -664,21 +664,29 @@ def bench_box(args, F, torch, rank, world, local, dist):
     if not args.no_e2e:
         hvp, hvs, hrho = (pinned_copy(torch, a) for a in (vp, vs, rho))
         hsu, hsw = (pinned_like(torch, s.seismograms(f)) for f in (0, 1))
-        times = []
+        times, parts = [], []
         seis_bytes = 0
         for _ in range(max(1, min(args.steps, 2))):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             s.set_model(hvp, hvs, hrho)
+            t1 = time.perf_counter()
             s.set_box(BOX_X0, BOX_Z0, BOX_BX, BOX_BZ)
+            t2 = time.perf_counter()
             s.set_box_incident(inc, 0)
+            t3 = time.perf_counter()
             shot()
             su, sw = s.seismograms(0, hsu), s.seismograms(1, hsw)
-            times.append(time.perf_counter() - t0)
+            t4 = time.perf_counter()
+            times.append(t4 - t0)
+            # host-side milliseconds of each call (the run's launches are asynchronous:
+            # its time lands in the seismogram read that waits for it)
+            parts.append({"set_model": round((t1 - t0) * 1e3, 1), "set_box": round((t2 - t1) * 1e3, 1),
+                          "set_box_incident": round((t3 - t2) * 1e3, 1), "run_and_read": round((t4 - t3) * 1e3, 1)})
             seis_bytes = su.nbytes + sw.nbytes
         e2e = {"value": NX * NZ * nt / statistics.mean(times) * world, "unit": "cell-updates/s",
                "h2d_bytes_per_step": 3 * NX * NZ * 8 + inc.nbytes, "d2h_bytes_per_step": seis_bytes,
-               "shot_ms": [round(t * 1e3, 1) for t in times],
+               "shot_ms": [round(t * 1e3, 1) for t in times], "parts_ms": parts,
                "note": "per step = one whole box shot; the incident field is uploaded from pinned "
                        "host memory inside the timed region"}
     hbm, peak_kind = load_peaks()
