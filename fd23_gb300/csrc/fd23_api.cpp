@@ -183,12 +183,14 @@ int step2_impl(fd23_solver *s, int rec_now, int rec_next)
 // (PD/main.cpp:153-199 order; the exchanges that read only fields the next
 // update leaves unchanged run earlier, with the same values).
 template <class S, class C>
-int step_impl(fd23_solver *s, int rec_now)
+int step_impl(fd23_solver *s, int rec_now, int more)
 {
     Shot<S, C> sh = make_shot<S, C>(s);
     const bool box = s->box_on;
     int rc = FD23_OK;
-    if (box && (rc = launch_box_pre<S, C>(sh, s->fused ? s->par : 0, s->fused, s->stream))) return rc;
+    if (box && !s->box_pre_ahead && (rc = launch_box_pre<S, C>(sh, s->fused ? s->par : 0, s->fused, s->stream)))
+        return rc;
+    s->box_pre_ahead = false;
     if (s->fused) {
         const WorkItem *items = s->d_items;
         const int *off = s->d_item_off;
@@ -215,7 +217,13 @@ int step_impl(fd23_solver *s, int rec_now)
     }
     if (box) {
         const int ri = rec_now ? s->nrec_steps++ : -1;
-        if ((rc = launch_box_post<S, C>(sh, s->fused ? s->par : 0, s->fused, ri, s->stream))) return rc;
+        // the fused sweep with another step to come: this step's end and the
+        // next step's start as one launch where the box allows it
+        rc = FD23_ERR_UNSUPPORTED;
+        if (s->fused && more) rc = launch_box_mid<S, C>(sh, s->par, ri, s->stream);
+        if (rc == FD23_OK) s->box_pre_ahead = true;
+        else if (rc != FD23_ERR_UNSUPPORTED) return rc;
+        else if ((rc = launch_box_post<S, C>(sh, s->fused ? s->par : 0, s->fused, ri, s->stream))) return rc;
     }
     s->it++;
     return FD23_OK;
@@ -231,13 +239,13 @@ int flush_records(fd23_solver *s)
     return rc;
 }
 
-int dispatch_step(fd23_solver *s, int rec_now)
+int dispatch_step(fd23_solver *s, int rec_now, int more)
 {
     switch (s->d.prec) {
-        case FD23_F64: return step_impl<double, double>(s, rec_now);
-        case FD23_BF16: return step_impl<__nv_bfloat16, float>(s, rec_now);
-        case FD23_F16: return step_impl<__half, float>(s, rec_now);
-        default: return step_impl<float, float>(s, rec_now);
+        case FD23_F64: return step_impl<double, double>(s, rec_now, more);
+        case FD23_BF16: return step_impl<__nv_bfloat16, float>(s, rec_now, more);
+        case FD23_F16: return step_impl<__half, float>(s, rec_now, more);
+        default: return step_impl<float, float>(s, rec_now, more);
     }
 }
 int dispatch_persist(fd23_solver *s, int nsteps, int itrecord, int any_rec)
@@ -995,8 +1003,11 @@ int fd23_run(fd23_solver *s, int nsteps, int itrecord)
             k += 2;
             continue;
         }
-        int rc = dispatch_step(s, rec_now);
-        if (rc) return rc;
+        int rc = dispatch_step(s, rec_now, k + 1 < nsteps);
+        if (rc) {
+            s->box_pre_ahead = false;
+            return rc;
+        }
         ++k;
     }
     return dispatch_flush(s);

@@ -41,8 +41,9 @@ __device__ __forceinline__ C dplus_r(const C *p, long long s)
 
 // ring exchange of fields F0 .. F1-1 on buffer set `par`, ring positions
 // [0, qend) (qend = nsub: the sub ring only)
+// (inc: the step's incident field, [5][nring])
 template <class S, class C, int F0, int F1>
-__device__ __forceinline__ void ring_cell(const Shot<S, C> &s, int par, int q)
+__device__ __forceinline__ void ring_cell(const Shot<S, C> &s, int par, int q, const C *inc)
 {
     const Box<C> &b = s.box;
     const int2 c = b.cells[q];
@@ -52,7 +53,7 @@ __device__ __forceinline__ void ring_cell(const Shot<S, C> &s, int par, int q)
 #pragma unroll
     for (int f = F0; f < F1; ++f) {
         S *G = par ? s.f[1][f] : s.f[0][f];
-        const C sv = b.inc[(long long)f * b.nring + q];
+        const C sv = inc[(long long)f * b.nring + q];
         if (add) G[g] = to_s<S>(b.r[f][r] + sv);
         else b.r[f][r] = to_c<C>(G[g]) - sv;
     }
@@ -73,7 +74,7 @@ __global__ void __launch_bounds__(256) box_ring_kernel(Shot<S, C> s, int par, in
 {
     pdl_enter();
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < qend; q += gridDim.x * blockDim.x)
-        ring_cell<S, C, F0, F1>(s, par, q);
+        ring_cell<S, C, F0, F1>(s, par, q, s.box.inc);
 }
 
 // residual stress update of box cell (ix, iz), 4 <= ix, iz < n-4; the
@@ -81,7 +82,7 @@ __global__ void __launch_bounds__(256) box_ring_kernel(Shot<S, C> s, int par, in
 // On add-ring cells it also stores g = r + s into the grid stresses of
 // buffer set `par` (the fused sweep's old-stress slot); add_g = 0 skips that.
 template <class S, class C>
-__device__ __forceinline__ void stress_r_cell(const Shot<S, C> &s, int par, int add_g, int ix, int iz)
+__device__ __forceinline__ void stress_r_cell(const Shot<S, C> &s, int par, int add_g, int ix, int iz, const C *inc)
 {
     const Box<C> &b = s.box;
     const long long o = (long long)iz * b.bx + ix, P = b.bx;
@@ -107,7 +108,7 @@ __device__ __forceinline__ void stress_r_cell(const Shot<S, C> &s, int par, int 
 #pragma unroll
             for (int f = 0; f < 3; ++f) {
                 S *G = par ? s.f[1][2 + f] : s.f[0][2 + f];
-                G[g] = to_s<S>(t[f] + b.inc[(long long)(2 + f) * b.nring + q]);
+                G[g] = to_s<S>(t[f] + inc[(long long)(2 + f) * b.nring + q]);
             }
         }
     }
@@ -119,7 +120,7 @@ __global__ void __launch_bounds__(256) box_stress_r(Shot<S, C> s, int par, int a
     pdl_enter();
     const int ix = 4 + blockIdx.x * 32 + threadIdx.x, iz = 4 + blockIdx.y * 8 + threadIdx.y;
     if (ix >= s.box.bx - 4 || iz >= s.box.bz - 4) return;
-    stress_r_cell<S, C>(s, par, add_g, ix, iz);
+    stress_r_cell<S, C>(s, par, add_g, ix, iz, s.box.inc);
 }
 
 // receivers of this step's output (buffer set `par`, before the next ring
@@ -179,33 +180,59 @@ constexpr int kSmallThreads = 1024;
 // before the sweep: ring U, W (sub: r = g - s, add: g = r + s), then the
 // residual stress update (+ g = r + s on the add ring for the fused sweep)
 template <class S, class C>
+__device__ __forceinline__ void small_pre_body(const Shot<S, C> &s, int par, int add_g, const C *inc)
+{
+    const Box<C> &b = s.box;
+    const int t = threadIdx.x;
+    for (int q = t; q < b.nring; q += kSmallThreads) ring_cell<S, C, 0, 2>(s, par, q, inc);
+    __syncthreads();
+    const int w = b.bx - 8, n = w * (b.bz - 8);
+    for (int k = t; k < n; k += kSmallThreads) stress_r_cell<S, C>(s, par, add_g, 4 + k % w, 4 + k / w, inc);
+}
+
+template <class S, class C>
 __global__ void __launch_bounds__(kSmallThreads, 1) box_small_pre(Shot<S, C> s, int par, int add_g)
 {
     pdl_enter();
-    const Box<C> &b = s.box;
-    const int t = threadIdx.x;
-    for (int q = t; q < b.nring; q += kSmallThreads) ring_cell<S, C, 0, 2>(s, par, q);
-    __syncthreads();
-    const int w = b.bx - 8, n = w * (b.bz - 8);
-    for (int k = t; k < n; k += kSmallThreads) stress_r_cell<S, C>(s, par, add_g, 4 + k % w, 4 + k / w);
+    small_pre_body<S, C>(s, par, add_g, s.box.inc);
 }
 
 // after the sweep: sub-ring stresses r = g - s (fused sweep only; the
 // two-pass sweep did the whole exchange), then this step's receivers and
 // the residual velocity update
 template <class S, class C>
-__global__ void __launch_bounds__(kSmallThreads, 1) box_small_post(Shot<S, C> s, int par, int sub_t, int rec_index)
+__device__ __forceinline__ void small_post_body(const Shot<S, C> &s, int par, int sub_t, int rec_index)
 {
-    pdl_enter();
     const Box<C> &b = s.box;
     const int t = threadIdx.x;
     if (sub_t) {
-        for (int q = t; q < b.nsub; q += kSmallThreads) ring_cell<S, C, 2, 5>(s, par, q);
+        for (int q = t; q < b.nsub; q += kSmallThreads) ring_cell<S, C, 2, 5>(s, par, q, b.inc);
         __syncthreads();
     }
     if (rec_index >= 0) box_receivers<S, C>(s, par, rec_index, t, kSmallThreads);
     const int w = b.bx - 8, n = w * (b.bz - 8);
     for (int k = t; k < n; k += kSmallThreads) velocity_r_cell<S, C>(s, 4 + k % w, 4 + k / w);
+}
+
+template <class S, class C>
+__global__ void __launch_bounds__(kSmallThreads, 1) box_small_post(Shot<S, C> s, int par, int sub_t, int rec_index)
+{
+    pdl_enter();
+    small_post_body<S, C>(s, par, sub_t, rec_index);
+}
+
+// Between two steps of the fused sweep: the end of one step and the start of
+// the next in one CTA, a barrier in place of a kernel boundary.  No sweep
+// runs between them, so both work on buffer set `par`; the next step's
+// incident field is inc_next.
+template <class S, class C>
+__global__ void __launch_bounds__(kSmallThreads, 1)
+    box_small_mid(Shot<S, C> s, int par, int rec_index, const C *inc_next)
+{
+    pdl_enter();
+    small_post_body<S, C>(s, par, 1, rec_index);
+    __syncthreads();
+    small_pre_body<S, C>(s, par, 1, inc_next);
 }
 
 // boxes whose interior and rings each fit a few passes of one CTA
@@ -266,10 +293,19 @@ int launch_box_post(const Shot<S, C> &s, int par, int fused, int rec_index, cuda
     return launch_pdl(box_velocity_r<S, C>, interior_grid(s.box.bx, s.box.bz), dim3(32, 8), st, s, par, rec_index);
 }
 
+template <class S, class C>
+int launch_box_mid(const Shot<S, C> &s, int par, int rec_index, cudaStream_t st)
+{
+    if (!small_box(s.box)) return FD23_ERR_UNSUPPORTED;
+    const C *inc_next = s.box.inc + (size_t)5 * s.box.nring;
+    return launch_pdl(box_small_mid<S, C>, dim3(1), dim3(kSmallThreads), st, s, par, rec_index, inc_next);
+}
+
 #define FD23_INST(S, C)                                                                  \
     template int launch_box_ring<S, C>(const Shot<S, C> &, int, int, cudaStream_t);     \
     template int launch_box_pre<S, C>(const Shot<S, C> &, int, int, cudaStream_t);      \
-    template int launch_box_post<S, C>(const Shot<S, C> &, int, int, int, cudaStream_t);
+    template int launch_box_post<S, C>(const Shot<S, C> &, int, int, int, cudaStream_t); \
+    template int launch_box_mid<S, C>(const Shot<S, C> &, int, int, cudaStream_t);
 FD23_INST(float, float)
 FD23_INST(double, double)
 FD23_INST(__nv_bfloat16, float)

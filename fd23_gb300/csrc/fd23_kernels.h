@@ -65,6 +65,12 @@ int launch_box_pre(const Shot<S, C> &s, int par, int fused, cudaStream_t st);
 // then the residual velocity update
 template <class S, class C>
 int launch_box_post(const Shot<S, C> &s, int par, int fused, int rec_index, cudaStream_t st);
+// fused sweep, boxes of the one-CTA path: launch_box_post of this step and
+// launch_box_pre of the next (incident field of step it+1 following that of
+// step it) as one launch; FD23_ERR_UNSUPPORTED (nothing launched) for boxes
+// too large for it
+template <class S, class C>
+int launch_box_mid(const Shot<S, C> &s, int par, int rec_index, cudaStream_t st);
 
 // The same sweep over several shots in one launch: `shots` = device array of
 // shot descriptors; every CTA's items belong to one shot (a WorkPlan).

@@ -124,6 +124,9 @@ struct fd23_solver {
     void *box_inc = nullptr;
     size_t box_inc_bytes = 0;
     int box_inc_it0 = 0, box_inc_n = 0;
+    // the box's start-of-step work of step `it` already ran (with the end of
+    // the step before, launch_box_mid)
+    bool box_pre_ahead = false;
 };
 
 namespace fd23 {
@@ -141,7 +144,8 @@ int fused_per_sm(int device, int wave, int prec, bool batch = false);
 int upload_plan(const WorkPlan &plan, WorkItem **d_items, int **d_off);
 int build_worklist(fd23_solver *s);
 int build_worklist2(fd23_solver *s);
-int dispatch_step(fd23_solver *s, int rec_now);
+// one step; more != 0: another step follows in the same run
+int dispatch_step(fd23_solver *s, int rec_now, int more = 0);
 // copies buffer set `par` (wavefields, memory variables) into the other set
 int mirror_sets(fd23_solver *s, cudaStream_t st);
 // the phase plan of step s->it (fd23_punch.cpp): slot of s->phase to use
