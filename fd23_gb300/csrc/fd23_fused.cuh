@@ -384,13 +384,16 @@ struct Cfg {
     static constexpr int MAX_ITEMS = 4;
     static constexpr int MAX_TERMS = 16;
     // CTAs per SM the register budget is built for: three (shared memory
-    // allows three) except FP64 (one); the single-shot P-SV 16-bit sweep is
-    // built for two, which it runs faster with while still fitting three
-    // (measured; the batched and SH 16-bit sweeps would grow past three)
+    // allows three) except FP64 (one).  With the stress ring in the
+    // arithmetic type, a two-CTA budget let the single-shot P-SV 16-bit
+    // sweep grow to 144 registers (two CTAs per SM), C1 FP16 7.67e10
+    // cell-updates/s against 8.71e10 with three (measured)
     template <bool BATCH>
-    static constexpr int minb() { return sizeof(S) == 8 ? 1 : (sizeof(S) == 2 && PSV && !BATCH ? 2 : 3); }
+    static constexpr int minb() { return sizeof(S) == 8 ? 1 : 3; }
+    // the stress ring holds arithmetic-type values (rounded through S when
+    // written): the velocity update reads each of them many times
     static constexpr size_t RING_BYTES =
-        (((size_t)(UW_ELEMS + PW_ELEMS + TR_ELEMS + TAB_ELEMS) * sizeof(S) + 15) & ~(size_t)15);
+        (((size_t)(UW_ELEMS + PW_ELEMS + TAB_ELEMS) * sizeof(S) + (size_t)TR_ELEMS * sizeof(C) + 15) & ~(size_t)15);
     static constexpr size_t SMEM = RING_BYTES + 256 /* 2*(NUW+NPW) barriers */ + MAX_ITEMS * 16 +
                                    (size_t)MAX_ITEMS * MAX_TERMS * 16;
 };
@@ -427,8 +430,8 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
     }
     S *uw_s = reinterpret_cast<S *>(smem_raw);
     S *pw_s = uw_s + K::UW_ELEMS;
-    S *tr_s = pw_s + K::PW_ELEMS;
-    S *tab_s = tr_s + K::TR_ELEMS;  // the material table (TABLE only)
+    C *tr_s = reinterpret_cast<C *>(pw_s + K::PW_ELEMS);  // stress ring (arithmetic type)
+    S *tab_s = reinterpret_cast<S *>(tr_s + K::TR_ELEMS);  // the material table (TABLE only)
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw + K::RING_BYTES);
     uint64_t *full_uw = bars, *empty_uw = bars + K::NUW;
     uint64_t *full_pw = bars + 2 * K::NUW, *empty_pw = full_pw + K::NPW;
@@ -994,9 +997,14 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                             for (int e = 0; e < 4; ++e) tnew[f][e] = told[f][e];
                 }
                 // ---- stress ring (every column) ----
-                S *tr = tr_s + ((4 * gflat + grp) & (4 * K::NTR - 1)) * (K::NT * K::SW) + 4 * lane;
+                C *tr = tr_s + ((4 * gflat + grp) & (4 * K::NTR - 1)) * (K::NT * K::SW) + 4 * lane;
 #pragma unroll
-                for (int f = 0; f < K::NT; ++f) Vec4<S, C>::st(tr + f * K::SW, tnew[f]);
+                for (int f = 0; f < K::NT; ++f) {
+                    C r[4];  // the values the stored stresses will hold
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) r[e] = through<S, C>(tnew[f][e]);
+                    Vec4<C, C>::st(tr + f * K::SW, r);
+                }
                 // ---- point source (terms in list order), as read-modify-writes of
                 // the ring cells just written (keeps tnew in registers) ----
                 if (ntl > 0) {
@@ -1005,14 +1013,14 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                         const int4 tm = tl[t];  // (field, ix, iz, term index)
                         const int fi = tm.x - K::NV;
                         if (fi >= 0 && tm.z == j && tm.y >= x && tm.y < x + 4) {
-                            S *cell = tr + fi * K::SW + (tm.y - x);
-                            *cell = to_s<S>(to_c<C>(*cell) + sh.tamp[(long long)tm.w * sh.tamp_nt + it]);
+                            C *cell = tr + fi * K::SW + (tm.y - x);
+                            *cell = through<S, C>(*cell + sh.tamp[(long long)tm.w * sh.tamp_nt + it]);
                             hit = true;
                         }
                     }
                     if (hit) {
 #pragma unroll
-                        for (int f = 0; f < K::NT; ++f) Vec4<S, C>::ld(tr + f * K::SW, tnew[f]);
+                        for (int f = 0; f < K::NT; ++f) Vec4<C, C>::ld(tr + f * K::SW, tnew[f]);
                     }
                 }
                 // ---- hybrid box, after the point source: an add-ring cell takes
@@ -1031,13 +1039,13 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                             const int ai = ai0 + e;
                             if (ai >= 0 && ai < aw && (aj < 4 || aj >= ah - 4 || ai < 4 || ai >= aw - 4)) {
 #pragma unroll
-                                for (int f = 0; f < K::NT; ++f) tr[f * K::SW + e] = pwrow(f)[e];
+                                for (int f = 0; f < K::NT; ++f) tr[f * K::SW + e] = to_c<C>(pwrow(f)[e]);
                                 changed = true;
                             }
                         }
                         if (changed) {
 #pragma unroll
-                            for (int f = 0; f < K::NT; ++f) Vec4<S, C>::ld(tr + f * K::SW, tnew[f]);
+                            for (int f = 0; f < K::NT; ++f) Vec4<C, C>::ld(tr + f * K::SW, tnew[f]);
                         }
                     }
                 }
@@ -1062,7 +1070,7 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
 
             // stress ring row r (absolute): ring row (4*(gflat-i) + r-(z0-4)) mod 4*NTR
             const int tseq = 4 * (gflat - i) - (I.z0 - 4);
-            auto trrow = [=](int r) -> const S * {
+            auto trrow = [=](int r) -> const C * {
                 return tr_s + ((tseq + r) & (4 * K::NTR - 1)) * (K::NT * K::SW) + 4 * lane;
             };
             if constexpr (!PSV) {
@@ -1072,13 +1080,13 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                     bool img = grp == 0;
                     if constexpr (PUNCH) img = img && punch_active(sh.punch, min(max(x, 0), nx - 1), 0, it);
                     if (img) {
-                        S *r0 = const_cast<S *>(trrow(0)) + K::SW;
-                        const S *r1 = trrow(1) + K::SW;
+                        C *r0 = const_cast<C *>(trrow(0)) + K::SW;
+                        const C *r1 = trrow(1) + K::SW;
                         C v1[4], v0[4];
-                        Vec4<S, C>::ld(r1, v1);
+                        Vec4<C, C>::ld(r1, v1);
 #pragma unroll
                         for (int e = 0; e < 4; ++e) v0[e] = -v1[e];
-                        Vec4<S, C>::st(r0, v0);
+                        Vec4<C, C>::st(r0, v0);
 #pragma unroll
                         for (int e = 0; e < 4; ++e)
                             if (own_x && x + e < nx && nz > 1) wr[K::NV + 1][origin + x + e] = to_s<S>(v0[e]);
@@ -1091,7 +1099,7 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
             {
                 const int a = I.z0 - 8 + 4 * i + grp;
                 if (a >= I.z0 && a < nz && own_x && x < nx) {
-                    const S *trow[9];
+                    const C *trow[9];
 #pragma unroll
                     for (int d = 0; d < 9; ++d) trow[d] = trrow(a - 4 + d);
                     C mv[K::NMV][4];
@@ -1140,24 +1148,24 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                         if constexpr (PSV) {
                             C h[12], dx[4];
                             const P bu = P::from(mv[0]), bw = P::from(mv[1]);
-                            ld12<S, C>(trow[4], h);  // Txx
+                            ld12<C, C>(trow[4], h);  // Txx
 #pragma unroll
                             for (int e = 0; e < 4; ++e) dx[e] = dpx<C>(h, e, c0, c1, c2, c3);
                             P u = P::fma(bu, P::from(dx), P::from(vold[0]));
-                            ld12<S, C>(trow[4] + K::SW, h);  // Txz
+                            ld12<C, C>(trow[4] + K::SW, h);  // Txz
 #pragma unroll
                             for (int e = 0; e < 4; ++e) dx[e] = dmx<C>(h, e, c0, c1, c2, c3);
                             P w = P::fma(bw, P::from(dx), P::from(vold[1]));
-                            P::fma(bu, dpz4p<S, C>(trow, K::SW), u).to(vnew[0]);      // d/dz Txz
-                            P::fma(bw, dmz4p<S, C>(trow, 2 * K::SW), w).to(vnew[1]);  // d/dz Tzz
+                            P::fma(bu, dpz4p<C, C>(trow, K::SW), u).to(vnew[0]);      // d/dz Txz
+                            P::fma(bw, dmz4p<C, C>(trow, 2 * K::SW), w).to(vnew[1]);  // d/dz Tzz
                         } else {
                             C h[12], dx[4];
                             const P bv = P::from(mv[0]);
-                            ld12<S, C>(trow[4], h);  // Tx
+                            ld12<C, C>(trow[4], h);  // Tx
 #pragma unroll
                             for (int e = 0; e < 4; ++e) dx[e] = dmx<C>(h, e, c0, c1, c2, c3);
                             const P t = P::fma(bv, P::from(dx), P::from(vold[0]));
-                            P::fma(bv, dpz4p<S, C>(trow, K::SW), t).to(vnew[0]);  // d/dz Tz
+                            P::fma(bv, dpz4p<C, C>(trow, K::SW), t).to(vnew[0]);  // d/dz Tz
                         }
                     } else if (!PUNCH && xfast && a >= 4 && a <= nz - 5) {
                         // x-interior cells of a z-CPML row, as in the stress update
@@ -1169,10 +1177,10 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
 #pragma unroll
                             for (int e = 0; e < 4; ++e) pst[e] = prd[2][pz0 + e];
                             C h[12], dxT[4], dzT[4];
-                            ld12<S, C>(trow[4], h);  // Tx
+                            ld12<C, C>(trow[4], h);  // Tx
 #pragma unroll
                             for (int e = 0; e < 4; ++e) dxT[e] = dmx<C>(h, e, c0, c1, c2, c3);
-                            dpz4p<S, C>(trow, K::SW).to(dzT);  // d/dz Tz
+                            dpz4p<C, C>(trow, K::SW).to(dzT);  // d/dz Tz
                             const int zb = 2 * nx;
                             const C bT = __ldg(cp + (zb + a)), cT = __ldg(cp + (B + zb + a)),
                                     kT = __ldg(cp + (2 * B + zb + a));
@@ -1196,14 +1204,14 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                                 psb[e] = prd[4][pz0 + e];
                             }
                             C h[12], dxTxx[4], dxTxz[4], dzTxz[4], dzTzz[4];
-                            ld12<S, C>(trow[4], h);  // Txx
+                            ld12<C, C>(trow[4], h);  // Txx
 #pragma unroll
                             for (int e = 0; e < 4; ++e) dxTxx[e] = dpx<C>(h, e, c0, c1, c2, c3);
-                            ld12<S, C>(trow[4] + K::SW, h);  // Txz
+                            ld12<C, C>(trow[4] + K::SW, h);  // Txz
 #pragma unroll
                             for (int e = 0; e < 4; ++e) dxTxz[e] = dmx<C>(h, e, c0, c1, c2, c3);
-                            dpz4p<S, C>(trow, K::SW).to(dzTxz);
-                            dmz4p<S, C>(trow, 2 * K::SW).to(dzTzz);
+                            dpz4p<C, C>(trow, K::SW).to(dzTxz);
+                            dmz4p<C, C>(trow, 2 * K::SW).to(dzTzz);
                             const int zb = 4 * nx;
                             const C bA = __ldg(cp + (zb + nz + a)), cA = __ldg(cp + (B + zb + nz + a)),
                                     kA = __ldg(cp + (2 * B + zb + nz + a));
@@ -1258,7 +1266,7 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                         C dA[4], dB[4], dC[4], dD[4];
                         {
                             C h[12];
-                            ld12<S, C>(trow[4], h);
+                            ld12<C, C>(trow[4], h);
 #pragma unroll
                             for (int e = 0; e < 4; ++e) {
                                 
@@ -1267,8 +1275,8 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                         }
                         {
                             C h[12], zv[9][4];
-                            if constexpr (PSV) ld12<S, C>(trow[4] + K::SW, h);
-                            zcol<S, C>(trow, K::SW, zv);
+                            if constexpr (PSV) ld12<C, C>(trow[4] + K::SW, h);
+                            zcol<C, C>(trow, K::SW, zv);
 #pragma unroll
                             for (int e = 0; e < 4; ++e) {
                                 
@@ -1279,7 +1287,7 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                         }
                         if constexpr (PSV) {
                             C zv[9][4];
-                            zcol<S, C>(trow, 2 * K::SW, zv);
+                            zcol<C, C>(trow, 2 * K::SW, zv);
 #pragma unroll
                             for (int e = 0; e < 4; ++e) {
                                 

@@ -381,3 +381,20 @@ def test_strip_origin_puts_the_cpml_into_fewest_strips(nx, nz, npml, want_xp):
         import numpy as np
         ref = F.work_plan([(nx, nz, npml, 0)], wx=5.0, wz=2.5, bands=0, live=[np.ones(34 * ((nz + 3) // 4), bool)])
         assert len(_xp_strips(nx, npml, sorted({it[1] for cta in ref for it in cta}))) == 3
+
+
+@pytest.mark.parametrize("es,wave", [(4, "psv"), (2, "psv"), (4, "sh"), (2, "sh")])
+@pytest.mark.parametrize("batch", [False, True])
+def test_three_ctas_fit_per_sm(es, wave, batch):
+    """Dynamic shared memory of the sweep (Cfg::SMEM in fd23_fused.cuh: the
+    two rings and the point-wise stages in the storage type, the stress ring
+    in the arithmetic type (4-byte floats for every form but FP64), barriers,
+    item and source-term tables), its static shared memory (the batched
+    sweep's copy of the descriptor head) and the 1 KB the runtime reserves
+    per CTA: three CTAs fit the 228 KB of one SM."""
+    lay = smem_layout(es, wave)
+    nt = lay["nt"]
+    ring = NUW * lay["uw_slot"] + NPW * lay["stage"] + NTR * 4 * nt * SW * 4
+    smem = (ring + 15) // 16 * 16 + 256 + MAX_ITEMS * 16 + MAX_ITEMS * 16 * 16
+    static = 512 if batch else 128
+    assert 3 * (smem + static + 1024) <= 228 * 1024, (smem, static)
