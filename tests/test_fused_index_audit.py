@@ -398,3 +398,31 @@ def test_three_ctas_fit_per_sm(es, wave, batch):
     smem = (ring + 15) // 16 * 16 + 256 + MAX_ITEMS * 16 + MAX_ITEMS * 16 * 16
     static = 512 if batch else 128
     assert 3 * (smem + static + 1024) <= 228 * 1024, (smem, static)
+
+
+@pytest.mark.parametrize("nx,nz,npml", [(60, 40, 0), (100, 64, 0), (130, 97, 10), (121, 33, 4), (500, 300, 0),
+                                        (4000, 2000, 0)])
+@pytest.mark.parametrize("bands", [0, 1])
+@pytest.mark.parametrize("ov", [1.0, 2.0])
+def test_plans_without_cpml_and_narrow_grids(nx, nz, npml, bands, ov):
+    """Grids without a CPML (only the reduced-order edge columns cost more),
+    grids narrower than one strip, and a strip boundary at the grid's edge:
+    every 4-row block planned once, copies and stores in bounds."""
+    F = pytest.importorskip("fd23_gb300")
+    try:
+        F.lib()
+    except ImportError as e:
+        pytest.skip(str(e))
+    ctas = F.work_plan([(nx, nz, npml, 0)], wx=5.0, wz=2.5, oversub=ov, bands=bands)
+    items = [it[1:] for cta in ctas for it in cta]
+    x0s = sorted({x0 for x0, _, _ in items})
+    xoff = x0s[0]
+    assert -TX < xoff <= 0 and xoff % 8 == 0
+    assert x0s == [xoff + TX * s for s in range(len(x0s))] and x0s[-1] + TX >= nx
+    nzb = (nz + 3) // 4
+    seen = {}
+    for x0, z0, z1 in items:
+        for zb in range(z0 // 4, z1 // 4):
+            seen[(x0, zb)] = seen.get((x0, zb), 0) + 1
+    assert len(seen) == len(x0s) * nzb and set(seen.values()) == {1}
+    audit(nx, nz, 4, "psv", ctas=[[it[1:] for it in cta] for cta in ctas])
