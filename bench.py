@@ -920,6 +920,9 @@ def bench_sh(args, F, torch, rank, world, local, dist):
     b = None if persist else F.Batch([s])
     stream = torch.cuda.ExternalStream(s.stream if persist else b.stream, device=local)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda:%d" % local)
+    # work plan picked by the autotuner (set-up, not timed)
+    tune = b.autotune(10) if b is not None and not args.no_tune else []
+    plan = b.plan() if tune else None
 
     def shot():
         s.reset()
@@ -982,7 +985,8 @@ def bench_sh(args, F, torch, rank, world, local, dist):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.prec,
             "data": "synthetic",
-            "config": {"workload": "sh_800x400_2000steps_c0", "nx": SH_NX, "nz": SH_NZ, "nt": nt,
+            "config": {"workload": "sh_800x400_2000steps_c0", "nx": SH_NX, "nz": SH_NZ, "nt": nt, "plan": plan,
+                       "autotune_trials": len(tune),
                        "source": "10 Hz Ricker line force", "traces": SH_NSTA,
                        "kernel": "persistent cooperative launch per shot" if persist else "fused sweep, one-shot batch graph",
                        "l2": "working set (about 10 MB) L2-resident within a shot; L2 flushed between "

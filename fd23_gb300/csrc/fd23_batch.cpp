@@ -457,7 +457,7 @@ int fd23_batch_set_graph(fd23_batch *b, int on)
 
 int fd23_batch_set_plan(fd23_batch *b, const fd23_tune_entry *tune)
 {
-    if (!b || !tune || !(tune->wx > 0) || !(tune->wz > 0) || tune->per_sm < 1 || !(tune->oversub >= 1.0) ||
+    if (!b || !tune || !(tune->wx > 0) || !(tune->wz > 0) || tune->per_sm < 1 || !(tune->oversub >= 1.0 / 16) ||
         tune->oversub > 64.0 || (tune->bands != 0 && tune->bands != 1))
         return FD23_ERR_ARG;
     CK(cudaSetDevice(b->device));
@@ -570,7 +570,7 @@ int fd23_work_plan(int nshots, const int *nx, const int *nz, const int *npml, co
 
 int fd23_set_plan(fd23_solver *s, const fd23_tune_entry *tune)
 {
-    if (!s || !tune || !(tune->wx > 0) || !(tune->wz > 0) || tune->per_sm < 1 || !(tune->oversub >= 1.0) ||
+    if (!s || !tune || !(tune->wx > 0) || !(tune->wz > 0) || tune->per_sm < 1 || !(tune->oversub >= 1.0 / 16) ||
         tune->oversub > 64.0 || (tune->bands != 0 && tune->bands != 1))
         return FD23_ERR_ARG;
     if (!s->fused) return FD23_ERR_UNSUPPORTED;

@@ -48,9 +48,9 @@ int strips_of(const ShotGeom &g, int tile_x) { return (g.nx - g.xoff + tile_x - 
 // cost least in total (ties: the one nearest 0).  Moving the origin left
 // can put both x-CPML zones and their 4-column halos into fewer strips: on
 // the 4000-column grid with a 40-cell CPML, origin 0 makes three strips run
-// the CPML path (0, 32 and 33, strip 32 through its halo only), origin -40
-// two.  Copies that start left of column -8 read zeros, as the padding
-// columns hold.
+// the CPML path (0, 32 and 33, strip 32 through its halo only), origin -8
+// (the first that does) two.  Copies that start left of column -8 read
+// zeros, as the padding columns hold.
 int best_xoff(ShotGeom g, int tile_x, const TuneParams &tp)
 {
     const int nzb = (g.nz + 3) / 4;

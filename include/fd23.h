@@ -351,7 +351,8 @@ int fd23_batch_get_plan(fd23_batch *b, fd23_tune_entry *current, int *nblocks);
 int fd23_batch_set_plan(fd23_batch *b, const fd23_tune_entry *tune);
 /* fd23_set_plan installs a plan without timing it (ms_per_step ignored;
  * per_sm is capped at the residency the device reports; oversub in
- * [1, 64]); fd23_get_plan reports the current one and its CTA count. */
+ * [1/16, 64]: below 1, part of a wave of CTAs, for small grids);
+ * fd23_get_plan reports the current one and its CTA count. */
 int fd23_set_plan(fd23_solver *s, const fd23_tune_entry *tune);
 int fd23_get_plan(fd23_solver *s, fd23_tune_entry *current, int *nblocks);
 /* The work plan for nshots grids under the given parameters (host only, for
