@@ -51,6 +51,7 @@ ABI_FUNCTIONS = [
     "fd23_get_seismograms", "fd23_reset", "fd23_get_stream", "fd23_get_step", "fd23_get_field_device", "fd23_state_bytes", "fd23_get_state",
     "fd23_set_state", "fd23_field_norm2", "fd23_build_material", "fd23_build_cpml",
     "fd23_build_source_terms", "fd23_sum_squares_noalloc", "fd23_set_box", "fd23_set_box_incident",
+    "fd23_set_box_incident_async",
     "fd23_box_state_bytes", "fd23_get_box_state", "fd23_set_box_state", "fd23_box_ring_size",
     "fd23_box_ring_index", "fd23_box_ring_cells", "fd23_box_incident_from_displacement",
     "fd23_box_material", "fd23_batch_create", "fd23_batch_destroy", "fd23_batch_run", "fd23_batch_sync",
@@ -145,6 +146,7 @@ def lib():
         "fd23_sum_squares_noalloc": ([i, vp, i, sz, vp, _C.POINTER(d), _C.POINTER(i)], i),
         "fd23_set_box": ([vp, i, i, i, i, vp], i),
         "fd23_set_box_incident": ([vp, vp, i, i], i),
+        "fd23_set_box_incident_async": ([vp, vp, i, i], i),
         "fd23_box_state_bytes": ([vp], sz),
         "fd23_get_box_state": ([vp, vp, sz], i),
         "fd23_set_box_state": ([vp, vp, sz], i),
@@ -715,16 +717,23 @@ class Solver:
         _check(lib().fd23_set_box(self._h, x0, z0, bx, bz, _p(bmat)), "fd23_set_box")
         self._box = (x0, z0, bx, bz) if bx else None
 
-    def set_box_incident(self, inc, it0=0):
+    def set_box_incident(self, inc, it0=0, wait=True):
         """inc [nsteps, 5, nring] (U W Txx Txz Tzz on the ring cells) for steps
-        it0 .. it0+nsteps-1."""
+        it0 .. it0+nsteps-1.  wait=False: fd23_set_box_incident_async (the
+        upload overlaps the run; the solver keeps a reference to the array
+        until the next upload)."""
         a = _np.ascontiguousarray(inc, dtype=self.dtype)
         if self._box is not None:
             nring = sum(box_ring_size(self._box[2], self._box[3]))
             if a.ndim != 3 or a.shape[1:] != (5, nring):
                 raise ValueError("set_box_incident: shape %s, expected (nsteps, 5, %d)" % (a.shape, nring))
-        _check(lib().fd23_set_box_incident(self._h, _p(a), it0, a.shape[0] if a.ndim == 3 else 0),
-               "fd23_set_box_incident")
+        n = a.shape[0] if a.ndim == 3 else 0
+        if wait:
+            _check(lib().fd23_set_box_incident(self._h, _p(a), it0, n), "fd23_set_box_incident")
+            self._inc_keep = None
+        else:
+            _check(lib().fd23_set_box_incident_async(self._h, _p(a), it0, n), "fd23_set_box_incident_async")
+            self._inc_keep = a
 
     def set_box_line_source(self, desc, src, bmat, it0, nsteps):
         """Incident field of steps it0 .. it0+nsteps-1 generated on the device

@@ -188,6 +188,8 @@ int step_impl(fd23_solver *s, int rec_now, int more)
     Shot<S, C> sh = make_shot<S, C>(s);
     const bool box = s->box_on;
     int rc = FD23_OK;
+    // incident field of this step and the next (a merged box launch reads both)
+    if (box && (rc = wait_incident(s, s->it + 1))) return rc;
     if (box && !s->box_pre_ahead && (rc = launch_box_pre<S, C>(sh, s->fused ? s->par : 0, s->fused, s->stream)))
         return rc;
     s->box_pre_ahead = false;
@@ -577,7 +579,11 @@ void free_all(fd23_solver *s)
         cudaFree(s->d_seis[c]);
     }
     free_box(s);
+    if (s->copy_stream) cudaStreamSynchronize(s->copy_stream);
     cudaFree(s->box_inc);
+    for (cudaEvent_t e : s->inc_ev) cudaEventDestroy(e);
+    if (s->inc_gate) cudaEventDestroy(s->inc_gate);
+    if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
     cudaFree(s->d_items);
     cudaFree(s->d_item_off);
     cudaFree(s->d_items2);
@@ -686,6 +692,18 @@ int material_done(fd23_solver *s)
     }
     return rc;
 }
+// the solver's stream waits for the asynchronous incident chunks up to the one
+// holding step `upto`
+int wait_incident(fd23_solver *s, int upto)
+{
+    if (s->inc_chunk <= 0 || s->box_inc_n <= 0) return FD23_OK;
+    upto = std::min(std::max(upto, s->box_inc_it0), s->box_inc_it0 + s->box_inc_n - 1);
+    const int need = (upto - s->box_inc_it0) / s->inc_chunk;
+    for (; s->inc_waited <= need; ++s->inc_waited)
+        CK(cudaStreamWaitEvent(s->stream, s->inc_ev[s->inc_waited], 0));
+    return FD23_OK;
+}
+
 }  // namespace fd23
 
 extern "C" {
@@ -1279,6 +1297,8 @@ int fd23_set_box_incident(fd23_solver *s, const void *inc, int it0, int nsteps)
     if (!s || it0 < 0 || nsteps < 0 || (nsteps > 0 && !inc)) return FD23_ERR_ARG;
     if (!s->box_on) return FD23_ERR_ORDER;
     CK(cudaSetDevice(s->d.device));
+    if (s->copy_stream) CK(cudaStreamSynchronize(s->copy_stream));  // an earlier asynchronous upload
+    s->inc_chunk = 0;
     const size_t bytes = (size_t)nsteps * 5 * s->box_nring * s->cs;
     if (bytes > s->box_inc_bytes) {
         CK(cudaStreamSynchronize(s->stream));
@@ -1298,6 +1318,54 @@ int fd23_set_box_incident(fd23_solver *s, const void *inc, int it0, int nsteps)
     s->box_inc_n = nsteps;
     return FD23_OK;
 }
+
+int fd23_set_box_incident_async(fd23_solver *s, const void *inc, int it0, int nsteps)
+{
+    if (!s || it0 < 0 || nsteps < 0 || (nsteps > 0 && !inc)) return FD23_ERR_ARG;
+    if (!s->box_on) return FD23_ERR_ORDER;
+    CK(cudaSetDevice(s->d.device));
+    if (!s->copy_stream) CK(cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking));
+    if (!s->inc_gate) CK(cudaEventCreateWithFlags(&s->inc_gate, cudaEventDisableTiming));
+    CK(cudaStreamSynchronize(s->copy_stream));  // an earlier asynchronous upload
+    s->inc_chunk = 0;
+    const size_t step_bytes = (size_t)5 * s->box_nring * s->cs;
+    const size_t bytes = (size_t)nsteps * step_bytes;
+    if (bytes > s->box_inc_bytes) {
+        CK(cudaStreamSynchronize(s->stream));
+        cudaFree(s->box_inc);
+        s->box_inc = nullptr;
+        s->box_inc_bytes = 0;
+        s->box_inc_n = 0;
+        int rc = dev_alloc(&s->box_inc, bytes);
+        if (rc) return rc;
+        s->box_inc_bytes = bytes;
+    } else {
+        // work already queued on the solver's stream may read the old field
+        CK(cudaEventRecord(s->inc_gate, s->stream));
+        CK(cudaStreamWaitEvent(s->copy_stream, s->inc_gate, 0));
+    }
+    // chunks of 64 steps, each followed by its event
+    const int chunk = 64;
+    const int nch = (nsteps + chunk - 1) / chunk;
+    while ((int)s->inc_ev.size() < nch) {
+        cudaEvent_t e = nullptr;
+        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        s->inc_ev.push_back(e);
+    }
+    for (int c = 0; c < nch; ++c) {
+        const size_t off = (size_t)c * chunk * step_bytes;
+        const size_t len = (size_t)std::min(chunk, nsteps - c * chunk) * step_bytes;
+        CK(cudaMemcpyAsync((unsigned char *)s->box_inc + off, (const unsigned char *)inc + off, len,
+                           cudaMemcpyHostToDevice, s->copy_stream));
+        CK(cudaEventRecord(s->inc_ev[c], s->copy_stream));
+    }
+    s->box_inc_it0 = it0;
+    s->box_inc_n = nsteps;
+    s->inc_chunk = nsteps > 0 ? chunk : 0;
+    s->inc_waited = 0;
+    return FD23_OK;
+}
+
 
 size_t fd23_box_state_bytes(fd23_solver *s)
 {

@@ -127,6 +127,14 @@ struct fd23_solver {
     // the box's start-of-step work of step `it` already ran (with the end of
     // the step before, launch_box_mid)
     bool box_pre_ahead = false;
+    // asynchronous incident upload (fd23_set_box_incident_async): chunk c
+    // holds steps box_inc_it0 + c*inc_chunk .. +inc_chunk-1 and is on the
+    // device once inc_ev[c] has completed; inc_waited: chunks the solver's
+    // stream already waits for
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t inc_gate = nullptr;  // the solver's queued work, before the copies
+    std::vector<cudaEvent_t> inc_ev;
+    int inc_chunk = 0, inc_waited = 0;
 };
 
 namespace fd23 {
@@ -144,6 +152,7 @@ int fused_per_sm(int device, int wave, int prec, bool batch = false);
 int upload_plan(const WorkPlan &plan, WorkItem **d_items, int **d_off);
 int build_worklist(fd23_solver *s);
 int build_worklist2(fd23_solver *s);
+int wait_incident(fd23_solver *s, int upto);  // asynchronous incident chunks up to step `upto`
 // one step; more != 0: another step follows in the same run
 int dispatch_step(fd23_solver *s, int rec_now, int more = 0);
 // copies buffer set `par` (wavefields, memory variables) into the other set

@@ -230,6 +230,12 @@ int fd23_set_state(fd23_solver *s, const void *buf, size_t bytes, int it0);
  *   (fd23_set_material_table): FD23_ERR_UNSUPPORTED. */
 int fd23_set_box(fd23_solver *s, int x0, int z0, int bx, int bz, const double *bmat);
 int fd23_set_box_incident(fd23_solver *s, const void *inc, int it0, int nsteps);
+/* The same upload without waiting for it: the copy runs on a copy stream in
+ * chunks of steps, each box step of the solver waits only for the chunk that
+ * holds its incident field, so the upload overlaps the run.  inc must stay
+ * valid and unchanged until the solver's work has finished (fd23_sync);
+ * page-locked host memory lets the copy run asynchronously. */
+int fd23_set_box_incident_async(fd23_solver *s, const void *inc, int it0, int nsteps);
 size_t fd23_box_state_bytes(fd23_solver *s);
 int fd23_get_box_state(fd23_solver *s, void *buf, size_t bytes);
 int fd23_set_box_state(fd23_solver *s, const void *buf, size_t bytes);

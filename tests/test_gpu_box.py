@@ -192,3 +192,37 @@ def test_array_size_checks():
     with pytest.raises(ValueError):
         s.set_box_incident(np.zeros((2, 5, 7), np.float32), 0)
     s.close()
+
+
+def test_box_incident_async_upload():
+    """fd23_set_box_incident_async (chunks of 64 steps on a copy stream, each
+    box step waiting only for its chunk) gives the results of the waiting
+    upload: one run over more than one chunk, a second upload into the same
+    buffer while the first run's work may still be queued, and split runs."""
+    nx, nz, nt = 200, 140, 150
+    c = Case("psv", nx, nz, npml=12, nt=nt, xs=40, zs=10, seed=4)
+    ci = Case("psv", nx, nz, npml=12, nt=nt, xs=110, zs=60, seed=5)
+    box = (80, 40, 48, 40)
+    inc, _ = O.psv_ring_history("f32", nx, nz, 12, 0, ci.mat, ci.bck, ci.terms, nt, box)
+    out = {}
+    for wait in (True, False):
+        s = _solver(c, "f32", "fused")
+        s.set_receivers(0, c.rx, c.rz)
+        s.set_box(*box)
+        s.set_box_incident(inc, 0, wait=wait)
+        s.run(nt, 1)
+        first = (s.seismograms(0), s.get_state(), s.get_box_state())
+        # again from the start, the upload queued behind nothing or behind the reset
+        s.reset()
+        s.set_box(*box)
+        s.set_box_incident(inc[:70], 0, wait=wait)
+        s.run(70, 1)
+        s.set_box_incident(inc[70:], 70, wait=wait)
+        s.run(nt - 70, 1)
+        second = (s.seismograms(0), s.get_state(), s.get_box_state())
+        for a, b in zip(first, second):
+            np.testing.assert_array_equal(a, b)
+        out[wait] = first
+        s.close()
+    for a, b in zip(out[True], out[False]):
+        np.testing.assert_array_equal(a, b)
