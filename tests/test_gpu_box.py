@@ -158,10 +158,21 @@ def test_box_argument_errors():
         s.set_box(10, 10, 15, 30)  # below the 16-cell minimum
     with pytest.raises(F.Fd23Error):
         s.set_box_incident(np.zeros((1, 5, 10), np.float32), 0)  # no box yet
+    with pytest.raises(F.Fd23Error) as e:
+        s.set_box_incident(np.zeros((1, 5, 10), np.float32), 0, wait=False)
+    assert e.value.status == F.ERR_ORDER
     s.set_box(10, 10, 40, 30)
     with pytest.raises(F.Fd23Error) as e:
         s.run(1, 1)  # incident field not loaded
     assert e.value.status == F.ERR_ORDER
+    # an asynchronous upload of 3 steps covers 3 steps only
+    nring = sum(F.box_ring_size(40, 30))
+    s.set_box_incident(np.zeros((3, 5, nring), np.float32), 0, wait=False)
+    with pytest.raises(F.Fd23Error) as e:
+        s.run(4, 1)
+    assert e.value.status == F.ERR_ORDER
+    s.run(3, 1)
+    s.sync()
     s.close()
     sh = F.Solver("sh", 120, 90, 10, c.h, c.dt, prec="f32", **c.pml)
     with pytest.raises(F.Fd23Error) as e:
