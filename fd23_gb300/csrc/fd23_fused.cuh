@@ -353,15 +353,9 @@ struct Cfg {
 #ifndef FD23_FUSED_NUW
 #define FD23_FUSED_NUW 4
 #endif
-    // 16-bit storage: the stencil inputs that land in the ring are converted
-    // once, a block ahead of their first use, into a ring of the arithmetic
-    // type (NCR slots) that the stencils read; the landing slots are free
-    // again as soon as a block is converted
-    static constexpr bool CVT = sizeof(S) == 2;
-    // ring depths (NTR, and NUW without CVT, powers of two): sized so that
-    // three CTAs fit in the 228 KB of shared memory of one SM
-    static constexpr int NUW = CVT ? 3 : FD23_FUSED_NUW, NPW = FD23_FUSED_NPW, NTR = 4;
-    static constexpr int NCR = CVT ? 5 : 0;
+    // ring depths (NUW and NTR powers of two): sized so that three CTAs of the
+    // 4-byte forms fit in the 228 KB of shared memory of one SM
+    static constexpr int NUW = FD23_FUSED_NUW, NPW = FD23_FUSED_NPW, NTR = 4;
     // Tensor copies land 128-byte aligned: a stencil-input slot holds one box
     // [NV fields][4 rows][UWW], a point-wise stage three boxes (old stresses,
     // stress-update material, velocity-update material) [fields][4 rows][PWW],
@@ -370,8 +364,6 @@ struct Cfg {
     static constexpr int UWF = 4 * UWW;                                  // field stride in a slot
     static constexpr int UW_SLOT = al128(NV * 4 * UWW * (int)sizeof(S));
     static constexpr int UW_ELEMS = NUW * UW_SLOT;
-    static constexpr int UWC_SLOT = NV * 4 * UWW;                        // converted slot (C elements)
-    static constexpr int UWC_ELEMS = NCR * UWC_SLOT;
     static constexpr int PG_MS = al128(NT * 4 * PWW * (int)sizeof(S));
     // with a material table the material groups give way to one box of
     // 8 index rows (velocity rows, then stress rows) of kIdxBoxW bytes
@@ -400,9 +392,8 @@ struct Cfg {
     static constexpr int minb() { return sizeof(S) == 8 ? 1 : 3; }
     // the stress ring holds arithmetic-type values (rounded through S when
     // written): the velocity update reads each of them many times
-    static constexpr size_t RING_BYTES = (((size_t)(UW_ELEMS + PW_ELEMS + TAB_ELEMS) * sizeof(S) +
-                                           (size_t)(TR_ELEMS + UWC_ELEMS) * sizeof(C) + 15) &
-                                          ~(size_t)15);
+    static constexpr size_t RING_BYTES =
+        (((size_t)(UW_ELEMS + PW_ELEMS + TAB_ELEMS) * sizeof(S) + (size_t)TR_ELEMS * sizeof(C) + 15) & ~(size_t)15);
     static constexpr size_t SMEM = RING_BYTES + 256 /* 2*(NUW+NPW) barriers */ + MAX_ITEMS * 16 +
                                    (size_t)MAX_ITEMS * MAX_TERMS * 16;
 };
@@ -429,7 +420,6 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
     using K = Cfg<S, C, WAVE, TABLE>;
     constexpr bool PSV = K::PSV;
     constexpr int NCT = 32 * K::NCW;  // compute threads
-    using UT = std::conditional_t<K::CVT, C, S>;  // element type the stencils read U, W as
     // an earlier launch gave up on a wait: do nothing until the host resets
     if (err_flag && *(volatile int *)err_flag) return;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -441,8 +431,7 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
     S *uw_s = reinterpret_cast<S *>(smem_raw);
     S *pw_s = uw_s + K::UW_ELEMS;
     C *tr_s = reinterpret_cast<C *>(pw_s + K::PW_ELEMS);  // stress ring (arithmetic type)
-    C *uwc_s = tr_s + K::TR_ELEMS;                         // converted stencil inputs (CVT only)
-    S *tab_s = reinterpret_cast<S *>(uwc_s + K::UWC_ELEMS);  // the material table (TABLE only)
+    S *tab_s = reinterpret_cast<S *>(tr_s + K::TR_ELEMS);  // the material table (TABLE only)
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw + K::RING_BYTES);
     uint64_t *full_uw = bars, *empty_uw = bars + K::NUW;
     uint64_t *full_pw = bars + 2 * K::NUW, *empty_pw = full_pw + K::NPW;
@@ -645,9 +634,7 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                 ++k;
             }
             const int i = g - base_it;
-            // iteration g reads blocks i .. i+2 of its item; with CVT it converts
-            // block i+3 (the item's blocks run to niter+1)
-            const int need = base_uw + (K::CVT ? min(i + 3, info[k].niter + 1) : i + 2);
+            const int need = base_uw + i + 2;  // iteration g reads blocks need-2 .. need
             while (ok && e_uw <= need) {
                 if (e_uw >= K::NUW)
                     ok = mbar_wait_bounded(&empty_uw[e_uw % K::NUW], (uint32_t)(((e_uw / K::NUW) - 1) & 1), err_flag);
@@ -684,34 +671,8 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
     const int B = sh.cpml_blk;
     bool ok = true;
     int uw_ready = 0, gflat = 0, uw_base = 0;
-    // CVT: stencil-input block e (row grp) from its landing slot into the
-    // converted ring, then the landing slot is released
-    auto convert_block = [&](int e) {
-        ok = ok && mbar_wait_bounded(&full_uw[e % K::NUW], (uint32_t)((e / K::NUW) & 1), err_flag);
-        if (ok) {
-            const S *src = uw_s + (e % K::NUW) * K::UW_SLOT + grp * K::UWW;
-            C *dst = uwc_s + (e % K::NCR) * K::UWC_SLOT + grp * K::UWW;
-#pragma unroll
-            for (int f = 0; f < K::NV; ++f)
-                for (int c = 4 * lane; c < K::UWW; c += 128) {
-                    C v[4];
-                    Vec4<S, C>::ld(src + f * K::UWF + c, v);
-                    Vec4<C, C>::st(dst + f * K::UWF + c, v);
-                }
-        }
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&empty_uw[e % K::NUW]);
-    };
     for (int k = 0; k < nitems && ok; ++k) {
         const ItemInfo I = info[k];
-        if constexpr (K::CVT) {
-            // the item's first three blocks, once every warp is done with the
-            // slots they replace (the previous item's last blocks)
-            if (k > 0) compute_bar(NCT);
-            for (int b = 0; b < 3; ++b) convert_block(uw_base + b);
-            ok = compute_bar_and(NCT, ok) != 0;
-            if (!ok) break;
-        }
         const int ntl = tcount[k];
         const int4 *tl = tlist + k * K::MAX_TERMS;
         const int x = I.x0 - 4 + 4 * lane;  // first of this thread's 4 cells
@@ -723,10 +684,8 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
         // the 4 cells are interior (8th order), outside the x-CPML and inside the grid
         const bool xfast = x >= max(4, npml) && x + 3 <= min(nx - 5, nx - npml - 1);
         for (int i = 0; i < I.niter; ++i, ++gflat) {
-            if constexpr (!K::CVT)
-                for (; ok && uw_ready <= uw_base + i + 2; ++uw_ready)
-                    ok = mbar_wait_bounded(&full_uw[uw_ready % K::NUW], (uint32_t)((uw_ready / K::NUW) & 1),
-                                           err_flag);
+            for (; ok && uw_ready <= uw_base + i + 2; ++uw_ready)
+                ok = mbar_wait_bounded(&full_uw[uw_ready % K::NUW], (uint32_t)((uw_ready / K::NUW) & 1), err_flag);
             if (ok) ok = mbar_wait_bounded(&full_pw[gflat % K::NPW], (uint32_t)((gflat / K::NPW) & 1), err_flag);
             const S *pws = pw_s + (gflat % K::NPW) * K::PW_STAGE;
             auto pwrow = [=](int f) { return pws + K::pw_field(f) + grp * K::PWW + K::PWOFF + 4 * lane; };
@@ -735,23 +694,12 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
             {
                 const int j = I.z0 - 4 + 4 * i + grp;
                 // stencil rows j-4 .. j+4: ring row (4*(uw_base+i) + grp + d) mod 4*NUW
-                // (CVT: block uw_base+i+(grp+d)/4 of the converted ring, row (grp+d)&3)
-                const UT *urow[9];
-                if constexpr (K::CVT) {
-                    const int s0 = (uw_base + i) % K::NCR;
+                const S *urow[9];
+                const int rseq = 4 * (uw_base + i) + grp;
 #pragma unroll
-                    for (int d = 0; d < 9; ++d) {
-                        int sl = s0 + ((grp + d) >> 2);
-                        sl = sl >= K::NCR ? sl - K::NCR : sl;
-                        urow[d] = uwc_s + sl * K::UWC_SLOT + ((grp + d) & 3) * K::UWW + 4 * lane + 4;
-                    }
-                } else {
-                    const int rseq = 4 * (uw_base + i) + grp;
-#pragma unroll
-                    for (int d = 0; d < 9; ++d) {
-                        const int r = (rseq + d) & (4 * K::NUW - 1);
-                        urow[d] = uw_s + (r >> 2) * K::UW_SLOT + (r & 3) * K::UWW + 4 * lane + 4;
-                    }
+                for (int d = 0; d < 9; ++d) {
+                    const int r = (rseq + d) & (4 * K::NUW - 1);
+                    urow[d] = uw_s + (r >> 2) * K::UW_SLOT + (r & 3) * K::UWW + 4 * lane + 4;
                 }
                 const bool inrow = j >= 0 && j < nz;
                 const bool zfast = j >= 4 && j <= nz - 5 && j < nz - npml && !(sh.topabsorb && j < npml);
@@ -781,10 +729,10 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                     if constexpr (PSV) {
                         C h[12];
                         C ux[4], wx[4];
-                        ld12<UT, C>(urow[4], h);
+                        ld12<S, C>(urow[4], h);
 #pragma unroll
                         for (int e = 0; e < 4; ++e) ux[e] = dmx<C>(h, e, c0, c1, c2, c3);
-                        ld12<UT, C>(urow[4] + K::UWF, h);
+                        ld12<S, C>(urow[4] + K::UWF, h);
 #pragma unroll
                         for (int e = 0; e < 4; ++e) wx[e] = dpx<C>(h, e, c0, c1, c2, c3);
                         const P lam = P::from(ms[0]), mua = P::from(ms[2]);
@@ -793,17 +741,17 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                         P t0 = P::fma(gam, UX, P::from(told[0]));
                         P t2 = P::fma(lam, UX, P::from(told[2]));
                         P t1 = P::fma(mua, WX, P::from(told[1]));
-                        const P UZ = dmz4p<UT, C>(urow, 0), WZ = dpz4p<UT, C>(urow, K::UWF);
+                        const P UZ = dmz4p<S, C>(urow, 0), WZ = dpz4p<S, C>(urow, K::UWF);
                         P::fma(lam, WZ, t0).to(tnew[0]);
                         P::fma(gam, WZ, t2).to(tnew[2]);
                         P::fma(mua, UZ, t1).to(tnew[1]);
                     } else {
                         C h[12], dx[4];
-                        ld12<UT, C>(urow[4], h);
+                        ld12<S, C>(urow[4], h);
 #pragma unroll
                         for (int e = 0; e < 4; ++e) dx[e] = dpx<C>(h, e, c0, c1, c2, c3);
                         P::fma(P::from(ms[0]), P::from(dx), P::from(told[0])).to(tnew[0]);
-                        P::fma(P::from(ms[1]), dmz4p<UT, C>(urow, 0), P::from(told[1])).to(tnew[1]);
+                        P::fma(P::from(ms[1]), dmz4p<S, C>(urow, 0), P::from(told[1])).to(tnew[1]);
                     }
                 } else if (!PUNCH && xfast && j >= 4 && j <= nz - 5) {
                     // x-interior cells of a z-CPML row (8th order everywhere): the
@@ -817,10 +765,10 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
 #pragma unroll
                         for (int e = 0; e < 4; ++e) psv[e] = prd[3][pz0 + e];
                         C h[12], dxv[4], dzv[4];
-                        ld12<UT, C>(urow[4], h);
+                        ld12<S, C>(urow[4], h);
 #pragma unroll
                         for (int e = 0; e < 4; ++e) dxv[e] = dpx<C>(h, e, c0, c1, c2, c3);
-                        dmz4p<UT, C>(urow, 0).to(dzv);
+                        dmz4p<S, C>(urow, 0).to(dzv);
                         const int zb = 2 * nx;
                         const C bZ = __ldg(cp + (zb + nz + j)), cZ = __ldg(cp + (B + zb + nz + j)),
                                 kZ = __ldg(cp + (2 * B + zb + nz + j));
@@ -845,14 +793,14 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                             psu[e] = prd[6][pz0 + e];
                         }
                         C h[12], ux[4], wx[4], uz[4], wz[4];
-                        ld12<UT, C>(urow[4], h);
+                        ld12<S, C>(urow[4], h);
 #pragma unroll
                         for (int e = 0; e < 4; ++e) ux[e] = dmx<C>(h, e, c0, c1, c2, c3);
-                        ld12<UT, C>(urow[4] + K::UWF, h);
+                        ld12<S, C>(urow[4] + K::UWF, h);
 #pragma unroll
                         for (int e = 0; e < 4; ++e) wx[e] = dpx<C>(h, e, c0, c1, c2, c3);
-                        dmz4p<UT, C>(urow, 0).to(uz);
-                        dpz4p<UT, C>(urow, K::UWF).to(wz);
+                        dmz4p<S, C>(urow, 0).to(uz);
+                        dpz4p<S, C>(urow, K::UWF).to(wz);
                         const int zb = 4 * nx;
                         const C bW = __ldg(cp + (zb + 3 * nz + j)), cW = __ldg(cp + (B + zb + 3 * nz + j)),
                                 kW = __ldg(cp + (2 * B + zb + 3 * nz + j));
@@ -918,8 +866,8 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                     C dA[4], dB[4], dC[4], dD[4];
                     {
                         C h[12], zv[9][4];
-                        ld12<UT, C>(urow[4], h);
-                        zcol<UT, C>(urow, 0, zv);
+                        ld12<S, C>(urow[4], h);
+                        zcol<S, C>(urow, 0, zv);
 #pragma unroll
                         for (int e = 0; e < 4; ++e) {
                             
@@ -930,8 +878,8 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                     }
                     if constexpr (PSV) {
                         C h[12], zv[9][4];
-                        ld12<UT, C>(urow[4] + K::UWF, h);
-                        zcol<UT, C>(urow, K::UWF, zv);
+                        ld12<S, C>(urow[4] + K::UWF, h);
+                        zcol<S, C>(urow, K::UWF, zv);
 #pragma unroll
                         for (int e = 0; e < 4; ++e) {
                             
@@ -1116,9 +1064,6 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                     }
                 }
             }
-            // CVT: the block iteration i+1 first reads, converted before the barrier
-            if constexpr (K::CVT)
-                if (i + 3 <= I.niter + 1) convert_block(uw_base + i + 3);
             // stresses of this block visible to every compute warp; all agree to go on
             ok = compute_bar_and(NCT, ok) != 0;
             if (!ok) break;
@@ -1171,16 +1116,11 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                         for (int m = 0; m < K::NMV; ++m) Vec4<S, C>::ld(pwrow(K::NT + K::NMS + m), mv[m]);
                     }
                     const int rel = 4 * i + grp;  // a - (z0-8): block i, row grp
-                    const UT *vrow;
-                    if constexpr (K::CVT) {
-                        vrow = uwc_s + ((uw_base + i) % K::NCR) * K::UWC_SLOT + grp * K::UWW + 4 * lane + 4;
-                    } else {
-                        const int vr = (4 * (uw_base + i) + (rel & 3)) & (4 * K::NUW - 1);
-                        vrow = uw_s + (vr >> 2) * K::UW_SLOT + (vr & 3) * K::UWW + 4 * lane + 4;
-                    }
+                    const int vr = (4 * (uw_base + i) + (rel & 3)) & (4 * K::NUW - 1);
+                    const S *vrow = uw_s + (vr >> 2) * K::UW_SLOT + (vr & 3) * K::UWW + 4 * lane + 4;
                     C vold[K::NV][4];
 #pragma unroll
-                    for (int v = 0; v < K::NV; ++v) Vec4<UT, C>::ld(vrow + v * K::UWF, vold[v]);
+                    for (int v = 0; v < K::NV; ++v) Vec4<S, C>::ld(vrow + v * K::UWF, vold[v]);
                     const bool zfast = a >= 4 && a <= nz - 5 && a < nz - npml && !(sh.topabsorb && a < npml);
                     bool vact = true;
                     if constexpr (PUNCH) vact = punch_active(sh.punch, x, a, it);
@@ -1194,14 +1134,12 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                             for (int t = 0; t < ntl; ++t) {
                                 const int4 tm = tl[t];
                                 if (tm.x == FD23_V && tm.z == a && tm.y >= x && tm.y < x + 4) {
-                                    UT *cell = const_cast<UT *>(vrow) + (tm.y - x);
-                                    const C nv = to_c<C>(*cell) + sh.tamp[(long long)tm.w * sh.tamp_nt + it];
-                                    if constexpr (K::CVT) *cell = through<S, C>(nv);  // the value S would hold
-                                    else *cell = to_s<S>(nv);
+                                    S *cell = const_cast<S *>(vrow) + (tm.y - x);
+                                    *cell = to_s<S>(to_c<C>(*cell) + sh.tamp[(long long)tm.w * sh.tamp_nt + it]);
                                     hit = true;
                                 }
                             }
-                            if (hit) Vec4<UT, C>::ld(vrow, vold[0]);
+                            if (hit) Vec4<S, C>::ld(vrow, vold[0]);
                         }
                     }
                     if (xfast && zfast) {
@@ -1462,12 +1400,10 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
             // release the ring slots this iteration was the last reader of
             __syncwarp();
             if (lane == 0) {
-                if constexpr (!K::CVT) {  // (CVT: released when converted)
-                    mbar_arrive(&empty_uw[(uw_base + i) % K::NUW]);
-                    if (i == I.niter - 1) {
-                        mbar_arrive(&empty_uw[(uw_base + i + 1) % K::NUW]);
-                        mbar_arrive(&empty_uw[(uw_base + i + 2) % K::NUW]);
-                    }
+                mbar_arrive(&empty_uw[(uw_base + i) % K::NUW]);
+                if (i == I.niter - 1) {
+                    mbar_arrive(&empty_uw[(uw_base + i + 1) % K::NUW]);
+                    mbar_arrive(&empty_uw[(uw_base + i + 2) % K::NUW]);
                 }
                 mbar_arrive(&empty_pw[gflat % K::NPW]);
             }

@@ -58,13 +58,8 @@ def smem_layout(es, wave):
     pg_ms = al128(nt * 4 * pww * es)
     pg_mv = pg_ms + al128(nms * 4 * pww * es)
     stage = pg_mv + al128(nmv * 4 * pww * es)
-    # 16-bit storage: 3 landing slots, and a 5-slot ring of the converted
-    # (4-byte) stencil inputs that the stencils read
-    nuw = 3 if es == 2 else NUW
-    ncr = 5 if es == 2 else 0
     return dict(nv=nv, nt=nt, nms=nms, nmv=nmv, pwoff=pwoff, pww=pww, uw_slot=uw_slot, pg_ms=pg_ms,
-                pg_mv=pg_mv, stage=stage, pw_base=nuw * uw_slot, nuw=nuw, ncr=ncr,
-                uwc_slot=nv * 4 * UWW * 4)
+                pg_mv=pg_mv, stage=stage, pw_base=NUW * uw_slot)
 
 
 def box_ok(x, y, z, w, nf, pitch, rows, nfields, es):
@@ -84,7 +79,7 @@ def audit(nx, nz, es, wave, per_sm=3, oversub=1.0, ctas=None, narrowed=False, ba
     elems = pitch * rows
     lay = smem_layout(es, wave)
     nfld = 5 if wave == "psv" else 3
-    for off in [k * lay["uw_slot"] for k in range(lay["nuw"])] + \
+    for off in [k * lay["uw_slot"] for k in range(NUW)] + \
                [lay["pw_base"] + g * lay["stage"] + o for g in range(NPW) for o in (0, lay["pg_ms"], lay["pg_mv"])]:
         assert off % 128 == 0
     nv = 2 if wave == "psv" else 1
@@ -392,15 +387,14 @@ def test_strip_origin_puts_the_cpml_into_fewest_strips(nx, nz, npml, want_xp):
 @pytest.mark.parametrize("batch", [False, True])
 def test_three_ctas_fit_per_sm(es, wave, batch):
     """Dynamic shared memory of the sweep (Cfg::SMEM in fd23_fused.cuh: the
-    landing ring and the point-wise stages in the storage type, the stress
-    ring and, for 16-bit storage, the converted stencil inputs in the
-    arithmetic type (4-byte floats for every form but FP64), barriers, item
-    and source-term tables), its static shared memory (the batched sweep's
-    copy of the descriptor head) and the 1 KB the runtime reserves per CTA:
-    three CTAs fit the 228 KB of one SM."""
+    two rings and the point-wise stages in the storage type, the stress ring
+    in the arithmetic type (4-byte floats for every form but FP64), barriers,
+    item and source-term tables), its static shared memory (the batched
+    sweep's copy of the descriptor head) and the 1 KB the runtime reserves
+    per CTA: three CTAs fit the 228 KB of one SM."""
     lay = smem_layout(es, wave)
     nt = lay["nt"]
-    ring = lay["nuw"] * lay["uw_slot"] + NPW * lay["stage"] + NTR * 4 * nt * SW * 4 + lay["ncr"] * lay["uwc_slot"]
+    ring = NUW * lay["uw_slot"] + NPW * lay["stage"] + NTR * 4 * nt * SW * 4
     smem = (ring + 15) // 16 * 16 + 256 + MAX_ITEMS * 16 + MAX_ITEMS * 16 * 16
     static = 512 if batch else 128
     assert 3 * (smem + static + 1024) <= 228 * 1024, (smem, static)
