@@ -51,7 +51,7 @@ ABI_FUNCTIONS = [
     "fd23_get_seismograms", "fd23_reset", "fd23_get_stream", "fd23_get_step", "fd23_get_field_device", "fd23_state_bytes", "fd23_get_state",
     "fd23_set_state", "fd23_field_norm2", "fd23_build_material", "fd23_build_cpml",
     "fd23_build_source_terms", "fd23_sum_squares_noalloc", "fd23_set_box", "fd23_set_box_incident",
-    "fd23_set_box_incident_async",
+    "fd23_set_box_incident_async", "fd23_set_model_box",
     "fd23_box_state_bytes", "fd23_get_box_state", "fd23_set_box_state", "fd23_box_ring_size",
     "fd23_box_ring_index", "fd23_box_ring_cells", "fd23_box_incident_from_displacement",
     "fd23_box_material", "fd23_batch_create", "fd23_batch_destroy", "fd23_batch_run", "fd23_batch_sync",
@@ -145,6 +145,7 @@ def lib():
         "fd23_build_source_terms": ([i, i, i, i, vp, d, d, vp, i, i, vp, vp, vp, vp, i], i),
         "fd23_sum_squares_noalloc": ([i, vp, i, sz, vp, _C.POINTER(d), _C.POINTER(i)], i),
         "fd23_set_box": ([vp, i, i, i, i, vp], i),
+        "fd23_set_model_box": ([vp, vp, vp, vp, i, i, i, i, d, d, d, vp, vp, vp], i),
         "fd23_set_box_incident": ([vp, vp, i, i], i),
         "fd23_set_box_incident_async": ([vp, vp, i, i], i),
         "fd23_box_state_bytes": ([vp], sz),
@@ -716,6 +717,23 @@ class Solver:
             bmat = _sized(_f64(bmat), 5 * max(bx, 0) * max(bz, 0), "bmat")
         _check(lib().fd23_set_box(self._h, x0, z0, bx, bz, _p(bmat)), "fd23_set_box")
         self._box = (x0, z0, bx, bz) if bx else None
+
+    def set_model_box(self, vp, vs, den, x0, z0, bx, bz, src_vp, src_vs, src_den):
+        """fd23_set_model_box: the material built on the device, the box at
+        (x0, z0) homogenised towards the source material and its box material
+        installed (box_material + set_material + set_box(bmat) on the host);
+        returns the number of box cells that took the source material and the
+        FP64 box material (5, bz, bx)."""
+        n = self.nx * self.nz
+        vp, vs, den = (_sized(_f64(a), n, nm) for a, nm in ((vp, "vp"), (vs, "vs"), (den, "den")))
+        stab = _C.c_double(0.0)
+        rep = _C.c_int(0)
+        bmat = _np.zeros((5, bz, bx))
+        _check(lib().fd23_set_model_box(self._h, _p(vp), _p(vs), _p(den), x0, z0, bx, bz, float(src_vp),
+                                        float(src_vs), float(src_den), _C.byref(stab), _C.byref(rep), _p(bmat)),
+               "fd23_set_model_box")
+        self._box = (x0, z0, bx, bz)
+        return rep.value, bmat
 
     def set_box_incident(self, inc, it0=0, wait=True):
         """inc [nsteps, 5, nring] (U W Txx Txz Tzz on the ring cells) for steps

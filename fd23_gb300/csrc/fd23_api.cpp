@@ -1236,16 +1236,9 @@ int fd23_set_box(fd23_solver *s, int x0, int z0, int bx, int bz, const double *b
     if (bx < kBoxMin || bz < kBoxMin || x0 < 0 || z0 < 0 || x0 + bx > s->d.nx || z0 + bz > s->d.nz)
         return FD23_ERR_ARG;
     if (!bmat && !s->have_material) return FD23_ERR_ORDER;
-    free_box(s);
+    int rc = box_alloc(s, x0, z0, bx, bz);
+    if (rc) return rc;
     const size_t nb = (size_t)bx * bz, bytes = nb * s->cs;
-    int rc = FD23_OK;
-    for (int f = 0; f < 5; ++f) {
-        if ((rc = dev_alloc(&s->box_r[f], bytes)) || (rc = dev_alloc(&s->box_mat[f], bytes))) {
-            free_box(s);
-            return rc;
-        }
-        CK(cudaMemsetAsync(s->box_r[f], 0, bytes, s->stream));
-    }
     if (bmat) {
         std::vector<unsigned char> tmp(bytes);
         for (int m = 0; m < 5; ++m) {
@@ -1260,6 +1253,51 @@ int fd23_set_box(fd23_solver *s, int x0, int z0, int bx, int bz, const double *b
                                      (size_t)(s->L.origin + (long long)z0 * s->L.pitch + x0) * s->es,
                                  (size_t)s->L.pitch * s->es, (size_t)bx * s->es, (size_t)bz,
                                  cudaMemcpyDeviceToDevice, s->stream));
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    return FD23_OK;
+}
+
+int fd23_set_model_box(fd23_solver *s, const double *vp, const double *vs, const double *den, int x0, int z0,
+                       int bx, int bz, double src_vp, double src_vs, double src_den, double *stab, int *replaced,
+                       double *bmat)
+{
+    if (!s || !vp || !vs || !den) return FD23_ERR_ARG;
+    if (s->d.wave != FD23_PSV || scaled_form(s) || s->d_punch || s->table_on) return FD23_ERR_UNSUPPORTED;
+    if (bx < kBoxMin || bz < kBoxMin || x0 < 0 || z0 < 0 || x0 + bx > s->d.nx || z0 + bz > s->d.nz)
+        return FD23_ERR_ARG;
+    const double st = material_stab(s->d.wave, vp, vs, (size_t)s->d.nx * s->d.nz, s->d.h, s->d.dt);
+    if (stab) *stab = st;
+    if (st > 1.0) return FD23_ERR_UNSTABLE;
+    CK(cudaSetDevice(s->d.device));
+    CK(cudaStreamSynchronize(s->stream));
+    int rc = box_alloc(s, x0, z0, bx, bz);
+    if (!rc)
+        rc = build_material_box_device(s, vp, vs, den, x0, z0, bx, bz, src_vp, src_vs, src_den, replaced, bmat);
+    if (rc) {
+        free_box(s);
+        return rc;
+    }
+    return material_done(s);
+}
+
+}  // extern "C"
+
+namespace fd23 {
+
+// The box's arrays (residual r zeroed; material arrays allocated, not filled)
+// and its ring list; the box is then on
+int box_alloc(fd23_solver *s, int x0, int z0, int bx, int bz)
+{
+    free_box(s);
+    const size_t nb = (size_t)bx * bz, bytes = nb * s->cs;
+    int rc = FD23_OK;
+    for (int f = 0; f < 5; ++f) {
+        if ((rc = dev_alloc(&s->box_r[f], bytes)) || (rc = dev_alloc(&s->box_mat[f], bytes))) {
+            free_box(s);
+            return rc;
+        }
+        CK(cudaMemsetAsync(s->box_r[f], 0, bytes, s->stream));
     }
     // ring cells in incident-field order; the closed-form position used by
     // the sweep must agree with the enumeration
@@ -1291,6 +1329,10 @@ int fd23_set_box(fd23_solver *s, int x0, int z0, int bx, int bz, const double *b
     s->box_inc_n = 0;
     return FD23_OK;
 }
+
+}  // namespace fd23
+
+extern "C" {
 
 int fd23_set_box_incident(fd23_solver *s, const void *inc, int it0, int nsteps)
 {

@@ -77,6 +77,18 @@ struct MatOut {
     unsigned long long *maxbits;   // kMax: [2] bit patterns of the group maxima
 };
 
+// Hybrid-box homogenisation applied while the material is stored (P-SV,
+// kStore): the cells of the box whose dt/h-scaled coefficients differ from
+// the source material's by more than 1e-4 (relative) take the source
+// material, and every box cell's final values go to bmat ([5][bz][bx],
+// FP64), as box_material does on the host (PD/material/material.cpp:39-97).
+struct BoxHomog {
+    int on, x0, z0, bx, bz;
+    double lam, mu, b;     // source material, dt/h scaled
+    double *bmat;
+    int *replaced;
+};
+
 template <class S, int MODE>
 struct MatSink {
     const MatOut &o;
@@ -126,7 +138,7 @@ struct MatSink {
 // free-surface row, the dt/h factor; written to the padded storage arrays
 template <class S, int MODE = kStore>
 __global__ void psv_rest(int nx, int nz, const double *den, const double *mu, const double *lam, double fac,
-                         MatOut out, S *LAM, S *MU, S *MUA, S *BU, S *BW)
+                         MatOut out, S *LAM, S *MU, S *MUA, S *BU, S *BW, BoxHomog hb)
 {
     MatSink<S, MODE> sink(out);
     const long long n = (long long)nx * nz;
@@ -150,11 +162,25 @@ __global__ void psv_rest(int nx, int nz, const double *den, const double *mu, co
             l = 0.0;
             m = 0.5 * m;
         }
-        sink.put(LAM, k, nx, true, l * fac);
-        sink.put(MU, k, nx, true, m * fac);
-        sink.put(MUA, k, nx, true, mua * fac);
-        sink.put(BU, k, nx, false, bu * fac);
-        sink.put(BW, k, nx, false, bw * fac);
+        double v[5] = {l * fac, m * fac, mua * fac, bu * fac, bw * fac};
+        if (hb.on && ix >= hb.x0 && ix < hb.x0 + hb.bx && iz >= hb.z0 && iz < hb.z0 + hb.bz) {
+            const double eps = 1e-4;
+            if (fabs(hb.b - v[3]) > hb.b * eps || fabs(hb.b - v[4]) > hb.b * eps || fabs(hb.mu - v[1]) > hb.mu * eps ||
+                fabs(hb.mu - v[2]) > hb.mu * eps || fabs(hb.lam - v[0]) > hb.lam * eps) {
+                v[0] = hb.lam;
+                v[1] = v[2] = hb.mu;
+                v[3] = v[4] = hb.b;
+                atomicAdd(hb.replaced, 1);
+            }
+            const long long nb = (long long)hb.bx * hb.bz, q = (long long)(iz - hb.z0) * hb.bx + (ix - hb.x0);
+#pragma unroll
+            for (int f = 0; f < 5; ++f) hb.bmat[f * nb + q] = v[f];
+        }
+        sink.put(LAM, k, nx, true, v[0]);
+        sink.put(MU, k, nx, true, v[1]);
+        sink.put(MUA, k, nx, true, v[2]);
+        sink.put(BU, k, nx, false, v[3]);
+        sink.put(BW, k, nx, false, v[4]);
     }
     sink.finish();
 }
@@ -181,7 +207,7 @@ __global__ void sh_all(int nx, int nz, const double *vs, const double *den, doub
 }
 
 template <class S, bool SCALED>
-int build_on_device(fd23_solver *s, const double *vp, const double *vs, const double *den)
+int build_on_device(fd23_solver *s, const double *vp, const double *vs, const double *den, const BoxHomog &hb)
 {
     const int nx = s->d.nx, nz = s->d.nz;
     const size_t n = (size_t)nx * nz, bytes = n * sizeof(double);
@@ -203,7 +229,7 @@ int build_on_device(fd23_solver *s, const double *vp, const double *vs, const do
         constexpr int M = decltype(mode)::value;
         if (s->d.wave == FD23_PSV)
             psv_rest<S, M><<<blocks, 256, 0, s->stream>>>(nx, nz, dden, dmu, dlam, fac, out, mm[0], mm[1], mm[2],
-                                                          mm[3], mm[4]);
+                                                          mm[3], mm[4], M == kStore ? hb : BoxHomog{});
         else
             sh_all<S, M><<<blocks, 256, 0, s->stream>>>(nx, nz, dvs, dden, fac, out, mm[0], mm[1], mm[2]);
     };
@@ -258,12 +284,68 @@ int build_on_device(fd23_solver *s, const double *vp, const double *vs, const do
 
 int build_material_device(fd23_solver *s, const double *vp, const double *vs, const double *den)
 {
+    const BoxHomog none{};
     switch (s->d.prec) {
-        case FD23_F64: return build_on_device<double, false>(s, vp, vs, den);
-        case FD23_F32: return build_on_device<float, false>(s, vp, vs, den);
-        case FD23_F16: return build_on_device<__half, true>(s, vp, vs, den);
-        default: return build_on_device<__nv_bfloat16, true>(s, vp, vs, den);
+        case FD23_F64: return build_on_device<double, false>(s, vp, vs, den, none);
+        case FD23_F32: return build_on_device<float, false>(s, vp, vs, den, none);
+        case FD23_F16: return build_on_device<__half, true>(s, vp, vs, den, none);
+        default: return build_on_device<__nv_bfloat16, true>(s, vp, vs, den, none);
     }
+}
+
+namespace {
+template <class C>
+__global__ void to_compute_kernel(long long n, const double *in, C *out)
+{
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+        out[k] = (C)in[k];
+}
+}  // namespace
+
+int build_material_box_device(fd23_solver *s, const double *vp, const double *vs, const double *den, int x0,
+                              int z0, int bx, int bz, double src_vp, double src_vs, double src_den, int *replaced,
+                              double *bmat_out)
+{
+    // the source material as the host's box_material computes it
+    const double dt = s->d.dt, h = s->d.h;
+    const double mu0 = src_vs * src_vs * src_den;
+    BoxHomog hb{1, x0, z0, bx, bz, (src_vp * src_vp * src_den - 2.0 * mu0) * dt / h, mu0 * dt / h,
+                1.0 / src_den * dt / h, nullptr, nullptr};
+    const size_t nb = (size_t)bx * bz;
+    void *scratch = nullptr;
+    int rc = dev_alloc(&scratch, 5 * nb * sizeof(double) + sizeof(int));
+    if (rc) return rc;
+    hb.bmat = static_cast<double *>(scratch);
+    hb.replaced = reinterpret_cast<int *>(hb.bmat + 5 * nb);
+    cudaError_t e = cudaMemsetAsync(hb.replaced, 0, sizeof(int), s->stream);
+    if (e == cudaSuccess) {
+        rc = s->d.prec == FD23_F64 ? build_on_device<double, false>(s, vp, vs, den, hb)
+                                   : build_on_device<float, false>(s, vp, vs, den, hb);
+    } else {
+        rc = FD23_ERR_CUDA;
+    }
+    // the box material in the compute type (the residual field's material)
+    for (int m = 0; m < 5 && rc == FD23_OK; ++m) {
+        const unsigned blocks = (unsigned)std::min<size_t>((nb + 255) / 256, 1024);
+        if (s->d.prec == FD23_F64)
+            to_compute_kernel<double><<<blocks, 256, 0, s->stream>>>((long long)nb, hb.bmat + m * nb,
+                                                                     static_cast<double *>(s->box_mat[m]));
+        else
+            to_compute_kernel<float><<<blocks, 256, 0, s->stream>>>((long long)nb, hb.bmat + m * nb,
+                                                                    static_cast<float *>(s->box_mat[m]));
+        if (cudaGetLastError() != cudaSuccess) rc = FD23_ERR_CUDA;
+    }
+    int nrep = 0;
+    if (rc == FD23_OK && bmat_out &&
+        cudaMemcpyAsync(bmat_out, hb.bmat, 5 * nb * sizeof(double), cudaMemcpyDeviceToHost, s->stream) != cudaSuccess)
+        rc = FD23_ERR_CUDA;
+    if (rc == FD23_OK && (cudaMemcpyAsync(&nrep, hb.replaced, sizeof(int), cudaMemcpyDeviceToHost, s->stream) !=
+                              cudaSuccess ||
+                          cudaStreamSynchronize(s->stream) != cudaSuccess))
+        rc = FD23_ERR_CUDA;
+    cudaFree(scratch);
+    if (rc == FD23_OK && replaced) *replaced = nrep;
+    return rc;
 }
 
 }  // namespace fd23

@@ -171,6 +171,12 @@ int encode_maps(fd23_solver *s);
 // the material of vp, vs, den built on the device into the storage arrays
 // (fd23_matgpu.cu; FP32 and FP64 storage, FD23_ERR_UNSUPPORTED otherwise)
 int build_material_device(fd23_solver *s, const double *vp, const double *vs, const double *den);
+// the same with the hybrid box homogenised (box_material's rule) and the box
+// material stored into the box's arrays (P-SV, FP32 / FP64)
+int build_material_box_device(fd23_solver *s, const double *vp, const double *vs, const double *den, int x0,
+                              int z0, int bx, int bz, double src_vp, double src_vs, double src_den, int *replaced,
+                              double *bmat_out);
+int box_alloc(fd23_solver *s, int x0, int z0, int bx, int bz);
 // 16-bit forms: the power-of-two scale of a value, the source amplitudes in
 // the scaled units (once kappa is known)
 double pow2_round(double v);

@@ -229,6 +229,18 @@ int fd23_set_state(fd23_solver *s, const void *buf, size_t bytes, int it0);
  * A box excludes tile step windows (fd23_set_punch) and material tables
  *   (fd23_set_material_table): FD23_ERR_UNSUPPORTED. */
 int fd23_set_box(fd23_solver *s, int x0, int z0, int bx, int bz, const double *bmat);
+/* fd23_set_model and the reference's box set-up in one call, on the device:
+ * the material from vp, vs, den (fd23_set_model), then the box at (x0, z0)
+ * homogenised towards the source material src_vp, src_vs, src_den and its
+ * box material installed, as fd23_box_material + fd23_set_material +
+ * fd23_set_box(..., bmat) do on the host (MATERIAL::init_for_box_from_full,
+ * PD/material/material.cpp:39-97), with the same values.  replaced (may be
+ * NULL) receives the number of box cells that took the source material, bmat
+ * (may be NULL) the box material as fd23_box_material returns it (FP64,
+ * 5 x bz x bx: what fd23_set_box_line_source takes). */
+int fd23_set_model_box(fd23_solver *s, const double *vp, const double *vs, const double *den, int x0, int z0,
+                       int bx, int bz, double src_vp, double src_vs, double src_den, double *stab, int *replaced,
+                       double *bmat);
 int fd23_set_box_incident(fd23_solver *s, const void *inc, int it0, int nsteps);
 /* The same upload without waiting for it: the copy runs on a copy stream in
  * chunks of steps, each box step of the solver waits only for the chunk that

@@ -237,3 +237,49 @@ def test_box_incident_async_upload():
         s.close()
     for a, b in zip(out[True], out[False]):
         np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_set_model_box_equals_host_path(prec):
+    """fd23_set_model_box (material built on the device, the box homogenised
+    towards the source material, the box material installed) gives the host
+    path's results (fd23_build_material, fd23_box_material, set_material,
+    set_box with bmat): the same number of replaced cells, and bit for bit the
+    same seismograms, state and residual field of a box run.  The box
+    straddles a layer boundary, so part of it takes the source material."""
+    nx, nz, npml, nt = 260, 180, 12, 50
+    c = Case("psv", nx, nz, npml=npml, nt=nt, xs=60, zs=10, seed=6)
+    vp = np.full((nz, nx), 4.0)
+    vp[90:, :] = 5.0
+    vp[:, 200:] += 0.5  # a lateral step outside the box
+    vs, den = vp / 1.73, 0.31 * vp ** 0.25 * 8.0
+    x0, z0, bw = 110, 76, 32
+    sv = (float(vp[z0 + 2, x0 + 2]), float(vs[z0 + 2, x0 + 2]), float(den[z0 + 2, x0 + 2]))
+    mat, stab, rc = F.build_material("psv", vp, vs, den, c.h, c.dt)
+    assert rc == 0
+    mat, bmat, nrep = F.box_material(mat, x0, z0, bw, bw, *sv, c.dt, c.h)
+    assert 0 < nrep < bw * bw
+    ci = Case("psv", nx, nz, npml=npml, nt=nt, xs=120, zs=92, seed=23)
+    box = (x0, z0, bw, bw)
+    inc, _ = O.psv_ring_history("f64", nx, nz, npml, 0, ci.mat, ci.bck, ci.terms, nt, box)
+    inc = inc.astype(np.float64 if prec == "f64" else np.float32)
+    out = {}
+    for path in ("host", "device"):
+        s = F.Solver("psv", nx, nz, npml, c.h, c.dt, prec=prec, kernel="fused", **c.pml)
+        if path == "host":
+            s.set_material(mat)
+            s.set_box(*box, bmat=bmat)
+        else:
+            n_dev, bmat_dev = s.set_model_box(vp, vs, den, *box, *sv)
+            assert n_dev == nrep
+            np.testing.assert_array_equal(bmat_dev, bmat)
+        s.set_source(c.kind, c.xs, c.zs, c.m, c.src, nt)
+        for f in range(5):
+            s.set_receivers(f, np.array([20, 111, 126, 140, 250], np.int32), np.array([0, 77, 92, 100, 5], np.int32))
+        s.set_box_incident(inc, 0)
+        s.run(nt, 1)
+        out[path] = [s.seismograms(f) for f in range(5)] + [s.get_state(), s.get_box_state()]
+        s.close()
+    assert np.abs(out["device"][-1]).max() > 0
+    for a, b in zip(out["host"], out["device"]):
+        np.testing.assert_array_equal(a, b)
