@@ -27,9 +27,12 @@
  *                                  PN/cpml/cu_cpml.cu:92,109     fd23_get_state / fd23_set_state
  *   BOX::init_box                  PD/box/box.cpp:10-119        fd23_set_box, fd23_box_ring_*
  *   MATERIAL::init_for_box_from_full PD/material/material.cpp:39  fd23_box_material
+ *                                  (with get_model + init_box on the device:
+ *                                                                fd23_set_model_box)
  *   BOX::setboxsource / cu_copy_source
  *                                  PD/box/box.cpp:120, PD/box/cu_box.cu:35
  *                                         fd23_box_incident_from_displacement + fd23_set_box_incident
+ *                                         (or fd23_set_box_incident_async)
  *   BOX::cu_addsource/cu_subsource, cu_step_stress_r/_velocity_r
  *                                  PD/box/cu_box.cu:55,71; PD/fd/cu_fd.cu:504,523  fd23_run (box set)
  *   the box-source generator ntde_line (compute_pQpW_mathematica + cu_con)
