@@ -374,11 +374,12 @@ struct Cfg {
     static constexpr int TR_ELEMS = NTR * 4 * NT * SW;
     static constexpr int TAB_ELEMS = TABLE ? (NMS + NMV) * kTabEntries : 0;  // the table, per CTA
     // Uniform fast iterations (interior rows of all-interior warps with no
-    // per-lane branch) for 16-bit storage, whose sweep is held by instruction
-    // issue: 10 % fewer instructions, C1 FP16 9.11e10 cell-updates/s against
-    // 8.71e10, C3 FP16 1.26e11 against 1.10e11.  The FP32 sweep is held by
-    // latency: 13 % fewer instructions gave C1 8.03e10 against 8.13e10 and
-    // spilled in the batched form (C4 7.28e10 against 7.81e10), same box.
+    // per-lane branch) for the single-shot 16-bit sweep, which is held by
+    // instruction issue: 14 % fewer instructions, C1 FP16 9.11e10
+    // cell-updates/s against 8.71e10, C3 FP16 1.26e11 against 1.10e11.  The
+    // FP32 sweep is held by latency: 13 % fewer instructions gave C1 8.03e10
+    // against 8.13e10.  In the batched sweeps the extra registers spill
+    // (C4 FP32 7.28e10 against 7.81e10, C4 FP16 8.14e10 against 8.64e10).
     static constexpr bool FAST_ITER = sizeof(S) == 2;
     // bytes the copies of one point-wise stage deliver
     static constexpr uint32_t PW_TX =
@@ -758,7 +759,7 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
         // velocity row belongs to the item, i.e. j in [fjlo, fjhi] (an empty
         // range when the item is not fast): every lane then takes the
         // interior arithmetic with no per-lane branch.
-        bool item_fast = K::FAST_ITER && !PUNCH && __all_sync(0xffffffffu, xfast) && ntl == 0;
+        bool item_fast = K::FAST_ITER && !BATCH && !PUNCH && __all_sync(0xffffffffu, xfast) && ntl == 0;
         if constexpr (PSV && std::is_same<S, C>::value && !BATCH) item_fast = item_fast && !sh.box.on;
         const int fjlo = item_fast ? max(I.z0, max(4, sh.topabsorb ? npml : 0)) + 4 : INT_MAX;
         const int fjhi = min(nz - 5, nz - npml - 1);
@@ -776,7 +777,7 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
             const int jf = I.z0 - 4 + 4 * i + grp;  // stress row; the velocity row is jf - 4
             // (an SH item starting at row 0 meets its free-surface barrier at
             // i = 1, where jf < 4: never fast, so every warp takes it)
-            if (K::FAST_ITER && !PUNCH && jf >= fjlo && jf <= fjhi) {
+            if (K::FAST_ITER && !BATCH && !PUNCH && jf >= fjlo && jf <= fjhi) {
                 // ---- stress of row jf, every lane ----
                 {
                     const S *urow[9];
