@@ -819,17 +819,23 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                 }
                 ok = compute_bar_and(NCT, ok) != 0;
                 if (!ok) break;
-                // ---- velocity of row jf - 4, every lane; the halo lanes' reads
-                // stay inside shared memory and their results are not stored ----
+                // ---- velocity of row jf - 4, every lane.  The halo lanes 0 and
+                // 31 read their neighbours' operands (lanes 1 and 30), so a
+                // warp's loads span the same shared-memory wavefronts as the
+                // owned lanes' alone, and their results are not stored ----
                 {
                     const int a = jf - 4;
+                    // (the lane id read here, not held across the loop)
+                    uint32_t lid;
+                    asm volatile("mov.u32 %0, %%laneid;" : "=r"(lid));
+                    const int dl = lid == 0 ? 4 : (lid == 31 ? -4 : 0);  // 0 on the owned lanes
                     const C *trow[9];
 #pragma unroll
-                    for (int d = 0; d < 9; ++d) trow[d] = trrow(a - 4 + d);
+                    for (int d = 0; d < 9; ++d) trow[d] = trrow(a - 4 + d) + dl;
                     C mv[K::NMV][4];
                     if constexpr (TABLE) {
                         const uint32_t q = *reinterpret_cast<const uint32_t *>(
-                            reinterpret_cast<const unsigned char *>(pws + K::PG_MS) + grp * kIdxBoxW + ixo);
+                            reinterpret_cast<const unsigned char *>(pws + K::PG_MS) + grp * kIdxBoxW + ixo + dl);
 #pragma unroll
                         for (int m = 0; m < K::NMV; ++m)
 #pragma unroll
@@ -837,10 +843,10 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                                 mv[m][e] = to_c<C>(tab_s[(K::NMS + m) * kTabEntries + ((q >> (8 * e)) & 255u)]);
                     } else {
 #pragma unroll
-                        for (int m = 0; m < K::NMV; ++m) Vec4<S, C>::ld(pwrow(K::NT + K::NMS + m), mv[m]);
+                        for (int m = 0; m < K::NMV; ++m) Vec4<S, C>::ld(pwrow(K::NT + K::NMS + m) + dl, mv[m]);
                     }
                     const int vr = (4 * (uw_base + i) + grp) & (4 * K::NUW - 1);
-                    const S *vrow = uw_s + (vr >> 2) * K::UW_SLOT + (vr & 3) * K::UWW + 4 * lane + 4;
+                    const S *vrow = uw_s + (vr >> 2) * K::UW_SLOT + (vr & 3) * K::UWW + 4 * lane + 4 + dl;
                     C vold[K::NV][4], vnew[K::NV][4];
 #pragma unroll
                     for (int v = 0; v < K::NV; ++v) Vec4<S, C>::ld(vrow + v * K::UWF, vold[v]);

@@ -1,0 +1,54 @@
+"""The uniform fast iterations of the single-shot 16-bit fused sweep
+(fd23_gb300/csrc/fd23_fused.cuh, Cfg::FAST_ITER).
+
+A warp takes them on rows that are z-interior in both its stress row and its
+velocity row, when all of its lanes are x-interior and its item has no source
+term.  The cases below move where they start and stop: no CPML (from row 4),
+an absorbing top (from row npml), a source item in mid-grid (per-lane
+iterations there), a grid barely wider than one strip (edge lanes in every
+warp), and two plans whose items start on different rows.  In every case the
+fused sweep equals the two-pass sweep bit for bit, as the two round through
+the same storage at the same points.
+"""
+import numpy as np
+import pytest
+
+from tests.fd23_cases import Case
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    dict(wave="psv", nx=500, nz=260, npml=0),
+    dict(wave="psv", nx=500, nz=260, npml=20, topabsorb=1),
+    dict(wave="psv", nx=500, nz=260, npml=12, xs=250, zs=130),
+    dict(wave="psv", nx=140, nz=200, npml=8),
+    dict(wave="sh", nx=500, nz=260, npml=0),
+    dict(wave="sh", nx=500, nz=260, npml=16, topabsorb=1),
+]
+
+
+def _ids(c):
+    return "%s_%dx%d_pml%d_top%d%s" % (c["wave"], c["nx"], c["nz"], c["npml"], c.get("topabsorb", 0),
+                                       "_src_mid" if "zs" in c else "")
+
+
+@pytest.mark.parametrize("oversub", [1.0, 3.0])
+@pytest.mark.parametrize("prec", ["f16", "bf16"])
+@pytest.mark.parametrize("cfg", CASES, ids=_ids)
+def test_fast_iterations_equal_twopass(cfg, prec, oversub):
+    F = pytest.importorskip("fd23_gb300")
+    c = Case(nt=50, seed=21, **cfg)
+
+    def run(kernel):
+        s = c.solver(prec, kernel)
+        if kernel == "fused":
+            s.set_plan(4.0, 2.5, 3, oversub)
+        s.run(c.nt, 1)
+        out = [s.seismograms(0)] + ([s.seismograms(1)] if c.wave == "psv" else []) + [s.get_state()]
+        s.close()
+        return out
+
+    fused, twopass = run("fused"), run("twopass")
+    assert np.isfinite(fused[-1]).all()
+    for a, b in zip(fused, twopass):
+        np.testing.assert_array_equal(a, b)
