@@ -6,7 +6,8 @@ velocity row, when all of its lanes are x-interior and its item has no source
 term.  The cases below move where they start and stop: no CPML (from row 4),
 an absorbing top (from row npml), a source item in mid-grid (per-lane
 iterations there), a grid barely wider than one strip (edge lanes in every
-warp), and two plans whose items start on different rows.  In every case the
+warp), a tall grid whose items run for dozens of blocks, and two plans whose
+items start on different rows.  In every case the
 fused sweep equals the two-pass sweep bit for bit, as the two round through
 the same storage at the same points.
 """
@@ -22,6 +23,9 @@ CASES = [
     dict(wave="psv", nx=500, nz=260, npml=20, topabsorb=1),
     dict(wave="psv", nx=500, nz=260, npml=12, xs=250, zs=130),
     dict(wave="psv", nx=140, nz=200, npml=8),
+    # long items (one CTA per SM, a sixteenth or an eighth of a wave):
+    # most iterations fast
+    dict(wave="psv", nx=1000, nz=1200, npml=20, per_sm=1, ov_scale=1 / 16),
     dict(wave="sh", nx=500, nz=260, npml=0),
     dict(wave="sh", nx=500, nz=260, npml=16, topabsorb=1),
 ]
@@ -37,12 +41,14 @@ def _ids(c):
 @pytest.mark.parametrize("cfg", CASES, ids=_ids)
 def test_fast_iterations_equal_twopass(cfg, prec, oversub):
     F = pytest.importorskip("fd23_gb300")
-    c = Case(nt=50, seed=21, **cfg)
+    plan = {k: cfg[k] for k in ("per_sm", "ov_scale") if k in cfg}
+    c = Case(nt=50, seed=21, **{k: v for k, v in cfg.items() if k not in plan})
+    per_sm, ov = plan.get("per_sm", 3), oversub * plan.get("ov_scale", 1.0)
 
     def run(kernel):
         s = c.solver(prec, kernel)
         if kernel == "fused":
-            s.set_plan(4.0, 2.5, 3, oversub)
+            s.set_plan(4.0, 2.5, per_sm, ov)
         s.run(c.nt, 1)
         out = [s.seismograms(0)] + ([s.seismograms(1)] if c.wave == "psv" else []) + [s.get_state()]
         s.close()
