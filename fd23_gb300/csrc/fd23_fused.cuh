@@ -181,7 +181,18 @@ struct Vec4Half {
     }
 };
 template <>
-struct Vec4<__nv_bfloat16, float> : Vec4Half<__nv_bfloat16> {};
+struct Vec4<__nv_bfloat16, float> : Vec4Half<__nv_bfloat16> {
+    // a BF16 value is the upper half of the FP32 value it converts to
+    // (exactly): one shift or one mask per value of a packed pair
+    static __device__ __forceinline__ void ld(const __nv_bfloat16 *p, float v[4])
+    {
+        const uint2 t = *reinterpret_cast<const uint2 *>(p);
+        v[0] = __uint_as_float(t.x << 16);
+        v[1] = __uint_as_float(t.x & 0xffff0000u);
+        v[2] = __uint_as_float(t.y << 16);
+        v[3] = __uint_as_float(t.y & 0xffff0000u);
+    }
+};
 template <>
 struct Vec4<__half, float> : Vec4Half<__half> {};
 
