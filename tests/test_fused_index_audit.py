@@ -426,3 +426,44 @@ def test_plans_without_cpml_and_narrow_grids(nx, nz, npml, bands, ov):
             seen[(x0, zb)] = seen.get((x0, zb), 0) + 1
     assert len(seen) == len(x0s) * nzb and set(seen.values()) == {1}
     audit(nx, nz, 4, "psv", ctas=[[it[1:] for it in cta] for cta in ctas])
+
+
+@pytest.mark.parametrize("nx,nz,npml,top", [(4000, 2000, 40, 0), (1000, 500, 20, 1), (500, 260, 0, 0),
+                                            (140, 200, 8, 0), (16000, 8000, 40, 0)])
+@pytest.mark.parametrize("bands", [0, 1])
+def test_fast_iterations_are_interior(nx, nz, npml, top, bands):
+    """The fast-iteration test of the single-shot 16-bit sweep (fd23_fused.cuh:
+    item_fast, fjlo, fjhi) restated.  On every warp-iteration it accepts, every
+    lane of the warp is x-interior and the stress row and the velocity row are
+    z-interior, so the per-lane path would take its interior branches for all
+    of them, and the velocity row belongs to the item (the fast stores check
+    only j < z1 and the owned lanes).  A source term in an item only removes
+    fast iterations.  On the benchmark grids most warp-iterations are fast."""
+    ctas = worklist(nx, nz, npml, 1.0, 3, bands)
+
+    def xfast(x):
+        return x >= max(4, npml) and x + 3 <= min(nx - 5, nx - npml - 1)
+
+    def zfast(j):
+        return 4 <= j <= nz - 5 and j < nz - npml and not (top and j < npml)
+
+    fast = total = 0
+    for items in ctas:
+        for (x0, z0, z1) in items:
+            niter = (z1 - z0) // 4 + 2
+            lanes_x = [x0 - 4 + 4 * q for q in range(32)]
+            item_fast = all(xfast(x) for x in lanes_x)
+            fjlo = max(z0, max(4, npml if top else 0)) + 4 if item_fast else 2 ** 31 - 1
+            fjhi = min(nz - 5, nz - npml - 1)
+            for i in range(niter):
+                for g in range(4):
+                    total += 1
+                    j = z0 - 4 + 4 * i + g
+                    if not fjlo <= j <= fjhi:
+                        continue
+                    fast += 1
+                    a = j - 4
+                    assert zfast(j) and zfast(a) and z0 <= a < nz and j >= z0
+                    assert all(xfast(x) and 0 <= x and x + 3 < nx for x in lanes_x)
+    if nx >= 4000:
+        assert fast > 0.75 * total, (fast, total)
