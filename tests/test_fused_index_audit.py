@@ -12,7 +12,9 @@ the benchmarks use (and the 64-shot batch), that
     shared-memory address;
   * every shared-memory read and write stays inside its ring;
   * every HBM store lands on a cell of the grid;
-  * no CTA holds more work items than its item table.
+  * no CTA holds more work items than its item table;
+  * the uniform fast iterations of the 16-bit sweep take only warps whose
+    lanes are all interior, on z-interior rows of their item.
 
 Index expressions are affine in the lane chunk q and the row group g, so the
 extreme values q in {0, 31}, g in {0, 3} bound every thread.
