@@ -534,12 +534,18 @@ def main():
             "e2e": e2e}
     if best_plan:
         line["config"]["plan"] = {"wx": best_plan["wx"], "wz": best_plan["wz"], "oversub": best_plan["oversub"],
-                                  "bands": best_plan.get("bands", 0), "autotune_trials": len(tune)}
+                                  "bands": best_plan.get("bands", 0), "fast_iter": best_plan.get("fast_iter", 0),
+                                  "autotune_trials": len(tune)}
         if tune:
-            # fastest trial of each way of cutting (ms per step)
+            # fastest trial of each way of cutting (ms per step); FP32: the
+            # best plan on the sweep with uniform fast iterations
             line["config"]["plan"]["best_trial_ms"] = {
-                "bands%d" % b: min((t["ms_per_step"] for t in tune if t["bands"] == b), default=None)
+                "bands%d" % b: min((t["ms_per_step"] for t in tune if t["bands"] == b and not t["fast_iter"]),
+                                   default=None)
                 for b in (0, 1)}
+            fast = [t["ms_per_step"] for t in tune if t["fast_iter"]]
+            if fast:
+                line["config"]["plan"]["best_trial_ms"]["fast_iter1"] = min(fast)
     if accuracy:
         line["accuracy"] = accuracy
     if punch is not None:

@@ -73,7 +73,7 @@ class Fd23Error(RuntimeError):
 
 class TuneEntry(_C.Structure):
     _fields_ = [("wx", _C.c_double), ("wz", _C.c_double), ("per_sm", _C.c_int), ("bands", _C.c_int),
-                ("oversub", _C.c_double), ("ms_per_step", _C.c_double)]
+                ("oversub", _C.c_double), ("ms_per_step", _C.c_double), ("fast_iter", _C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -670,9 +670,10 @@ class Solver:
         n = _check(lib().fd23_autotune(self._h, trial_steps, _C.cast(tab, _C.c_void_p), 256), "fd23_autotune")
         return [tab[k].as_dict() for k in range(min(n, 256))]
 
-    def set_plan(self, wx=4.0, wz=3.0, per_sm=3, oversub=1.0, bands=1):
-        """Install a work plan without timing it (fd23_set_plan)."""
-        t = TuneEntry(wx=wx, wz=wz, per_sm=per_sm, bands=bands, oversub=oversub)
+    def set_plan(self, wx=4.0, wz=3.0, per_sm=3, oversub=1.0, bands=1, fast_iter=0):
+        """Install a work plan without timing it (fd23_set_plan); fast_iter=1
+        selects the FP32 sweep with uniform fast iterations."""
+        t = TuneEntry(wx=wx, wz=wz, per_sm=per_sm, bands=bands, oversub=oversub, fast_iter=fast_iter)
         _check(lib().fd23_set_plan(self._h, _C.cast(_C.pointer(t), _C.c_void_p)), "fd23_set_plan")
 
     def plan(self):

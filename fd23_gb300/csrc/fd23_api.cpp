@@ -206,7 +206,7 @@ int step_impl(fd23_solver *s, int rec_now, int more)
             sh.ncta = nblocks;
         }
         rc = launch_step_fused<S, C>(sh, s->d.wave, items, off, nblocks, s->par, s->it, s->pending_rec,
-                                     s->err_flag, s->stream);
+                                     s->err_flag, s->stream, s->tune.fast);
         if (rc) return rc;
         if (slot >= 0) CK(cudaEventRecord(s->phase[slot].done, s->stream));
         s->pending_rec = -1;

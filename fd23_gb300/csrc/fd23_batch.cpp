@@ -298,7 +298,7 @@ std::vector<TuneParams> candidates()
 // recording on `st`.  The table gets every trial, the second round last.
 template <class Apply, class Steps>
 int autotune_core(const std::vector<fd23_solver *> &ss, cudaStream_t st, int trial_steps, Apply apply,
-                  Steps steps, fd23_tune_entry *table, int cap)
+                  Steps steps, fd23_tune_entry *table, int cap, bool try_fast)
 {
     Snapshot sn;
     int rc = snapshot_take(ss, st, sn);
@@ -320,7 +320,9 @@ int autotune_core(const std::vector<fd23_solver *> &ss, cudaStream_t st, int tri
         float ms = 0.f;
         CK(cudaEventElapsedTime(&ms, e0, e1));
         *per = ms / k;
-        if (table && n < cap) table[n] = fd23_tune_entry{cand[i].wx, cand[i].wz, cand[i].per_sm, cand[i].bands, cand[i].oversub, *per};
+        if (table && n < cap)
+            table[n] = fd23_tune_entry{cand[i].wx,    cand[i].wz, cand[i].per_sm, cand[i].bands,
+                                       cand[i].oversub, *per,     cand[i].fast};
         ++n;
         return snapshot_restore(ss, st, sn);
     };
@@ -354,6 +356,18 @@ int autotune_core(const std::vector<fd23_solver *> &ss, cudaStream_t st, int tri
                     best_ms = per;
                 }
             }
+        // last: the best plan on the sweep instantiation with fast iterations
+        if (try_fast && !rc) {
+            TuneParams t = cand[best];
+            t.fast = 1;
+            cand.push_back(t);
+            double per = 0.0;
+            rc = trial(cand.size() - 1, 3 * trial_steps, &per);
+            if (!rc && per < best_ms) {
+                best = (int)cand.size() - 1;
+                best_ms = per;
+            }
+        }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -458,7 +472,7 @@ int fd23_batch_set_graph(fd23_batch *b, int on)
 int fd23_batch_set_plan(fd23_batch *b, const fd23_tune_entry *tune)
 {
     if (!b || !tune || !(tune->wx > 0) || !(tune->wz > 0) || tune->per_sm < 1 || !(tune->oversub >= 1.0 / 16) ||
-        tune->oversub > 64.0 || (tune->bands != 0 && tune->bands != 1))
+        tune->oversub > 64.0 || (tune->bands != 0 && tune->bands != 1) || (tune->fast_iter != 0 && tune->fast_iter != 1))
         return FD23_ERR_ARG;
     CK(cudaSetDevice(b->device));
     CK(cudaStreamSynchronize(b->stream));  // the old work list may still be in use
@@ -469,7 +483,7 @@ int fd23_batch_set_plan(fd23_batch *b, const fd23_tune_entry *tune)
 int fd23_batch_get_plan(fd23_batch *b, fd23_tune_entry *cur, int *nblocks)
 {
     if (!b) return FD23_ERR_ARG;
-    if (cur) *cur = fd23_tune_entry{b->tune.wx, b->tune.wz, b->tune.per_sm, b->tune.bands, b->tune.oversub, 0.0};
+    if (cur) *cur = fd23_tune_entry{b->tune.wx, b->tune.wz, b->tune.per_sm, b->tune.bands, b->tune.oversub, 0.0, 0};
     if (nblocks) *nblocks = b->plan.nblocks;
     return FD23_OK;
 }
@@ -517,7 +531,7 @@ int fd23_batch_autotune(fd23_batch *b, int trial_steps, fd23_tune_entry *table, 
         }
         return FD23_OK;
     };
-    rc = autotune_core(b->s, b->stream, trial_steps, apply, steps, table, cap);
+    rc = autotune_core(b->s, b->stream, trial_steps, apply, steps, table, cap, false);
     const int jr = join_out(b);
     return rc < 0 ? rc : (jr ? jr : rc);
 }
@@ -571,13 +585,14 @@ int fd23_work_plan(int nshots, const int *nx, const int *nz, const int *npml, co
 int fd23_set_plan(fd23_solver *s, const fd23_tune_entry *tune)
 {
     if (!s || !tune || !(tune->wx > 0) || !(tune->wz > 0) || tune->per_sm < 1 || !(tune->oversub >= 1.0 / 16) ||
-        tune->oversub > 64.0 || (tune->bands != 0 && tune->bands != 1))
+        tune->oversub > 64.0 || (tune->bands != 0 && tune->bands != 1) || (tune->fast_iter != 0 && tune->fast_iter != 1))
         return FD23_ERR_ARG;
     if (!s->fused) return FD23_ERR_UNSUPPORTED;
     CK(cudaSetDevice(s->d.device));
     CK(cudaStreamSynchronize(s->stream));  // the old work list may still be in use
     TuneParams t{tune->wx, tune->wz, tune->per_sm, tune->oversub, tune->bands};
     t.shift = s->tune.shift;
+    t.fast = tune->fast_iter;
     s->tune = t;
     int rc = build_worklist(s);
     // the two-step sweep's plan takes the same weights and cut (its own CTAs per SM)
@@ -588,7 +603,9 @@ int fd23_set_plan(fd23_solver *s, const fd23_tune_entry *tune)
 int fd23_get_plan(fd23_solver *s, fd23_tune_entry *cur, int *nblocks)
 {
     if (!s) return FD23_ERR_ARG;
-    if (cur) *cur = fd23_tune_entry{s->tune.wx, s->tune.wz, s->tune.per_sm, s->tune.bands, s->tune.oversub, 0.0};
+    if (cur)
+        *cur = fd23_tune_entry{s->tune.wx, s->tune.wz, s->tune.per_sm, s->tune.bands, s->tune.oversub, 0.0,
+                               s->tune.fast};
     if (nblocks) *nblocks = s->nblocks;
     return FD23_OK;
 }
@@ -616,7 +633,7 @@ int fd23_autotune(fd23_solver *s, int trial_steps, fd23_tune_entry *table, int c
         }
         return FD23_OK;
     };
-    return autotune_core(ss, s->stream, trial_steps, apply, steps, table, cap);
+    return autotune_core(ss, s->stream, trial_steps, apply, steps, table, cap, s->d.prec == FD23_F32);
 }
 
 }  // extern "C"

@@ -1,5 +1,7 @@
 // Plain fused sweep: entry points and the instantiations without tile step
 // windows (the kernel template is in fd23_fused.cuh).
+#include <type_traits>
+
 #include "fd23_fused.cuh"
 
 namespace fd23 {
@@ -60,7 +62,7 @@ FusedGeom fused_geom(int wave, int prec)
 
 template <class S, class C>
 int launch_step_fused(const Shot<S, C> &s, int wave, const WorkItem *items, const int *item_off,
-                      int nblocks, int par, int it, int rec_index, int *err_flag, cudaStream_t st)
+                      int nblocks, int par, int it, int rec_index, int *err_flag, cudaStream_t st, int fast)
 {
     if (s.midx)
         return s.punch.win ? launch_step_fused_table_punch<S, C>(s, nullptr, wave, items, item_off, nblocks, par, it,
@@ -70,6 +72,16 @@ int launch_step_fused(const Shot<S, C> &s, int wave, const WorkItem *items, cons
     if (s.punch.win)
         return launch_step_fused_punch<S, C>(s, nullptr, wave, items, item_off, nblocks, par, it, rec_index,
                                              err_flag, st);
+    if constexpr (std::is_same<S, float>::value) {
+        if (fast)
+            return wave == FD23_PSV
+                       ? launch_fused_impl<S, C, FD23_PSV, false, false, false, true>(s, nullptr, items, item_off,
+                                                                                    nblocks, par, it, rec_index,
+                                                                                    err_flag, st)
+                       : launch_fused_impl<S, C, FD23_SH, false, false, false, true>(s, nullptr, items, item_off,
+                                                                                   nblocks, par, it, rec_index,
+                                                                                   err_flag, st);
+    }
     if (wave == FD23_PSV)
         return launch_fused_impl<S, C, FD23_PSV, false, false>(s, nullptr, items, item_off, nblocks, par, it,
                                                                rec_index, err_flag, st);
@@ -117,6 +129,7 @@ int fused_prepare(int wave, int prec)
             default: rc = prepare_one<float, float, FD23_SH, false>();
         }
     }
+    if (!rc && prec == FD23_F32) rc = wave == FD23_PSV ? prepare_fast<FD23_PSV>() : prepare_fast<FD23_SH>();
     if (!rc) rc = fused_prepare_punch(wave, prec);
     if (!rc) rc = fused_prepare_table(wave, prec);
     if (!rc) rc = fused_prepare_table_punch(wave, prec);
@@ -175,7 +188,7 @@ size_t fused_smem_bytes(int wave, int prec)
 
 #define FD23_INST(S, C)                                                                                  \
     template int launch_step_fused<S, C>(const Shot<S, C> &, int, const WorkItem *, const int *,       \
-                                         int, int, int, int, int *, cudaStream_t);                     \
+                                         int, int, int, int, int *, cudaStream_t, int);                \
     template int launch_step_fused_batch<S, C>(const Shot<S, C> *, int, const WorkItem *, const int *, \
                                                int, int, int, int, int *, bool, bool, cudaStream_t);
 FD23_INST(float, float)

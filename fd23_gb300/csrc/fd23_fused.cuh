@@ -391,6 +391,8 @@ struct Cfg {
     // FP32 sweep is held by latency: 13 % fewer instructions gave C1 8.03e10
     // against 8.13e10.  In the batched sweeps the extra registers spill
     // (C4 FP32 7.28e10 against 7.81e10, C4 FP16 8.14e10 against 8.64e10).
+    // The single-shot FP32 sweep has a second instantiation with them
+    // (FASTF), which the autotuner picks where it is faster.
     static constexpr bool FAST_ITER = sizeof(S) == 2;
     // bytes the copies of one point-wise stage deliver
     static constexpr uint32_t PW_TX =
@@ -430,7 +432,10 @@ struct ItemInfo {
 // the last, so both buffer sets already hold their values).
 // TABLE = true: the shots carry material tables; the material of a cell is
 // its index byte looked up in the CTA's shared-memory copy of the table.
-template <class S, class C, int WAVE, bool BATCH, bool PUNCH, bool TABLE>
+// FASTF = true: the uniform fast iterations in a sweep whose storage does
+// not take them by default (FP32; a separate instantiation, so that the
+// plain one compiles as before).
+template <class S, class C, int WAVE, bool BATCH, bool PUNCH, bool TABLE, bool FASTF = false>
 __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::template minb<BATCH>())
     fused_step(const __grid_constant__ Shot<S, C> sh_param, const Shot<S, C> *__restrict__ shots,
                const WorkItem *__restrict__ items, const int *__restrict__ item_off, int par, int it,
@@ -770,7 +775,8 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
         // velocity row belongs to the item, i.e. j in [fjlo, fjhi] (an empty
         // range when the item is not fast): every lane then takes the
         // interior arithmetic with no per-lane branch.
-        bool item_fast = K::FAST_ITER && !BATCH && !PUNCH && __all_sync(0xffffffffu, xfast) && ntl == 0;
+        constexpr bool kFast = (K::FAST_ITER || FASTF) && !BATCH && !PUNCH;
+        bool item_fast = kFast && __all_sync(0xffffffffu, xfast) && ntl == 0;
         if constexpr (PSV && std::is_same<S, C>::value && !BATCH) item_fast = item_fast && !sh.box.on;
         const int fjlo = item_fast ? max(I.z0, max(4, sh.topabsorb ? npml : 0)) + 4 : INT_MAX;
         const int fjhi = min(nz - 5, nz - npml - 1);
@@ -788,7 +794,7 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
             const int jf = I.z0 - 4 + 4 * i + grp;  // stress row; the velocity row is jf - 4
             // (an SH item starting at row 0 meets its free-surface barrier at
             // i = 1, where jf < 4: never fast, so every warp takes it)
-            if (K::FAST_ITER && !BATCH && !PUNCH && jf >= fjlo && jf <= fjhi) {
+            if (kFast && jf >= fjlo && jf <= fjhi) {
                 // ---- stress of row jf, every lane ----
                 {
                     const S *urow[9];
@@ -1534,7 +1540,7 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
     }
 }
 
-template <class S, class C, int WAVE, bool BATCH, bool PUNCH, bool TABLE = false>
+template <class S, class C, int WAVE, bool BATCH, bool PUNCH, bool TABLE = false, bool FASTF = false>
 int launch_fused_impl(const Shot<S, C> &s, const Shot<S, C> *shots, const WorkItem *items, const int *item_off,
                       int nblocks, int par, int it, int rec_index, int *err_flag, cudaStream_t st)
 {
@@ -1549,9 +1555,20 @@ int launch_fused_impl(const Shot<S, C> &s, const Shot<S, C> *shots, const WorkIt
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    const cudaError_t e = cudaLaunchKernelEx(&cfg, fused_step<S, C, WAVE, BATCH, PUNCH, TABLE>, s, shots, items, item_off,
-                                             par, it, rec_index, err_flag);
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, fused_step<S, C, WAVE, BATCH, PUNCH, TABLE, FASTF>, s, shots, items,
+                                             item_off, par, it, rec_index, err_flag);
     return e == cudaSuccess ? FD23_OK : FD23_ERR_CUDA;
+}
+
+// the FP32 instantiation with the fast iterations (single shot, plain)
+template <int WAVE>
+int prepare_fast()
+{
+    return cudaFuncSetAttribute(fused_step<float, float, WAVE, false, false, false, true>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)Cfg<float, float, WAVE>::SMEM) == cudaSuccess
+               ? FD23_OK
+               : FD23_ERR_CUDA;
 }
 
 template <class S, class C, int WAVE, bool PUNCH, bool TABLE = false>

@@ -209,6 +209,7 @@ struct TuneParams {
     double oversub = 1.0;       // CTAs launched per resident slot
     int bands = 1;              // cut every strip on its own (plan_work)
     int shift = 1;              // let plan_work move the strips' origin left of column 0
+    int fast = 0;               // single-shot FP32: the sweep with uniform fast iterations
 };
 struct WorkPlan {
     std::vector<WorkItem> items;

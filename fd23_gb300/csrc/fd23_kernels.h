@@ -45,10 +45,12 @@ int fused_occupancy(int wave, int prec, bool batch);  // resident CTAs per SM (c
 
 // One time step of every work item: reads buffer set `par`, writes `1-par`.
 // `rec_index` >= 0 gathers the receivers of the previous step from buffer set
-// `par` into that record row on the way.
+// `par` into that record row on the way.  `fast` != 0 selects the FP32
+// sweep's instantiation with uniform fast iterations (other storage types and
+// the window / table sweeps ignore it).
 template <class S, class C>
 int launch_step_fused(const Shot<S, C> &s, int wave, const WorkItem *items, const int *item_off,
-                      int nblocks, int par, int it, int rec_index, int *err_flag, cudaStream_t st);
+                      int nblocks, int par, int it, int rec_index, int *err_flag, cudaStream_t st, int fast = 0);
 
 // Hybrid box (P-SV), fd23_box.cu.  Ring exchange on buffer set `par`:
 // which = 0 for U, W (start of a step), 1 for the stresses (after the stress

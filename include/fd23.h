@@ -349,9 +349,10 @@ int fd23_batch_set_graph(fd23_batch *b, int on);
  * fd23_autotune / fd23_batch_autotune time every candidate plan (144: wx
  * 2..7, wz 2..5, oversub 1..3, bands 0..1) for trial_steps steps on the live
  * shot(s), then the five fastest and the 8 half-step
- * neighbours of the best weights for 3 x trial_steps, restore the
- * wavefields, memory variables and step counters after each trial, and
- * keep the fastest plan of the long trials.  table (cap
+ * neighbours of the best weights for 3 x trial_steps (single-shot FP32:
+ * then the best plan with fast_iter = 1), restore the wavefields, memory
+ * variables and step counters after each trial, and keep the fastest plan
+ * of the long trials.  table (cap
  * entries) receives every trial, the second round last; returns the number
  * of trials or a negative status. */
 typedef struct {
@@ -363,6 +364,11 @@ typedef struct {
                          * CTAs than strips; others fall back to 0) */
     double oversub;     /* CTAs launched per resident slot */
     double ms_per_step; /* measured (0 for the current plan) */
+    int fast_iter;      /* 1: the single-shot FP32 sweep with uniform fast
+                         * iterations (interior rows of all-interior warps
+                         * without per-lane branches; same results), 0: the
+                         * plain one.  16-bit storage always takes them; FP64,
+                         * the batch and the window / table sweeps ignore it. */
 } fd23_tune_entry;
 int fd23_autotune(fd23_solver *s, int trial_steps, fd23_tune_entry *table, int cap);
 int fd23_batch_autotune(fd23_batch *b, int trial_steps, fd23_tune_entry *table, int cap);

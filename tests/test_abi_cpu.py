@@ -30,15 +30,32 @@ def test_library_exports_every_declared_function():
     assert sorted(F.ABI_FUNCTIONS) == names
 
 
-def test_tune_entry_layout():
-    """fd23_tune_entry: bands fills the padding after per_sm, so the struct
-    keeps the size and offsets it had without it (40 bytes, oversub at 24)."""
+def test_tune_entry_layout(tmp_path):
+    """fd23_tune_entry: bands fills the padding after per_sm, fast_iter comes
+    last (48 bytes with its padding); the ctypes mirror matches the header as
+    a C compiler lays it out."""
     import ctypes
-    assert ctypes.sizeof(F.TuneEntry) == 40
+    import shutil
+    import subprocess
+    assert ctypes.sizeof(F.TuneEntry) == 48
     assert F.TuneEntry.per_sm.offset == 16 and F.TuneEntry.bands.offset == 20
     assert F.TuneEntry.oversub.offset == 24 and F.TuneEntry.ms_per_step.offset == 32
+    assert F.TuneEntry.fast_iter.offset == 40
     t = F.TuneEntry()
-    assert t.bands == 0  # zero-filled: the strip-major cut
+    assert t.bands == 0 and t.fast_iter == 0  # zero-filled: strip-major cut, plain sweep
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    src = tmp_path / "layout.c"
+    src.write_text('#include <stddef.h>\n#include <stdio.h>\n#include "fd23.h"\n'
+                   'int main(void) { printf("%zu %zu %zu %zu %zu\\n", sizeof(fd23_tune_entry), '
+                   'offsetof(fd23_tune_entry, bands), offsetof(fd23_tune_entry, oversub), '
+                   'offsetof(fd23_tune_entry, ms_per_step), offsetof(fd23_tune_entry, fast_iter)); return 0; }\n')
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", inc, str(src), "-o", str(exe)], check=True)
+    got = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+    assert [int(v) for v in got] == [48, 20, 24, 32, 40]
 
 
 def test_create_without_gpu_fails_cleanly():

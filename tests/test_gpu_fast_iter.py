@@ -37,9 +37,11 @@ def _ids(c):
 
 
 @pytest.mark.parametrize("oversub", [1.0, 3.0])
-@pytest.mark.parametrize("prec", ["f16", "bf16"])
+@pytest.mark.parametrize("prec", ["f16", "bf16", "f32"])
 @pytest.mark.parametrize("cfg", CASES, ids=_ids)
 def test_fast_iterations_equal_twopass(cfg, prec, oversub):
+    """FP32 runs the instantiation with fast iterations (fast_iter = 1), the
+    16-bit forms the one they always take."""
     F = pytest.importorskip("fd23_gb300")
     plan = {k: cfg[k] for k in ("per_sm", "ov_scale") if k in cfg}
     c = Case(nt=50, seed=21, **{k: v for k, v in cfg.items() if k not in plan})
@@ -48,7 +50,8 @@ def test_fast_iterations_equal_twopass(cfg, prec, oversub):
     def run(kernel):
         s = c.solver(prec, kernel)
         if kernel == "fused":
-            s.set_plan(4.0, 2.5, per_sm, ov)
+            s.set_plan(4.0, 2.5, per_sm, ov, fast_iter=int(prec == "f32"))
+            assert s.plan()["fast_iter"] == int(prec == "f32")
         s.run(c.nt, 1)
         out = [s.seismograms(0)] + ([s.seismograms(1)] if c.wave == "psv" else []) + [s.get_state()]
         s.close()
@@ -58,3 +61,22 @@ def test_fast_iterations_equal_twopass(cfg, prec, oversub):
     assert np.isfinite(fused[-1]).all()
     for a, b in zip(fused, twopass):
         np.testing.assert_array_equal(a, b)
+
+
+def test_fp32_autotune_tries_the_fast_instantiation():
+    """The single-shot FP32 autotune times its best plan once more on the
+    sweep with fast iterations (the last trial) and keeps the faster; the
+    batch and 16-bit storage do not add that trial."""
+    F = pytest.importorskip("fd23_gb300")
+    c = Case("psv", 600, 300, npml=20, nt=40, seed=22)
+    s = c.solver("f32", "fused")
+    tab = s.autotune(2)
+    assert tab[-1]["fast_iter"] == 1 and all(t["fast_iter"] == 0 for t in tab[:-1])
+    assert s.plan()["fast_iter"] in (0, 1)
+    s.run(c.nt, 1)
+    seis, st = c.oracle("f32")
+    np.testing.assert_array_equal(s.get_state(), st)
+    s.close()
+    h = c.solver("f16", "fused")
+    assert all(t["fast_iter"] == 0 for t in h.autotune(2))
+    h.close()
