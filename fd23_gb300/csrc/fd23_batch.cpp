@@ -633,7 +633,10 @@ int fd23_autotune(fd23_solver *s, int trial_steps, fd23_tune_entry *table, int c
         }
         return FD23_OK;
     };
-    return autotune_core(ss, s->stream, trial_steps, apply, steps, table, cap, s->d.prec == FD23_F32);
+    // the fast-iteration instantiation exists for the plain FP32 sweep only
+    // (window, table and box runs launch other sweeps, which ignore it)
+    const bool try_fast = s->d.prec == FD23_F32 && !s->d_punch && !s->d_midx && !s->box_on;
+    return autotune_core(ss, s->stream, trial_steps, apply, steps, table, cap, try_fast);
 }
 
 }  // extern "C"

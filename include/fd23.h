@@ -349,8 +349,9 @@ int fd23_batch_set_graph(fd23_batch *b, int on);
  * fd23_autotune / fd23_batch_autotune time every candidate plan (144: wx
  * 2..7, wz 2..5, oversub 1..3, bands 0..1) for trial_steps steps on the live
  * shot(s), then the five fastest and the 8 half-step
- * neighbours of the best weights for 3 x trial_steps (single-shot FP32:
- * then the best plan with fast_iter = 1), restore the wavefields, memory
+ * neighbours of the best weights for 3 x trial_steps (a single FP32 shot
+ * without windows, table or box: then the best plan with fast_iter = 1),
+ * restore the wavefields, memory
  * variables and step counters after each trial, and keep the fastest plan
  * of the long trials.  table (cap
  * entries) receives every trial, the second round last; returns the number
