@@ -394,6 +394,12 @@ struct Cfg {
     // The single-shot FP32 sweep has a second instantiation with them
     // (FASTF), which the autotuner picks where it is faster.
     static constexpr bool FAST_ITER = sizeof(S) == 2;
+    // 16-bit storage: the strip's x-CPML coefficients (b, c, k of the four
+    // staggered positions, 12 x SW) in shared memory for the general path,
+    // which otherwise waits on a read-only global load per use (there is no
+    // room for the table beside three CTAs of the 4-byte forms)
+    static constexpr bool XTAB = sizeof(S) == 2;
+    static constexpr int XT_ELEMS = XTAB ? 12 * SW : 0;
     // bytes the copies of one point-wise stage deliver
     static constexpr uint32_t PW_TX =
         TABLE ? (uint32_t)(NT * 4 * PWW * sizeof(S) + 8 * kIdxBoxW) : (uint32_t)(NPF * 4 * PWW * sizeof(S));
@@ -413,8 +419,9 @@ struct Cfg {
     static constexpr int minb() { return sizeof(S) == 8 ? 1 : 3; }
     // the stress ring holds arithmetic-type values (rounded through S when
     // written): the velocity update reads each of them many times
-    static constexpr size_t RING_BYTES =
-        (((size_t)(UW_ELEMS + PW_ELEMS + TAB_ELEMS) * sizeof(S) + (size_t)TR_ELEMS * sizeof(C) + 15) & ~(size_t)15);
+    static constexpr size_t RING_BYTES = (((size_t)(UW_ELEMS + PW_ELEMS + TAB_ELEMS) * sizeof(S) +
+                                           (size_t)(TR_ELEMS + XT_ELEMS) * sizeof(C) + 15) &
+                                          ~(size_t)15);
     static constexpr size_t SMEM = RING_BYTES + 256 /* 2*(NUW+NPW) barriers */ + MAX_ITEMS * 16 +
                                    (size_t)MAX_ITEMS * MAX_TERMS * 16;
 };
@@ -455,7 +462,8 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
     S *uw_s = reinterpret_cast<S *>(smem_raw);
     S *pw_s = uw_s + K::UW_ELEMS;
     C *tr_s = reinterpret_cast<C *>(pw_s + K::PW_ELEMS);  // stress ring (arithmetic type)
-    S *tab_s = reinterpret_cast<S *>(tr_s + K::TR_ELEMS);  // the material table (TABLE only)
+    C *cx_s = tr_s + K::TR_ELEMS;                          // x-CPML coefficients of the strip (XTAB)
+    S *tab_s = reinterpret_cast<S *>(cx_s + K::XT_ELEMS);  // the material table (TABLE only)
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw + K::RING_BYTES);
     uint64_t *full_uw = bars, *empty_uw = bars + K::NUW;
     uint64_t *full_pw = bars + 2 * K::NUW, *empty_pw = full_pw + K::NPW;
@@ -707,6 +715,24 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
         const int ixo = ((kXPad + I.x0 - 4 - K::PWOFF) & 15) + K::PWOFF + 4 * lane;
         // the 4 cells are interior (8th order), outside the x-CPML and inside the grid
         const bool xfast = x >= max(4, npml) && x + 3 <= min(nx - 5, nx - npml - 1);
+        // x-CPML coefficient kc (0 b, 1 c, 2 k) of staggered position ac at
+        // column ix of this item's strip
+        auto cxc = [&](int kc, int ac, int ix) -> C {
+            if constexpr (K::XTAB) return cx_s[(4 * kc + ac) * K::SW + 4 * lane + (ix - x)];  // ix - x: the cell
+            else return __ldg(cp + (kc * B + ac * nx + ix));
+        };
+        if constexpr (K::XTAB) {
+            // an item whose strip reaches into the x-CPML fills the table; the
+            // test is the same for every compute warp (one item for all)
+            if (npml > 0 && (I.x0 - 4 < npml || I.x0 - 4 + K::SW > nx - npml)) {
+                compute_bar(NCT);  // the previous item's reads of the table are done
+                for (int q = tid; q < K::XT_ELEMS; q += NCT) {
+                    const int r = q / K::SW, ix = I.x0 - 4 + (q - r * K::SW);
+                    cx_s[q] = ix >= 0 && ix < nx ? __ldg(cp + ((r >> 2) * B + (r & 3) * nx + ix)) : (C)0;
+                }
+                compute_bar(NCT);
+            }
+        }
         // ---- interior arithmetic (8th order, no CPML), shared by the uniform
         // fast iteration below and the per-lane path: one operation sequence.
         // Stress: packed operands (x differences stay per cell);
@@ -1080,12 +1106,12 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                             C txx = told[0][e], txz = told[1][e], tzz = told[2][e];
                             // x chain, PD/fd/cu_fd.cu:303-326
                             if (xp) {
-                                const C pu = fmaC<C>(__ldg(cp + (2 * nx + ix)), psx[0][e], __ldg(cp + (B + 2 * nx + ix)) * ux);
-                                const C t = fmaC<C>(ux, __ldg(cp + (2 * B + 2 * nx + ix)), pu);
+                                const C pu = fmaC<C>(cxc(0, 2, ix), psx[0][e], cxc(1, 2, ix) * ux);
+                                const C t = fmaC<C>(ux, cxc(2, 2, ix), pu);
                                 txx = fmaC<C>(gam, t, txx);
                                 tzz = fmaC<C>(lam, t, tzz);
-                                const C pw = fmaC<C>(__ldg(cp + (3 * nx + ix)), psx[1][e], __ldg(cp + (B + 3 * nx + ix)) * wx);
-                                txz = fmaC<C>(mua, fmaC<C>(wx, __ldg(cp + (2 * B + 3 * nx + ix)), pw), txz);
+                                const C pw = fmaC<C>(cxc(0, 3, ix), psx[1][e], cxc(1, 3, ix) * wx);
+                                txz = fmaC<C>(mua, fmaC<C>(wx, cxc(2, 3, ix), pw), txz);
                                 if (own) { pwr[2][px] = pu; pwr[3][px] = pw; }
                             } else if (j != 0) {
                                 txx = fmaC<C>(gam, ux, txx);
@@ -1125,9 +1151,9 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                             const C mux = ms[0][e], muz = ms[1][e];
                             C tx = told[0][e], tz = told[1][e];
                             if (xp) {
-                                const C a = fmaC<C>(__ldg(cp + (nx + ix)), psx[0][e], __ldg(cp + (B + nx + ix)) * dxv);
+                                const C a = fmaC<C>(cxc(0, 1, ix), psx[0][e], cxc(1, 1, ix) * dxv);
                                 if (own) pwr[1][px] = a;
-                                tx = fmaC<C>(mux, fmaC<C>(dxv, __ldg(cp + (2 * B + nx + ix)), a), tx);
+                                tx = fmaC<C>(mux, fmaC<C>(dxv, cxc(2, 1, ix), a), tx);
                             } else {
                                 tx = fmaC<C>(mux, dxv, tx);
                             }
@@ -1453,12 +1479,12 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                                 C u = vold[0][e], w = vold[1][e];
                                 // x chain, PD/fd/cu_fd.cu:455-474
                                 if (xp) {
-                                    const C pa = fmaC<C>(__ldg(cp + (ix)), psx[0][e], __ldg(cp + (B + ix)) * dxTxx);
+                                    const C pa = fmaC<C>(cxc(0, 0, ix), psx[0][e], cxc(1, 0, ix) * dxTxx);
                                     pwr[0][px] = pa;
-                                    u = fmaC<C>(bu, fmaC<C>(dxTxx, __ldg(cp + (2 * B + ix)), pa), u);
-                                    const C pb = fmaC<C>(__ldg(cp + (nx + ix)), psx[1][e], __ldg(cp + (B + nx + ix)) * dxTxz);
+                                    u = fmaC<C>(bu, fmaC<C>(dxTxx, cxc(2, 0, ix), pa), u);
+                                    const C pb = fmaC<C>(cxc(0, 1, ix), psx[1][e], cxc(1, 1, ix) * dxTxz);
                                     pwr[1][px] = pb;
-                                    w = fmaC<C>(bw, fmaC<C>(dxTxz, __ldg(cp + (2 * B + nx + ix)), pb), w);
+                                    w = fmaC<C>(bw, fmaC<C>(dxTxz, cxc(2, 1, ix), pb), w);
                                 } else if (a != 0) {
                                     u = fmaC<C>(bu, dxTxx, u);
                                     w = fmaC<C>(bw, dxTxz, w);
@@ -1486,9 +1512,9 @@ __global__ void __launch_bounds__(Cfg<S, C, WAVE>::NTH, Cfg<S, C, WAVE>::templat
                                 const C bv = mv[0][e];
                                 C v = vold[0][e];
                                 if (xp) {
-                                    const C pa = fmaC<C>(__ldg(cp + (ix)), psx[0][e], __ldg(cp + (B + ix)) * dxT);
+                                    const C pa = fmaC<C>(cxc(0, 0, ix), psx[0][e], cxc(1, 0, ix) * dxT);
                                     pwr[0][px] = pa;
-                                    v = fmaC<C>(bv, fmaC<C>(dxT, __ldg(cp + (2 * B + ix)), pa), v);
+                                    v = fmaC<C>(bv, fmaC<C>(dxT, cxc(2, 0, ix), pa), v);
                                 } else {
                                     v = fmaC<C>(bv, dxT, v);
                                 }

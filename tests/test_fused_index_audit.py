@@ -390,13 +390,16 @@ def test_strip_origin_puts_the_cpml_into_fewest_strips(nx, nz, npml, want_xp):
 def test_three_ctas_fit_per_sm(es, wave, batch):
     """Dynamic shared memory of the sweep (Cfg::SMEM in fd23_fused.cuh: the
     two rings and the point-wise stages in the storage type, the stress ring
-    in the arithmetic type (4-byte floats for every form but FP64), barriers,
+    in the arithmetic type (4-byte floats for every form but FP64), with
+    16-bit storage the strip's x-CPML coefficient table, barriers,
     item and source-term tables), its static shared memory (the batched
     sweep's copy of the descriptor head) and the 1 KB the runtime reserves
     per CTA: three CTAs fit the 228 KB of one SM."""
     lay = smem_layout(es, wave)
     nt = lay["nt"]
     ring = NUW * lay["uw_slot"] + NPW * lay["stage"] + NTR * 4 * nt * SW * 4
+    if es == 2:
+        ring += 12 * SW * 4  # the strip's x-CPML coefficients (b, c, k at 4 positions)
     smem = (ring + 15) // 16 * 16 + 256 + MAX_ITEMS * 16 + MAX_ITEMS * 16 * 16
     static = 512 if batch else 128
     assert 3 * (smem + static + 1024) <= 228 * 1024, (smem, static)
