@@ -73,6 +73,8 @@ def test_fp32_autotune_tries_the_fast_instantiation():
     tab = s.autotune(2)
     assert tab[-1]["fast_iter"] == 1 and all(t["fast_iter"] == 0 for t in tab[:-1])
     assert s.plan()["fast_iter"] in (0, 1)
+    with pytest.raises(F.Fd23Error):
+        s.set_plan(4.0, 2.5, 3, 1.0, fast_iter=2)  # 0 or 1 only
     s.run(c.nt, 1)
     seis, st = c.oracle("f32")
     np.testing.assert_array_equal(s.get_state(), st)
